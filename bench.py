@@ -1,0 +1,346 @@
+"""Benchmark of the noisy-circuit hot path on GB300: gate applications per second
+on the large state-vector workload (33-qubit complex64 random brickwork, depth
+30, from |0...0>), with achieved HBM bandwidth against the measured peak.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one brickwork layer of the depth-30 circuit (33 one-qubit gates and
+16 or 17 CNOTs = 49 logical gates; steps cycle through the 30 layers).  The
+state (64 GiB) is far larger than L2, so no flush is needed between steps.
+Multi-GPU runs are independent replicas (one state per GPU, no collective on
+the data path; weak scaling).  `--impl reference` times the CPU restatement of
+the reference's path (the reference is Julia, not runnable here) on the host
+cores for the same metric.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "bluetangle.jl_gb300")
+sys.path.insert(0, PKG)
+
+import numpy as np  # noqa: E402
+
+METRIC = "gate-apps/s"
+# ncu-measured DRAM bytes per amplitude of one gate sweep (read + write), from
+# the capture summarised in profiles/k_gate_sweep_c64.md; None until captured.
+TRAFFIC_BYTES_PER_AMP = None
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=33)
+    ap.add_argument("--depth", type=int, default=30)
+    ap.add_argument("--prec", default="c64", choices=["c64", "c128"])
+    ap.add_argument("--mode", default="fused2", choices=["unfused", "fused2"])
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--cpu-n", type=int, default=24, help="qubits of the CPU baseline sample")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ workload
+def layers_of(n, depth, seed):
+    """Brickwork layers: list of (ones, cnots) with ones[q] = 2x2 matrix, cnots = [(q, q+1)]."""
+    import bluetangle_gpu.circuits as C
+    ops = C.brickwork(n, depth, np.random.default_rng(seed))
+    out, i = [], 0
+    for layer in range(depth):
+        ones = {}
+        for _ in range(n):
+            ones[ops[i].qubit] = ops[i].mat
+            i += 1
+        ncx = len(range(1 if layer % 2 == 0 else 2, n, 2))
+        cx = [(ops[i + j].qubit, ops[i + j].target_qubit) for j in range(ncx)]
+        i += ncx
+        out.append((ones, cx))
+    return out
+
+
+CNOT = np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 0, 1], [0, 0, 1, 0]], dtype=complex)
+
+
+def layer_program(layer, mode):
+    """List of (matrix, qubits) passes for one layer and its logical gate count."""
+    ones, cx = layer
+    logical = len(ones) + len(cx)
+    if mode == "unfused":
+        prog = [(m, [q]) for q, m in sorted(ones.items())] + [(CNOT, [a, b]) for a, b in cx]
+        return prog, logical
+    prog, used = [], set()
+    for a, b in cx:  # the layer's one-qubit gates precede its CNOTs
+        prog.append((CNOT @ np.kron(ones[a], ones[b]), [a, b]))
+        used |= {a, b}
+    prog += [(m, [q]) for q, m in sorted(ones.items()) if q not in used]
+    return prog, logical
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ helpers
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return ws, rank, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ CPU baseline
+def cpu_baseline(args, seconds):
+    """The oracle (CPU restatement of the reference's path, complex128) on the host
+    cores: brickwork layers on a cpu_n-qubit state until `seconds` elapse; the
+    rate is scaled by 2^(cpu_n - n) to the workload's qubit count (work per gate
+    is proportional to 2^n)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    n = args.cpu_n
+    layers = layers_of(n, args.depth, args.seed)
+    psi = np.zeros(2 ** n, dtype=np.complex128)
+    psi[0] = 1
+    gates = 0
+    t0 = time.perf_counter()
+    li = 0
+    while time.perf_counter() - t0 < seconds:
+        prog, logical = layer_program(layers[li % len(layers)], "unfused")
+        O.run_gates(psi, prog)
+        gates += logical
+        li += 1
+    dt = time.perf_counter() - t0
+    rate = gates / dt / 2 ** (args.n - n)
+    return {"value": rate, "unit": METRIC, "cores": O.num_threads(), "kind": "port",
+            "sample": f"{li} brickwork layers ({gates} gates) on a {n}-qubit complex128 state in {dt:.1f} s, "
+                      f"OpenMP {O.num_threads()} threads; rate scaled by 2^-{args.n - n} to {args.n} qubits"}
+
+
+def run_reference(args):
+    ws, rank, _, dist = dist_setup(args)
+    if rank != 0:
+        return
+    per_step = max(2.0, args.cpu_seconds / 2)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(args, per_step)
+        if i >= args.warmup:
+            vals.append(r["value"])
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": f"brickwork-{args.n}q-depth{args.depth}", "global_batch": 1, "seq_len": None,
+                       "parallelism": "replicas", "l2": "state larger than L2"},
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": r["cores"], "kind": "port",
+                             "sample": r["sample"]},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_ours(args):
+    ws, rank, local, dist = dist_setup(args)
+    import bluetangle_gpu as bt
+    import torch
+
+    torch.cuda.set_device(local)
+    ctx = bt.Context(local, seed=args.seed + rank)
+    bt.Context._default = ctx
+    layers = layers_of(args.n, args.depth, args.seed)
+    progs = [layer_program(l, args.mode) for l in layers]
+    st = bt.zero_state(args.n, args.prec, 1, ctx)
+    lib = bt.lib()
+    # pre-packed column-major matrices and qubit arrays (the circuit is resident on the host)
+    packed = []
+    for prog, logical in progs:
+        pk = []
+        for m, qs in prog:
+            M = np.ascontiguousarray(np.asarray(m, dtype=np.complex128).T)
+            Q = np.ascontiguousarray(qs, dtype=np.int32)
+            pk.append((M, Q))
+        packed.append((pk, logical))
+    import ctypes
+    P = ctypes.c_void_p
+
+    def step(i):
+        pk, logical = packed[i % len(packed)]
+        for M, Q in pk:
+            rc = lib.bt_apply_matrix(st.h, len(Q), Q.ctypes.data_as(P), M.ctypes.data_as(P), 0, None, -1)
+            if rc:
+                ctx.check(rc)
+        return logical, len(pk)
+
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    for i in range(args.warmup):
+        step(i)
+    ctx.synchronize()
+    barrier(dist)
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.5)
+    l0 = ctx.launch_count
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    t_host = time.perf_counter()
+    logical_total = passes = 0
+    for i in range(args.warmup, args.warmup + args.steps):
+        lg, ps = step(i)
+        logical_total += lg
+        passes += ps
+    ev1.record(stream)
+    ev1.synchronize()
+    ctx.synchronize()
+    host_dt = time.perf_counter() - t_host
+    launches = ctx.launch_count - l0
+    ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    barrier(dist)
+    ms_max = max_over_ranks(dist, ms)
+    value = logical_total * ws / (ms_max / 1e3)
+
+    # roofline of the dominant kernel (the gate sweep: every launch in the region)
+    esize = 8 if args.prec == "c64" else 16
+    bytes_per_launch = 2 * (2 ** args.n) * esize
+    achieved = bytes_per_launch / ((ms / 1e3) / launches) / 1e9
+    peak, peak_kind = measured_peak()
+    traffic = TRAFFIC_BYTES_PER_AMP * 2 ** args.n if TRAFFIC_BYTES_PER_AMP else None
+
+    # end to end through the public API: per step the layer's matrices go from host
+    # memory into the launches, and <Z_i> for every qubit comes back to the host
+    zout = np.empty(args.n, dtype=np.float64)
+    e2e_steps = max(3, args.steps // 2)
+    h2d = 0
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        pk, _ = packed[i % len(packed)]
+        for M, Q in pk:
+            rc = lib.bt_apply_matrix(st.h, len(Q), Q.ctypes.data_as(P), M.ctypes.data_as(P), 0, None, -1)
+            if rc:
+                ctx.check(rc)
+            h2d += M.nbytes + Q.nbytes
+        ctx.check(lib.bt_expect_z_all(st.h, 0, zout.ctypes.data_as(P)))
+    e2e_dt = time.perf_counter() - t0
+    e2e_dt = max_over_ranks(dist, e2e_dt)
+    e2e_logical = sum(packed[i % len(packed)][1] for i in range(e2e_steps))
+    e2e = {"value": e2e_logical * ws / e2e_dt, "unit": METRIC, "h2d_bytes_per_step": h2d // e2e_steps,
+           "d2h_bytes_per_step": zout.nbytes, "readout": "<Z_i> for all qubits each step"}
+    assert np.all(np.isfinite(zout))
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        cpu = cpu_baseline(args, args.cpu_seconds)
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": args.prec, "data": "synthetic",
+                "config": {"workload": f"brickwork-{args.n}q-{args.prec}-depth{args.depth}", "mode": args.mode,
+                           "step": "one brickwork layer (logical gates: n one-qubit + CNOTs)",
+                           "passes_per_step": passes / args.steps, "global_batch": 1, "seq_len": None,
+                           "parallelism": f"replicas x{ws}", "l2": "state larger than L2, no flush needed",
+                           "state_bytes": (2 ** args.n) * esize},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                             "kernel": "k_gate (dense sweep)", "bytes_per_launch": bytes_per_launch,
+                             "launches": launches},
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+                "host_s": host_dt}
+        print(json.dumps(line), flush=True)
+    st.free()
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

@@ -1,0 +1,23 @@
+"""bluetangle_gpu — host-side mirror of BlueTangle.jl's noisy-circuit API over libbtgpu.
+
+The hot path (gates, channels, measurement, sampling, observables) runs in the
+sm_103a CUDA library libbtgpu.so through its C ABI (include/btgpu.h); this
+package only builds the reference's op descriptors and small host tables and
+calls the library.  Importing it loads the library and fails if it is absent.
+"""
+from ._lib import BTError, lib
+from .engine import (Context, GPUDensity, GPUState, Measurement, apply, apply_channel, apply_matrix, apply_noise,
+                     born_measure_Z, channel_probs, correlation, expect, fidelity, measure, partial_trace,
+                     pauli_masks, rho_from, run, sample, sample_exact, state_from, to_rho, to_state, zero_rho,
+                     zero_state)
+from .gates import gate, gates
+from .noise import NoiseModel, Noise1, Noise2, QuantumChannel, apply_twirl, noise_model
+from .ops import Op, OpQC, ifOp
+
+lib()  # load now: no silent fallback exists
+
+__all__ = ["BTError", "Context", "GPUState", "GPUDensity", "Measurement", "apply", "apply_channel", "apply_matrix",
+           "apply_noise", "born_measure_Z", "channel_probs", "correlation", "expect", "fidelity", "measure",
+           "partial_trace", "pauli_masks", "rho_from", "run", "sample", "sample_exact", "state_from", "to_rho",
+           "to_state", "zero_rho", "zero_state", "gate", "gates", "NoiseModel", "Noise1", "Noise2",
+           "QuantumChannel", "apply_twirl", "noise_model", "Op", "OpQC", "ifOp"]

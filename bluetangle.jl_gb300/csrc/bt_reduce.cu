@@ -1,0 +1,646 @@
+// Reductions (FP64 accumulation for every precision), measurement collapse,
+// density-matrix dephasing and the device-side branch/outcome decisions.
+//
+// Every reduction writes one partial per (member, block) and a second kernel
+// sums the partials of a member in a fixed order, so results are bit-for-bit
+// reproducible run to run.  Replaces the reference's partial traces
+// (BlueTangle.jl src/linalg.jl:83-230), Born probabilities
+// (src/hilbert.jl:682-696), Kraus branch probabilities (src/struct.jl:9-29)
+// and observables (src/func.jl:91-147).
+#include "bt_internal.cuh"
+
+#define FULL 0xffffffffu
+
+// ------------------------------------------------------------ block reduce
+// sums acc[0..W-1] over the block and writes the W results to out (thread 0..W-1)
+template <int W>
+__device__ __forceinline__ void block_sum_store(double (&acc)[W], double* out, int wcount) {
+  __shared__ double sh[BT_THREADS / 32][W];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    double v = acc[w];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+    if (lane == 0) sh[warp][w] = v;
+  }
+  __syncthreads();
+  for (int w = threadIdx.x; w < wcount; w += blockDim.x) {
+    double s = 0;
+#pragma unroll
+    for (int i = 0; i < BT_THREADS / 32; ++i) s += sh[i][w];
+    out[w] = s;
+  }
+}
+
+// out[mem][w] = sum over blocks of part[mem][blk][w] (fixed order)
+__global__ void k_finalize(const double* __restrict__ part, int nblk, int W, double* __restrict__ out) {
+  const int64_t mem = blockIdx.x;
+  for (int w = threadIdx.x; w < W; w += blockDim.x) {
+    double s = 0;
+    const double* p = part + (mem * nblk) * W + w;
+    for (int b = 0; b < nblk; ++b) s += p[(int64_t)b * W];
+    out[mem * W + w] = s;
+  }
+}
+
+// blocks per member for a reduction over `units` thread-units per member
+static int blocks_per_member(const bt_ctx* ctx, int64_t units, int64_t nmem) {
+  int64_t want = (int64_t)ctx->sm_count * 8;
+  int64_t per = (want + nmem - 1) / nmem;
+  int64_t maxb = (units + BT_THREADS - 1) / BT_THREADS;
+  if (per > maxb) per = maxb;
+  if (per > 1024) per = 1024;
+  if (per < 1) per = 1;
+  return (int)per;
+}
+
+static int finalize(bt_ctx* ctx, double* part, int nblk, int W, int64_t nmem, double* out) {
+  k_finalize<<<(unsigned)nmem, 64, 0, ctx->stream>>>(part, nblk, W, out);
+  ctx->launches++;
+  return bt_cuda_check(ctx, cudaGetLastError(), "finalize launch");
+}
+
+// partials live in ctx->work, a device buffer separate from ctx->scratch so that
+// they never alias API-level results and tables carved from the scratch buffer
+int bt_work(bt_ctx* ctx, size_t bytes, double** out) {
+  if (ctx->work_bytes < bytes) {
+    if (ctx->work) {
+      cudaStreamSynchronize(ctx->stream);
+      cudaFree(ctx->work);
+      ctx->work = nullptr;
+      ctx->work_bytes = 0;
+    }
+    size_t nb = bytes < (1u << 20) ? (1u << 20) : bytes;
+    cudaError_t e = cudaMalloc(&ctx->work, nb);
+    if (e != cudaSuccess) return bt_fail(ctx, BT_ERR_OOM, "reduction workspace allocation failed");
+    ctx->work_bytes = nb;
+  }
+  *out = (double*)ctx->work;
+  return BT_OK;
+}
+
+// ------------------------------------------------------------ reduced density matrix
+template <typename R, int K>
+__global__ void __launch_bounds__(BT_THREADS) k_rdm(const typename CT<R>::T* __restrict__ psi, int nbits,
+                                                    int4 bits4, int4 sorted4, int64_t mem_lo, int nblk,
+                                                    double* __restrict__ part) {
+  constexpr int D = 1 << K, W = 2 * D * D;
+  const int bits[4] = {bits4.x, bits4.y, bits4.z, bits4.w};
+  const int sorted[4] = {sorted4.x, sorted4.y, sorted4.z, sorted4.w};
+  int64_t off[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) {
+    int64_t o = 0;
+#pragma unroll
+    for (int b = 0; b < K; ++b)
+      if ((j >> (K - 1 - b)) & 1) o |= 1LL << bits[b];
+    off[j] = o;
+  }
+  const int64_t mem = mem_lo + blockIdx.y;
+  const typename CT<R>::T* s = psi + (mem << nbits);
+  const int64_t ng = 1LL << (nbits - K);
+  double acc[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) acc[w] = 0;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += (int64_t)nblk * blockDim.x) {
+    uint64_t base = (uint64_t)g;
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+      const int p = sorted[i];
+      base = ((base >> p) << (p + 1)) | (base & ((1ULL << p) - 1));
+    }
+    double xr[D], xi[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      typename CT<R>::T v = s[base + off[j]];
+      xr[j] = (double)v.x;
+      xi[j] = (double)v.y;
+    }
+    // rho[a, b] += x_a conj(x_b), row-major interleaved
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+#pragma unroll
+      for (int b = 0; b < D; ++b) {
+        acc[2 * (a * D + b)] += xr[a] * xr[b] + xi[a] * xi[b];
+        acc[2 * (a * D + b) + 1] += xi[a] * xr[b] - xr[a] * xi[b];
+      }
+  }
+  block_sum_store<W>(acc, part + ((int64_t)blockIdx.y * nblk + blockIdx.x) * W, W);
+}
+
+template <typename R, int K>
+static int rdm_t(bt_state* s, const int* bits, int64_t mem_lo, int64_t nmem, double* out) {
+  bt_ctx* ctx = s->ctx;
+  constexpr int W = 2 * (1 << K) * (1 << K);
+  int b4[4] = {0, 0, 0, 0}, s4[4] = {0, 0, 0, 0};
+  for (int i = 0; i < K; ++i) b4[i] = s4[i] = bits[i];
+  for (int i = 0; i < K; ++i)
+    for (int j = i + 1; j < K; ++j)
+      if (s4[j] < s4[i]) { int t = s4[i]; s4[i] = s4[j]; s4[j] = t; }
+  int64_t ng = 1LL << (s->nbits - K);
+  int nblk = blocks_per_member(ctx, ng, nmem);
+  double* part;
+  int rc = bt_work(ctx, sizeof(double) * (size_t)nmem * nblk * W, &part);
+  if (rc) return rc;
+  dim3 grid(nblk, (unsigned)nmem);
+  k_rdm<R, K><<<grid, BT_THREADS, 0, ctx->stream>>>((const typename CT<R>::T*)s->d, s->nbits,
+                                                    make_int4(b4[0], b4[1], b4[2], b4[3]),
+                                                    make_int4(s4[0], s4[1], s4[2], s4[3]), mem_lo, nblk, part);
+  ctx->launches++;
+  rc = bt_cuda_check(ctx, cudaGetLastError(), "rdm launch");
+  if (rc) return rc;
+  return finalize(ctx, part, nblk, W, nmem, out);
+}
+
+int bt_launch_rdm(bt_state* s, int k, const int* bits, int64_t mem_lo, int64_t nmem, double* out) {
+  if (nmem > 65535) return bt_fail(s->ctx, BT_ERR_UNSUPPORTED, "at most 65535 members per reduction");
+  bool c64 = s->prec == BT_PREC_C64;
+  switch (k) {
+    case 1: return c64 ? rdm_t<float, 1>(s, bits, mem_lo, nmem, out) : rdm_t<double, 1>(s, bits, mem_lo, nmem, out);
+    case 2: return c64 ? rdm_t<float, 2>(s, bits, mem_lo, nmem, out) : rdm_t<double, 2>(s, bits, mem_lo, nmem, out);
+    case 3: return c64 ? rdm_t<float, 3>(s, bits, mem_lo, nmem, out) : rdm_t<double, 3>(s, bits, mem_lo, nmem, out);
+  }
+  return bt_fail(s->ctx, BT_ERR_UNSUPPORTED, "reduced density matrix supports 1 <= k <= 3");
+}
+
+// ------------------------------------------------------------ Pauli strings
+struct PauliArgs {
+  uint64_t x;
+  uint64_t z[8];
+  int T;
+  int hbit;  // highest set bit of x, or -1
+  int nbits, nsys;
+  int dm;    // 1: density matrix, element rho[a, a^x] at a + ((a^x) << nsys)
+};
+
+__device__ __forceinline__ void phase_of(uint64_t i, uint64_t x, uint64_t z, double& pr, double& pi) {
+  // P|i> = i^{popcount(x&z)} (-1)^{popcount(i&z)} |i^x>
+  int ny = __popcll(x & z) & 3;
+  int sg = __popcll(i & z) & 1;
+  pr = (ny == 0) ? 1.0 : (ny == 2 ? -1.0 : 0.0);
+  pi = (ny == 1) ? 1.0 : (ny == 3 ? -1.0 : 0.0);
+  if (sg) { pr = -pr; pi = -pi; }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(BT_THREADS) k_pauli(const typename CT<R>::T* __restrict__ psi, PauliArgs a,
+                                                      int64_t mem_lo, int nblk, double* __restrict__ part) {
+  double acc[8];
+#pragma unroll
+  for (int t = 0; t < 8; ++t) acc[t] = 0;
+  const int64_t mem = mem_lo + blockIdx.y;
+  const typename CT<R>::T* s = psi + (mem << a.nbits);
+  if (a.dm) {
+    const int64_t n = 1LL << a.nsys;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)nblk * blockDim.x) {
+      uint64_t j = (uint64_t)i ^ a.x;
+      typename CT<R>::T v = s[(uint64_t)i + (j << a.nsys)];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        if (t < a.T) {
+          double pr, pi;
+          phase_of((uint64_t)i, a.x, a.z[t], pr, pi);
+          acc[t] += pr * (double)v.x - pi * (double)v.y;
+        }
+      }
+    }
+  } else if (a.hbit < 0) {
+    const int64_t n = 1LL << a.nbits;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)nblk * blockDim.x) {
+      typename CT<R>::T v = s[i];
+      double p = (double)v.x * v.x + (double)v.y * v.y;
+#pragma unroll
+      for (int t = 0; t < 8; ++t)
+        if (t < a.T) acc[t] += (__popcll((uint64_t)i & a.z[t]) & 1) ? -p : p;
+    }
+  } else {
+    const int64_t n = 1LL << (a.nbits - 1);
+    const int h = a.hbit;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (int64_t)nblk * blockDim.x) {
+      uint64_t i = (((uint64_t)g >> h) << (h + 1)) | ((uint64_t)g & ((1ULL << h) - 1));
+      uint64_t j = i ^ a.x;
+      typename CT<R>::T vi = s[i], vj = s[j];
+      // c = conj(psi_j) * psi_i
+      double cr = (double)vj.x * vi.x + (double)vj.y * vi.y;
+      double ci = (double)vj.x * vi.y - (double)vj.y * vi.x;
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        if (t < a.T) {
+          double p1r, p1i, p2r, p2i;
+          phase_of(i, a.x, a.z[t], p1r, p1i);
+          phase_of(j, a.x, a.z[t], p2r, p2i);
+          // Re(ph_i c) + Re(conj(ph_j) c)
+          acc[t] += (p1r + p2r) * cr - (p1i - p2i) * ci;
+        }
+      }
+    }
+  }
+  block_sum_store<8>(acc, part + ((int64_t)blockIdx.y * nblk + blockIdx.x) * 8, 8);
+}
+
+int bt_launch_pauli(bt_state* s, uint64_t x, int T, const uint64_t* z, int64_t mem_lo, int64_t nmem, double* out) {
+  bt_ctx* ctx = s->ctx;
+  if (T < 1 || T > 8) return bt_fail(ctx, BT_ERR_BAD_ARG, "pauli batch must hold 1..8 terms");
+  if (nmem > 65535) return bt_fail(ctx, BT_ERR_UNSUPPORTED, "at most 65535 members per reduction");
+  PauliArgs a;
+  a.x = x;
+  for (int t = 0; t < 8; ++t) a.z[t] = t < T ? z[t] : 0;
+  a.T = T;
+  a.hbit = x ? 63 - __builtin_clzll(x) : -1;
+  a.nbits = s->nbits;
+  a.nsys = s->n;
+  a.dm = s->repr == BT_REPR_DM;
+  int64_t units = a.dm ? (1LL << s->n) : (a.hbit < 0 ? (1LL << s->nbits) : (1LL << (s->nbits - 1)));
+  int nblk = blocks_per_member(ctx, units, nmem);
+  double* part;
+  int rc = bt_work(ctx, sizeof(double) * (size_t)nmem * nblk * 8, &part);
+  if (rc) return rc;
+  dim3 grid(nblk, (unsigned)nmem);
+  if (s->prec == BT_PREC_C64)
+    k_pauli<float><<<grid, BT_THREADS, 0, ctx->stream>>>((const float2*)s->d, a, mem_lo, nblk, part);
+  else
+    k_pauli<double><<<grid, BT_THREADS, 0, ctx->stream>>>((const double2*)s->d, a, mem_lo, nblk, part);
+  ctx->launches++;
+  rc = bt_cuda_check(ctx, cudaGetLastError(), "pauli launch");
+  if (rc) return rc;
+  return finalize(ctx, part, nblk, 8, nmem, out);
+}
+
+// ------------------------------------------------------------ per-bit sums
+// out[mem][0] = total weight, out[mem][1+b] = weight with bit b set (b < nsys).
+// A warp walks chunks of 1024 consecutive amplitudes, lane l taking entries
+// l + 32 j: bits 0-4 are the lane's, bits 5-9 the unrolled j's, and bits >= 10
+// are constant over the chunk, so each weight costs a handful of FP64 adds.
+#define BS_W 36
+template <typename R>
+__global__ void __launch_bounds__(BT_THREADS) k_bitsums(const typename CT<R>::T* __restrict__ psi, int nbits,
+                                                        int nsys, int dm, int64_t mem_lo, int nblk,
+                                                        double* __restrict__ part) {
+  double acc[BS_W];
+#pragma unroll
+  for (int w = 0; w < BS_W; ++w) acc[w] = 0;
+  const int64_t mem = mem_lo + blockIdx.y;
+  const typename CT<R>::T* s = psi + (mem << nbits);
+  const int lane = threadIdx.x & 31;
+  const int64_t nent = 1LL << nsys;
+  const int64_t warps_total = (int64_t)nblk * (blockDim.x >> 5);
+  const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (nsys >= 10) {
+    const int64_t nchunk = nent >> 10;
+    double lanetot = 0;
+    for (int64_t c = wid; c < nchunk; c += warps_total) {
+      double csum = 0;
+      double jb[5] = {0, 0, 0, 0, 0};
+#pragma unroll 8
+      for (int j = 0; j < 32; ++j) {
+        uint64_t i = ((uint64_t)c << 10) + ((uint64_t)j << 5) + lane;
+        typename CT<R>::T v = dm ? s[i + (i << nsys)] : s[i];
+        double p = dm ? (double)v.x : (double)v.x * v.x + (double)v.y * v.y;
+        csum += p;
+#pragma unroll
+        for (int b = 0; b < 5; ++b)
+          if ((j >> b) & 1) jb[b] += p;
+      }
+      lanetot += csum;
+#pragma unroll
+      for (int b = 0; b < 5; ++b) acc[1 + 5 + b] += jb[b];
+      for (int b = 10; b < nsys; ++b)
+        if (((uint64_t)c << 10 >> b) & 1) acc[1 + b] += csum;
+    }
+    acc[0] += lanetot;
+#pragma unroll
+    for (int b = 0; b < 5; ++b)
+      if ((lane >> b) & 1) acc[1 + b] += lanetot;
+  } else {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nent; i += (int64_t)nblk * blockDim.x) {
+      typename CT<R>::T v = dm ? s[(uint64_t)i + ((uint64_t)i << nsys)] : s[i];
+      double p = dm ? (double)v.x : (double)v.x * v.x + (double)v.y * v.y;
+      acc[0] += p;
+      for (int b = 0; b < nsys; ++b)
+        if ((i >> b) & 1) acc[1 + b] += p;
+    }
+  }
+  block_sum_store<BS_W>(acc, part + ((int64_t)blockIdx.y * nblk + blockIdx.x) * BS_W, BS_W);
+}
+
+int bt_launch_bitsums(bt_state* s, int64_t mem_lo, int64_t nmem, double* out) {
+  bt_ctx* ctx = s->ctx;
+  if (s->n > BS_W - 1) return bt_fail(ctx, BT_ERR_UNSUPPORTED, "too many qubits for per-bit sums");
+  if (nmem > 65535) return bt_fail(ctx, BT_ERR_UNSUPPORTED, "at most 65535 members per reduction");
+  int64_t units = s->n >= 10 ? (1LL << s->n) / 32 : (1LL << s->n);
+  int nblk = blocks_per_member(ctx, units, nmem);
+  double* part;
+  int rc = bt_work(ctx, sizeof(double) * (size_t)nmem * nblk * BS_W, &part);
+  if (rc) return rc;
+  dim3 grid(nblk, (unsigned)nmem);
+  int dm = s->repr == BT_REPR_DM;
+  if (s->prec == BT_PREC_C64)
+    k_bitsums<float><<<grid, BT_THREADS, 0, ctx->stream>>>((const float2*)s->d, s->nbits, s->n, dm, mem_lo, nblk, part);
+  else
+    k_bitsums<double><<<grid, BT_THREADS, 0, ctx->stream>>>((const double2*)s->d, s->nbits, s->n, dm, mem_lo, nblk, part);
+  ctx->launches++;
+  rc = bt_cuda_check(ctx, cudaGetLastError(), "bitsums launch");
+  if (rc) return rc;
+  // out receives BS_W values per member
+  return finalize(ctx, part, nblk, BS_W, nmem, out);
+}
+
+// ------------------------------------------------------------ inner product
+template <typename Ra, typename Rb>
+__global__ void __launch_bounds__(BT_THREADS) k_inner(const typename CT<Ra>::T* __restrict__ a,
+                                                      const typename CT<Rb>::T* __restrict__ b, int64_t n,
+                                                      int nblk, double* __restrict__ part) {
+  double acc[2] = {0, 0};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)nblk * blockDim.x) {
+    typename CT<Ra>::T x = a[i];
+    typename CT<Rb>::T y = b[i];
+    acc[0] += (double)x.x * y.x + (double)x.y * y.y;
+    acc[1] += (double)x.x * y.y - (double)x.y * y.x;
+  }
+  block_sum_store<2>(acc, part + (int64_t)blockIdx.x * 2, 2);
+}
+
+int bt_launch_inner(bt_state* a, int64_t am, bt_state* b, int64_t bm, double* out) {
+  bt_ctx* ctx = a->ctx;
+  int64_t n = a->member_elems;
+  int nblk = blocks_per_member(ctx, n, 1);
+  double* part;
+  int rc = bt_work(ctx, sizeof(double) * nblk * 2, &part);
+  if (rc) return rc;
+  const char* pa = (const char*)a->d + am * n * elem_bytes(a->prec);
+  const char* pb = (const char*)b->d + bm * n * elem_bytes(b->prec);
+  bool fa = a->prec == BT_PREC_C64, fb = b->prec == BT_PREC_C64;
+  if (fa && fb) k_inner<float, float><<<nblk, BT_THREADS, 0, ctx->stream>>>((const float2*)pa, (const float2*)pb, n, nblk, part);
+  else if (fa) k_inner<float, double><<<nblk, BT_THREADS, 0, ctx->stream>>>((const float2*)pa, (const double2*)pb, n, nblk, part);
+  else if (fb) k_inner<double, float><<<nblk, BT_THREADS, 0, ctx->stream>>>((const double2*)pa, (const float2*)pb, n, nblk, part);
+  else k_inner<double, double><<<nblk, BT_THREADS, 0, ctx->stream>>>((const double2*)pa, (const double2*)pb, n, nblk, part);
+  ctx->launches++;
+  rc = bt_cuda_check(ctx, cudaGetLastError(), "inner launch");
+  if (rc) return rc;
+  return finalize(ctx, part, nblk, 2, 1, out);
+}
+
+// ------------------------------------------------------------ <psi|M|psi>
+template <typename R, int K>
+__global__ void __launch_bounds__(BT_THREADS) k_expect_matrix(const typename CT<R>::T* __restrict__ s, int nbits,
+                                                              int4 bits4, int4 sorted4, uint64_t cmask,
+                                                              const double* __restrict__ m, int nblk,
+                                                              double* __restrict__ part) {
+  constexpr int D = 1 << K;
+  const int bits[4] = {bits4.x, bits4.y, bits4.z, bits4.w};
+  const int sorted[4] = {sorted4.x, sorted4.y, sorted4.z, sorted4.w};
+  int64_t off[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) {
+    int64_t o = 0;
+#pragma unroll
+    for (int b = 0; b < K; ++b)
+      if ((j >> (K - 1 - b)) & 1) o |= 1LL << bits[b];
+    off[j] = o;
+  }
+  double acc[1] = {0};
+  const int64_t ng = 1LL << (nbits - K);
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += (int64_t)nblk * blockDim.x) {
+    uint64_t base = (uint64_t)g;
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+      const int p = sorted[i];
+      base = ((base >> p) << (p + 1)) | (base & ((1ULL << p) - 1));
+    }
+    double xr[D], xi[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      typename CT<R>::T v = s[base + off[j]];
+      xr[j] = v.x;
+      xi[j] = v.y;
+    }
+    if ((base & cmask) != cmask) {
+      // identity on this group: sum |x|^2
+#pragma unroll
+      for (int j = 0; j < D; ++j) acc[0] += xr[j] * xr[j] + xi[j] * xi[j];
+      continue;
+    }
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      double yr = 0, yi = 0;
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        double mr = m[2 * (r * D + c)], mi = m[2 * (r * D + c) + 1];
+        yr += mr * xr[c] - mi * xi[c];
+        yi += mr * xi[c] + mi * xr[c];
+      }
+      acc[0] += xr[r] * yr + xi[r] * yi;
+    }
+  }
+  block_sum_store<1>(acc, part + (int64_t)blockIdx.x, 1);
+}
+
+int bt_launch_expect_matrix(bt_state* s, int k, const int* bits, const double* m_rowmajor_dev, uint64_t cmask,
+                            int64_t mem, double* out) {
+  bt_ctx* ctx = s->ctx;
+  int b4[4] = {0, 0, 0, 0}, s4[4] = {0, 0, 0, 0};
+  for (int i = 0; i < k; ++i) b4[i] = s4[i] = bits[i];
+  for (int i = 0; i < k; ++i)
+    for (int j = i + 1; j < k; ++j)
+      if (s4[j] < s4[i]) { int t = s4[i]; s4[i] = s4[j]; s4[j] = t; }
+  int64_t ng = 1LL << (s->nbits - k);
+  int nblk = blocks_per_member(ctx, ng, 1);
+  double* part;
+  int rc = bt_work(ctx, sizeof(double) * nblk, &part);
+  if (rc) return rc;
+  const char* p = (const char*)s->d + mem * s->member_elems * elem_bytes(s->prec);
+  int4 bb = make_int4(b4[0], b4[1], b4[2], b4[3]), ss = make_int4(s4[0], s4[1], s4[2], s4[3]);
+  bool f = s->prec == BT_PREC_C64;
+  if (k == 1) {
+    if (f) k_expect_matrix<float, 1><<<nblk, BT_THREADS, 0, ctx->stream>>>((const float2*)p, s->nbits, bb, ss, cmask, m_rowmajor_dev, nblk, part);
+    else k_expect_matrix<double, 1><<<nblk, BT_THREADS, 0, ctx->stream>>>((const double2*)p, s->nbits, bb, ss, cmask, m_rowmajor_dev, nblk, part);
+  } else if (k == 2) {
+    if (f) k_expect_matrix<float, 2><<<nblk, BT_THREADS, 0, ctx->stream>>>((const float2*)p, s->nbits, bb, ss, cmask, m_rowmajor_dev, nblk, part);
+    else k_expect_matrix<double, 2><<<nblk, BT_THREADS, 0, ctx->stream>>>((const double2*)p, s->nbits, bb, ss, cmask, m_rowmajor_dev, nblk, part);
+  } else {
+    return bt_fail(ctx, BT_ERR_UNSUPPORTED, "expect_matrix supports k <= 2");
+  }
+  ctx->launches++;
+  rc = bt_cuda_check(ctx, cudaGetLastError(), "expect_matrix launch");
+  if (rc) return rc;
+  return finalize(ctx, part, nblk, 1, 1, out);
+}
+
+// ------------------------------------------------------------ collapse / dephase
+template <typename R>
+__global__ void __launch_bounds__(BT_THREADS) k_collapse(typename CT<R>::T* __restrict__ psi, int nbits, int bit,
+                                                         const int* __restrict__ outcome,
+                                                         const double* __restrict__ scale, int64_t mem_lo,
+                                                         int64_t nmem) {
+  const int64_t per = 1LL << nbits;
+  const int64_t total = per * nmem;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t mi = t >> nbits;
+    const int64_t mem = mem_lo + mi;
+    const int64_t i = t & (per - 1);
+    typename CT<R>::T* p = psi + (mem << nbits) + i;
+    if ((int)((i >> bit) & 1) == outcome[mi]) {
+      const R sc = (R)scale[mi];
+      typename CT<R>::T v = *p;
+      v.x *= sc;
+      v.y *= sc;
+      *p = v;
+    } else {
+      typename CT<R>::T z;
+      z.x = 0;
+      z.y = 0;
+      *p = z;
+    }
+  }
+}
+
+int bt_launch_collapse(bt_state* s, int bit, const int* d_outcome, const double* d_scale, int64_t mem_lo, int64_t nmem) {
+  bt_ctx* ctx = s->ctx;
+  int64_t work = (1LL << s->nbits) * nmem;
+  int grid = bt_grid(ctx, work, BT_THREADS, 32);
+  if (s->prec == BT_PREC_C64)
+    k_collapse<float><<<grid, BT_THREADS, 0, ctx->stream>>>((float2*)s->d, s->nbits, bit, d_outcome, d_scale, mem_lo, nmem);
+  else
+    k_collapse<double><<<grid, BT_THREADS, 0, ctx->stream>>>((double2*)s->d, s->nbits, bit, d_outcome, d_scale, mem_lo, nmem);
+  ctx->launches++;
+  return bt_cuda_check(ctx, cudaGetLastError(), "collapse launch");
+}
+
+template <typename R>
+__global__ void __launch_bounds__(BT_THREADS) k_dephase(typename CT<R>::T* __restrict__ rho, int nbits, int nsys, int b,
+                                                        int64_t mem_lo, int64_t nmem) {
+  const int64_t per = 1LL << nbits;
+  const int64_t total = per * nmem;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t mem = mem_lo + (t >> nbits);
+    const int64_t e = t & (per - 1);
+    if (((e >> b) & 1) != ((e >> (b + nsys)) & 1)) {
+      typename CT<R>::T z;
+      z.x = 0;
+      z.y = 0;
+      rho[(mem << nbits) + e] = z;
+    }
+  }
+}
+
+int bt_launch_dephase(bt_state* s, int b, int64_t mem_lo, int64_t nmem) {
+  bt_ctx* ctx = s->ctx;
+  int64_t work = (1LL << s->nbits) * nmem;
+  int grid = bt_grid(ctx, work, BT_THREADS, 32);
+  if (s->prec == BT_PREC_C64)
+    k_dephase<float><<<grid, BT_THREADS, 0, ctx->stream>>>((float2*)s->d, s->nbits, s->n, b, mem_lo, nmem);
+  else
+    k_dephase<double><<<grid, BT_THREADS, 0, ctx->stream>>>((double2*)s->d, s->nbits, s->n, b, mem_lo, nmem);
+  ctx->launches++;
+  return bt_cuda_check(ctx, cudaGetLastError(), "dephase launch");
+}
+
+// ------------------------------------------------------------ decisions
+// measurement: rdm[mem] is the 2x2 reduced matrix (row-major interleaved, 8 doubles)
+__global__ void k_decide_measure(int64_t nmem, const double* __restrict__ rdm, const double* __restrict__ u,
+                                 const int* __restrict__ forced, uint64_t key, uint64_t stream,
+                                 int* __restrict__ outcome, double* __restrict__ scale, double* __restrict__ p0,
+                                 int* __restrict__ status) {
+  int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nmem) return;
+  const double s0 = rdm[m * 8 + 0], s1 = rdm[m * 8 + 6];
+  int f = forced ? forced[m] : -1;
+  double uu = u ? u[m] : bt_uniform(key, stream, (uint64_t)m);
+  int ind = f >= 0 ? f : (uu < s0 ? 0 : 1);
+  double keep = ind ? s1 : s0;
+  if (!(keep > 0)) atomicExch(status, 1);
+  outcome[m] = ind;
+  scale[m] = 1.0 / sqrt(keep);
+  p0[m] = s0;
+}
+
+int bt_launch_decide_measure(bt_ctx* ctx, int64_t nmem, const double* rdm, const double* u, const int* forced,
+                             uint64_t rng_stream, int* outcome, double* scale, double* p0) {
+  unsigned grid = (unsigned)((nmem + 127) / 128);
+  k_decide_measure<<<grid, 128, 0, ctx->stream>>>(nmem, rdm, u, forced, ctx->seed, rng_stream, outcome, scale, p0,
+                                                  ctx->d_status);
+  ctx->launches++;
+  return bt_cuda_check(ctx, cudaGetLastError(), "decide_measure launch");
+}
+
+// Kraus branch: rdm[mem] is the D x D reduced matrix in application order (q, t);
+// kraus holds nk row-major interleaved D x D matrices (FP64).
+template <typename R>
+__global__ void k_decide_kraus(int64_t nmem, int k, int nk, int ref_perm, const double* __restrict__ rdm,
+                               const double* __restrict__ kraus, const double* __restrict__ u,
+                               const int* __restrict__ forced, uint64_t key, uint64_t stream,
+                               int* __restrict__ branch, double* __restrict__ probs, R* __restrict__ pm,
+                               int* __restrict__ status) {
+  int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nmem) return;
+  const int D = 1 << k;
+  const double* r = rdm + m * 2 * D * D;
+  // reference-order reduced matrix: for a pair with q > t the reference reads
+  // rho_A in (t, q) order, i.e. indices permuted by [0, 2, 1, 3]
+  const int perm[4] = {0, 2, 1, 3};
+  double cum = 0;
+  double uu = u ? u[m] : bt_uniform(key, stream, (uint64_t)m);
+  int f = forced ? forced[m] : -1;
+  int ind = -1;
+  for (int i = 0; i < nk; ++i) {
+    const double* K = kraus + (int64_t)i * 2 * D * D;
+    // p = Re tr(K rho K^dagger) = Re sum_{a,b,c} K[c,a] rho[a,b] conj(K[c,b])
+    double p = 0;
+    for (int c = 0; c < D; ++c)
+      for (int a = 0; a < D; ++a) {
+        double kar = K[2 * (c * D + a)], kai = K[2 * (c * D + a) + 1];
+        for (int b = 0; b < D; ++b) {
+          int ra = ref_perm ? perm[a] : a, rb = ref_perm ? perm[b] : b;
+          double rr = r[2 * (ra * D + rb)], ri = r[2 * (ra * D + rb) + 1];
+          double kbr = K[2 * (c * D + b)], kbi = -K[2 * (c * D + b) + 1];
+          // (ka * rho) * conj(kb)
+          double tr_ = kar * rr - kai * ri, ti = kar * ri + kai * rr;
+          p += tr_ * kbr - ti * kbi;
+        }
+      }
+    if (probs) probs[m * nk + i] = p;
+    cum += p;
+    if (ind < 0 && uu <= cum) ind = i;
+  }
+  if (f >= 0) ind = f;
+  if (ind < 0 || ind >= nk) {
+    atomicExch(status, 2);
+    ind = nk - 1;
+  }
+  branch[m] = ind;
+  // norm of K_ind psi in application order
+  const double* K = kraus + (int64_t)ind * 2 * D * D;
+  double nrm = 0;
+  for (int c = 0; c < D; ++c)
+    for (int a = 0; a < D; ++a) {
+      double kar = K[2 * (c * D + a)], kai = K[2 * (c * D + a) + 1];
+      for (int b = 0; b < D; ++b) {
+        double rr = r[2 * (a * D + b)], ri = r[2 * (a * D + b) + 1];
+        double kbr = K[2 * (c * D + b)], kbi = -K[2 * (c * D + b) + 1];
+        double tr_ = kar * rr - kai * ri, ti = kar * ri + kai * rr;
+        nrm += tr_ * kbr - ti * kbi;
+      }
+    }
+  if (!(nrm > 0)) atomicExch(status, 3);
+  const double sc = 1.0 / sqrt(nrm);
+  R* out = pm + m * 2 * D * D;
+  for (int e = 0; e < 2 * D * D; ++e) out[e] = (R)(K[e] * sc);
+}
+
+int bt_launch_decide_kraus(bt_state* s, bt_kraus_desc kd, int64_t nmem, const double* rdm, const double* kraus,
+                           const double* u, const int* forced, uint64_t rng_stream, int* branch, double* probs,
+                           void* pm) {
+  bt_ctx* ctx = s->ctx;
+  unsigned grid = (unsigned)((nmem + 127) / 128);
+  if (s->prec == BT_PREC_C64)
+    k_decide_kraus<float><<<grid, 128, 0, ctx->stream>>>(nmem, kd.k, kd.nk, kd.ref_perm, rdm, kraus, u, forced,
+                                                         ctx->seed, rng_stream, branch, probs, (float*)pm,
+                                                         ctx->d_status);
+  else
+    k_decide_kraus<double><<<grid, 128, 0, ctx->stream>>>(nmem, kd.k, kd.nk, kd.ref_perm, rdm, kraus, u, forced,
+                                                          ctx->seed, rng_stream, branch, probs, (double*)pm,
+                                                          ctx->d_status);
+  ctx->launches++;
+  return bt_cuda_check(ctx, cudaGetLastError(), "decide_kraus launch");
+}

@@ -1,0 +1,166 @@
+/*
+ * btgpu.h — C ABI of the GB300 engine for BlueTangle.jl's noisy-circuit hot path.
+ *
+ * The reference has no FFI: its boundary is Julia multiple dispatch on the
+ * state argument of apply / measure / sample / expect / correlation /
+ * born_measure_Z (BlueTangle.jl src/BlueTangle.jl:5-22).  Each entry point
+ * below replaces the reference function cited beside it; a Julia package adds
+ * methods of those generics for GPU-resident states and `ccall`s these symbols.
+ *
+ * Conventions
+ *   qubits      1-based, exactly as in the reference; qubit q of an n-qubit
+ *               register is bit (n - q) of the 0-based amplitude index, so
+ *               qubit 1 is the most significant bit (src/bit.jl:9-14).
+ *   complex     interleaved (re, im) float64 pairs on the host (Julia ComplexF64).
+ *   matrices    column-major on the host (Julia layout): m[r + c*d] = M[r, c],
+ *               d = 2^k; the first listed qubit is the most significant bit of
+ *               the matrix index (the |b_q b_t> order of src/hilbert.jl:30).
+ *   density     rho[i, j] at i + j*2^n (column-major), as a Julia Matrix.
+ *   member      states hold `batch` independent members (trajectories,
+ *               twirl/ZNE copies, serving slots); member = -1 means all.
+ *   errors      every call returns a status (BT_OK or a negative BT_ERR_*);
+ *               bt_last_error() gives the message.  Nothing aborts.
+ *   threading   one ctx = one CUDA stream; calls on a ctx are serialised by the
+ *               caller.  Separate ctxs may be used from separate threads.
+ * Host pointers are borrowed for the duration of the call only.
+ */
+#ifndef BTGPU_H
+#define BTGPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BT_ABI_VERSION 1
+
+#define BT_OK 0
+#define BT_ERR_BAD_ARG (-1)
+#define BT_ERR_NOT_CPTP (-2)
+#define BT_ERR_OOM (-3)
+#define BT_ERR_DEVICE (-4)
+#define BT_ERR_TIMEOUT (-5)
+#define BT_ERR_UNSUPPORTED (-6)
+#define BT_ERR_NO_BRANCH (-7)
+
+#define BT_REPR_SV 0 /* state vector, 2^n amplitudes per member */
+#define BT_REPR_DM 1 /* density matrix, 4^n entries per member */
+
+#define BT_PREC_C128 0 /* complex float64 (the drop-in precision) */
+#define BT_PREC_C64 1  /* complex float32 bulk; norms, cdf and branch probabilities stay float64 */
+
+/* bt_apply_kraus modes */
+#define BT_KRAUS_TRAJ 0 /* Monte-Carlo branch per member (state vector) */
+#define BT_KRAUS_SUM 1  /* rho <- sum_k K rho K^dagger (density matrix) */
+/* flag: branch probabilities from the reduced state of the pair in ascending
+ * qubit order while the branch operator acts in (q, t) order, which is what
+ * __calc_prob does for a pair with q > t (src/struct.jl:17-29 with
+ * src/linalg.jl:198-230 and src/hilbert.jl:30). */
+#define BT_KRAUS_REF_ORDER 0x100
+
+typedef struct bt_ctx bt_ctx;
+typedef struct bt_state bt_state;
+typedef struct bt_plan bt_plan;
+
+/* ------------------------------------------------------------------ context */
+int bt_abi_version(void);
+const char* bt_status_string(int status);
+/* Creates a context on CUDA device `device` with its own stream; `seed` keys the
+ * on-device counter-based RNG (Philox4x32-10) used when no uniforms are given. */
+int bt_ctx_create(int device, uint64_t seed, bt_ctx** out);
+int bt_ctx_destroy(bt_ctx* ctx);
+const char* bt_last_error(const bt_ctx* ctx); /* NULL ctx: last error of this thread */
+int bt_ctx_synchronize(bt_ctx* ctx);
+/* number of engine kernels this ctx has launched (instrumentation) */
+int bt_ctx_launch_count(const bt_ctx* ctx, int64_t* out);
+/* the ctx's cudaStream_t, for interop (events, CUDA.jl/torch stream sharing) */
+int bt_ctx_stream(const bt_ctx* ctx, void** out);
+
+/* -------------------------------------------------------------------- state */
+/* zero_state / the 2^N vector and 4^N matrix the reference allocates
+ * (src/hilbert.jl:866, src/ops.jl:806-810).  n <= 34 (SV) / 17 (DM). */
+int bt_state_alloc(bt_ctx* ctx, int n, int repr, int prec, int batch, bt_state** out);
+int bt_state_free(bt_state* s);
+int bt_state_info(const bt_state* s, int* n, int* repr, int* prec, int* batch);
+/* device address of member 0 (interop, e.g. DLPack); members are contiguous */
+void* bt_state_device_ptr(bt_state* s);
+/* |0...0> or |0..0><0..0| (zero_state, src/hilbert.jl:866) */
+int bt_state_set_zero(bt_state* s, int64_t member);
+/* computational basis state |index> (product_state of bits, src/hilbert.jl:835) */
+int bt_state_set_basis(bt_state* s, int64_t member, uint64_t index);
+/* copies member `src_member` of src into member `dst_member` of dst (same n/repr/prec);
+ * dst_member = -1 broadcasts it to every member of dst */
+int bt_state_copy(bt_state* dst, int64_t dst_member, const bt_state* src, int64_t src_member);
+/* host complex128 <-> device, `len` complex entries starting at entry `offset`
+ * of one member; converted to/from complex64 for BT_PREC_C64 states */
+int bt_state_upload(bt_state* s, int64_t member, int64_t offset, int64_t len, const double* host);
+int bt_state_download(const bt_state* s, int64_t member, int64_t offset, int64_t len, double* host);
+
+/* ------------------------------------------------------------------- gates */
+/* op.expand(N)*state for a k-qubit matrix with optional controls (all must read 1):
+ * hilbert(N,U,q;control) (src/hilbert.jl:143-159), hilbert(N,U,q,t;control)
+ * (src/hilbert.jl:18-70, including non-adjacent pairs and CCZX :73-103),
+ * hilbert3 (src/hilbert.jl:106-128) and fused k <= 6 blocks.
+ * On a density matrix it is e_op*rho*e_op' (src/hilbert.jl:655-656). */
+int bt_apply_matrix(bt_state* s, int k, const int32_t* qubits, const double* mat, int nctrl,
+                    const int32_t* ctrls, int64_t member);
+
+/* Kraus channel on qubits (1 <= k <= 3; qubits[0] = q, qubits[1] = t).
+ *  BT_KRAUS_TRAJ (state vector): __QuantumChannel_new_apply (src/struct.jl:31-41,
+ *    :51-55): p_i = Re tr(K_i rho_A K_i^dagger) from the reduced state
+ *    (__calc_prob, src/struct.jl:9-29), branch = first i with u <= cumsum(p)[i]
+ *    (_weighted_sample, src/hilbert.jl:810-819), psi <- normalize(K_branch psi).
+ *    uniforms[m] is member m's draw (NULL: on-device Philox); forced[m] >= 0
+ *    skips the draw (NULL: none).  branch_out[m] and probs_out[m*nk + i]
+ *    (either may be NULL) receive the branch and the probabilities.
+ *  BT_KRAUS_SUM (density matrix): rho <- sum_i K_i rho K_i^dagger
+ *    (src/struct.jl:58-76) in one pass over rho.
+ * `kraus` holds nk column-major 2^k x 2^k matrices back to back. */
+int bt_apply_kraus(bt_state* s, int k, const int32_t* qubits, int nk, const double* kraus, int mode,
+                   const double* uniforms, const int32_t* forced, int32_t* branch_out,
+                   double* probs_out);
+
+/* -------------------------------------------------------------- measurement */
+/* born_measure_Z(N, psi, q) (src/hilbert.jl:682-696) for every member:
+ * p0 = rho_q[1,1]; outcome = u < p0 ? 0 : 1 (or forced); the other half is set
+ * to exactly zero and the kept half renormalised.  outcome/p0 per member (may be NULL).
+ * On a density matrix: born_measure_Z(N, rho, q) = sum_b P_b rho P_b
+ * (src/hilbert.jl:784-796); uniforms/forced/outcome are ignored and p0 is
+ * still reported. */
+int bt_measure_z(bt_state* s, int qubit, const double* uniforms, const int32_t* forced,
+                 int32_t* outcome, double* p0);
+/* partial_trace(psi, keep) for k <= 3 kept qubits, in the listed order
+ * (src/linalg.jl:83-230); out is a column-major 2^k x 2^k complex matrix */
+int bt_reduced_dm(const bt_state* s, int k, const int32_t* qubits, int64_t member, double* out);
+
+/* ---------------------------------------------------------------- sampling */
+/* sample(psi, shots) (src/ops.jl:46-62): per shot t = u*sum|psi|^2, outcome =
+ * first index with cumsum >= t.  uniforms (shots values) or NULL for on-device
+ * Philox keyed by (ctx seed, seed).  On a density matrix samples diag(rho). */
+int bt_sample(const bt_state* s, int64_t member, int64_t shots, const double* uniforms, uint64_t seed,
+              int64_t* out);
+/* abs2.(psi) or real(diag(rho)) (sample_exact, src/ops.jl:98-101, :129-132) */
+int bt_probabilities(const bt_state* s, int64_t member, double* out);
+
+/* ------------------------------------------------------------- observables */
+/* Pauli strings as masks over the amplitude index (bit n-q for qubit q); Y sets
+ * both masks.  out[t] = coef[t] * Re <P_t> (coef may be NULL = 1):
+ *   state:   real(state'*expand_multi_op(...)*state) (src/func.jl:97, :139-142)
+ *   density: real(tr(rho*M)) (src/func.jl:98, :144-147)
+ * member = -1 writes batch*nterms values (member-major). */
+int bt_expect_pauli(const bt_state* s, int nterms, const uint64_t* xmask, const uint64_t* zmask,
+                    const double* coef, int64_t member, double* out);
+/* <Z_q> for every qubit q = 1..n (expect(state, "Z"), src/func.jl:97-98) in one pass */
+int bt_expect_z_all(const bt_state* s, int64_t member, double* out);
+/* real(state' * op.expand(N) * state) for a k <= 2 qubit matrix (src/func.jl:91) */
+int bt_expect_matrix(const bt_state* s, int k, const int32_t* qubits, const double* mat, int nctrl,
+                     const int32_t* ctrls, int64_t member, double* out);
+/* sum |psi|^2 (or tr rho) per member */
+int bt_norm2(const bt_state* s, int64_t member, double* out);
+/* fidelity(psi, phi) = |<psi|phi>|^2 (src/tensor.jl:219) */
+int bt_fidelity(const bt_state* a, int64_t amember, const bt_state* b, int64_t bmember, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

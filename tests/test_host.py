@@ -1,0 +1,84 @@
+"""Host-side mirror of the reference interface: gate table, noise tables, op
+descriptors, twirl frames.  CPU only (no kernels)."""
+import math
+
+import numpy as np
+import pytest
+
+
+def test_gate_values_match_reference_tables(kref):
+    from bluetangle_gpu.gates import gate, gates
+    for name, m in kref.GATE.items():
+        assert np.array_equal(gate[name], m), name
+    # T rounded to 10 significant digits (src/gates.jl:32)
+    assert gate["T"][1, 1] == complex(0.7071067812, 0.7071067812)
+    assert np.allclose(gates("RX(0.1pi)"), kref.rx(0.1 * math.pi), atol=0, rtol=0)
+    assert np.allclose(gates("RZ(.3π)"), kref.rz(0.3 * math.pi), atol=0, rtol=0)
+    assert np.array_equal(gates("RZZ(0.7)"), kref.rzz(0.7))
+    assert np.array_equal(gates("CP(1.25)"), kref.cp(1.25))
+    assert np.array_equal(gates("MX"), gate["H"]) and np.array_equal(gates("MY"), gate["HSP"])
+    with pytest.raises(KeyError):
+        gates("NOPE")
+
+
+def test_noise_tables_and_quirks(kref):
+    from bluetangle_gpu.noise import noise_model
+    for model in ("amplitude_damping", "phase_damping", "bit_flip", "phase_flip", "bit_phase_flip",
+                  "depolarizing", "depolarizing_amp", "rot_x", "rot_y", "rot_z", "rot_p", "rot_xyz", "MZ"):
+        for two in (False, True):
+            a, b = noise_model(model, 0.13, two), kref.noise_model(model, 0.13, two)
+            assert len(a) == len(b) and all(np.array_equal(x, y) for x, y in zip(a, b)), model
+    # phase_flip yields Y (src/noise.jl:78-81); 2-qubit depolarizing is a 16-term product channel
+    assert np.array_equal(noise_model("phase_flip", 0.25)[1], 0.5 * np.array([[0, -1j], [1j, 0]]))
+    assert len(noise_model("depolarizing", 0.1, True)) == 16
+
+
+def test_channel_validation_and_noise_model():
+    from bluetangle_gpu import NoiseModel, QuantumChannel
+    from bluetangle_gpu.noise import is_valid_quantum_channel
+    with pytest.raises(ValueError, match="CPTP"):
+        QuantumChannel("bad", [np.eye(2) * 1.1], 0.0)
+    assert is_valid_quantum_channel([np.eye(2)])
+    nm = NoiseModel("depolarizing", 0.1)
+    assert nm.q1.q == 1 and nm.q2.q == 2 and len(nm.q2.kraus) == 16
+    with pytest.raises(ValueError):
+        NoiseModel(QuantumChannel(2, "bit_flip", 0.1), False)
+
+
+def test_op_descriptors():
+    from bluetangle_gpu import Op, OpQC, ifOp
+    o = Op("CNOT", 2, 5)
+    assert o.q == 2 and o.type == "op" and o.control == -2
+    assert Op("RX(0.2)", 1).type == "phase"
+    m = Op("MZ", 3)
+    assert m.type == "🔬" and not m.noisy
+    assert isinstance(Op("RES", 1), OpQC)
+    t = Op("CCX", 1, 2, 3)
+    assert t.name == "CX" and t.qubit == 1 and t.target_qubit == 3 and t.control == 2
+    with pytest.raises(ValueError):
+        Op("CNOT", 2, 2)
+    with pytest.raises(ValueError):
+        Op("X", 2, control=2)
+    with pytest.raises(ValueError):
+        Op("MZ", 1, control=2)
+    with pytest.raises(ValueError):
+        OpQC("depolarizing", 0.1, 1, 2).__class__("x", [np.eye(4)], 1)  # 2-qubit channel needs a target
+    f = ifOp("MZ", 1, Op("I", 1), Op("X", 1))
+    assert f.type == "🔬" and len(f.if01[1]) == 1
+
+
+def test_twirl_frames_preserve_cnot():
+    """Each Pauli frame P_a(x)P_b . CNOT . P_c(x)P_d equals CNOT up to a phase."""
+    from bluetangle_gpu.gates import gate
+    from bluetangle_gpu.noise import _LIST_CNOT, _LIST_CNOT_REV, _LIST_ECR, _LIST_ECR_REV
+    P = {c: gate[c] for c in "IXYZ"}
+    for frames, G, rev in ((_LIST_CNOT, gate["CNOT"], False), (_LIST_CNOT_REV, gate["CNOT"], True),
+                           (_LIST_ECR, gate["ECR"], False), (_LIST_ECR_REV, gate["ECR"], True)):
+        # applied on (least, least+1); the op acts on (q, t) = (least+1, least) when reversed
+        Gq = G if not rev else G[np.ix_([0, 2, 1, 3], [0, 2, 1, 3])]
+        for f in frames:
+            before = np.kron(P[f[0]], P[f[1]])
+            after = np.kron(P[f[2]], P[f[3]])
+            tot = after @ Gq @ before
+            ph = tot[np.nonzero(np.abs(tot) > 1e-12)][0] / Gq[np.nonzero(np.abs(Gq) > 1e-12)][0]
+            assert np.allclose(tot, ph * Gq, atol=1e-12), f

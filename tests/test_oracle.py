@@ -1,0 +1,226 @@
+"""The oracle (oracle/btoracle.c) pinned before it is trusted as the checker.
+
+1. Against the golden fixtures frozen from the literal restatement of the
+   reference's operator construction (tests/golden/make_golden.py).
+2. Against every property the reference's own test suite asserts for this
+   path (BlueTangle.jl test/runtests.jl), run on the oracle.
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "kron_ref_cases.npz")
+
+
+def rstate(rng, n):
+    v = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
+    return v / np.linalg.norm(v)
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return np.load(GOLD)
+
+
+def test_golden_gates(oracle, gold):
+    for i in range(int(gold["ngates"][0])):
+        kind = int(gold[f"gate{i}_kind"][0])
+        q, t, c = (int(x) for x in gold[f"gate{i}_meta"])
+        m, psi = gold[f"gate{i}_mat"], gold[f"gate{i}_in"]
+        if kind == 1:
+            out = oracle.hilbert1(psi, m, q, c)
+        elif kind == 2:
+            out = oracle.hilbert2(psi, m, q, t, c)
+        else:
+            out = oracle.hilbert3(psi, m, q)
+        assert np.abs(out - gold[f"gate{i}_out"]).max() < 1e-13, (i, kind, q, t, c)
+
+
+def test_golden_traces_probs_measure(oracle, gold, kref):
+    kr2 = kref.noise_model("depolarizing", 0.5, two_qubit=True)
+    kr1 = kref.noise_model("amplitude_damping", 0.3)
+    for i in range(int(gold["npt"][0])):
+        psi = gold[f"pt{i}_in"]
+        q, t = (int(x) for x in gold[f"pt{i}_meta"])
+        assert np.abs(oracle.partial_trace2(psi, q, t) - gold[f"pt{i}_rho2"]).max() < 1e-14
+        assert np.abs(oracle.partial_trace(psi, [q]) - gold[f"pt{i}_rho1"]).max() < 1e-14
+        assert np.abs(oracle.calc_prob(psi, kr2, q, t) - gold[f"pt{i}_probs2"]).max() < 1e-14
+        assert np.abs(oracle.calc_prob(psi, kr1, q) - gold[f"pt{i}_probs1"]).max() < 1e-14
+        out, br, _ = oracle.channel_traj(psi, kr2, q, t, forced=5)
+        assert br == 5 and np.abs(out - gold[f"pt{i}_traj_forced5"]).max() < 1e-13
+        out, br, _ = oracle.channel_traj(psi, kr1, q, u=float(gold[f"pt{i}_traj_u"][0]))
+        assert br == int(gold[f"pt{i}_traj_branch"][0])
+        assert np.abs(out - gold[f"pt{i}_traj_out"]).max() < 1e-13
+        for o in (0, 1):
+            out, ind, p0 = oracle.born_measure_z(psi, q, forced=o)
+            assert ind == o and abs(p0 - gold[f"pt{i}_p0"][0]) < 1e-14
+            assert np.abs(out - gold[f"pt{i}_meas{o}"]).max() < 1e-13
+            assert np.array_equal(out == 0, gold[f"pt{i}_meas{o}"] == 0)
+
+
+def test_golden_density_and_observables(oracle, gold, kref):
+    rho = gold["dm_in"]
+    U = gold["dm_U"]
+    assert np.abs(oracle.dm_hilbert2(rho, U, 3, 1) - gold["dm_gate_out"]).max() < 1e-13
+    kr2 = kref.noise_model("depolarizing", 0.5, two_qubit=True)
+    kr1 = kref.noise_model("amplitude_damping", 0.3)
+    assert np.abs(oracle.dm_channel(rho, kr2, 1, 2) - gold["dm_ch2_out"]).max() < 1e-13
+    assert np.abs(oracle.dm_channel(rho, kr1, 3) - gold["dm_ch1_out"]).max() < 1e-13
+    psi = gold["obs_in"]
+    n = 5
+    from kron_ref import GATE
+
+    def masks(names, qs, nn):
+        x = z = 0
+        for s, q in zip(names, qs):
+            b = 1 << (nn - q)
+            x |= b if s in "XY" else 0
+            z |= b if s in "ZY" else 0
+        return x, z
+    strings = [(["Z"], [3]), (["X", "Y"], [1, 4]), (["Z", "Z"], [2, 3]), (["Y", "X", "Z"], [5, 1, 2])]
+    for (names, qs), v in zip(strings, gold["obs_vals"][:4]):
+        assert abs(oracle.expect_pauli_sv(psi, *masks(names, qs, n)) - v) < 1e-13
+    # non-Pauli one-qubit observable through the matrix form
+    assert abs(oracle.expect_matrix_sv(psi, GATE["T"], [2]) - gold["obs_vals"][4]) < 1e-13
+    for (names, qs), v in zip([(["Z"], [1]), (["X", "Z"], [1, 3]), (["Y", "Y"], [2, 3])], gold["obs_rho_vals"]):
+        assert abs(oracle.expect_pauli_dm(rho, *masks(names, qs, 3)) - v) < 1e-13
+    assert np.array_equal(oracle.sample(gold["samp_in"], gold["samp_u"]), gold["samp_out"])
+
+
+# ---------------------------------------------------------------- reference test properties
+def test_ref_int2bin_bit_order(oracle, kref):
+    """int2bin(2,4) == [0,0,1,0] (test/runtests.jl:8): qubit 3 of 4 is bit 1."""
+    psi = np.zeros(16, complex)
+    psi[0] = 1
+    out = oracle.hilbert1(psi, kref.GATE["X"], 3)
+    assert np.argmax(np.abs(out)) == 2
+
+
+def test_ref_nonlocal_cnot_equals_controlled_x(oracle, kref):
+    """Op("CNOT",2,5).expand(6) == Op("X",5;control=2).expand(6) (test/runtests.jl:10-17)."""
+    N = 6
+    assert np.array_equal(kref.hilbert2(N, kref.GATE["CNOT"], 2, 5), kref.hilbert1(N, kref.GATE["X"], 5, control=2))
+    for b in range(2 ** N):
+        e = np.zeros(2 ** N, complex)
+        e[b] = 1
+        assert np.array_equal(oracle.hilbert2(e, kref.GATE["CNOT"], 2, 5), oracle.hilbert1(e, kref.GATE["X"], 5, 2))
+
+
+def test_ref_kraus_probabilities(oracle, kref):
+    """probs from partial trace == ||E_k psi||^2 == op.prob (test/runtests.jl:19-35)."""
+    rng = np.random.default_rng(3)
+    N = 6
+    psi = rstate(rng, N)
+    kr = kref.noise_model("depolarizing", 0.5, two_qubit=True)
+    p1 = oracle.calc_prob(psi, kr, 2, 3)
+    p2 = np.array([np.sum(np.abs(oracle.hilbert2(psi, K, 2, 3)) ** 2) for K in kr])
+    p3 = kref.calc_prob(psi, kr, 2, 3)
+    assert np.allclose(p1, p2, atol=1e-14) and np.allclose(p1, p3, atol=1e-14)
+
+
+def test_ref_circuit_unitary(oracle, kref):
+    """sequential apply == compiled operator (test/runtests.jl:54-73), atol 1e-12."""
+    import bluetangle_gpu.circuits as C
+    rng = np.random.default_rng(4)
+    N = 7
+    ops = C.random_ops(N, 12, rng)
+    psi = rstate(rng, N)
+    s1 = psi.copy()
+    U = np.eye(2 ** N, dtype=complex)
+    for o in ops:
+        if o.q == 1:
+            s1 = oracle.hilbert1(s1, o.mat, o.qubit, o.control)
+            U = kref.hilbert1(N, o.mat, o.qubit, o.control) @ U
+        else:
+            s1 = oracle.hilbert2(s1, o.mat, o.qubit, o.target_qubit, o.control)
+            U = kref.hilbert2(N, o.mat, o.qubit, o.target_qubit, o.control) @ U
+    assert np.abs(s1 - U @ psi).max() < 1e-12
+
+
+def test_ref_density_vs_state_and_trajectories(oracle, kref):
+    """noiseless rho == psi psi' (atol 1e-10) and the mean of noisy trajectories
+    matches the noisy density matrix (atol 10/1000) (test/runtests.jl:89-133)."""
+    import bluetangle_gpu.circuits as C
+    rng = np.random.default_rng(5)
+    N = 4
+    ops = C.random_ops(N, 8, rng)
+    psi = np.zeros(2 ** N, complex)
+    psi[0] = 1
+    rho = np.outer(psi, psi.conj())
+    for o in ops:
+        if o.q == 1:
+            psi = oracle.hilbert1(psi, o.mat, o.qubit, o.control)
+            rho = oracle.dm_hilbert1(rho, o.mat, o.qubit, o.control)
+        else:
+            psi = oracle.hilbert2(psi, o.mat, o.qubit, o.target_qubit, o.control)
+            rho = oracle.dm_hilbert2(rho, o.mat, o.qubit, o.target_qubit, o.control)
+    assert np.abs(np.outer(psi, psi.conj()) - rho).max() < 1e-10
+    # noisy: NoiseModel("depolarizing", 0.1) after every gate
+    k1 = kref.noise_model("depolarizing", 0.1)
+    k2 = kref.noise_model("depolarizing", 0.1, two_qubit=True)
+    rho = np.zeros((2 ** N, 2 ** N), complex)
+    rho[0, 0] = 1
+    for o in ops:
+        if o.q == 1:
+            rho = oracle.dm_hilbert1(rho, o.mat, o.qubit)
+            rho = oracle.dm_channel(rho, k1, o.qubit)
+        else:
+            rho = oracle.dm_hilbert2(rho, o.mat, o.qubit, o.target_qubit)
+            rho = oracle.dm_channel(rho, k2, o.qubit, o.target_qubit)
+    zmask = [1 << (N - q) for q in range(1, N + 1)]
+    mag_r = sum(oracle.expect_pauli_dm(rho, 0, z) for z in zmask)
+    mags = []
+    for _ in range(1000):
+        s = np.zeros(2 ** N, complex)
+        s[0] = 1
+        for o in ops:
+            if o.q == 1:
+                s = oracle.hilbert1(s, o.mat, o.qubit)
+                s, _, _ = oracle.channel_traj(s, k1, o.qubit, u=rng.random())
+            else:
+                s = oracle.hilbert2(s, o.mat, o.qubit, o.target_qubit)
+                s, _, _ = oracle.channel_traj(s, k2, o.qubit, o.target_qubit, u=rng.random())
+        mags.append(sum(oracle.expect_pauli_sv(s, 0, z) for z in zmask))
+    assert abs(np.mean(mags) - mag_r) < 10 / 1000 * N
+
+
+def test_ref_mid_circuit_exact_outcomes(oracle, kref):
+    """X,RES,MZ -> [0]; X, ifOp(MZ, I, X) -> [1]; the 11-op circuit -> [1]
+    (test/runtests.jl:195-231), for any uniform draw."""
+    X = kref.GATE["X"]
+    rng = np.random.default_rng(6)
+    for _ in range(20):
+        s = np.array([1, 0], complex)
+        s = oracle.hilbert1(s, X, 1)
+        s, ind, _ = oracle.born_measure_z(s, 1, u=rng.random())
+        if ind == 1:
+            s = oracle.hilbert1(s, X, 1)
+        s, ind, _ = oracle.born_measure_z(s, 1, u=rng.random())
+        assert ind == 0
+        s = oracle.hilbert1(np.array([1, 0], complex), X, 1)
+        s, ind, _ = oracle.born_measure_z(s, 1, u=rng.random())
+        assert ind == 1
+        s = np.zeros(8, complex)
+        s[0] = 1
+        CX = kref.GATE["CX"]
+        s = oracle.hilbert1(s, X, 1)
+        s = oracle.hilbert1(s, X, 2)
+        s = oracle.hilbert2(s, CX, 2, 3)
+        s = oracle.hilbert2(s, CX, 1, 2)
+        s = oracle.hilbert1(s, X, 2)
+        s, ind, _ = oracle.born_measure_z(s, 2, u=rng.random())
+        assert ind == 1
+
+
+def test_ref_channel_cptp_and_sample_semantics(oracle):
+    """weighted sample: first i with u <= cumsum(p) (src/hilbert.jl:810-819); sample
+    picks the first index whose cumulative weight reaches u*sum (StatsBase direct)."""
+    p = np.array([0.2, 0.3, 0.5])
+    assert oracle.weighted_sample(p, 0.2) == 0
+    assert oracle.weighted_sample(p, 0.2000001) == 1
+    assert oracle.weighted_sample(p, 0.9999) == 2
+    assert oracle.weighted_sample(np.array([0.2, 0.3]), 0.9) is None
+    psi = np.sqrt(np.array([0.25, 0, 0.25, 0.5], complex))
+    assert list(oracle.sample(psi, [0.0, 0.2, 0.25, 0.26, 0.5, 0.51, 0.999])) == [0, 0, 0, 2, 2, 3, 3]

@@ -480,7 +480,9 @@ __global__ void __launch_bounds__(BT_THREADS) k_collapse(typename CT<R>::T* __re
     const int64_t mem = mem_lo + mi;
     const int64_t i = t & (per - 1);
     typename CT<R>::T* p = psi + (mem << nbits) + i;
-    if ((int)((i >> bit) & 1) == outcome[mi]) {
+    const int oc = outcome[mi];
+    if (oc < 0) continue;  // member whose decision failed: left untouched
+    if ((int)((i >> bit) & 1) == oc) {
       const R sc = (R)scale[mi];
       typename CT<R>::T v = *p;
       v.x *= sc;
@@ -549,10 +551,16 @@ __global__ void k_decide_measure(int64_t nmem, const double* __restrict__ rdm, c
   double uu = u ? u[m] : bt_uniform(key, stream, (uint64_t)m);
   int ind = f >= 0 ? f : (uu < s0 ? 0 : 1);
   double keep = ind ? s1 : s0;
-  if (!(keep > 0)) atomicExch(status, 1);
+  p0[m] = s0;
+  if (!(keep > 0) || ind > 1) {
+    // an outcome of zero probability: report it and leave this member untouched
+    atomicExch(status, 1);
+    outcome[m] = -1;
+    scale[m] = 1.0;
+    return;
+  }
   outcome[m] = ind;
   scale[m] = 1.0 / sqrt(keep);
-  p0[m] = s0;
 }
 
 int bt_launch_decide_measure(bt_ctx* ctx, int64_t nmem, const double* rdm, const double* u, const int* forced,
@@ -604,9 +612,14 @@ __global__ void k_decide_kraus(int64_t nmem, int k, int nk, int ref_perm, const 
     if (ind < 0 && uu <= cum) ind = i;
   }
   if (f >= 0) ind = f;
+  R* out = pm + m * 2 * D * D;
   if (ind < 0 || ind >= nk) {
+    // no branch (the reference's _weighted_sample returns nothing): report it and
+    // leave this member untouched with an identity matrix
     atomicExch(status, 2);
-    ind = nk - 1;
+    branch[m] = -1;
+    for (int e = 0; e < 2 * D * D; ++e) out[e] = (R)((e % (2 * D + 2)) == 0 ? 1.0 : 0.0);
+    return;
   }
   branch[m] = ind;
   // norm of K_ind psi in application order
@@ -622,9 +635,12 @@ __global__ void k_decide_kraus(int64_t nmem, int k, int nk, int ref_perm, const 
         nrm += tr_ * kbr - ti * kbi;
       }
     }
-  if (!(nrm > 0)) atomicExch(status, 3);
+  if (!(nrm > 0)) {
+    atomicExch(status, 3);
+    for (int e = 0; e < 2 * D * D; ++e) out[e] = (R)((e % (2 * D + 2)) == 0 ? 1.0 : 0.0);
+    return;
+  }
   const double sc = 1.0 / sqrt(nrm);
-  R* out = pm + m * 2 * D * D;
   for (int e = 0; e < 2 * D * D; ++e) out[e] = (R)(K[e] * sc);
 }
 

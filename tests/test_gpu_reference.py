@@ -232,5 +232,8 @@ def test_config_density_matrix_noisy_brickwork(ctx, oracle, kref, prec, tol):
     tr = sum(bt.expect(rho, "Z"))  # finite
     assert np.isfinite(tr)
     R = rho.to_numpy()
-    assert abs(np.trace(R) - 1) < (1e-12 if prec == "c128" else 1e-4)
+    # T/TD are rounded to 10 significant digits in the reference (src/gates.jl:32-33),
+    # so |T[2,2]|^2 = 1 + 1.0e-10: the trace grows by up to that per T gate
+    nT = sum(1 for o in ops if getattr(o, "name", "") == "T")
+    assert abs(np.trace(R) - 1) < (1e-12 + nT * 1.01e-10 if prec == "c128" else 1e-4)
     assert np.abs(R - R.conj().T).max() < (1e-13 if prec == "c128" else 1e-6)

@@ -64,6 +64,7 @@ SIGNATURES = {
     "bt_reduced_dm": (i32, [P, i32, P, i64, P]),
     "bt_sample": (i32, [P, i64, i64, P, u64, P]),
     "bt_probabilities": (i32, [P, i64, P]),
+    "bt_sample_noalloc": (i32, [P, i32, i32, i64, P, u64, u64, P, P]),
     "bt_expect_pauli": (i32, [P, i32, P, P, P, i64, P]),
     "bt_expect_z_all": (i32, [P, i64, P]),
     "bt_expect_matrix": (i32, [P, i32, P, P, i32, P, i64, P]),

@@ -193,3 +193,72 @@ int bt_launch_convert_out(bt_state* s, int64_t mem, int64_t offset, int64_t len,
   ctx->launches++;
   return bt_cuda_check(ctx, cudaGetLastError(), "convert launch");
 }
+
+// ------------------------------------------------------------ allocation-free sampling
+// bt_sample_noalloc: the sampler above for callers that must not allocate device
+// memory.  Its only scratch, the chunk-sum prefix, lives in this file-scope
+// device array, so the entry point calls no cudaMalloc/cudaFree and allocates
+// nothing on the host side of the CUDA runtime either.
+//   size: BT_NOALLOC_CHUNKS doubles (512 KiB), i.e. states of at most
+//         2^(12 + 16) = 2^28 amplitudes (n <= 28); every GPU that loads the
+//         library holds the array until the process exits.
+//   sharing: all calls share the array and it keeps the last call's contents.
+//         Each call overwrites every entry it reads before reading it (chunk
+//         sums, then the in-place scan), so nothing needs clearing, but calls
+//         whose work overlaps on the GPU (different streams, or devices sharing
+//         nothing but the same call sequence) race on it.
+#define BT_NOALLOC_CHUNKS (1 << 16)
+#define BT_NOALLOC_MAX_QUBITS (CHUNK_LG + 16)
+static __device__ __align__(256) double g_noalloc_cum[BT_NOALLOC_CHUNKS];
+
+#include <mutex>
+static std::mutex g_noalloc_mu;
+static double* g_noalloc_ptr[64];  // device address of g_noalloc_cum, per device
+
+// Host code must not take the address of g_noalloc_cum directly (that is a
+// host-side shadow, not a device address): it asks the runtime once per device,
+// with that device current.
+static int noalloc_scratch(int dev, double** out) {
+  if (dev < 0 || dev >= 64) return bt_fail(nullptr, BT_ERR_DEVICE, "device index beyond 63");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_cum);
+    if (e != cudaSuccess || !p)
+      return bt_fail(nullptr, BT_ERR_DEVICE, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = (double*)p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return BT_OK;
+}
+
+extern "C" int bt_sample_noalloc(const void* d_state, int n, int prec, int64_t shots, const double* d_uniforms,
+                                 uint64_t key, uint64_t seed, int64_t* d_out, void* stream) {
+  if (!d_state || (shots > 0 && !d_out)) return bt_fail(nullptr, BT_ERR_BAD_ARG, "state or output pointer is NULL");
+  if (prec != BT_PREC_C128 && prec != BT_PREC_C64) return bt_fail(nullptr, BT_ERR_BAD_ARG, "prec must be C128 or C64");
+  if (n < 1 || n > BT_NOALLOC_MAX_QUBITS)
+    return bt_fail(nullptr, BT_ERR_BAD_ARG,
+                   "bt_sample_noalloc supports 1 <= n <= 28 qubits (its static prefix holds 65536 chunk sums)");
+  if (shots < 0 || shots > (1LL << 33)) return bt_fail(nullptr, BT_ERR_BAD_ARG, "shots must be in [0, 2^33]");
+  if (shots == 0) return BT_OK;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return bt_fail(nullptr, BT_ERR_DEVICE, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  double* cum = nullptr;
+  int rc = noalloc_scratch(dev, &cum);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int clg = n < CHUNK_LG ? n : CHUNK_LG;
+  const int64_t nchunk = 1LL << (n - clg);
+  const bool f = prec == BT_PREC_C64;
+  if (f) k_chunk_sums<float><<<(unsigned)nchunk, BT_THREADS, 0, st>>>((const float2*)d_state, 0, n, clg, cum);
+  else k_chunk_sums<double><<<(unsigned)nchunk, BT_THREADS, 0, st>>>((const double2*)d_state, 0, n, clg, cum);
+  k_scan<<<1, 1024, 0, st>>>(cum, nchunk);
+  const unsigned grid = (unsigned)((shots * 32 + 255) / 256);
+  const uint64_t sstream = seed ^ 0x53414d5000000000ULL;
+  if (f) k_shots<float><<<grid, 256, 0, st>>>((const float2*)d_state, 0, n, clg, cum, nchunk, shots, d_uniforms, key, sstream, d_out);
+  else k_shots<double><<<grid, 256, 0, st>>>((const double2*)d_state, 0, n, clg, cum, nchunk, shots, d_uniforms, key, sstream, d_out);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return bt_fail(nullptr, BT_ERR_DEVICE, std::string("sample launch: ") + cudaGetErrorString(e));
+  return BT_OK;
+}

@@ -141,6 +141,24 @@ int bt_sample(const bt_state* s, int64_t member, int64_t shots, const double* un
               int64_t* out);
 /* abs2.(psi) or real(diag(rho)) (sample_exact, src/ops.jl:98-101, :129-132) */
 int bt_probabilities(const bt_state* s, int64_t member, double* out);
+/* No counterpart in the reference.  bt_sample for callers that must not allocate
+ * device memory: callers whose device memory is owned by a host framework's pool
+ * (CUDA.jl, PyTorch) that may hold nearly all of HBM, so a library cudaMalloc
+ * could fail and a cudaFree would stall every stream, and callers recording
+ * into CUDA graphs, where cudaMalloc/cudaFree are not captured.  It allocates
+ * nothing: its only scratch (the chunk prefix) is a 512 KiB file-scope device
+ * array, so it accepts state vectors of 1 <= n <= 28 qubits and rejects larger
+ * ones.  Everything else is the caller's: d_state (2^n interleaved complex128 or
+ * complex64 amplitudes in device memory), d_uniforms (shots draws in device
+ * memory, or NULL for Philox keyed by `key` and `seed`; key = the ctx seed and
+ * the same seed reproduce bt_sample's stream), d_out (shots int64 in device
+ * memory) and the cudaStream_t `stream` (NULL = the legacy default stream).
+ * The call only enqueues work and returns.  The first call on a device looks up
+ * the array's device address (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race on it. */
+int bt_sample_noalloc(const void* d_state, int n, int prec, int64_t shots, const double* d_uniforms, uint64_t key,
+                      uint64_t seed, int64_t* d_out, void* stream);
 
 /* ------------------------------------------------------------- observables */
 /* Pauli strings as masks over the amplitude index (bit n-q for qubit q); Y sets

@@ -6,7 +6,7 @@ package only builds the reference's op descriptors and small host tables and
 calls the library.  Importing it loads the library and fails if it is absent.
 """
 from ._lib import BTError, lib
-from .engine import (Context, GPUDensity, GPUState, Measurement, apply, apply_channel, apply_matrix, apply_noise,
+from .engine import (Context, GPUDensity, GPUState, Measurement, Plan, plan_from_ops, apply, apply_channel, apply_matrix, apply_noise,
                      born_measure_Z, channel_probs, correlation, expect, fidelity, measure, partial_trace,
                      pauli_masks, rho_from, run, sample, sample_exact, state_from, to_rho, to_state, zero_rho,
                      zero_state)
@@ -16,7 +16,7 @@ from .ops import Op, OpQC, ifOp
 
 lib()  # load now: no silent fallback exists
 
-__all__ = ["BTError", "Context", "GPUState", "GPUDensity", "Measurement", "apply", "apply_channel", "apply_matrix",
+__all__ = ["BTError", "Context", "Plan", "plan_from_ops", "GPUState", "GPUDensity", "Measurement", "apply", "apply_channel", "apply_matrix",
            "apply_noise", "born_measure_Z", "channel_probs", "correlation", "expect", "fidelity", "measure",
            "partial_trace", "pauli_masks", "rho_from", "run", "sample", "sample_exact", "state_from", "to_rho",
            "to_state", "zero_rho", "zero_state", "gate", "gates", "NoiseModel", "Noise1", "Noise2",

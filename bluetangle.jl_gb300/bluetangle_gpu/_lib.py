@@ -62,6 +62,13 @@ SIGNATURES = {
     "bt_apply_kraus": (i32, [P, i32, P, i32, P, i32, P, P, P, P]),
     "bt_measure_z": (i32, [P, i32, P, P, P, P]),
     "bt_reduced_dm": (i32, [P, i32, P, i64, P]),
+    "bt_plan_create": (i32, [P, i32, i32, i32, ctypes.POINTER(P)]),
+    "bt_plan_free": (i32, [P]),
+    "bt_plan_add_matrix": (i32, [P, i32, P, P, i32, P]),
+    "bt_plan_add_kraus_sum": (i32, [P, i32, P, i32, P]),
+    "bt_plan_compile": (i32, [P, i32]),
+    "bt_plan_stats": (i32, [P, P, P, P, P]),
+    "bt_plan_run": (i32, [P, P, i64]),
     "bt_sample": (i32, [P, i64, i64, P, u64, P]),
     "bt_probabilities": (i32, [P, i64, P]),
     "bt_sample_noalloc": (i32, [P, i32, i32, i64, P, u64, u64, P, P]),

@@ -410,6 +410,79 @@ def _apply_one(state, op, noise, rng, pars, forced_iter):
     return state, mids
 
 
+# ------------------------------------------------------------------ plans (fused circuits)
+class Plan:
+    """A compiled circuit (bt_plan): gates (and, for density matrices, Kraus sums)
+    fused into tile passes; running it equals applying the ops one by one."""
+
+    def __init__(self, n, repr="sv", prec="c128", ctx=None):
+        self.ctx = ctx or Context.default()
+        self.n = n
+        self.repr_code = L.BT_REPR_DM if repr in ("dm", "density", L.BT_REPR_DM) else L.BT_REPR_SV
+        self.prec = prec
+        h = _P()
+        self.ctx.check(L.lib().bt_plan_create(self.ctx.h, n, self.repr_code, _PREC[prec], ctypes.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                L.lib().bt_plan_free(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def add_matrix(self, mat, qubits, controls=()):
+        q = _i32(list(qubits))
+        c = _i32(list(controls) or [0])
+        M = _cm(mat)
+        self.ctx.check(L.lib().bt_plan_add_matrix(self.h, len(q), _ptr(q), _ptr(M), len(controls),
+                                                  _ptr(c) if controls else None))
+        return self
+
+    def add_kraus_sum(self, kraus, qubits):
+        q = _i32(list(qubits))
+        K = np.ascontiguousarray(np.concatenate([_cm(m).ravel() for m in kraus]))
+        self.ctx.check(L.lib().bt_plan_add_kraus_sum(self.h, len(q), _ptr(q), len(kraus), _ptr(K)))
+        return self
+
+    def add(self, op, pars=None):
+        """Appends a gate Op (any density/state plan) or an OpQC (density plans)."""
+        if isinstance(op, OpQC):
+            if self.repr_code != L.BT_REPR_DM:
+                raise ValueError("channels in a state-vector plan need trajectories; apply them with apply()")
+            qs = [op.qubit] if op.q == 1 else ([op.qubit, op.target_qubit] if op.q == 2 else None)
+            if qs is None:
+                raise ValueError("3-qubit OpQC has no density-matrix method in the reference")
+            return self.add_kraus_sum(op.kraus, qs)
+        if op.type == "🔬":
+            raise ValueError("measurements end a plan")
+        mat = _op_matrix(op, pars)
+        qs = [op.qubit] if op.q == 1 else [op.qubit, op.target_qubit]
+        ctrls = [op.control] if op.control != -2 else []
+        return self.add_matrix(mat, qs, ctrls)
+
+    def compile(self, fused=True):
+        self.ctx.check(L.lib().bt_plan_compile(self.h, 0 if fused else 1))
+        return self
+
+    def stats(self):
+        v = [ctypes.c_int64(0) for _ in range(4)]
+        self.ctx.check(L.lib().bt_plan_stats(self.h, *[ctypes.byref(x) for x in v]))
+        return dict(zip(("gates", "passes", "fused_passes", "phases"), (x.value for x in v)))
+
+    def run(self, state, member=-1):
+        self.ctx.check(L.lib().bt_plan_run(self.h, state.h, member))
+        return state
+
+
+def plan_from_ops(ops, n, repr="sv", prec="c128", fused=True, ctx=None):
+    p = Plan(n, repr, prec, ctx)
+    for op in ops:
+        p.add(op)
+    return p.compile(fused)
+
+
 # ------------------------------------------------------------------ sampling / observables
 def sample(state, shots, rng=None, seed=0, member=0):
     """sample(psi, shots) (src/ops.jl:46-62): basis indices 0..2^N-1."""

@@ -1,0 +1,50 @@
+// Shared declarations of the fused tile pass (bt_fused.cu) and its planner (bt_plan.cu).
+#pragma once
+#include "bt_internal.cuh"
+
+#define BT_FUSED_MAX_PHASES 48
+#define BT_FUSED_MAX_OPS 192
+#define BT_FUSED_MAX_REALS_F 4096  // float matrix entries per pass (16 KiB)
+#define BT_FUSED_MAX_REALS_D 2048  // double matrix entries per pass (16 KiB)
+
+// tile geometry: M tile bits held in shared memory (64 KiB), RB register bits per thread
+#define BT_TILE_M_C64 13
+#define BT_TILE_RB_C64 5
+#define BT_TILE_M_C128 12
+#define BT_TILE_RB_C128 4
+#define BT_TILE_LOW_C64 5   // the lowest global bits always in a tile: 256-byte contiguous runs
+#define BT_TILE_LOW_C128 4
+#define BT_TILE_THREADS 256
+
+enum {
+  FOP_G1 = 1,  // general 2x2: m00 m01 m10 m11 (8 reals)
+  FOP_D1 = 2,  // diagonal 2x2: d0 d1 (4 reals)
+  FOP_G2 = 3,  // general 4x4 on (b0 = high bit, b1 = low bit) (32 reals)
+  FOP_D2 = 4,  // diagonal 4x4 (8 reals)
+  FOP_P2 = 5,  // monomial 4x4: out[r] = ph[r] * in[perm[r]]; perm packed in flags, phases 8 reals
+};
+
+struct FOp {
+  uint8_t type, b0, b1, flags;  // flags for P2: perm[r] = (flags >> 2r) & 3
+  uint16_t moff, unit;          // unit: P2 phases are all exactly 1
+};
+
+struct FPhase {
+  uint8_t reg[5];  // tile-local bits held in registers (ascending), register bit b = reg[b]
+  uint8_t nreg;
+  uint16_t op0, nop;
+};
+
+template <typename R>
+struct FusedArgs {
+  int nbits, M, c, nphase;
+  int tbits[16];            // tile-local bit -> global bit (ascending; tbits[i] = i for i < c)
+  int64_t member_lo, nmem;  // members processed
+  int lg_tiles;             // log2(tiles per member) = nbits - M
+  FPhase ph[BT_FUSED_MAX_PHASES];
+  FOp op[BT_FUSED_MAX_OPS];
+  R mat[sizeof(R) == 4 ? BT_FUSED_MAX_REALS_F : BT_FUSED_MAX_REALS_D];
+};
+
+int bt_launch_fused_f(bt_ctx* ctx, void* psi, const FusedArgs<float>& a);
+int bt_launch_fused_d(bt_ctx* ctx, void* psi, const FusedArgs<double>& a);

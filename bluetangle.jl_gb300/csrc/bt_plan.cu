@@ -1,0 +1,421 @@
+// Circuit plans: the gate-fusion pass of the circuit compiler (the role of the
+// reference's compile/get_layers, BlueTangle.jl src/ops.jl:278-329, :421-445) and
+// their execution.
+//
+// A plan is a list of dense gates over the bits of a state (n bits for a state
+// vector; 2n for a density matrix, where a gate U on qubit q becomes U on row bit
+// n-q and conj(U) on column bit 2n-q, and a Kraus sum becomes one superoperator
+// on both).  compile() groups the gates into passes:
+//   * fused passes: a set of at most M bits (always containing the lowest c
+//     bits) and every gate that acts inside it and is not ordered behind a gate
+//     left out; gates inside a pass are grouped into register phases of at most
+//     RB bits.  Each fused pass is one k_fused launch (bt_fused.cu).
+//   * sweep passes: gates of more than two bits, or with controls that do not fit
+//     a two-bit matrix, run as one k_gate sweep (bt_gate.cu).
+// Gates are only reordered past gates on disjoint bits, so the plan applies the
+// same linear map as the gates in their given order.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "bt_fused.cuh"
+
+struct PGate {
+  int k = 0;
+  int bits[2 * BT_MAX_K] = {0};  // bits[0] = most significant bit of the matrix index
+  uint64_t cmask = 0;
+  std::vector<double> m;  // row-major interleaved 2^k x 2^k
+  uint64_t allbits() const {
+    uint64_t b = cmask;
+    for (int i = 0; i < k; ++i) b |= 1ULL << bits[i];
+    return b;
+  }
+};
+
+struct PPass {
+  int kind = 0;  // 0 fused, 1 sweep
+  int gate = -1;
+  int ngates = 0;
+  std::vector<unsigned char> args;  // FusedArgs<float> or <double>, bytes
+};
+
+struct bt_plan {
+  bt_ctx* ctx = nullptr;
+  int n = 0, repr = 0, prec = 0, nbits = 0;
+  std::vector<PGate> gates;
+  std::vector<PPass> passes;
+  bool compiled = false;
+  int64_t nphases = 0;
+};
+
+static int popc(uint64_t x) { return __builtin_popcountll(x); }
+
+static void kron_ctrl(int k, const double* u_rm, int nc, std::vector<double>& out) {
+  // controlled-U on (controls..., targets...): identity except the block where all controls are 1
+  const int d = 1 << k, D = 1 << (k + nc);
+  out.assign(2 * D * D, 0.0);
+  for (int i = 0; i < D; ++i) out[2 * (i * D + i)] = 1.0;
+  const int off = D - d;
+  for (int r = 0; r < d; ++r)
+    for (int c = 0; c < d; ++c) {
+      out[2 * ((off + r) * D + off + c)] = u_rm[2 * (r * d + c)];
+      out[2 * ((off + r) * D + off + c) + 1] = u_rm[2 * (r * d + c) + 1];
+    }
+}
+
+static void add_gate(bt_plan* p, int k, const int* bits, const double* rm, int nc, const int* cbits) {
+  PGate g;
+  if (nc > 0 && k + nc <= 2) {
+    // fold the control into a dense two-bit matrix so the gate can join a tile
+    kron_ctrl(k, rm, nc, g.m);
+    g.k = k + nc;
+    for (int i = 0; i < nc; ++i) g.bits[i] = cbits[i];
+    for (int i = 0; i < k; ++i) g.bits[nc + i] = bits[i];
+  } else {
+    g.k = k;
+    for (int i = 0; i < k; ++i) g.bits[i] = bits[i];
+    for (int i = 0; i < nc; ++i) g.cmask |= 1ULL << cbits[i];
+    g.m.assign(rm, rm + 2 * (1 << k) * (1 << k));
+  }
+  p->gates.push_back(std::move(g));
+  p->compiled = false;
+}
+
+static bool eligible(const PGate& g) { return g.cmask == 0 && g.k <= 2; }
+
+// classify a 2^k x 2^k matrix: 2 diagonal, 1 monomial (one non-zero per row and
+// column), 0 general
+static int classify(const PGate& g, int* perm) {
+  const int d = 1 << g.k;
+  bool diag = true, mono = true;
+  for (int r = 0; r < d; ++r) {
+    int nz = 0;
+    for (int c = 0; c < d; ++c) {
+      bool z = g.m[2 * (r * d + c)] == 0.0 && g.m[2 * (r * d + c) + 1] == 0.0;
+      if (!z) {
+        ++nz;
+        if (c != r) diag = false;
+        perm[r] = c;
+      }
+    }
+    if (nz != 1) mono = false;
+  }
+  if (mono) {
+    int seen = 0;
+    for (int r = 0; r < d; ++r) seen |= 1 << perm[r];
+    if (seen != (1 << d) - 1) mono = false;
+  }
+  return diag ? 2 : (mono ? 1 : 0);
+}
+
+template <typename R>
+static bool build_fused(bt_plan* p, const std::vector<int>& take, uint64_t tilemask, int M, int NB, int c,
+                        std::vector<int>& kept, FusedArgs<R>& a, int64_t* nph) {
+  memset(&a, 0, sizeof(a));
+  a.nbits = p->nbits;
+  a.M = M;
+  a.c = c;
+  int nb = 0, local[64];
+  for (int b = 0; b < p->nbits; ++b) {
+    local[b] = -1;
+    if ((tilemask >> b) & 1) {
+      a.tbits[nb] = b;
+      local[b] = nb++;
+    }
+  }
+  a.lg_tiles = p->nbits - M;
+  const int maxreals = sizeof(R) == 4 ? BT_FUSED_MAX_REALS_F : BT_FUSED_MAX_REALS_D;
+  // register phases: greedy over the pass's gates with blocking, in order
+  std::vector<int> rem = take;
+  int nop = 0, nreal = 0;
+  kept.clear();
+  while (!rem.empty()) {
+    if (a.nphase >= BT_FUSED_MAX_PHASES) break;
+    uint32_t regs = 0, blocked = 0;
+    std::vector<int> ph, rest;
+    for (int gi : rem) {
+      const PGate& g = p->gates[gi];
+      uint32_t lb = 0;
+      for (int i = 0; i < g.k; ++i) lb |= 1u << local[g.bits[i]];
+      const int need = g.k == 1 ? 8 : 32;
+      if ((lb & blocked) || popc(regs | lb) > NB || nop + (int)ph.size() + 1 > BT_FUSED_MAX_OPS ||
+          nreal + need > maxreals) {
+        blocked |= lb;
+        rest.push_back(gi);
+        continue;
+      }
+      regs |= lb;
+      ph.push_back(gi);
+      nreal += need;
+    }
+    if (ph.empty()) break;
+    // pad the register set to NB bits with the highest unused tile bits
+    for (int b = M - 1; b >= 0 && popc(regs) < NB; --b) regs |= 1u << b;
+    FPhase& P = a.ph[a.nphase++];
+    int rb = 0, regidx[32];
+    for (int b = 0; b < M; ++b)
+      if ((regs >> b) & 1) {
+        regidx[b] = rb;
+        P.reg[rb++] = (uint8_t)b;
+      }
+    P.nreg = (uint8_t)NB;
+    P.op0 = (uint16_t)nop;
+    P.nop = (uint16_t)ph.size();
+    for (int gi : ph) {
+      const PGate& g = p->gates[gi];
+      FOp& o = a.op[nop++];
+      int perm[4] = {0, 1, 2, 3};
+      const int cls = classify(g, perm);
+      o.moff = (uint16_t)(nreal - (g.k == 1 ? 8 : 32));  // provisional; rewritten below
+      o.b0 = (uint8_t)regidx[local[g.bits[0]]];
+      o.b1 = g.k == 2 ? (uint8_t)regidx[local[g.bits[1]]] : 0;
+      kept.push_back(gi);
+      (void)cls;
+    }
+    rem.swap(rest);
+  }
+  // write matrices compactly in op order
+  int w = 0;
+  for (int i = 0; i < nop; ++i) {
+    const PGate& g = p->gates[kept[i]];
+    FOp& o = a.op[i];
+    int perm[4] = {0, 1, 2, 3};
+    const int cls = classify(g, perm);
+    o.moff = (uint16_t)w;
+    if (g.k == 1) {
+      if (cls == 2) {
+        o.type = FOP_D1;
+        a.mat[w++] = (R)g.m[0];
+        a.mat[w++] = (R)g.m[1];
+        a.mat[w++] = (R)g.m[6];
+        a.mat[w++] = (R)g.m[7];
+      } else {
+        o.type = FOP_G1;
+        for (int e = 0; e < 8; ++e) a.mat[w++] = (R)g.m[e];
+      }
+    } else if (cls == 2) {
+      o.type = FOP_D2;
+      for (int r = 0; r < 4; ++r) {
+        a.mat[w++] = (R)g.m[2 * (r * 4 + r)];
+        a.mat[w++] = (R)g.m[2 * (r * 4 + r) + 1];
+      }
+    } else if (cls == 1) {
+      o.type = FOP_P2;
+      o.flags = (uint8_t)(perm[0] | (perm[1] << 2) | (perm[2] << 4) | (perm[3] << 6));
+      bool unit = true;
+      for (int r = 0; r < 4; ++r) {
+        double pr = g.m[2 * (r * 4 + perm[r])], pi = g.m[2 * (r * 4 + perm[r]) + 1];
+        if (pr != 1.0 || pi != 0.0) unit = false;
+        a.mat[w++] = (R)pr;
+        a.mat[w++] = (R)pi;
+      }
+      o.unit = unit ? 1 : 0;
+    } else {
+      o.type = FOP_G2;
+      for (int e = 0; e < 32; ++e) a.mat[w++] = (R)g.m[e];
+    }
+  }
+  *nph = a.nphase;
+  return !kept.empty();
+}
+
+extern "C" {
+
+int bt_plan_create(bt_ctx* ctx, int n, int repr, int prec, bt_plan** out) {
+  if (!ctx || !out) return bt_fail(ctx, BT_ERR_BAD_ARG, "NULL argument");
+  if (repr != BT_REPR_SV && repr != BT_REPR_DM) return bt_fail(ctx, BT_ERR_BAD_ARG, "repr must be SV or DM");
+  if (prec != BT_PREC_C128 && prec != BT_PREC_C64) return bt_fail(ctx, BT_ERR_BAD_ARG, "prec must be C128 or C64");
+  if (n < 1 || n > (repr == BT_REPR_DM ? 17 : 34)) return bt_fail(ctx, BT_ERR_BAD_ARG, "qubit count out of range");
+  bt_plan* p = new bt_plan();
+  p->ctx = ctx;
+  p->n = n;
+  p->repr = repr;
+  p->prec = prec;
+  p->nbits = repr == BT_REPR_DM ? 2 * n : n;
+  *out = p;
+  return BT_OK;
+}
+
+int bt_plan_free(bt_plan* p) {
+  delete p;
+  return BT_OK;
+}
+
+int bt_plan_add_matrix(bt_plan* p, int k, const int32_t* qubits, const double* mat, int nctrl, const int32_t* ctrls) {
+  if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "plan is NULL");
+  bt_ctx* ctx = p->ctx;
+  if (k < 1 || k > BT_MAX_K || !qubits || !mat) return bt_fail(ctx, BT_ERR_BAD_ARG, "bad gate (1 <= k <= 5)");
+  if (nctrl < 0 || (nctrl && !ctrls)) return bt_fail(ctx, BT_ERR_BAD_ARG, "bad control list");
+  uint64_t seen = 0;
+  for (int i = 0; i < k + nctrl; ++i) {
+    int q = i < k ? qubits[i] : ctrls[i - k];
+    if (q < 1 || q > p->n) return bt_fail(ctx, BT_ERR_BAD_ARG, "N must be larger than qubits");
+    if (seen & (1ULL << q)) return bt_fail(ctx, BT_ERR_BAD_ARG, "qubits and controls must differ");
+    seen |= 1ULL << q;
+  }
+  const int d = 1 << k;
+  std::vector<double> rm(2 * d * d);
+  for (int r = 0; r < d; ++r)
+    for (int c = 0; c < d; ++c) {
+      rm[2 * (r * d + c)] = mat[2 * (r + c * d)];
+      rm[2 * (r * d + c) + 1] = mat[2 * (r + c * d) + 1];
+    }
+  int bits[BT_MAX_K], cb[64];
+  const int n = p->n;
+  for (int i = 0; i < k; ++i) bits[i] = n - qubits[i];
+  for (int i = 0; i < nctrl; ++i) cb[i] = n - ctrls[i];
+  add_gate(p, k, bits, rm.data(), nctrl, cb);
+  if (p->repr == BT_REPR_DM) {
+    for (int i = 0; i < d * d; ++i) rm[2 * i + 1] = -rm[2 * i + 1];
+    for (int i = 0; i < k; ++i) bits[i] = 2 * n - qubits[i];
+    for (int i = 0; i < nctrl; ++i) cb[i] = 2 * n - ctrls[i];
+    add_gate(p, k, bits, rm.data(), nctrl, cb);
+  }
+  return BT_OK;
+}
+
+int bt_plan_add_kraus_sum(bt_plan* p, int k, const int32_t* qubits, int nk, const double* kraus) {
+  if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "plan is NULL");
+  bt_ctx* ctx = p->ctx;
+  if (p->repr != BT_REPR_DM) return bt_fail(ctx, BT_ERR_BAD_ARG, "a Kraus sum needs a density-matrix plan");
+  if (k < 1 || k > 2 || !qubits || nk < 1 || !kraus) return bt_fail(ctx, BT_ERR_BAD_ARG, "bad channel (k <= 2)");
+  const int n = p->n, d = 1 << k, dd = d * d;
+  for (int i = 0; i < k; ++i)
+    if (qubits[i] < 1 || qubits[i] > n) return bt_fail(ctx, BT_ERR_BAD_ARG, "N must be larger than qubits");
+  if (k == 2 && qubits[0] == qubits[1]) return bt_fail(ctx, BT_ERR_BAD_ARG, "qubits must differ");
+  std::vector<double> sup(2 * dd * dd, 0.0);
+  for (int i = 0; i < nk; ++i) {
+    const double* K = kraus + (size_t)i * 2 * dd;  // column-major
+    for (int ir = 0; ir < d; ++ir)
+      for (int ic = 0; ic < d; ++ic)
+        for (int jr = 0; jr < d; ++jr)
+          for (int jc = 0; jc < d; ++jc) {
+            double ar = K[2 * (ir + jr * d)], ai = K[2 * (ir + jr * d) + 1];
+            double br = K[2 * (ic + jc * d)], bi = -K[2 * (ic + jc * d) + 1];
+            int r = ir * d + ic, c = jr * d + jc;
+            sup[2 * (r * dd + c)] += ar * br - ai * bi;
+            sup[2 * (r * dd + c) + 1] += ar * bi + ai * br;
+          }
+  }
+  int bits[4];
+  for (int i = 0; i < k; ++i) {
+    bits[i] = n - qubits[i];
+    bits[k + i] = 2 * n - qubits[i];
+  }
+  add_gate(p, 2 * k, bits, sup.data(), 0, nullptr);
+  return BT_OK;
+}
+
+int bt_plan_compile(bt_plan* p, int mode) {
+  if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "plan is NULL");
+  p->passes.clear();
+  p->nphases = 0;
+  const bool c64 = p->prec == BT_PREC_C64;
+  const int M = c64 ? BT_TILE_M_C64 : BT_TILE_M_C128;
+  const int NB = c64 ? BT_TILE_RB_C64 : BT_TILE_RB_C128;
+  const int c = c64 ? BT_TILE_LOW_C64 : BT_TILE_LOW_C128;
+  const bool fuse = mode == 0 && p->nbits >= M;
+  std::vector<int> rem(p->gates.size());
+  for (size_t i = 0; i < rem.size(); ++i) rem[i] = (int)i;
+  const uint64_t lowmask = (1ULL << c) - 1;
+  while (!rem.empty()) {
+    const PGate& g0 = p->gates[rem[0]];
+    if (!fuse || !eligible(g0)) {
+      PPass ps;
+      ps.kind = 1;
+      ps.gate = rem[0];
+      ps.ngates = 1;
+      p->passes.push_back(std::move(ps));
+      rem.erase(rem.begin());
+      continue;
+    }
+    uint64_t Q = lowmask, blocked = 0;
+    std::vector<int> take;
+    for (int gi : rem) {
+      const PGate& g = p->gates[gi];
+      const uint64_t b = g.allbits();
+      if (!eligible(g) || (b & blocked) || popc(Q | b) > M || (int)take.size() >= BT_FUSED_MAX_OPS) {
+        blocked |= b;
+        continue;
+      }
+      Q |= b;
+      take.push_back(gi);
+    }
+    for (int b = 0; b < p->nbits && popc(Q) < M; ++b) Q |= 1ULL << b;  // pad with the lowest free bits
+    std::vector<int> kept;
+    PPass ps;
+    ps.kind = 0;
+    int64_t nph = 0;
+    if (c64) {
+      ps.args.resize(sizeof(FusedArgs<float>));
+      build_fused<float>(p, take, Q, M, NB, c, kept, *reinterpret_cast<FusedArgs<float>*>(ps.args.data()), &nph);
+    } else {
+      ps.args.resize(sizeof(FusedArgs<double>));
+      build_fused<double>(p, take, Q, M, NB, c, kept, *reinterpret_cast<FusedArgs<double>*>(ps.args.data()), &nph);
+    }
+    ps.ngates = (int)kept.size();
+    p->nphases += nph;
+    p->passes.push_back(std::move(ps));
+    // remove the kept gates; the rest keep their order
+    std::vector<char> done(p->gates.size(), 0);
+    for (int gi : kept) done[gi] = 1;
+    std::vector<int> nr;
+    for (int gi : rem)
+      if (!done[gi]) nr.push_back(gi);
+    rem.swap(nr);
+  }
+  p->compiled = true;
+  return BT_OK;
+}
+
+int bt_plan_stats(const bt_plan* p, int64_t* ngates, int64_t* npasses, int64_t* nfused, int64_t* nphases) {
+  if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "plan is NULL");
+  int64_t nf = 0;
+  for (auto& ps : p->passes) nf += ps.kind == 0;
+  if (ngates) *ngates = (int64_t)p->gates.size();
+  if (npasses) *npasses = (int64_t)p->passes.size();
+  if (nfused) *nfused = nf;
+  if (nphases) *nphases = p->nphases;
+  return BT_OK;
+}
+
+int bt_plan_run(bt_plan* p, bt_state* s, int64_t member) {
+  if (!p || !s) return bt_fail(p ? p->ctx : nullptr, BT_ERR_BAD_ARG, "NULL argument");
+  bt_ctx* ctx = s->ctx;
+  if (s->n != p->n || s->repr != p->repr || s->prec != p->prec)
+    return bt_fail(ctx, BT_ERR_BAD_ARG, "plan and state differ in n, repr or prec");
+  if (!p->compiled) {
+    int rc = bt_plan_compile(p, 0);
+    if (rc) return rc;
+  }
+  int64_t lo = 0, nm = s->batch;
+  if (member != -1) {
+    if (member < 0 || member >= s->batch) return bt_fail(ctx, BT_ERR_BAD_ARG, "member out of range");
+    lo = member;
+    nm = 1;
+  }
+  int rc = bt_cuda_check(ctx, cudaSetDevice(ctx->device), "cudaSetDevice");
+  for (size_t i = 0; i < p->passes.size() && !rc; ++i) {
+    PPass& ps = p->passes[i];
+    if (ps.kind == 1) {
+      const PGate& g = p->gates[ps.gate];
+      rc = bt_launch_gate(s, g.k, g.bits, g.m.data(), g.cmask, lo, nm, nullptr, 0);
+    } else if (p->prec == BT_PREC_C64) {
+      FusedArgs<float>& a = *reinterpret_cast<FusedArgs<float>*>(ps.args.data());
+      a.member_lo = lo;
+      a.nmem = nm;
+      rc = bt_launch_fused_f(ctx, s->d, a);
+    } else {
+      FusedArgs<double>& a = *reinterpret_cast<FusedArgs<double>*>(ps.args.data());
+      a.member_lo = lo;
+      a.nmem = nm;
+      rc = bt_launch_fused_d(ctx, s->d, a);
+    }
+  }
+  return rc;
+}
+
+}  // extern "C"

@@ -305,8 +305,11 @@ __global__ void __launch_bounds__(BT_THREADS) k_bitsums(const typename CT<R>::T*
       lanetot += csum;
 #pragma unroll
       for (int b = 0; b < 5; ++b) acc[1 + 5 + b] += jb[b];
-      for (int b = 10; b < nsys; ++b)
-        if (((uint64_t)c << 10 >> b) & 1) acc[1 + b] += csum;
+      // compile-time accumulator indices (a run-time index would spill acc[] to
+      // local memory); bits at or above nsys are never set in the chunk index
+      const uint64_t hi = (uint64_t)c << 10;
+#pragma unroll
+      for (int b = 10; b < BS_W - 1; ++b) acc[1 + b] += ((hi >> b) & 1) ? csum : 0.0;
     }
     acc[0] += lanetot;
 #pragma unroll
@@ -317,8 +320,8 @@ __global__ void __launch_bounds__(BT_THREADS) k_bitsums(const typename CT<R>::T*
       typename CT<R>::T v = dm ? s[(uint64_t)i + ((uint64_t)i << nsys)] : s[i];
       double p = dm ? (double)v.x : (double)v.x * v.x + (double)v.y * v.y;
       acc[0] += p;
-      for (int b = 0; b < nsys; ++b)
-        if ((i >> b) & 1) acc[1 + b] += p;
+#pragma unroll
+      for (int b = 0; b < 10; ++b) acc[1 + b] += ((i >> b) & 1) ? p : 0.0;
     }
   }
   block_sum_store<BS_W>(acc, part + ((int64_t)blockIdx.y * nblk + blockIdx.x) * BS_W, BS_W);

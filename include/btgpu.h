@@ -133,6 +133,25 @@ int bt_measure_z(bt_state* s, int qubit, const double* uniforms, const int32_t* 
  * (src/linalg.jl:83-230); out is a column-major 2^k x 2^k complex matrix */
 int bt_reduced_dm(const bt_state* s, int k, const int32_t* qubits, int64_t member, double* out);
 
+/* ------------------------------------------------------------------- plans */
+/* A plan is a circuit of dense gates compiled once and run many times: the
+ * gate-fusion pass of the circuit compiler (the role of compile/get_layers,
+ * src/ops.jl:278-329, :421-445).  Each fused pass applies every gate acting
+ * inside a 13-bit (complex64) / 12-bit (complex128) tile in one HBM round trip;
+ * the result equals applying the gates one by one (bt_apply_matrix). */
+int bt_plan_create(bt_ctx* ctx, int n, int repr, int prec, bt_plan** out);
+int bt_plan_free(bt_plan* p);
+/* appends op.expand(N) (state) or e_op*rho*e_op' (density), as bt_apply_matrix */
+int bt_plan_add_matrix(bt_plan* p, int k, const int32_t* qubits, const double* mat, int nctrl,
+                       const int32_t* ctrls);
+/* appends rho <- sum_i K_i rho K_i^dagger (density plans, k <= 2; src/struct.jl:58-76) */
+int bt_plan_add_kraus_sum(bt_plan* p, int k, const int32_t* qubits, int nk, const double* kraus);
+/* mode 0: fused passes; mode 1: one sweep per gate (the unfused reference form) */
+int bt_plan_compile(bt_plan* p, int mode);
+int bt_plan_stats(const bt_plan* p, int64_t* ngates, int64_t* npasses, int64_t* nfused, int64_t* nphases);
+/* runs the plan on member `member` (-1: every member) of a state of the same n/repr/prec */
+int bt_plan_run(bt_plan* p, bt_state* s, int64_t member);
+
 /* ---------------------------------------------------------------- sampling */
 /* sample(psi, shots) (src/ops.jl:46-62): per shot t = u*sum|psi|^2, outcome =
  * first index with cumsum >= t.  uniforms (shots values) or NULL for on-device

@@ -1,0 +1,142 @@
+"""Fused plans (bt_plan_*): the fused tile passes apply the same map as the gates
+one by one.  Checked against the oracle on state vectors and density matrices,
+both precisions, batched members, and mixes with gates the tile cannot hold."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def rstate(rng, n):
+    v = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
+    return v / np.linalg.norm(v)
+
+
+def runitary(rng, d):
+    z = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    q, r = np.linalg.qr(z)
+    return q * (np.diag(r) / np.abs(np.diag(r)))
+
+
+def oracle_op(oracle, psi, op):
+    ctrls = [op.control] if op.control != -2 else []
+    qs = [op.qubit] if op.q == 1 else [op.qubit, op.target_qubit]
+    return oracle.apply_k(psi, op.mat, qs, ctrls)
+
+
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-12), ("c64", 5e-5)])
+@pytest.mark.parametrize("n", [12, 13, 16])
+def test_plan_brickwork_matches_oracle(ctx, oracle, prec, tol, n):
+    import bluetangle_gpu as bt
+    import bluetangle_gpu.circuits as C
+    rng = np.random.default_rng(100 + n)
+    ops = C.brickwork(n, 12, rng)
+    plan = bt.plan_from_ops(ops, n, prec=prec)
+    st = plan.stats()
+    assert st["gates"] == len(ops)
+    psi = rstate(rng, n)
+    s = bt.state_from(psi, prec)
+    plan.run(s)
+    ref = psi
+    for o in ops:
+        ref = oracle_op(oracle, ref, o)
+    assert np.abs(s.to_numpy() - ref).max() < tol
+    if n >= (13 if prec == "c64" else 12):
+        assert st["fused_passes"] >= 1 and st["passes"] < len(ops) / 4
+
+
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-12), ("c64", 5e-5)])
+def test_plan_random_gates_controls_and_wide_gates(ctx, oracle, prec, tol):
+    """random one/two-qubit gates on arbitrary pairs, controlled gates (folded or
+    swept), three-qubit dense gates and Toffolis interleaved."""
+    import bluetangle_gpu as bt
+    rng = np.random.default_rng(7)
+    n = 15
+    plan = bt.Plan(n, prec=prec)
+    psi = rstate(rng, n)
+    ref = psi.copy()
+    for i in range(160):
+        kind = rng.integers(0, 7)
+        qs = [int(x) for x in rng.choice(np.arange(1, n + 1), size=4, replace=False)]
+        if kind <= 1:
+            U = runitary(rng, 2)
+            g = ([qs[0]], [])
+        elif kind == 2:
+            U = np.diag(np.exp(1j * rng.uniform(0, 6, 2)))
+            g = ([qs[0]], [])
+        elif kind == 3:
+            U = runitary(rng, 4)
+            g = (qs[:2], [])
+        elif kind == 4:
+            U = np.eye(4, dtype=complex)[[0, 1, 3, 2]] * np.exp(1j * rng.uniform(0, 6, 4))[:, None]
+            g = (qs[:2], [])
+        elif kind == 5:
+            U = runitary(rng, 2)
+            g = ([qs[0]], [qs[1]])
+        else:
+            if rng.random() < 0.5:
+                U = runitary(rng, 8)
+                g = (qs[:3], [])
+            else:
+                U = np.array([[0, 1], [1, 0]], dtype=complex)
+                g = ([qs[0]], qs[1:3])
+        plan.add_matrix(U, g[0], g[1])
+        ref = oracle.apply_k(ref, U, g[0], g[1])
+    plan.compile()
+    s = bt.state_from(psi, prec)
+    plan.run(s)
+    assert np.abs(s.to_numpy() - ref).max() < tol * 3
+    # unfused compilation of the same plan gives the same state
+    plan.compile(fused=False)
+    s2 = bt.state_from(psi, prec)
+    plan.run(s2)
+    assert np.abs(s2.to_numpy() - ref).max() < tol * 3
+
+
+def test_plan_batched_members(ctx, oracle):
+    import bluetangle_gpu as bt
+    import bluetangle_gpu.circuits as C
+    rng = np.random.default_rng(9)
+    n, B = 14, 6
+    ops = C.tfim_trotter(n, 5, 0.05, 1.0, rng.uniform(0.5, 1.5, n))
+    plan = bt.plan_from_ops(ops, n, prec="c128")
+    st = bt.zero_state(n, "c128", batch=B)
+    psis = [rstate(rng, n) for _ in range(B)]
+    for m, p in enumerate(psis):
+        st.upload(p, m)
+    plan.run(st)
+    plan.run(st, member=3)
+    for m, p in enumerate(psis):
+        ref = p
+        for rep in range(2 if m == 3 else 1):
+            for o in ops:
+                ref = oracle_op(oracle, ref, o)
+        assert np.abs(st.to_numpy(m) - ref).max() < 1e-12
+
+
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-12), ("c64", 5e-5)])
+def test_plan_density_matrix_noisy(ctx, oracle, prec, tol):
+    """density-matrix plan: gates become row/column passes and Kraus sums become
+    superoperators, fused over the 2n bits of vec(rho)."""
+    import bluetangle_gpu as bt
+    import bluetangle_gpu.circuits as C
+    rng = np.random.default_rng(11)
+    n = 7
+    ops = C.noisy_brickwork_dm(n, 4, rng)
+    plan = bt.plan_from_ops(ops, n, repr="dm", prec=prec)
+    assert plan.stats()["fused_passes"] >= 1
+    rho = bt.zero_rho(n, prec)
+    plan.run(rho)
+    ref = np.zeros((2 ** n, 2 ** n), complex)
+    ref[0, 0] = 1
+    for o in ops:
+        if isinstance(o, bt.OpQC):
+            ref = oracle.dm_channel(ref, o.kraus, o.qubit, o.target_qubit if o.q == 2 else -1)
+        elif o.q == 1:
+            ref = oracle.dm_hilbert1(ref, o.mat, o.qubit)
+        else:
+            ref = oracle.dm_hilbert2(ref, o.mat, o.qubit, o.target_qubit)
+    assert np.abs(rho.to_numpy() - ref).max() < tol
+    # the per-op path gives the same density matrix
+    rho2 = bt.apply(ops, bt.zero_rho(n, prec))
+    assert np.abs(rho2.to_numpy() - ref).max() < tol

@@ -43,7 +43,7 @@ def parse():
     ap.add_argument("--n", type=int, default=33)
     ap.add_argument("--depth", type=int, default=30)
     ap.add_argument("--prec", default="c64", choices=["c64", "c128"])
-    ap.add_argument("--mode", default="fused2", choices=["unfused", "fused2"])
+    ap.add_argument("--mode", default="plan", choices=["unfused", "fused2", "plan"])
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--cpu-n", type=int, default=24, help="qubits of the CPU baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -235,6 +235,15 @@ def run_ours(args):
     progs = [layer_program(l, args.mode) for l in layers]
     st = bt.zero_state(args.n, args.prec, 1, ctx)
     lib = bt.lib()
+    plan = None
+    if args.mode == "plan":
+        # the whole circuit compiled once into fused tile passes; a step runs all of it
+        plan = bt.Plan(args.n, "sv", args.prec, ctx)
+        for prog, _ in [layer_program(l, "unfused") for l in layers]:
+            for m, qs in prog:
+                plan.add_matrix(m, qs)
+        plan.compile(True)
+        pstats = plan.stats()
     # pre-packed column-major matrices and qubit arrays (the circuit is resident on the host)
     packed = []
     for prog, logical in progs:
@@ -248,6 +257,9 @@ def run_ours(args):
     P = ctypes.c_void_p
 
     def step(i):
+        if plan is not None:
+            plan.run(st)
+            return sum(lg for _, lg in packed), pstats["passes"]
         pk, logical = packed[i % len(packed)]
         for M, Q in pk:
             rc = lib.bt_apply_matrix(st.h, len(Q), Q.ctypes.data_as(P), M.ctypes.data_as(P), 0, None, -1)
@@ -295,20 +307,27 @@ def run_ours(args):
     # end to end through the public API: per step the layer's matrices go from host
     # memory into the launches, and <Z_i> for every qubit comes back to the host
     zout = np.empty(args.n, dtype=np.float64)
-    e2e_steps = max(3, args.steps // 2)
+    e2e_steps = max(3, args.steps // 2) if plan is None else max(2, args.steps // 3)
     h2d = 0
     t0 = time.perf_counter()
     for i in range(e2e_steps):
-        pk, _ = packed[i % len(packed)]
-        for M, Q in pk:
-            rc = lib.bt_apply_matrix(st.h, len(Q), Q.ctypes.data_as(P), M.ctypes.data_as(P), 0, None, -1)
-            if rc:
-                ctx.check(rc)
-            h2d += M.nbytes + Q.nbytes
+        if plan is not None:
+            ctx.check(lib.bt_plan_run(plan.h, st.h, -1))
+            h2d += sum(M.nbytes + Q.nbytes for pk, _ in packed for M, Q in pk)
+        else:
+            pk, _ = packed[i % len(packed)]
+            for M, Q in pk:
+                rc = lib.bt_apply_matrix(st.h, len(Q), Q.ctypes.data_as(P), M.ctypes.data_as(P), 0, None, -1)
+                if rc:
+                    ctx.check(rc)
+                h2d += M.nbytes + Q.nbytes
         ctx.check(lib.bt_expect_z_all(st.h, 0, zout.ctypes.data_as(P)))
     e2e_dt = time.perf_counter() - t0
     e2e_dt = max_over_ranks(dist, e2e_dt)
-    e2e_logical = sum(packed[i % len(packed)][1] for i in range(e2e_steps))
+    if plan is not None:
+        e2e_logical = e2e_steps * sum(lg for _, lg in packed)
+    else:
+        e2e_logical = sum(packed[i % len(packed)][1] for i in range(e2e_steps))
     e2e = {"value": e2e_logical * ws / e2e_dt, "unit": METRIC, "h2d_bytes_per_step": h2d // e2e_steps,
            "d2h_bytes_per_step": zout.nbytes, "readout": "<Z_i> for all qubits each step"}
     assert np.all(np.isfinite(zout))
@@ -321,13 +340,17 @@ def run_ours(args):
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": args.prec, "data": "synthetic",
                 "config": {"workload": f"brickwork-{args.n}q-{args.prec}-depth{args.depth}", "mode": args.mode,
-                           "step": "one brickwork layer (logical gates: n one-qubit + CNOTs)",
+                           "step": ("the whole depth-%d circuit (%d logical gates) as fused tile passes"
+                                    % (args.depth, sum(lg for _, lg in packed))) if plan is not None else
+                                   "one brickwork layer (logical gates: n one-qubit + CNOTs)",
+                           "plan": pstats if plan is not None else None,
                            "passes_per_step": passes / args.steps, "global_batch": 1, "seq_len": None,
                            "parallelism": f"replicas x{ws}", "l2": "state larger than L2, no flush needed",
                            "state_bytes": (2 ** args.n) * esize},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-                             "kernel": "k_gate (dense sweep)", "bytes_per_launch": bytes_per_launch,
+                             "kernel": "k_fused (tile pass)" if plan is not None else "k_gate (dense sweep)",
+                             "bytes_per_launch": bytes_per_launch,
                              "launches": launches},
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
                 "host_s": host_dt}

@@ -59,9 +59,9 @@ def tfim_trotter(n, steps, dt, J, h):
     ops = []
     for _ in range(steps):
         for q in range(1, n):
-            ops.append(Op(f"RZZ({2 * J * dt!r})", q, q + 1))
+            ops.append(Op(f"RZZ({float(2 * J * dt)!r})", q, q + 1))
         for q in range(1, n + 1):
-            ops.append(Op(f"RX({2 * h[q - 1] * dt!r})", q))
+            ops.append(Op(f"RX({float(2 * h[q - 1] * dt)!r})", q))
     return ops
 
 

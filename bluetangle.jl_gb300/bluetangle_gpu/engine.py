@@ -467,9 +467,9 @@ class Plan:
         return self
 
     def stats(self):
-        v = [ctypes.c_int64(0) for _ in range(4)]
+        v = [ctypes.c_int64(0) for _ in range(5)]
         self.ctx.check(L.lib().bt_plan_stats(self.h, *[ctypes.byref(x) for x in v]))
-        return dict(zip(("gates", "passes", "fused_passes", "phases"), (x.value for x in v)))
+        return dict(zip(("gates", "passes", "fused_passes", "phases", "jit_passes"), (x.value for x in v)))
 
     def run(self, state, member=-1):
         self.ctx.check(L.lib().bt_plan_run(self.h, state.h, member))

@@ -136,7 +136,98 @@ __device__ __forceinline__ void op_p2(R (&xr)[1 << NB], R (&xi)[1 << NB], const 
   }
 }
 
-#define BT_PAIRS(X)                                                                                       \
+// CNOT with control register bit BC and target BT: swap the pair where the control is 1
+template <typename R, int NB, int BC, int BT>
+__device__ __forceinline__ void op_cx(R (&xr)[1 << NB], R (&xi)[1 << NB]) {
+  if constexpr (BC < NB && BT < NB && BC != BT) {
+#pragma unroll
+    for (int j = 0; j < (1 << NB); ++j) {
+      if (!(j & (1 << BC)) || (j & (1 << BT))) continue;
+      const int k = j | (1 << BT);
+      const R tr = xr[j], ti = xi[j];
+      xr[j] = xr[k];
+      xi[j] = xi[k];
+      xr[k] = tr;
+      xi[k] = ti;
+    }
+  }
+}
+
+template <typename R, int NB, int B0, int B1>
+__device__ __forceinline__ void op_sw(R (&xr)[1 << NB], R (&xi)[1 << NB]) {
+  if constexpr (B0 < NB && B1 < NB && B0 != B1) {
+#pragma unroll
+    for (int j = 0; j < (1 << NB); ++j) {
+      if (!(j & (1 << B0)) || (j & (1 << B1))) continue;
+      const int k = (j & ~(1 << B0)) | (1 << B1);
+      const R tr = xr[j], ti = xi[j];
+      xr[j] = xr[k];
+      xi[j] = xi[k];
+      xr[k] = tr;
+      xi[k] = ti;
+    }
+  }
+}
+
+// out0 = p0 * in1, out1 = p1 * in0
+template <typename R, int NB, int B>
+__device__ __forceinline__ void op_x1(R (&xr)[1 << NB], R (&xi)[1 << NB], const R* __restrict__ m, int unit) {
+  if constexpr (B < NB) {
+    const R p0r = m[0], p0i = m[1], p1r = m[2], p1i = m[3];
+#pragma unroll
+    for (int j = 0; j < (1 << NB); ++j) {
+      if (j & (1 << B)) continue;
+      const int k = j | (1 << B);
+      const R ar = xr[j], ai = xi[j], br = xr[k], bi = xi[k];
+      if (unit) {
+        xr[j] = br; xi[j] = bi; xr[k] = ar; xi[k] = ai;
+      } else {
+        xr[j] = fma(p0r, br, -p0i * bi);
+        xi[j] = fma(p0r, bi, p0i * br);
+        xr[k] = fma(p1r, ar, -p1i * ai);
+        xi[k] = fma(p1r, ai, p1i * ar);
+      }
+    }
+  }
+}
+
+// real 2x2 matrix [[a, b], [c, d]]
+template <typename R, int NB, int B>
+__device__ __forceinline__ void op_r1(R (&xr)[1 << NB], R (&xi)[1 << NB], const R* __restrict__ m) {
+  if constexpr (B < NB) {
+    const R a = m[0], b = m[1], c = m[2], d = m[3];
+#pragma unroll
+    for (int j = 0; j < (1 << NB); ++j) {
+      if (j & (1 << B)) continue;
+      const int k = j | (1 << B);
+      const R ar = xr[j], ai = xi[j], br = xr[k], bi = xi[k];
+      xr[j] = fma(a, ar, b * br);
+      xi[j] = fma(a, ai, b * bi);
+      xr[k] = fma(c, ar, d * br);
+      xi[k] = fma(c, ai, d * bi);
+    }
+  }
+}
+
+// [[a, i b], [i b, a]]: out0 = a in0 + i b in1, out1 = i b in0 + a in1
+template <typename R, int NB, int B>
+__device__ __forceinline__ void op_rx1(R (&xr)[1 << NB], R (&xi)[1 << NB], const R* __restrict__ m) {
+  if constexpr (B < NB) {
+    const R a = m[0], b = m[1];
+#pragma unroll
+    for (int j = 0; j < (1 << NB); ++j) {
+      if (j & (1 << B)) continue;
+      const int k = j | (1 << B);
+      const R ar = xr[j], ai = xi[j], br = xr[k], bi = xi[k];
+      xr[j] = fma(a, ar, -b * bi);
+      xi[j] = fma(a, ai, b * br);
+      xr[k] = fma(a, br, -b * ai);
+      xi[k] = fma(a, bi, b * ar);
+    }
+  }
+}
+
+#define BT_PAIRS(X)                                                                                     \
   X(0, 1) X(0, 2) X(0, 3) X(0, 4) X(1, 0) X(1, 2) X(1, 3) X(1, 4) X(2, 0) X(2, 1) X(2, 3) X(2, 4) X(3, 0) \
   X(3, 1) X(3, 2) X(3, 4) X(4, 0) X(4, 1) X(4, 2) X(4, 3)
 
@@ -183,14 +274,44 @@ __device__ __forceinline__ void apply_op(R (&xr)[1 << NB], R (&xi)[1 << NB], con
 #undef X
       }
       break;
+    case FOP_CX:
+      switch (o.b0 * 8 + o.b1) {
+#define X(a, b) case a * 8 + b: op_cx<R, NB, a, b>(xr, xi); break;
+        BT_PAIRS(X)
+#undef X
+      }
+      break;
+    case FOP_SW:
+      switch (o.b0 * 8 + o.b1) {
+#define X(a, b) case a * 8 + b: op_sw<R, NB, a, b>(xr, xi); break;
+        BT_PAIRS(X)
+#undef X
+      }
+      break;
+#define ONE(FN, ...)                             \
+  switch (o.b0) {                                \
+    case 0: FN<R, NB, 0>(xr, xi, ##__VA_ARGS__); break; \
+    case 1: FN<R, NB, 1>(xr, xi, ##__VA_ARGS__); break; \
+    case 2: FN<R, NB, 2>(xr, xi, ##__VA_ARGS__); break; \
+    case 3: FN<R, NB, 3>(xr, xi, ##__VA_ARGS__); break; \
+    case 4: FN<R, NB, 4>(xr, xi, ##__VA_ARGS__); break; \
+  }
+    case FOP_X1: ONE(op_x1, m, o.unit) break;
+    case FOP_R1: ONE(op_r1, m) break;
+    case FOP_RX1: ONE(op_rx1, m) break;
+#undef ONE
   }
 }
 
+// offsets of the 2^NB register amplitudes: off[j] = XOR of s[b] over the set bits b
+// of j.  The swizzle is XOR-linear on disjoint bit sets (swz(a|b) = swz(a)^swz(b)),
+// so with s[b] = swz(1 << reg[b]) the shared-memory index of amplitude j is
+// swz(lbase) ^ off[j]: one XOR per access.
 template <typename R, int NB, int J>
 struct Offs {
   static __device__ __forceinline__ void fill(int (&off)[1 << NB], const int (&s)[NB]) {
     if constexpr (J < (1 << NB)) {
-      off[J] = off[J & (J - 1)] + s[LowBit<J>::v];
+      off[J] = off[J & (J - 1)] ^ s[LowBit<J>::v];
       Offs<R, NB, J + 1>::fill(off, s);
     }
   }
@@ -225,16 +346,24 @@ __global__ void __launch_bounds__(BT_TILE_THREADS, 2) k_fused(typename CT<R>::T*
       base = ((base >> p) << (p + 1)) | (base & ((1ULL << p) - 1));
     }
     C2* g = psi + (mem << a.nbits) + base;
-#pragma unroll 4
-    for (int q = threadIdx.x; q < NCHUNK; q += BT_TILE_THREADS) {
-      const int l = q * V;
-      const C2* src = g + runoff[l >> c] + (l & cmask);
-      if constexpr (V == 2) {
-        const float4 v = *reinterpret_cast<const float4*>(src);
-        tile[swz<R>(l)] = make_float2(v.x, v.y);
-        tile[swz<R>(l + 1)] = make_float2(v.z, v.w);
-      } else {
-        tile[swz<R>(l)] = *src;
+    // every 16-byte load of the tile in flight at once (NPT per thread), then to smem
+    constexpr int NPT = NCHUNK / BT_TILE_THREADS;
+    {
+      float4 buf[NPT];
+#pragma unroll
+      for (int i = 0; i < NPT; ++i) {
+        const int l = (threadIdx.x + i * BT_TILE_THREADS) * V;
+        buf[i] = __ldcs(reinterpret_cast<const float4*>(g + runoff[l >> c] + (l & cmask)));
+      }
+#pragma unroll
+      for (int i = 0; i < NPT; ++i) {
+        const int l = (threadIdx.x + i * BT_TILE_THREADS) * V;
+        if constexpr (V == 2) {
+          tile[swz<R>(l)] = make_float2(buf[i].x, buf[i].y);
+          tile[swz<R>(l + 1)] = make_float2(buf[i].z, buf[i].w);
+        } else {
+          *reinterpret_cast<float4*>(&tile[swz<R>(l)]) = buf[i];
+        }
       }
     }
     __syncthreads();
@@ -245,7 +374,7 @@ __global__ void __launch_bounds__(BT_TILE_THREADS, 2) k_fused(typename CT<R>::T*
 #pragma unroll
       for (int b = 0; b < NB; ++b) {
         regmask |= 1u << ph.reg[b];
-        s[b] = 1 << ph.reg[b];
+        s[b] = swz<R>(1 << ph.reg[b]);
       }
       int lbase = 0;
       {
@@ -257,35 +386,53 @@ __global__ void __launch_bounds__(BT_TILE_THREADS, 2) k_fused(typename CT<R>::T*
             ++nb;
           }
       }
-      int off[1 << NB];
-      off[0] = 0;
-      Offs<R, NB, 1>::fill(off, s);
+      const int sbase = swz<R>(lbase);
       R xr[1 << NB], xi[1 << NB];
+      {
+        int off[1 << NB];
+        off[0] = 0;
+        Offs<R, NB, 1>::fill(off, s);
 #pragma unroll
-      for (int j = 0; j < (1 << NB); ++j) {
-        const C2 v = tile[swz<R>(lbase | off[j])];
-        xr[j] = v.x;
-        xi[j] = v.y;
+        for (int j = 0; j < (1 << NB); ++j) {
+          const C2 v = tile[sbase ^ off[j]];
+          xr[j] = v.x;
+          xi[j] = v.y;
+        }
       }
       for (int o = ph.op0; o < ph.op0 + ph.nop; ++o) apply_op<R, NB>(xr, xi, a.op[o], a.mat);
+      // the offsets are recomputed rather than kept live across the op loop
 #pragma unroll
-      for (int j = 0; j < (1 << NB); ++j) {
-        C2 v;
-        v.x = xr[j];
-        v.y = xi[j];
-        tile[swz<R>(lbase | off[j])] = v;
+      for (int b = 0; b < NB; ++b) asm volatile("" : "+r"(s[b]));
+      {
+        int off[1 << NB];
+        off[0] = 0;
+        Offs<R, NB, 1>::fill(off, s);
+#pragma unroll
+        for (int j = 0; j < (1 << NB); ++j) {
+          C2 v;
+          v.x = xr[j];
+          v.y = xi[j];
+          tile[sbase ^ off[j]] = v;
+        }
       }
       __syncthreads();
     }
-#pragma unroll 4
-    for (int q = threadIdx.x; q < NCHUNK; q += BT_TILE_THREADS) {
-      const int l = q * V;
-      C2* dst = g + runoff[l >> c] + (l & cmask);
-      if constexpr (V == 2) {
-        const C2 v0 = tile[swz<R>(l)], v1 = tile[swz<R>(l + 1)];
-        *reinterpret_cast<float4*>(dst) = make_float4(v0.x, v0.y, v1.x, v1.y);
-      } else {
-        *dst = tile[swz<R>(l)];
+    {
+      float4 buf[NPT];
+#pragma unroll
+      for (int i = 0; i < NPT; ++i) {
+        const int l = (threadIdx.x + i * BT_TILE_THREADS) * V;
+        if constexpr (V == 2) {
+          const C2 v0 = tile[swz<R>(l)], v1 = tile[swz<R>(l + 1)];
+          buf[i] = make_float4(v0.x, v0.y, v1.x, v1.y);
+        } else {
+          buf[i] = *reinterpret_cast<const float4*>(&tile[swz<R>(l)]);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < NPT; ++i) {
+        const int l = (threadIdx.x + i * BT_TILE_THREADS) * V;
+        __stcs(reinterpret_cast<float4*>(g + runoff[l >> c] + (l & cmask)), buf[i]);
       }
     }
     __syncthreads();

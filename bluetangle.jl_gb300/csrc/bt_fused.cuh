@@ -22,6 +22,11 @@ enum {
   FOP_G2 = 3,  // general 4x4 on (b0 = high bit, b1 = low bit) (32 reals)
   FOP_D2 = 4,  // diagonal 4x4 (8 reals)
   FOP_P2 = 5,  // monomial 4x4: out[r] = ph[r] * in[perm[r]]; perm packed in flags, phases 8 reals
+  FOP_CX = 6,  // CNOT, control register bit b0, target b1 (register renaming, no arithmetic)
+  FOP_SW = 7,  // SWAP of register bits b0, b1
+  FOP_X1 = 8,  // anti-diagonal 2x2: out0 = p0*in1, out1 = p1*in0 (4 reals); unit: plain swap
+  FOP_R1 = 9,  // real 2x2 (4 reals): H, RY, ...
+  FOP_RX1 = 10,  // [[a, ib], [ib, a]] with a, b real (2 reals): RX
 };
 
 struct FOp {

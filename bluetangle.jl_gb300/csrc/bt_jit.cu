@@ -1,0 +1,534 @@
+// Plan specialisation: each distinct fused-pass structure (tile bits, register
+// sets of its phases, op types and register bits) becomes its own kernel with the
+// whole op sequence as straight-line scalar code, compiled at plan-compile time
+// with NVRTC for sm_103a.  Register indices, swaps and shared-memory offsets are
+// then compile-time constants and no register is shuffled between ops (in the
+// generic k_fused the runtime op switch costs several register moves per
+// amplitude per gate).  Matrix entries stay in the kernel parameters at fixed
+// offsets, so passes that differ only in angles share one kernel.
+//
+// The generator emits already-expanded code (no templates or loops for the
+// compiler to unroll), kernels are compiled in parallel batches, and cubins are
+// cached on disk by a hash of their source.  NVRTC is loaded with dlopen: without
+// it plans run on the generic k_fused kernel.
+#include <dlfcn.h>
+#include <stdio.h>
+#include <string.h>
+#include <sys/stat.h>
+
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "bt_fused.cuh"
+#include "bt_jit.cuh"
+
+// ------------------------------------------------------------------ NVRTC by dlopen
+typedef int nvrtcResult_t;
+typedef struct _nvrtcProgram* nvrtcProgram_t;
+struct Nvrtc {
+  bool ok = false;
+  nvrtcResult_t (*create)(nvrtcProgram_t*, const char*, const char*, int, const char* const*, const char* const*);
+  nvrtcResult_t (*compile)(nvrtcProgram_t, int, const char* const*);
+  nvrtcResult_t (*cubin_size)(nvrtcProgram_t, size_t*);
+  nvrtcResult_t (*cubin)(nvrtcProgram_t, char*);
+  nvrtcResult_t (*log_size)(nvrtcProgram_t, size_t*);
+  nvrtcResult_t (*log)(nvrtcProgram_t, char*);
+  nvrtcResult_t (*destroy)(nvrtcProgram_t*);
+};
+
+static Nvrtc* nvrtc() {
+  static Nvrtc n;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    const char* names[] = {"libnvrtc.so", "libnvrtc.so.13", "/usr/local/cuda/lib64/libnvrtc.so"};
+    void* h = nullptr;
+    for (const char* nm : names)
+      if ((h = dlopen(nm, RTLD_NOW | RTLD_LOCAL))) break;
+    if (!h) return;
+    n.create = (decltype(n.create))dlsym(h, "nvrtcCreateProgram");
+    n.compile = (decltype(n.compile))dlsym(h, "nvrtcCompileProgram");
+    n.cubin_size = (decltype(n.cubin_size))dlsym(h, "nvrtcGetCUBINSize");
+    n.cubin = (decltype(n.cubin))dlsym(h, "nvrtcGetCUBIN");
+    n.log_size = (decltype(n.log_size))dlsym(h, "nvrtcGetProgramLogSize");
+    n.log = (decltype(n.log))dlsym(h, "nvrtcGetProgramLog");
+    n.destroy = (decltype(n.destroy))dlsym(h, "nvrtcDestroyProgram");
+    n.ok = n.create && n.compile && n.cubin_size && n.cubin && n.log_size && n.log && n.destroy;
+  });
+  return n.ok ? &n : nullptr;
+}
+
+bool bt_jit_available() { return nvrtc() != nullptr && getenv("BTGPU_NO_JIT") == nullptr; }
+
+// ------------------------------------------------------------------ generated source
+static const char* kPrelude = R"PRELUDE(
+typedef long long i64;
+typedef unsigned long long u64;
+struct __align__(8) cf { float x, y; };
+struct __align__(16) cd { double x, y; };
+struct __align__(16) f4 { float x, y, z, w; };
+__device__ __forceinline__ float fm(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fm(double a, double b, double c) { return __fma_rn(a, b, c); }
+template <int NM> struct JitArgsF { i64 member_lo, nmem; int nbits, lg_tiles; float mat[NM]; };
+template <int NM> struct JitArgsD { i64 member_lo, nmem; int nbits, lg_tiles; double mat[NM]; };
+)PRELUDE";
+
+static std::string fmt_u64(uint64_t v) {
+  char b[32];
+  snprintf(b, sizeof b, "%lluULL", (unsigned long long)v);
+  return b;
+}
+
+static int swz_host(bool f, int l) { return f ? (l ^ ((l >> 4) & 15)) : (l ^ ((l >> 3) & 7)); }
+
+// emits one op on the scalar registers x<j> (real) / y<j> (imaginary), j < 2^NB
+static void emit_op(std::ostringstream& o, const FOp& op, int NB) {
+  const int D = 1 << NB;
+  auto M = [&](int e) {
+    std::ostringstream s;
+    s << "a.mat[" << (op.moff + e) << "]";
+    return s.str();
+  };
+  auto pairs = [&](int B, auto&& body) {
+    for (int j = 0; j < D; ++j)
+      if (!(j & (1 << B))) body(j, j | (1 << B));
+  };
+  auto quads = [&](int B0, int B1, auto&& body) {
+    for (int j = 0; j < D; ++j)
+      if (!(j & ((1 << B0) | (1 << B1)))) {
+        const int q[4] = {j, j | (1 << B1), j | (1 << B0), j | (1 << B0) | (1 << B1)};
+        body(q);
+      }
+  };
+  const int b0 = op.b0, b1 = op.b1;
+  switch (op.type) {
+    case FOP_G1:
+      o << "    { const R m0=" << M(0) << ",m1=" << M(1) << ",m2=" << M(2) << ",m3=" << M(3) << ",m4=" << M(4)
+        << ",m5=" << M(5) << ",m6=" << M(6) << ",m7=" << M(7) << ";\n";
+      pairs(b0, [&](int j, int k) {
+        o << "      { const R ar=x" << j << ",ai=y" << j << ",br=x" << k << ",bi=y" << k << ";"
+          << " x" << j << "=fm(m0,ar,fm(-m1,ai,fm(m2,br,-m3*bi)));"
+          << " y" << j << "=fm(m0,ai,fm(m1,ar,fm(m2,bi,m3*br)));"
+          << " x" << k << "=fm(m4,ar,fm(-m5,ai,fm(m6,br,-m7*bi)));"
+          << " y" << k << "=fm(m4,ai,fm(m5,ar,fm(m6,bi,m7*br))); }\n";
+      });
+      o << "    }\n";
+      break;
+    case FOP_D1:
+      o << "    { const R d0r=" << M(0) << ",d0i=" << M(1) << ",d1r=" << M(2) << ",d1i=" << M(3) << ";\n";
+      for (int j = 0; j < D; ++j) {
+        const char* s = (j & (1 << b0)) ? "d1" : "d0";
+        o << "      { const R ar=x" << j << ",ai=y" << j << "; x" << j << "=fm(" << s << "r,ar,-" << s << "i*ai); y" << j
+          << "=fm(" << s << "r,ai," << s << "i*ar); }\n";
+      }
+      o << "    }\n";
+      break;
+    case FOP_R1:
+      o << "    { const R a0=" << M(0) << ",a1=" << M(1) << ",a2=" << M(2) << ",a3=" << M(3) << ";\n";
+      pairs(b0, [&](int j, int k) {
+        o << "      { const R ar=x" << j << ",ai=y" << j << ",br=x" << k << ",bi=y" << k << "; x" << j
+          << "=fm(a0,ar,a1*br); y" << j << "=fm(a0,ai,a1*bi); x" << k << "=fm(a2,ar,a3*br); y" << k
+          << "=fm(a2,ai,a3*bi); }\n";
+      });
+      o << "    }\n";
+      break;
+    case FOP_RX1:
+      o << "    { const R ca=" << M(0) << ",cb=" << M(1) << ";\n";
+      pairs(b0, [&](int j, int k) {
+        o << "      { const R ar=x" << j << ",ai=y" << j << ",br=x" << k << ",bi=y" << k << "; x" << j
+          << "=fm(ca,ar,-cb*bi); y" << j << "=fm(ca,ai,cb*br); x" << k << "=fm(ca,br,-cb*ai); y" << k
+          << "=fm(ca,bi,cb*ar); }\n";
+      });
+      o << "    }\n";
+      break;
+    case FOP_X1:
+      if (op.unit) {
+        pairs(b0, [&](int j, int k) {
+          o << "    { const R tr=x" << j << ",ti=y" << j << "; x" << j << "=x" << k << "; y" << j << "=y" << k << "; x" << k
+            << "=tr; y" << k << "=ti; }\n";
+        });
+      } else {
+        o << "    { const R p0r=" << M(0) << ",p0i=" << M(1) << ",p1r=" << M(2) << ",p1i=" << M(3) << ";\n";
+        pairs(b0, [&](int j, int k) {
+          o << "      { const R ar=x" << j << ",ai=y" << j << ",br=x" << k << ",bi=y" << k << "; x" << j
+            << "=fm(p0r,br,-p0i*bi); y" << j << "=fm(p0r,bi,p0i*br); x" << k << "=fm(p1r,ar,-p1i*ai); y" << k
+            << "=fm(p1r,ai,p1i*ar); }\n";
+        });
+        o << "    }\n";
+      }
+      break;
+    case FOP_D2:
+      o << "    { const R e0r=" << M(0) << ",e0i=" << M(1) << ",e1r=" << M(2) << ",e1i=" << M(3) << ",e2r=" << M(4)
+        << ",e2i=" << M(5) << ",e3r=" << M(6) << ",e3i=" << M(7) << ";\n";
+      for (int j = 0; j < D; ++j) {
+        const int r = ((j >> b0) & 1) * 2 + ((j >> b1) & 1);
+        o << "      { const R ar=x" << j << ",ai=y" << j << "; x" << j << "=fm(e" << r << "r,ar,-e" << r << "i*ai); y" << j
+          << "=fm(e" << r << "r,ai,e" << r << "i*ar); }\n";
+      }
+      o << "    }\n";
+      break;
+    case FOP_G2:
+      o << "    {";
+      for (int e = 0; e < 32; ++e) o << (e ? "," : " const R ") << "g" << e << "=" << M(e);
+      o << ";\n";
+      quads(b0, b1, [&](const int* q) {
+        o << "      { const R ";
+        for (int c = 0; c < 4; ++c) o << (c ? "," : "") << "r" << c << "=x" << q[c] << ",i" << c << "=y" << q[c];
+        o << ";";
+        for (int r = 0; r < 4; ++r) {
+          std::ostringstream re, im;
+          re << "0";
+          im << "0";
+          for (int c = 0; c < 4; ++c) {
+            re.str("fm(g" + std::to_string(8 * r + 2 * c) + ",r" + std::to_string(c) + ",fm(-g" +
+                   std::to_string(8 * r + 2 * c + 1) + ",i" + std::to_string(c) + "," + re.str() + "))");
+            im.str("fm(g" + std::to_string(8 * r + 2 * c) + ",i" + std::to_string(c) + ",fm(g" +
+                   std::to_string(8 * r + 2 * c + 1) + ",r" + std::to_string(c) + "," + im.str() + "))");
+          }
+          o << " x" << q[r] << "=" << re.str() << "; y" << q[r] << "=" << im.str() << ";";
+        }
+        o << " }\n";
+      });
+      o << "    }\n";
+      break;
+    case FOP_P2:
+    case FOP_CX:
+    case FOP_SW: {
+      int P[4];
+      bool unit = true;
+      if (op.type == FOP_CX) {  // control b0, target b1: rows 2 and 3 swap
+        P[0] = 0, P[1] = 1, P[2] = 3, P[3] = 2;
+      } else if (op.type == FOP_SW) {
+        P[0] = 0, P[1] = 2, P[2] = 1, P[3] = 3;
+      } else {
+        for (int r = 0; r < 4; ++r) P[r] = (op.flags >> (2 * r)) & 3;
+        unit = op.unit != 0;
+      }
+      o << "    {";
+      if (!unit)
+        for (int e = 0; e < 8; ++e) o << (e ? "," : " const R ") << "h" << e << "=" << M(e);
+      o << (unit ? "\n" : ";\n");
+      quads(b0, b1, [&](const int* q) {
+        o << "      { const R ";
+        for (int c = 0; c < 4; ++c) o << (c ? "," : "") << "r" << c << "=x" << q[c] << ",i" << c << "=y" << q[c];
+        o << ";";
+        for (int r = 0; r < 4; ++r) {
+          if (unit) {
+            o << " x" << q[r] << "=r" << P[r] << "; y" << q[r] << "=i" << P[r] << ";";
+          } else {
+            o << " x" << q[r] << "=fm(h" << 2 * r << ",r" << P[r] << ",-h" << 2 * r + 1 << "*i" << P[r] << "); y" << q[r]
+              << "=fm(h" << 2 * r << ",i" << P[r] << ",h" << 2 * r + 1 << "*r" << P[r] << ");";
+          }
+        }
+        o << " }\n";
+      });
+      o << "    }\n";
+      break;
+    }
+  }
+}
+
+template <typename R>
+static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, const std::string& name) {
+  const bool f = sizeof(R) == 4;
+  const int M = a.M, c = a.c, D = 1 << NB;
+  const int NM = f ? BT_FUSED_MAX_REALS_F : BT_FUSED_MAX_REALS_D;
+  const int V = f ? 2 : 1;
+  const int NPT = (1 << M) / V / BT_TILE_THREADS;
+  const char* T2 = f ? "cf" : "cd";
+  o << "extern \"C\" __global__ void __launch_bounds__(256, 2) " << name << "(" << T2 << "* __restrict__ psi, const "
+    << (f ? "JitArgsF<" : "JitArgsD<") << NM << "> a) {\n";
+  o << "  typedef " << (f ? "float" : "double") << " R;\n";
+  o << "  extern __shared__ __align__(16) unsigned char smem_raw[];\n";
+  o << "  " << T2 << "* tile = reinterpret_cast<" << T2 << "*>(smem_raw);\n";
+  o << "  i64* runoff = reinterpret_cast<i64*>(smem_raw + " << ((f ? 8 : 16) << M) << ");\n";
+  o << "  for (int r = threadIdx.x; r < " << (1 << (M - c)) << "; r += 256) { i64 v = 0;";
+  for (int b = 0; b < M - c; ++b) o << " v |= (i64)((r >> " << b << ") & 1) << " << a.tbits[c + b] << ";";
+  o << " runoff[r] = v; }\n  __syncthreads();\n";
+  o << "  const i64 per = 1LL << a.lg_tiles, total = per * a.nmem;\n";
+  o << "  for (i64 tid = blockIdx.x; tid < total; tid += gridDim.x) {\n";
+  o << "    const i64 mem = a.member_lo + (tid >> a.lg_tiles);\n    u64 base = (u64)(tid & (per - 1));\n";
+  for (int i = 0; i < M; ++i) {
+    const int p = a.tbits[i];
+    o << "    base = ((base >> " << p << ") << " << (p + 1) << ") | (base & " << fmt_u64((1ULL << p) - 1) << ");\n";
+  }
+  o << "    " << T2 << "* g = psi + (mem << a.nbits) + base;\n";
+  // tile load: every 16-byte load in flight, then into the swizzled tile
+  o << "    {\n";
+  for (int i = 0; i < NPT; ++i)
+    o << "      const int l" << i << " = (threadIdx.x + " << i * BT_TILE_THREADS << ") * " << V << "; const f4 b" << i
+      << " = *reinterpret_cast<const f4*>(g + runoff[l" << i << " >> " << c << "] + (l" << i << " & " << ((1 << c) - 1)
+      << "));\n";
+  for (int i = 0; i < NPT; ++i) {
+    if (f)
+      o << "      { const int s0 = l" << i << " ^ ((l" << i << " >> 4) & 15), s1 = (l" << i << " + 1) ^ (((l" << i
+        << " + 1) >> 4) & 15); tile[s0] = cf{b" << i << ".x, b" << i << ".y}; tile[s1] = cf{b" << i << ".z, b" << i
+        << ".w}; }\n";
+    else
+      o << "      *reinterpret_cast<f4*>(&tile[l" << i << " ^ ((l" << i << " >> 3) & 7)]) = b" << i << ";\n";
+  }
+  o << "    }\n    __syncthreads();\n";
+  for (int p = 0; p < a.nphase; ++p) {
+    const FPhase& ph = a.ph[p];
+    uint32_t regmask = 0;
+    for (int b = 0; b < NB; ++b) regmask |= 1u << ph.reg[b];
+    o << "    { // phase " << p << "\n    const int t = threadIdx.x; const int lb = 0";
+    int nb = 0;
+    for (int bit = 0; bit < M; ++bit)
+      if (!((regmask >> bit) & 1)) {
+        o << " | (((t >> " << nb << ") & 1) << " << bit << ")";
+        ++nb;
+      }
+    o << ";\n    const int sb = " << (f ? "lb ^ ((lb >> 4) & 15)" : "lb ^ ((lb >> 3) & 7)") << ";\n    R ";
+    for (int j = 0; j < D; ++j) o << (j ? ", " : "") << "x" << j << ", y" << j;
+    o << ";\n";
+    std::vector<int> offs(D);
+    for (int j = 0; j < D; ++j) {
+      int l = 0;
+      for (int b = 0; b < NB; ++b)
+        if ((j >> b) & 1) l |= 1 << ph.reg[b];
+      offs[j] = swz_host(f, l);  // the swizzle is XOR-linear: swz(lb | l) = swz(lb) ^ swz(l)
+    }
+    for (int j = 0; j < D; ++j)
+      o << "    { const " << T2 << " v = tile[sb ^ " << offs[j] << "]; x" << j << " = v.x; y" << j << " = v.y; }\n";
+    for (int oi = ph.op0; oi < ph.op0 + ph.nop; ++oi) emit_op(o, a.op[oi], NB);
+    for (int j = 0; j < D; ++j) o << "    tile[sb ^ " << offs[j] << "] = " << T2 << "{x" << j << ", y" << j << "};\n";
+    o << "    __syncthreads();\n    }\n";
+  }
+  o << "    {\n";
+  for (int i = 0; i < NPT; ++i) {
+    o << "      const int l" << i << " = (threadIdx.x + " << i * BT_TILE_THREADS << ") * " << V << ";";
+    if (f)
+      o << " const cf u" << i << " = tile[l" << i << " ^ ((l" << i << " >> 4) & 15)], v" << i << " = tile[(l" << i
+        << " + 1) ^ (((l" << i << " + 1) >> 4) & 15)]; const f4 b" << i << " = f4{u" << i << ".x, u" << i << ".y, v" << i
+        << ".x, v" << i << ".y};\n";
+    else
+      o << " const f4 b" << i << " = *reinterpret_cast<const f4*>(&tile[l" << i << " ^ ((l" << i << " >> 3) & 7)]);\n";
+  }
+  for (int i = 0; i < NPT; ++i)
+    o << "      *reinterpret_cast<f4*>(g + runoff[l" << i << " >> " << c << "] + (l" << i << " & " << ((1 << c) - 1)
+      << ")) = b" << i << ";\n";
+  o << "    }\n    __syncthreads();\n  }\n}\n";
+}
+
+// structure key: everything that shapes the code (not the matrix values)
+template <typename R>
+static std::string structure_key(const FusedArgs<R>& a) {
+  std::ostringstream k;
+  k << (sizeof(R) == 4 ? 'f' : 'd') << a.M << ':' << a.c << ':';
+  for (int i = 0; i < a.M; ++i) k << a.tbits[i] << ',';
+  for (int p = 0; p < a.nphase; ++p) {
+    const FPhase& ph = a.ph[p];
+    k << '|';
+    for (int b = 0; b < 5; ++b) k << (int)ph.reg[b] << '.';
+    for (int oi = ph.op0; oi < ph.op0 + ph.nop; ++oi) {
+      const FOp& op = a.op[oi];
+      k << (int)op.type << (int)op.b0 << (int)op.b1 << '_' << (int)op.flags << (int)op.unit << '@' << op.moff << ';';
+    }
+  }
+  return k.str();
+}
+
+// one NVRTC program (cubin) per compile batch; loaded as a CUDA library on first use
+struct JitModule {
+  std::vector<char> cubin;
+  cudaLibrary_t lib = nullptr;
+};
+struct JitEntry {
+  JitModule* mod = nullptr;
+  std::string name;
+  cudaKernel_t kernel = nullptr;
+  bool attr_set[64] = {false};
+};
+static std::mutex g_jit_mu;
+static std::map<std::string, JitEntry*> g_jit_cache;
+
+static uint64_t fnv1a(const std::string& s) {
+  uint64_t h = 1469598103934665603ULL;
+  for (unsigned char ch : s) h = (h ^ ch) * 1099511628211ULL;
+  return h;
+}
+
+static std::string cache_dir() {
+  const char* d = getenv("BTGPU_JIT_CACHE");
+  std::string dir;
+  if (d && *d) dir = d;
+  else {
+    const char* home = getenv("HOME");
+    dir = std::string(home && *home ? home : "/tmp") + "/.cache/btgpu_jit";
+  }
+  std::string acc;
+  for (size_t i = 0; i < dir.size(); ++i) {  // mkdir -p
+    acc += dir[i];
+    if (dir[i] == '/' || i + 1 == dir.size()) mkdir(acc.c_str(), 0755);
+  }
+  return dir;
+}
+
+static const char* kOpts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-default-device"};
+
+// compiles one source to a cubin (disk cache keyed by the source hash); "" on success
+static std::string compile_cubin(const std::string& code, std::vector<char>& cubin) {
+  const std::string path = cache_dir() + "/btk_" + std::to_string(fnv1a(code + kOpts[0])) + ".cubin";
+  if (FILE* fd = fopen(path.c_str(), "rb")) {
+    fseek(fd, 0, SEEK_END);
+    long sz = ftell(fd);
+    fseek(fd, 0, SEEK_SET);
+    cubin.resize(sz > 0 ? (size_t)sz : 0);
+    size_t got = sz > 0 ? fread(cubin.data(), 1, (size_t)sz, fd) : 0;
+    fclose(fd);
+    if (sz > 0 && got == (size_t)sz) return "";
+  }
+  Nvrtc* nv = nvrtc();
+  nvrtcProgram_t prog = nullptr;
+  if (nv->create(&prog, code.c_str(), "bt_plan_jit.cu", 0, nullptr, nullptr)) return "nvrtcCreateProgram failed";
+  if (nv->compile(prog, 3, kOpts)) {
+    size_t ls = 0;
+    nv->log_size(prog, &ls);
+    std::string log(ls, '\0');
+    nv->log(prog, &log[0]);
+    nv->destroy(&prog);
+    return "NVRTC compile of a plan failed: " + log.substr(0, 2000);
+  }
+  size_t cs = 0;
+  nv->cubin_size(prog, &cs);
+  cubin.resize(cs);
+  nv->cubin(prog, cubin.data());
+  nv->destroy(&prog);
+  const std::string tmp = path + ".tmp" + std::to_string((uint64_t)(uintptr_t)&cubin);
+  if (FILE* fd = fopen(tmp.c_str(), "wb")) {  // write-then-rename: concurrent processes never read a partial file
+    fwrite(cubin.data(), 1, cubin.size(), fd);
+    fclose(fd);
+    rename(tmp.c_str(), path.c_str());
+  }
+  return "";
+}
+
+template <typename R>
+static int jit_prepare_t(bt_ctx* ctx, std::vector<const FusedArgs<R>*>& passes, std::vector<void*>& out) {
+  out.assign(passes.size(), nullptr);
+  if (!nvrtc()) return bt_fail(ctx, BT_ERR_UNSUPPORTED, "NVRTC is not available");
+  std::lock_guard<std::mutex> lk(g_jit_mu);
+  std::vector<std::string> keys(passes.size());
+  std::vector<std::string> order;                     // new structures in first-seen order
+  std::map<std::string, const FusedArgs<R>*> first;
+  for (size_t i = 0; i < passes.size(); ++i) {
+    keys[i] = structure_key(*passes[i]);
+    if (!g_jit_cache.count(keys[i]) && !first.count(keys[i])) {
+      first[keys[i]] = passes[i];
+      order.push_back(keys[i]);
+    }
+  }
+  if (!order.empty()) {
+    const int NB = sizeof(R) == 4 ? BT_TILE_RB_C64 : BT_TILE_RB_C128;
+    // batches of kernels compiled concurrently (NVRTC programs are independent)
+    int hw = (int)std::thread::hardware_concurrency();
+    if (hw < 1) hw = 1;
+    const int nb = (int)std::min<size_t>(order.size(), (size_t)std::min(hw, 32));
+    std::vector<std::string> srcs(nb), errs(nb);
+    std::vector<std::vector<std::string>> names(nb), bkeys(nb);
+    for (int b = 0; b < nb; ++b) {
+      std::ostringstream src;
+      src << kPrelude;
+      for (size_t i = b; i < order.size(); i += nb) {
+        const std::string nm = "btk_" + std::to_string(i);
+        gen_kernel<R>(src, *first[order[i]], NB, nm);
+        names[b].push_back(nm);
+        bkeys[b].push_back(order[i]);
+      }
+      srcs[b] = src.str();
+    }
+    if (const char* dump = getenv("BTGPU_JIT_DUMP")) {  // debugging aid: the generated source of batch 0
+      if (FILE* fd = fopen(dump, "w")) {
+        fwrite(srcs[0].data(), 1, srcs[0].size(), fd);
+        fclose(fd);
+      }
+    }
+    std::vector<JitModule*> mods(nb);
+    std::vector<std::thread> th;
+    for (int b = 0; b < nb; ++b) {
+      mods[b] = new JitModule();
+      th.emplace_back([&, b] { errs[b] = compile_cubin(srcs[b], mods[b]->cubin); });
+    }
+    for (auto& t : th) t.join();
+    for (int b = 0; b < nb; ++b)
+      if (!errs[b].empty()) {
+        for (auto* m : mods) delete m;
+        return bt_fail(ctx, BT_ERR_DEVICE, errs[b]);
+      }
+    for (int b = 0; b < nb; ++b)
+      for (size_t i = 0; i < names[b].size(); ++i) {
+        JitEntry* je = new JitEntry();
+        je->mod = mods[b];
+        je->name = names[b][i];
+        g_jit_cache[bkeys[b][i]] = je;
+      }
+  }
+  for (size_t i = 0; i < passes.size(); ++i) out[i] = g_jit_cache[keys[i]];
+  return BT_OK;
+}
+
+int bt_jit_prepare_f(bt_ctx* ctx, std::vector<const FusedArgs<float>*>& passes, std::vector<void*>& out) {
+  return jit_prepare_t<float>(ctx, passes, out);
+}
+int bt_jit_prepare_d(bt_ctx* ctx, std::vector<const FusedArgs<double>*>& passes, std::vector<void*>& out) {
+  return jit_prepare_t<double>(ctx, passes, out);
+}
+
+// the generated kernels take (psi, JitArgs{member_lo, nmem, nbits, lg_tiles, mat[]})
+template <typename R>
+struct JitArgsHost {
+  int64_t member_lo, nmem;
+  int nbits, lg_tiles;
+  R mat[sizeof(R) == 4 ? BT_FUSED_MAX_REALS_F : BT_FUSED_MAX_REALS_D];
+};
+
+template <typename R>
+static int jit_launch_t(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<R>& a) {
+  JitEntry* je = (JitEntry*)entry;
+  typedef typename CT<R>::T C2;
+  const int M = a.M;
+  const size_t smem = (sizeof(C2) << M) + sizeof(int64_t) * (1 << (M - a.c));
+  if (!je->kernel) {  // first launch: load the batch's cubin and resolve the kernel
+    std::lock_guard<std::mutex> lk(g_jit_mu);
+    if (!je->mod->lib) {
+      cudaError_t e = cudaLibraryLoadData(&je->mod->lib, je->mod->cubin.data(), nullptr, nullptr, 0, nullptr,
+                                          nullptr, 0);
+      if (e != cudaSuccess) return bt_cuda_check(ctx, e, "cudaLibraryLoadData of a plan");
+    }
+    cudaKernel_t k = nullptr;
+    cudaError_t e = cudaLibraryGetKernel(&k, je->mod->lib, je->name.c_str());
+    if (e != cudaSuccess) return bt_cuda_check(ctx, e, "cudaLibraryGetKernel");
+    je->kernel = k;
+  }
+  if (ctx->device < 64 && !je->attr_set[ctx->device]) {
+    cudaError_t e = cudaKernelSetAttributeForDevice(je->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)smem, ctx->device);
+    if (e != cudaSuccess) return bt_cuda_check(ctx, e, "jit kernel smem attribute");
+    je->attr_set[ctx->device] = true;
+  }
+  static thread_local JitArgsHost<R> h;
+  h.member_lo = a.member_lo;
+  h.nmem = a.nmem;
+  h.nbits = a.nbits;
+  h.lg_tiles = a.lg_tiles;
+  memcpy(h.mat, a.mat, sizeof(h.mat));
+  void* args[] = {&psi, &h};
+  int64_t total = (1LL << a.lg_tiles) * a.nmem;
+  int64_t grid = (int64_t)ctx->sm_count * 2 * 4;
+  if (grid > total) grid = total;
+  cudaError_t e = cudaLaunchKernel((const void*)je->kernel, dim3((unsigned)grid), dim3(BT_TILE_THREADS), args, smem,
+                                   ctx->stream);
+  ctx->launches++;
+  return bt_cuda_check(ctx, e, "jit pass launch");
+}
+
+int bt_jit_launch_f(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<float>& a) {
+  return jit_launch_t<float>(ctx, entry, psi, a);
+}
+int bt_jit_launch_d(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<double>& a) {
+  return jit_launch_t<double>(ctx, entry, psi, a);
+}

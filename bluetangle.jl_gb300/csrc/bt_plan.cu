@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "bt_fused.cuh"
+#include "bt_jit.cuh"
 
 struct PGate {
   int k = 0;
@@ -40,6 +41,7 @@ struct PPass {
   int gate = -1;
   int ngates = 0;
   std::vector<unsigned char> args;  // FusedArgs<float> or <double>, bytes
+  void* jit = nullptr;              // specialised kernel of this pass (bt_jit.cu), if compiled
 };
 
 struct bt_plan {
@@ -49,6 +51,7 @@ struct bt_plan {
   std::vector<PPass> passes;
   bool compiled = false;
   int64_t nphases = 0;
+  int64_t njit = 0;
 };
 
 static int popc(uint64_t x) { return __builtin_popcountll(x); }
@@ -109,6 +112,17 @@ static int classify(const PGate& g, int* perm) {
     if (seen != (1 << d) - 1) mono = false;
   }
   return diag ? 2 : (mono ? 1 : 0);
+}
+
+// a monomial matrix whose non-zero entries are all exactly 1
+static bool classify_unit(const PGate& g) {
+  const int d = 1 << g.k;
+  for (int r = 0; r < d; ++r)
+    for (int c = 0; c < d; ++c) {
+      const double re = g.m[2 * (r * d + c)], im = g.m[2 * (r * d + c) + 1];
+      if (!(re == 0 && im == 0) && !(re == 1 && im == 0)) return false;
+    }
+  return true;
 }
 
 template <typename R>
@@ -185,17 +199,46 @@ static bool build_fused(bt_plan* p, const std::vector<int>& take, uint64_t tilem
     int perm[4] = {0, 1, 2, 3};
     const int cls = classify(g, perm);
     o.moff = (uint16_t)w;
+    const double* m = g.m.data();
     if (g.k == 1) {
+      // m = [m00r m00i m01r m01i m10r m10i m11r m11i]
+      const bool real = m[1] == 0 && m[3] == 0 && m[5] == 0 && m[7] == 0;
       if (cls == 2) {
         o.type = FOP_D1;
-        a.mat[w++] = (R)g.m[0];
-        a.mat[w++] = (R)g.m[1];
-        a.mat[w++] = (R)g.m[6];
-        a.mat[w++] = (R)g.m[7];
+        a.mat[w++] = (R)m[0];
+        a.mat[w++] = (R)m[1];
+        a.mat[w++] = (R)m[6];
+        a.mat[w++] = (R)m[7];
+      } else if (cls == 1) {  // anti-diagonal
+        o.type = FOP_X1;
+        o.unit = (m[2] == 1 && m[3] == 0 && m[4] == 1 && m[5] == 0) ? 1 : 0;
+        a.mat[w++] = (R)m[2];
+        a.mat[w++] = (R)m[3];
+        a.mat[w++] = (R)m[4];
+        a.mat[w++] = (R)m[5];
+      } else if (real) {
+        o.type = FOP_R1;
+        a.mat[w++] = (R)m[0];
+        a.mat[w++] = (R)m[2];
+        a.mat[w++] = (R)m[4];
+        a.mat[w++] = (R)m[6];
+      } else if (m[0] == m[6] && m[1] == 0 && m[7] == 0 && m[2] == 0 && m[4] == 0 && m[3] == m[5]) {
+        o.type = FOP_RX1;
+        a.mat[w++] = (R)m[0];
+        a.mat[w++] = (R)m[3];
       } else {
         o.type = FOP_G1;
-        for (int e = 0; e < 8; ++e) a.mat[w++] = (R)g.m[e];
+        for (int e = 0; e < 8; ++e) a.mat[w++] = (R)m[e];
       }
+    } else if (cls == 1 && classify_unit(g) && perm[0] == 0 && perm[1] == 1 && perm[2] == 3 && perm[3] == 2) {
+      o.type = FOP_CX;  // control = matrix MSB (register b0), target = LSB (b1)
+    } else if (cls == 1 && classify_unit(g) && perm[0] == 0 && perm[1] == 3 && perm[2] == 2 && perm[3] == 1) {
+      o.type = FOP_CX;  // control = matrix LSB, target = MSB
+      const uint8_t t = o.b0;
+      o.b0 = o.b1;
+      o.b1 = t;
+    } else if (cls == 1 && classify_unit(g) && perm[0] == 0 && perm[1] == 2 && perm[2] == 1 && perm[3] == 3) {
+      o.type = FOP_SW;
     } else if (cls == 2) {
       o.type = FOP_D2;
       for (int r = 0; r < 4; ++r) {
@@ -225,7 +268,9 @@ static bool build_fused(bt_plan* p, const std::vector<int>& take, uint64_t tilem
 extern "C" {
 
 int bt_plan_create(bt_ctx* ctx, int n, int repr, int prec, bt_plan** out) {
-  if (!ctx || !out) return bt_fail(ctx, BT_ERR_BAD_ARG, "NULL argument");
+  // ctx may be NULL: planning and specialisation need no device (errors then go to
+  // the thread's bt_last_error(NULL)); running needs a state, which carries a ctx
+  if (!out) return bt_fail(ctx, BT_ERR_BAD_ARG, "NULL argument");
   if (repr != BT_REPR_SV && repr != BT_REPR_DM) return bt_fail(ctx, BT_ERR_BAD_ARG, "repr must be SV or DM");
   if (prec != BT_PREC_C128 && prec != BT_PREC_C64) return bt_fail(ctx, BT_ERR_BAD_ARG, "prec must be C128 or C64");
   if (n < 1 || n > (repr == BT_REPR_DM ? 17 : 34)) return bt_fail(ctx, BT_ERR_BAD_ARG, "qubit count out of range");
@@ -367,11 +412,38 @@ int bt_plan_compile(bt_plan* p, int mode) {
       if (!done[gi]) nr.push_back(gi);
     rem.swap(nr);
   }
+  // specialise the fused passes (one NVRTC program for every new pass structure);
+  // without NVRTC, or if it fails, the passes run on the generic k_fused kernel
+  p->njit = 0;
+  if (fuse && bt_jit_available()) {
+    std::vector<void*> ent;
+    int rc;
+    if (c64) {
+      std::vector<const FusedArgs<float>*> v;
+      for (auto& ps : p->passes)
+        if (ps.kind == 0) v.push_back(reinterpret_cast<const FusedArgs<float>*>(ps.args.data()));
+      rc = bt_jit_prepare_f(p->ctx, v, ent);
+    } else {
+      std::vector<const FusedArgs<double>*> v;
+      for (auto& ps : p->passes)
+        if (ps.kind == 0) v.push_back(reinterpret_cast<const FusedArgs<double>*>(ps.args.data()));
+      rc = bt_jit_prepare_d(p->ctx, v, ent);
+    }
+    if (rc == BT_OK) {
+      size_t j = 0;
+      for (auto& ps : p->passes)
+        if (ps.kind == 0) {
+          ps.jit = ent[j++];
+          p->njit += ps.jit != nullptr;
+        }
+    }
+  }
   p->compiled = true;
   return BT_OK;
 }
 
-int bt_plan_stats(const bt_plan* p, int64_t* ngates, int64_t* npasses, int64_t* nfused, int64_t* nphases) {
+int bt_plan_stats(const bt_plan* p, int64_t* ngates, int64_t* npasses, int64_t* nfused, int64_t* nphases,
+                  int64_t* njit) {
   if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "plan is NULL");
   int64_t nf = 0;
   for (auto& ps : p->passes) nf += ps.kind == 0;
@@ -379,6 +451,7 @@ int bt_plan_stats(const bt_plan* p, int64_t* ngates, int64_t* npasses, int64_t* 
   if (npasses) *npasses = (int64_t)p->passes.size();
   if (nfused) *nfused = nf;
   if (nphases) *nphases = p->nphases;
+  if (njit) *njit = p->njit;
   return BT_OK;
 }
 
@@ -407,12 +480,12 @@ int bt_plan_run(bt_plan* p, bt_state* s, int64_t member) {
       FusedArgs<float>& a = *reinterpret_cast<FusedArgs<float>*>(ps.args.data());
       a.member_lo = lo;
       a.nmem = nm;
-      rc = bt_launch_fused_f(ctx, s->d, a);
+      rc = ps.jit ? bt_jit_launch_f(ctx, ps.jit, s->d, a) : bt_launch_fused_f(ctx, s->d, a);
     } else {
       FusedArgs<double>& a = *reinterpret_cast<FusedArgs<double>*>(ps.args.data());
       a.member_lo = lo;
       a.nmem = nm;
-      rc = bt_launch_fused_d(ctx, s->d, a);
+      rc = ps.jit ? bt_jit_launch_d(ctx, ps.jit, s->d, a) : bt_launch_fused_d(ctx, s->d, a);
     }
   }
   return rc;

@@ -138,7 +138,8 @@ int bt_reduced_dm(const bt_state* s, int k, const int32_t* qubits, int64_t membe
  * gate-fusion pass of the circuit compiler (the role of compile/get_layers,
  * src/ops.jl:278-329, :421-445).  Each fused pass applies every gate acting
  * inside a 13-bit (complex64) / 12-bit (complex128) tile in one HBM round trip;
- * the result equals applying the gates one by one (bt_apply_matrix). */
+ * the result equals applying the gates one by one (bt_apply_matrix).
+ * ctx may be NULL: planning and kernel specialisation need no GPU. */
 int bt_plan_create(bt_ctx* ctx, int n, int repr, int prec, bt_plan** out);
 int bt_plan_free(bt_plan* p);
 /* appends op.expand(N) (state) or e_op*rho*e_op' (density), as bt_apply_matrix */
@@ -148,7 +149,10 @@ int bt_plan_add_matrix(bt_plan* p, int k, const int32_t* qubits, const double* m
 int bt_plan_add_kraus_sum(bt_plan* p, int k, const int32_t* qubits, int nk, const double* kraus);
 /* mode 0: fused passes; mode 1: one sweep per gate (the unfused reference form) */
 int bt_plan_compile(bt_plan* p, int mode);
-int bt_plan_stats(const bt_plan* p, int64_t* ngates, int64_t* npasses, int64_t* nfused, int64_t* nphases);
+/* njit: fused passes running as kernels specialised for the plan (NVRTC, compiled
+ * by bt_plan_compile); the others run on the generic fused kernel */
+int bt_plan_stats(const bt_plan* p, int64_t* ngates, int64_t* npasses, int64_t* nfused, int64_t* nphases,
+                  int64_t* njit);
 /* runs the plan on member `member` (-1: every member) of a state of the same n/repr/prec */
 int bt_plan_run(bt_plan* p, bt_state* s, int64_t member);
 

@@ -4,9 +4,11 @@ on the large state-vector workload (33-qubit complex64 random brickwork, depth
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-A step is one brickwork layer of the depth-30 circuit (33 one-qubit gates and
-16 or 17 CNOTs = 49 logical gates; steps cycle through the 30 layers).  The
-state (64 GiB) is far larger than L2, so no flush is needed between steps.
+Default mode "plan": the circuit is compiled once into fused tile passes
+(kernels specialised per pass structure) and a step runs the whole depth-30
+circuit (1470 logical gates).  Modes "fused2"/"unfused" run one brickwork layer
+per step as dense gate sweeps (the per-gate form).  The state (64 GiB) is far
+larger than L2, so no flush is needed between steps.
 Multi-GPU runs are independent replicas (one state per GPU, no collective on
 the data path; weak scaling).  `--impl reference` times the CPU restatement of
 the reference's path (the reference is Julia, not runnable here) on the host
@@ -29,9 +31,13 @@ sys.path.insert(0, PKG)
 import numpy as np  # noqa: E402
 
 METRIC = "gate-apps/s"
-# ncu-measured DRAM bytes per amplitude of one gate sweep (read + write), from
-# the capture summarised in profiles/k_gate_sweep_c64.md; None until captured.
-TRAFFIC_BYTES_PER_AMP = None
+# ncu-measured DRAM bytes per amplitude of one pass (read + write) of the dominant
+# kernel, from single-launch captures at 28 qubits (traffic grows in proportion to
+# the state, so it is scaled to the workload's 2^n amplitudes):
+# profiles/btk_fused_pass_c64_brickwork28.md (JIT fused pass, plan mode) and
+# profiles/k_gate_sweep_c64_brickwork28.md (dense sweep, layer modes).
+TRAFFIC_BYTES_PER_AMP = {"plan": (2.147571e9 + 2.086315e9) / 2 ** 28,
+                         "sweep": (2.147591e9 + 2.087163e9) / 2 ** 28}
 
 
 def parse():
@@ -302,7 +308,9 @@ def run_ours(args):
     bytes_per_launch = 2 * (2 ** args.n) * esize
     achieved = bytes_per_launch / ((ms / 1e3) / launches) / 1e9
     peak, peak_kind = measured_peak()
-    traffic = TRAFFIC_BYTES_PER_AMP * 2 ** args.n if TRAFFIC_BYTES_PER_AMP else None
+    traffic = None
+    if args.prec == "c64":
+        traffic = TRAFFIC_BYTES_PER_AMP["plan" if plan is not None else "sweep"] * 2 ** args.n
 
     # end to end through the public API: per step the layer's matrices go from host
     # memory into the launches, and <Z_i> for every qubit comes back to the host

@@ -26,6 +26,7 @@ BT_PREC_C64 = 1
 BT_KRAUS_TRAJ = 0
 BT_KRAUS_SUM = 1
 BT_KRAUS_REF_ORDER = 0x100
+BT_KRAUS_UNITARY_MIX = 0x200
 
 
 class BTError(RuntimeError):
@@ -60,6 +61,7 @@ SIGNATURES = {
     "bt_state_download": (i32, [P, i64, i64, i64, P]),
     "bt_apply_matrix": (i32, [P, i32, P, P, i32, P, i64]),
     "bt_apply_kraus": (i32, [P, i32, P, i32, P, i32, P, P, P, P]),
+    "bt_apply_matrix_members": (i32, [P, i32, P, P, i32, P]),
     "bt_measure_z": (i32, [P, i32, P, P, P, P]),
     "bt_reduced_dm": (i32, [P, i32, P, i64, P]),
     "bt_plan_create": (i32, [P, i32, i32, i32, ctypes.POINTER(P)]),

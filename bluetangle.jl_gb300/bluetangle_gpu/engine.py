@@ -554,9 +554,10 @@ def expect(state, what, qubit=None, member=0):
     n = state.n
     if isinstance(what, str):
         if what.upper() == "Z" and qubit is None:
-            out = np.empty(n, dtype=np.float64)
+            rows = state.batch if member == -1 else 1
+            out = np.empty(rows * n, dtype=np.float64)
             state.ctx.check(L.lib().bt_expect_z_all(state.h, member, _ptr(out)))
-            return list(out)
+            return out.reshape(rows, n) if member == -1 else list(out)
         M = gates(what)
         qs = range(1, n + 1) if qubit is None else [qubit]
         vals = [_expect_terms(state, _pauli_terms([M], [q], n), member) for q in qs]

@@ -1,0 +1,226 @@
+"""Batched Monte-Carlo trajectories: many noisy shots of one circuit in lock-step.
+
+The reference re-simulates the whole circuit once per shot
+(`measure(circuit, shots)`, BlueTangle.jl src/ops.jl:619-630), each shot drawing
+its own Kraus branches (src/struct.jl:31-41), mid-circuit outcomes
+(src/hilbert.jl:682-696), Pauli-twirl frames (src/noise.jl:230-255) and, for
+zero-noise extrapolation, repeating every CNOT 2*id+1 times (src/ops.jl:555-573).
+Here all shots are members of one batched GPU state and every op is one launch
+over the whole batch: a gate is one pass (one matrix for all members, or a
+matrix per member for twirl frames), a channel is one reduction + one device-side
+branch decision per member + one pass, and a measurement likewise.  Members whose
+expanded op sequence is shorter (fewer ZNE repetitions, no measurement at that
+point) are masked: they keep an identity matrix and skip channels and
+measurements (forced = -2), so uneven depths run in the same launches.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+from .engine import GPUState, _cm, _i32, _ptr, apply_matrix
+from .gates import gate
+from .noise import NoiseModel, QuantumChannel, twirl_set
+from .ops import Op, OpQC, ifOp
+
+__all__ = ["Slot", "expand_member", "build_slots", "run_slots", "run_trajectories"]
+
+_ID2 = np.eye(2, dtype=np.complex128)
+
+
+class Slot:
+    """One lock-step position: kind in {"gate", "channel", "measure"}; per member a
+    payload or None (masked).  Gates carry (matrix, qubits, controls); channels
+    (kraus, qubits); measurements (name, qubit)."""
+
+    def __init__(self, kind, items):
+        self.kind = kind
+        self.items = items
+
+
+def expand_member(op, zne_id=0, twirl=False, rng=None):
+    """The reference's per-shot expansion of one circuit op (src/ops.jl:555-573 with
+    apply_twirl, src/noise.jl:230-255), as a list of ops."""
+    cnot = op.q == 2 and op.name.upper() in ("CNOT", "CX")
+    reps = 2 * zne_id + 1 if (zne_id > 0 and cnot) else 1
+    out = []
+    for _ in range(reps):
+        if twirl and op.q == 2 and op.name.upper() in ("CNOT", "CX", "ECR"):
+            least = min(op.qubit, op.target_qubit)
+            frame = twirl_set(op.name, op.qubit, op.target_qubit, rng)
+            for i, p in enumerate(frame, start=1):
+                if i == 3:
+                    out.append(op)
+                out.append(Op(p, least if i % 2 == 1 else least + 1))
+        else:
+            out.append(op)
+    return out
+
+
+def _noise_ops(op, noise):
+    """Channel ops a NoiseModel adds after `op` (src/hilbert.jl:322-340)."""
+    if not isinstance(noise, NoiseModel) or not getattr(op, "noisy", False):
+        return []
+    if op.q == 1:
+        ch = noise.q1 if op.control == -2 else noise.q2
+        if not isinstance(ch, QuantumChannel):
+            return []
+        return [(ch.kraus, [op.qubit] if op.control == -2 else [op.control, op.qubit])]
+    if isinstance(noise.q2, QuantumChannel):
+        return [(noise.q2.kraus, [op.qubit, op.target_qubit])]
+    return []
+
+
+def _op_slots(op, noise):
+    """Slots of one op for one member (gate followed by its NoiseModel channels)."""
+    if isinstance(op, OpQC):
+        qs = [op.qubit] if op.q == 1 else ([op.qubit, op.target_qubit] if op.q == 2 else [op.qubit, op.qubit + 1, op.qubit + 2])
+        return [("channel", (op.kraus, qs))]
+    if op.type == "🔬":
+        return [("measure", (op.name, op.qubit))]
+    ctrls = [op.control] if op.control != -2 else []
+    qs = [op.qubit] if op.q == 1 else [op.qubit, op.target_qubit]
+    return [("gate", (op.mat, qs, ctrls))] + [("channel", c) for c in _noise_ops(op, noise)]
+
+
+def build_slots(member_ops, noise=False):
+    """Aligns per-member op sequences into lock-step slots.  member_ops[m] is a list
+    of segments (one per circuit position), each a list of ops for that member;
+    segments are padded to the longest member at that position."""
+    B = len(member_ops)
+    nseg = len(member_ops[0])
+    slots = []
+    for s in range(nseg):
+        seqs = []
+        for m in range(B):
+            seq = []
+            for op in member_ops[m][s]:
+                seq.extend(_op_slots(op, noise))
+            seqs.append(seq)
+        L_ = max(len(x) for x in seqs)
+        for i in range(L_):
+            kinds = {x[i][0] for x in seqs if i < len(x)}
+            if len(kinds) != 1:
+                raise ValueError("members disagree on the kind of op at one position")
+            kind = kinds.pop()
+            slots.append(Slot(kind, [x[i][1] if i < len(x) else None for x in seqs]))
+    return slots
+
+
+def _same_gate(items):
+    first = None
+    for it in items:
+        if it is None:
+            return False
+        if first is None:
+            first = it
+        elif not (np.array_equal(it[0], first[0]) and it[1] == first[1] and it[2] == first[2]):
+            return False
+    return True
+
+
+def _unitary_mix(kraus):
+    for K in kraus:
+        P = K.conj().T @ K
+        if not np.allclose(P, P[0, 0] * np.eye(K.shape[0]), atol=1e-12):
+            return False
+    return True
+
+
+def run_slots(state, slots, rng=None, records=True):
+    """Runs lock-step slots on a batched state.  rng: numpy Generator whose draws
+    decide branches/outcomes (one per member per channel or measurement), or None
+    for the engine's on-device Philox stream.  Returns the per-member measurement
+    records (-1 where a member was not measured)."""
+    lib = L.lib()
+    B = state.batch
+    recs = [[] for _ in range(B)] if records else None
+    for sl in slots:
+        items = sl.items
+        if sl.kind == "gate":
+            live = [it for it in items if it is not None]
+            if _same_gate(items):
+                mat, qs, ctrls = items[0]
+                apply_matrix(state, mat, qs, ctrls)
+                continue
+            qs, ctrls = live[0][1], live[0][2]
+            if any(it[1] != qs or it[2] != ctrls for it in live):
+                raise ValueError("members disagree on the qubits of a gate position")
+            d = 2 ** len(qs)
+            mats = np.concatenate([_cm(it[0] if it is not None else np.eye(d)).ravel() for it in items])
+            q = _i32(qs)
+            c = _i32(ctrls or [0])
+            state.ctx.check(lib.bt_apply_matrix_members(state.h, len(qs), _ptr(q), _ptr(np.ascontiguousarray(mats)),
+                                                         len(ctrls), _ptr(c) if ctrls else None))
+        elif sl.kind == "channel":
+            live = [it for it in items if it is not None]
+            kraus, qs = live[0]
+            if any(it[1] != qs or (it[0] is not kraus and not all(np.array_equal(a, b) for a, b in zip(it[0], kraus)))
+                   for it in live):
+                raise ValueError("members disagree on the channel at one position")
+            forced = None if len(live) == B else _i32([-1 if it is not None else -2 for it in items])
+            K = np.ascontiguousarray(np.concatenate([_cm(k).ravel() for k in kraus]))
+            q = _i32(qs)
+            u = None if rng is None else np.ascontiguousarray(rng.random(B))
+            mode = L.BT_KRAUS_TRAJ | L.BT_KRAUS_REF_ORDER
+            if rng is None and _unitary_mix(kraus):
+                mode |= L.BT_KRAUS_UNITARY_MIX
+            state.ctx.check(lib.bt_apply_kraus(state.h, len(qs), _ptr(q), len(kraus), _ptr(K), mode, _ptr(u),
+                                               _ptr(forced), None, None))
+        else:  # measure
+            live = [it for it in items if it is not None]
+            name, qubit = live[0]
+            forced = None if len(live) == B else _i32([-1 if it is not None else -2 for it in items])
+            up = name.upper()
+            rot = None if up in ("MZ", "M(Z)") else (gate["H"] if up in ("MX", "M(X)") else gate["HSP"])
+            if rot is not None:
+                apply_matrix(state, rot, [qubit])
+            u = None if rng is None else np.ascontiguousarray(rng.random(B))
+            out = np.empty(B, dtype=np.int32)
+            state.ctx.check(lib.bt_measure_z(state.h, int(qubit), _ptr(u), _ptr(forced), _ptr(out), None))
+            if rot is not None:
+                apply_matrix(state, rot.conj().T, [qubit])
+            if records:
+                for m in range(B):
+                    if items[m] is not None:
+                        recs[m].append(int(out[m]))
+    return recs
+
+
+def member_programs(steps, n, batch, zne_ids=None, twirl=False, frame_rng=None, measure_prob=0.0,
+                    measure_rng=None):
+    """Per-member segment lists: each circuit op expanded for the member (ZNE,
+    twirl), and after every step a Z measurement of each qubit with probability
+    measure_prob, drawn independently per member."""
+    zne_ids = list(zne_ids) if zne_ids is not None else [0] * batch
+    frame_rng = frame_rng if frame_rng is not None else np.random.default_rng(0)
+    measure_rng = measure_rng if measure_rng is not None else np.random.default_rng(1)
+    member_ops = [[] for _ in range(batch)]
+    for step in steps:
+        for op in step:
+            for m in range(batch):
+                member_ops[m].append(expand_member(op, zne_ids[m], twirl, frame_rng))
+        if measure_prob > 0:
+            for q in range(1, n + 1):
+                mask = measure_rng.random(batch) < measure_prob
+                for m in range(batch):
+                    member_ops[m].append([Op("MZ", q)] if mask[m] else [])
+    return member_ops
+
+
+def run_trajectories(steps, n, batch, noise=False, zne_ids=None, twirl=False, prec="c64", rng=None, frame_rng=None,
+                     measure_prob=0.0, measure_rng=None, ctx=None, state=None):
+    """`batch` trajectories of a circuit given as a list of steps (lists of ops)
+    from |0...0> (or the given batched `state`) in one batched state.
+
+    zne_ids: per-member ZNE id (None: all 0).  twirl: Pauli-twirl CNOTs per member
+    (frames drawn from frame_rng).  measure_prob: after each step every qubit of
+    every member is measured in Z with this probability (masks from measure_rng).
+    Returns (state, records)."""
+    if steps and not isinstance(steps[0], (list, tuple)):
+        steps = [steps]
+    member_ops = member_programs(steps, n, batch, zne_ids, twirl, frame_rng, measure_prob, measure_rng)
+    slots = build_slots(member_ops, noise)
+    st = state if state is not None else GPUState(n, prec, batch, ctx)
+    recs = run_slots(st, slots, rng=rng)
+    return st, recs

@@ -424,6 +424,72 @@ static bool trace_preserving(int d, int nk, const double* kraus_cm) {
   return sqrt(diff2) <= 1.4901161193847656e-08 * sqrt((double)d);
 }
 
+// every K_i^dagger K_i is a multiple of the identity (K_i = c_i U_i)
+static bool unitary_mixture(int d, int nk, const double* kraus_cm) {
+  for (int i = 0; i < nk; ++i) {
+    const double* K = kraus_cm + (size_t)i * 2 * d * d;
+    double diag0 = -1;
+    for (int r = 0; r < d; ++r)
+      for (int c = 0; c < d; ++c) {
+        double sr = 0, si = 0;
+        for (int a = 0; a < d; ++a) {
+          double xr = K[2 * (a + r * d)], xi = -K[2 * (a + r * d) + 1];
+          double yr = K[2 * (a + c * d)], yi = K[2 * (a + c * d) + 1];
+          sr += xr * yr - xi * yi;
+          si += xr * yi + xi * yr;
+        }
+        if (r == c) {
+          if (diag0 < 0) diag0 = sr;
+          if (fabs(sr - diag0) > 1e-12 || fabs(si) > 1e-12) return false;
+        } else if (fabs(sr) > 1e-12 || fabs(si) > 1e-12) {
+          return false;
+        }
+      }
+  }
+  return true;
+}
+
+int bt_apply_matrix_members(bt_state* s, int k, const int32_t* qubits, const double* mats, int nctrl,
+                            const int32_t* ctrls) {
+  if (!s) return bt_fail(nullptr, BT_ERR_BAD_ARG, "state is NULL");
+  bt_ctx* ctx = s->ctx;
+  if (!mats) return bt_fail(ctx, BT_ERR_BAD_ARG, "matrices are NULL");
+  if (s->repr != BT_REPR_SV) return bt_fail(ctx, BT_ERR_UNSUPPORTED, "per-member matrices need state vectors");
+  int rc = check_qubits(ctx, s->n, k, qubits, nctrl, ctrls);
+  if (rc) return rc;
+  if (k > BT_MAX_K) return bt_fail(ctx, BT_ERR_UNSUPPORTED, "dense gates act on at most 5 qubits");
+  if ((rc = set_dev(ctx))) return rc;
+  const int d = 1 << k;
+  const int64_t B = s->batch;
+  const size_t per = 2 * (size_t)d * d;
+  const bool f = s->prec == BT_PREC_C64;
+  Carve cv;
+  int iM = cv.add((size_t)B * per * (f ? 4 : 8));
+  if ((rc = cv.commit(ctx))) return rc;
+  std::vector<float> hf(f ? B * per : 0);
+  std::vector<double> hd(f ? 0 : B * per);
+  for (int64_t m = 0; m < B; ++m) {
+    const double* cm = mats + (size_t)m * per;
+    for (int r = 0; r < d; ++r)
+      for (int c = 0; c < d; ++c)
+        for (int z = 0; z < 2; ++z) {
+          const double v = cm[2 * (r + c * d) + z];
+          if (f) hf[m * per + 2 * (r * d + c) + z] = (float)v;
+          else hd[m * per + 2 * (r * d + c) + z] = v;
+        }
+  }
+  rc = bt_cuda_check(ctx, cudaMemcpyAsync(cv.at<void>(iM), f ? (const void*)hf.data() : (const void*)hd.data(),
+                                          (size_t)B * per * (f ? 4 : 8), cudaMemcpyHostToDevice, ctx->stream),
+                     "matrix upload");
+  if (rc) return rc;
+  int bits[BT_MAX_K];
+  uint64_t cmask = 0;
+  for (int i = 0; i < k; ++i) bits[i] = s->n - qubits[i];
+  for (int i = 0; i < nctrl; ++i) cmask |= 1ULL << (s->n - ctrls[i]);
+  // a copy from pageable memory has left the host vectors once cudaMemcpyAsync returns
+  return bt_launch_gate(s, k, bits, nullptr, cmask, 0, B, cv.at<void>(iM), (int64_t)per);
+}
+
 int bt_apply_kraus(bt_state* s, int k, const int32_t* qubits, int nk, const double* kraus, int mode,
                    const double* uniforms, const int32_t* forced, int32_t* branch_out, double* probs_out) {
   if (!s) return bt_fail(nullptr, BT_ERR_BAD_ARG, "state is NULL");
@@ -485,13 +551,17 @@ int bt_apply_kraus(bt_state* s, int k, const int32_t* qubits, int nk, const doub
   if (rc) return rc;
   int bits[3];
   for (int i = 0; i < k; ++i) bits[i] = n - qubits[i];
-  if ((rc = bt_launch_rdm(s, k, bits, 0, B, cv.at<double>(iR)))) return rc;
+  const bool umix = (flags & BT_KRAUS_UNITARY_MIX) != 0;
+  if (umix && !unitary_mixture(d, nk, kraus))
+    return bt_fail(ctx, BT_ERR_BAD_ARG, "BT_KRAUS_UNITARY_MIX needs Kraus operators that are multiples of unitaries");
+  if (!umix && (rc = bt_launch_rdm(s, k, bits, 0, B, cv.at<double>(iR)))) return rc;
   bt_kraus_desc kd;
   kd.k = k;
   kd.nk = nk;
   kd.ref_perm = (flags & BT_KRAUS_REF_ORDER) && k == 2 && qubits[0] > qubits[1];
   uint64_t stream = 0x4b52000000000000ULL ^ ctx->rng_calls++;
-  rc = bt_launch_decide_kraus(s, kd, B, cv.at<double>(iR), cv.at<double>(iK), uniforms ? cv.at<double>(iU) : nullptr,
+  rc = bt_launch_decide_kraus(s, kd, B, umix ? nullptr : cv.at<double>(iR), cv.at<double>(iK),
+                              uniforms ? cv.at<double>(iU) : nullptr,
                               forced ? cv.at<int>(iF) : nullptr, stream, cv.at<int>(iB), cv.at<double>(iP),
                               cv.at<void>(iM));
   if (rc) return rc;

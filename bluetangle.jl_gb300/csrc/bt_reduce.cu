@@ -551,6 +551,12 @@ __global__ void k_decide_measure(int64_t nmem, const double* __restrict__ rdm, c
   if (m >= nmem) return;
   const double s0 = rdm[m * 8 + 0], s1 = rdm[m * 8 + 6];
   int f = forced ? forced[m] : -1;
+  if (f == -2) {  // this member is not measured
+    outcome[m] = -1;
+    scale[m] = 1.0;
+    p0[m] = s0;
+    return;
+  }
   double uu = u ? u[m] : bt_uniform(key, stream, (uint64_t)m);
   int ind = f >= 0 ? f : (uu < s0 ? 0 : 1);
   double keep = ind ? s1 : s0;
@@ -586,13 +592,22 @@ __global__ void k_decide_kraus(int64_t nmem, int k, int nk, int ref_perm, const 
   int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= nmem) return;
   const int D = 1 << k;
-  const double* r = rdm + m * 2 * D * D;
+  R* out = pm + m * 2 * D * D;
+  int f = forced ? forced[m] : -1;
+  if (f == -2) {  // this member skips the channel: identity, no draw consumed
+    branch[m] = -1;
+    for (int e = 0; e < 2 * D * D; ++e) out[e] = (R)((e % (2 * D + 2)) == 0 ? 1.0 : 0.0);
+    return;
+  }
+  // rdm == nullptr: the Kraus operators are multiples of unitaries, so the branch
+  // probabilities |c_i|^2 do not depend on the (normalised) state: rho_A = I/D
+  const double* r = rdm ? rdm + m * 2 * D * D : nullptr;
+  const double diag = 1.0 / D;
   // reference-order reduced matrix: for a pair with q > t the reference reads
   // rho_A in (t, q) order, i.e. indices permuted by [0, 2, 1, 3]
   const int perm[4] = {0, 2, 1, 3};
   double cum = 0;
   double uu = u ? u[m] : bt_uniform(key, stream, (uint64_t)m);
-  int f = forced ? forced[m] : -1;
   int ind = -1;
   for (int i = 0; i < nk; ++i) {
     const double* K = kraus + (int64_t)i * 2 * D * D;
@@ -603,7 +618,8 @@ __global__ void k_decide_kraus(int64_t nmem, int k, int nk, int ref_perm, const 
         double kar = K[2 * (c * D + a)], kai = K[2 * (c * D + a) + 1];
         for (int b = 0; b < D; ++b) {
           int ra = ref_perm ? perm[a] : a, rb = ref_perm ? perm[b] : b;
-          double rr = r[2 * (ra * D + rb)], ri = r[2 * (ra * D + rb) + 1];
+          double rr = r ? r[2 * (ra * D + rb)] : (ra == rb ? diag : 0.0);
+          double ri = r ? r[2 * (ra * D + rb) + 1] : 0.0;
           double kbr = K[2 * (c * D + b)], kbi = -K[2 * (c * D + b) + 1];
           // (ka * rho) * conj(kb)
           double tr_ = kar * rr - kai * ri, ti = kar * ri + kai * rr;
@@ -615,7 +631,6 @@ __global__ void k_decide_kraus(int64_t nmem, int k, int nk, int ref_perm, const 
     if (ind < 0 && uu <= cum) ind = i;
   }
   if (f >= 0) ind = f;
-  R* out = pm + m * 2 * D * D;
   if (ind < 0 || ind >= nk) {
     // no branch (the reference's _weighted_sample returns nothing): report it and
     // leave this member untouched with an identity matrix
@@ -632,7 +647,8 @@ __global__ void k_decide_kraus(int64_t nmem, int k, int nk, int ref_perm, const 
     for (int a = 0; a < D; ++a) {
       double kar = K[2 * (c * D + a)], kai = K[2 * (c * D + a) + 1];
       for (int b = 0; b < D; ++b) {
-        double rr = r[2 * (a * D + b)], ri = r[2 * (a * D + b) + 1];
+        double rr = r ? r[2 * (a * D + b)] : (a == b ? diag : 0.0);
+        double ri = r ? r[2 * (a * D + b) + 1] : 0.0;
         double kbr = K[2 * (c * D + b)], kbi = -K[2 * (c * D + b) + 1];
         double tr_ = kar * rr - kai * ri, ti = kar * ri + kai * rr;
         nrm += tr_ * kbr - ti * kbi;

@@ -57,6 +57,12 @@ extern "C" {
  * __calc_prob does for a pair with q > t (src/struct.jl:17-29 with
  * src/linalg.jl:198-230 and src/hilbert.jl:30). */
 #define BT_KRAUS_REF_ORDER 0x100
+/* flag: every K_i is a multiple of a unitary (depolarizing, bit/phase flips,
+ * rot_xyz): the branch probabilities |c_i|^2 do not depend on the normalised
+ * state, so no reduction pass is made (the reference's probabilities differ only
+ * by the state's norm, 1 to rounding).  Rejected when the Kraus set is not of
+ * that form. */
+#define BT_KRAUS_UNITARY_MIX 0x200
 
 typedef struct bt_ctx bt_ctx;
 typedef struct bt_state bt_state;
@@ -104,6 +110,12 @@ int bt_state_download(const bt_state* s, int64_t member, int64_t offset, int64_t
  * On a density matrix it is e_op*rho*e_op' (src/hilbert.jl:655-656). */
 int bt_apply_matrix(bt_state* s, int k, const int32_t* qubits, const double* mat, int nctrl,
                     const int32_t* ctrls, int64_t member);
+/* the same gate position with a different matrix per member, in one pass over the
+ * batch (state vectors): per-trajectory twirl frames, ZNE repetitions (identity
+ * for members without them), per-client angles.  mats holds batch column-major
+ * 2^k x 2^k matrices back to back. */
+int bt_apply_matrix_members(bt_state* s, int k, const int32_t* qubits, const double* mats, int nctrl,
+                            const int32_t* ctrls);
 
 /* Kraus channel on qubits (1 <= k <= 3; qubits[0] = q, qubits[1] = t).
  *  BT_KRAUS_TRAJ (state vector): __QuantumChannel_new_apply (src/struct.jl:31-41,
@@ -115,7 +127,9 @@ int bt_apply_matrix(bt_state* s, int k, const int32_t* qubits, const double* mat
  *    (either may be NULL) receive the branch and the probabilities.
  *  BT_KRAUS_SUM (density matrix): rho <- sum_i K_i rho K_i^dagger
  *    (src/struct.jl:58-76) in one pass over rho.
- * `kraus` holds nk column-major 2^k x 2^k matrices back to back. */
+ * `kraus` holds nk column-major 2^k x 2^k matrices back to back.
+ * forced[m] = -2 makes member m skip the channel (no draw, state untouched):
+ * members of one batch can follow different op sequences (ZNE repetitions). */
 int bt_apply_kraus(bt_state* s, int k, const int32_t* qubits, int nk, const double* kraus, int mode,
                    const double* uniforms, const int32_t* forced, int32_t* branch_out,
                    double* probs_out);
@@ -126,7 +140,7 @@ int bt_apply_kraus(bt_state* s, int k, const int32_t* qubits, int nk, const doub
  * to exactly zero and the kept half renormalised.  outcome/p0 per member (may be NULL).
  * On a density matrix: born_measure_Z(N, rho, q) = sum_b P_b rho P_b
  * (src/hilbert.jl:784-796); uniforms/forced/outcome are ignored and p0 is
- * still reported. */
+ * still reported.  forced[m] = -2: member m is not measured (outcome -1). */
 int bt_measure_z(bt_state* s, int qubit, const double* uniforms, const int32_t* forced,
                  int32_t* outcome, double* p0);
 /* partial_trace(psi, keep) for k <= 3 kept qubits, in the listed order

@@ -54,6 +54,9 @@ def parse():
     ap.add_argument("--cpu-n", type=int, default=24, help="qubits of the CPU baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="brickwork", choices=["brickwork", "serve"])
+    ap.add_argument("--rate", type=float, default=2000.0, help="serving: Poisson arrival rate (req/s)")
+    ap.add_argument("--lanes", type=int, default=8, help="serving: concurrent lanes (contexts/streams)")
     return ap.parse_args()
 
 
@@ -369,9 +372,106 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+# ------------------------------------------------------------------ serving workload
+def serve_specs(seed, clients=32):
+    """The serving mix: 70% state-vector jobs (n ~ U{8..26}), 20% trajectory
+    batches of 64 (n ~ U{8..16}: a 64-member batch then has the footprint of one
+    <= 22-qubit state), 10% density-matrix jobs (n ~ U{8..12}); hardware-efficient
+    ansatz of depth U{4..12}; <H> of 4n random 2-local Pauli terms."""
+    import bluetangle_gpu.serving as S
+    rng = np.random.default_rng(seed)
+    out = []
+    for cid in range(clients):
+        kind = rng.choice(["sv", "traj", "dm"], p=[0.7, 0.2, 0.1])
+        n = int(rng.integers(8, 27) if kind == "sv" else (rng.integers(8, 17) if kind == "traj" else rng.integers(8, 13)))
+        out.append(S.make_client(rng, cid, str(kind), n, int(rng.integers(4, 13))))
+    return out
+
+
+def run_serve(args):
+    import bluetangle_gpu as bt
+    import bluetangle_gpu.serving as S
+    specs = serve_specs(args.seed)
+    rng = np.random.default_rng(args.seed + 1)
+    per = max(2, args.steps)
+    total = per * len(specs)
+    arrivals = np.cumsum(rng.exponential(1 / args.rate, total))
+    owners = rng.integers(0, len(specs), total)
+    reqs = [S.Request(i, int(owners[i]), rng.normal(0, 0.3, specs[owners[i]].nparams), seed=7000 + i)
+            for i in range(total)]
+    srv = S.Server(specs, lanes=args.lanes, prec="c64")
+    try:
+        # warm-up: every client admitted once, then wait for the specialised kernels
+        warm = [S.Request(-1 - c.cid, c.cid, rng.normal(0, 0.3, c.nparams), seed=c.cid) for c in specs]
+        for w in warm:
+            srv.submit(w)
+        for w in warm:
+            w.done.wait(600)
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 600:
+            ready = all(r.plan is None or r.plan.stats()["jit_passes"] == r.plan.stats()["fused_passes"]
+                        for r, _ in srv.resident.values() if r is not None)
+            if ready:
+                break
+            time.sleep(0.2)
+        srv.completed.clear()
+        start = time.perf_counter()
+        for r, at in zip(reqs, arrivals):
+            dt = start + at - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            srv.submit(r)
+        for r in reqs:
+            r.done.wait(600)
+        makespan = max(r.t_done for r in reqs) - start
+    finally:
+        srv.close()
+    errs = [r.error for r in reqs if r.error is not None]
+    if errs:
+        raise errs[0]
+    lat = np.array([r.t_done - r.t_submit for r in reqs]) * 1e3
+    served = total / makespan
+    # plain per-call complex128 path on a sample: one request per client, serially
+    pctx = bt.Context(0, seed=5)
+    sample = [next(r for r in reqs if r.cid == c.cid) for c in specs if any(r.cid == c.cid for r in reqs)]
+    t = time.perf_counter()
+    plain_vals = [S.plain_request(specs[r.cid], r.theta, r.seed, pctx, prec="c128") for r in sample]
+    plain_rate = len(sample) / (time.perf_counter() - t)
+    dev = max(abs(r.value - v) / max(1e-12, sum(abs(x[0]) for x in specs[r.cid].terms))
+              for r, v in zip(sample, plain_vals))
+    # state infidelity of the served precision (c64 fused plan) against c128 for the sv clients
+    infid = 0.0
+    for c in [c for c in specs if c.kind == "sv"][:6]:
+        th = rng.normal(0, 0.3, c.nparams)
+        a = bt.zero_state(c.n, "c64", ctx=pctx)
+        p = bt.Plan(c.n, "sv", "c64", pctx)
+        for op in S.hea_ops(c.n, c.depth, th):
+            p.add(op)
+        p.compile(True).run(a)
+        b = bt.apply(S.hea_ops(c.n, c.depth, th), bt.zero_state(c.n, "c128", ctx=pctx))
+        infid = max(infid, 1 - bt.fidelity(a, b))
+        a.free()
+        b.free()
+    pctx.close()
+    line = {"metric": "served circuits/s", "value": served, "unit": "circuits/s", "n_gpus": 1, "steps": per,
+            "warmup": 1, "ms_per_step": makespan * 1e3 / per, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+            "config": {"workload": f"serving-{len(specs)}clients-poisson{args.rate:g}",
+                       "mix": {k: sum(1 for c in specs if c.kind == k) for k in ("sv", "traj", "dm")},
+                       "requests": total, "lanes": args.lanes},
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                           "mean": float(lat.mean())},
+            "plain_c128_circuits_per_s": plain_rate, "vs_plain": served / plain_rate,
+            "max_rel_dev_vs_c128": dev, "max_infidelity_c64": infid,
+            "roofline": None, "cpu_baseline": None, "e2e": None, "gpu_launches": None}
+    print(json.dumps(line), flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "serve":
+        run_serve(a)
     else:
         run_ours(a)

@@ -69,6 +69,7 @@ SIGNATURES = {
     "bt_plan_add_matrix": (i32, [P, i32, P, P, i32, P]),
     "bt_plan_add_kraus_sum": (i32, [P, i32, P, i32, P]),
     "bt_plan_compile": (i32, [P, i32]),
+    "bt_plan_set_matrices": (i32, [P, i32, P, P]),
     "bt_plan_stats": (i32, [P, P, P, P, P, P]),
     "bt_plan_run": (i32, [P, P, i64]),
     "bt_sample": (i32, [P, i64, i64, P, u64, P]),

@@ -462,8 +462,21 @@ class Plan:
         ctrls = [op.control] if op.control != -2 else []
         return self.add_matrix(mat, qs, ctrls)
 
-    def compile(self, fused=True):
-        self.ctx.check(L.lib().bt_plan_compile(self.h, 0 if fused else 1))
+    def compile(self, fused=True, tiered=False):
+        """fused: tile passes (else one sweep per gate); tiered: run the generic
+        kernel at once and switch to specialised kernels when their background
+        compile finishes."""
+        self.ctx.check(L.lib().bt_plan_compile(self.h, (2 if tiered else 0) if fused else 1))
+        return self
+
+    def set_matrices(self, updates):
+        """updates: list of (add_index, matrix) — new matrices for gates already added
+        (add_index counts add_* calls from 0)."""
+        if not updates:
+            return self
+        idx = np.ascontiguousarray([u[0] for u in updates], dtype=np.int64)
+        mats = np.ascontiguousarray(np.concatenate([_cm(u[1]).ravel() for u in updates]))
+        self.ctx.check(L.lib().bt_plan_set_matrices(self.h, len(updates), _ptr(idx), _ptr(mats)))
         return self
 
     def stats(self):

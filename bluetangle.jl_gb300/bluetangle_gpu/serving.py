@@ -1,0 +1,313 @@
+"""Serving loop: continuous batching of variational circuit jobs on one GPU.
+
+A client is a VQE/Trotter-style loop of the reference (variational_apply +
+expect(state, H), BlueTangle.jl src/vqa.jl:420-456, src/func.jl:100): a fixed
+circuit structure (a hardware-efficient ansatz, src/vqa.jl:302-314) evaluated
+again and again at new parameters, each time returning <H> of a Pauli-sum
+Hamiltonian.  The server
+
+  * admits clients by HBM footprint: a client's state (and plan) stay resident
+    between its requests; when the budget is exhausted, idle clients are evicted
+    oldest-first and admission waits until memory frees up;
+  * compiles each client's circuit once into a fused plan (kernels specialised
+    per pass structure); a request only rewrites the angles in place;
+  * runs requests on `lanes` worker threads, each with its own context and CUDA
+    stream, so requests that arrive while others are on the GPU start as soon as
+    a lane is free and their kernels overlap on the device (a small circuit is a
+    single fused launch);
+  * serves each client's requests in arrival order (they share its state) and
+    records per-request latency (submit to result) for p50/p99.
+
+Job kinds: "sv" (state vector, one fused plan), "traj" (a batch of Monte-Carlo
+trajectories with depolarizing and amplitude-damping noise after every gate,
+<H> averaged over members), "dm" (density matrix with the same noise as Kraus
+sums, one fused plan).
+"""
+import ctypes
+import heapq
+import math
+import threading
+import time
+from collections import deque
+
+import numpy as np
+
+from . import _lib as L
+from .engine import Context, GPUDensity, GPUState, Plan, _ptr
+from .gates import gates
+from .noise import noise_model
+from .ops import Op, OpQC
+
+__all__ = ["ClientSpec", "make_client", "Server", "plain_request", "hea_ops"]
+
+
+def _ry(t):
+    c, s = math.cos(t / 2), math.sin(t / 2)
+    return np.array([[c, -s], [s, c]], dtype=np.complex128)
+
+
+def _rz(t):
+    return np.array([[np.exp(-0.5j * t), 0], [0, np.exp(0.5j * t)]], dtype=np.complex128)
+
+
+CNOT = np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 0, 1], [0, 0, 1, 0]], dtype=np.complex128)
+
+
+class ClientSpec:
+    """kind, n, depth, Hamiltonian terms (coef, xmask, zmask) and trajectory count."""
+
+    def __init__(self, cid, kind, n, depth, terms, ntraj=64, p1=1e-3, p2=1e-2, gamma=5e-3):
+        self.cid, self.kind, self.n, self.depth, self.terms = cid, kind, n, depth, terms
+        self.ntraj, self.p1, self.p2, self.gamma = ntraj, p1, p2, gamma
+
+    @property
+    def nparams(self):
+        return 2 * self.n * self.depth
+
+    def footprint(self, prec):
+        es = 8 if prec == "c64" else 16
+        if self.kind == "dm":
+            return (4 ** self.n) * es
+        if self.kind == "traj":
+            return self.ntraj * (2 ** self.n) * es
+        return (2 ** self.n) * es
+
+
+def random_terms(rng, n, count):
+    """count random 2-local Pauli terms on any pair of qubits with N(0,1) coefficients."""
+    terms = []
+    for _ in range(count):
+        a, b = rng.choice(np.arange(1, n + 1), size=2, replace=False)
+        x = z = 0
+        for q in (a, b):
+            p = "XYZ"[rng.integers(0, 3)]
+            bit = 1 << (n - int(q))
+            if p in "XY":
+                x |= bit
+            if p in "ZY":
+                z |= bit
+        terms.append((float(rng.normal()), x, z))
+    return terms
+
+
+def make_client(rng, cid, kind, n, depth):
+    return ClientSpec(cid, kind, n, depth, random_terms(rng, n, 4 * n))
+
+
+def hea_ops(n, depth, theta):
+    """The ansatz as reference ops: per layer RY, RZ on every qubit, then a CNOT ladder."""
+    ops, i = [], 0
+    for _ in range(depth):
+        for q in range(1, n + 1):
+            ops.append(Op("RY", _ry(theta[i]), q))
+            ops.append(Op("RZ", _rz(theta[i + 1]), q))
+            i += 2
+        for q in range(1, n):
+            ops.append(Op("CNOT", q, q + 1))
+    return ops
+
+
+def _noisy(spec, ops):
+    """config-2 style noise after every gate: depolarizing (p1 / p2, the two-qubit
+    one a 16-term kron channel) and amplitude damping on each touched qubit."""
+    out = []
+    for op in ops:
+        out.append(op)
+        if op.q == 1:
+            out += [OpQC("depolarizing", spec.p1, op.qubit), OpQC("amplitude_damping", spec.gamma, op.qubit)]
+        else:
+            out += [OpQC("depolarizing", spec.p2, op.qubit, op.target_qubit),
+                    OpQC("amplitude_damping", spec.gamma, op.qubit),
+                    OpQC("amplitude_damping", spec.gamma, op.target_qubit)]
+    return out
+
+
+def _expect_h(st, terms, member=-1):
+    lib = L.lib()
+    xs = np.ascontiguousarray([t[1] for t in terms], dtype=np.uint64)
+    zs = np.ascontiguousarray([t[2] for t in terms], dtype=np.uint64)
+    cs = np.ascontiguousarray([t[0] for t in terms], dtype=np.float64)
+    rows = st.batch if member == -1 else 1
+    out = np.empty(rows * len(terms), dtype=np.float64)
+    st.ctx.check(lib.bt_expect_pauli(st.h, len(terms), _ptr(xs), _ptr(zs), _ptr(cs), member, _ptr(out)))
+    return float(out.reshape(rows, len(terms)).sum(axis=1).mean())
+
+
+class _Resident:
+    """A client's resident GPU objects (on one lane's context)."""
+
+    def __init__(self, spec, ctx, prec, tiered=True):
+        self.spec, self.ctx, self.prec = spec, ctx, prec
+        n = spec.n
+        theta0 = np.full(spec.nparams, 0.1)
+        self.pidx = []  # add indices of the parametrised gates, in theta order
+        self.plan = None
+        if spec.kind in ("sv", "dm"):
+            dm = spec.kind == "dm"
+            self.state = (GPUDensity if dm else GPUState)(n, prec, 1, ctx)
+            self.plan = Plan(n, spec.kind, prec, ctx)
+            ops = hea_ops(n, spec.depth, theta0)
+            for i, op in enumerate(_noisy(spec, ops) if dm else ops):
+                self.plan.add(op)
+                if op.name in ("RY", "RZ"):
+                    self.pidx.append(i)
+            self.plan.compile(True, tiered=tiered)
+        else:
+            self.state = GPUState(n, prec, spec.ntraj, ctx)
+        self.last_used = time.perf_counter()
+
+    def free(self):
+        self.state.free()
+        self.plan = None
+
+    def run(self, theta, seed):
+        spec = self.spec
+        self.state.set_zero()
+        if spec.kind in ("sv", "dm"):
+            ups = []
+            for j, ai in enumerate(self.pidx):
+                ups.append((ai, _ry(theta[j]) if j % 2 == 0 else _rz(theta[j])))
+            self.plan.set_matrices(ups).run(self.state)
+            return _expect_h(self.state, spec.terms)
+        from .trajectories import run_trajectories
+        steps = [_noisy(spec, hea_ops(spec.n, spec.depth, theta))]
+        run_trajectories(steps, spec.n, spec.ntraj, prec=self.prec, rng=np.random.default_rng(seed),
+                         state=self.state)
+        return _expect_h(self.state, spec.terms, -1)
+
+
+class Request:
+    def __init__(self, rid, cid, theta, seed):
+        self.rid, self.cid, self.theta, self.seed = rid, cid, theta, seed
+        self.t_submit = None
+        self.t_start = None
+        self.t_done = None
+        self.value = None
+        self.error = None
+        self.done = threading.Event()
+
+
+class Server:
+    def __init__(self, specs, lanes=8, prec="c64", hbm_budget=None, device=0, seed=1234, tiered=True):
+        self.specs = {s.cid: s for s in specs}
+        self.prec = prec
+        self.tiered = tiered
+        self.lanes = [Context(device, seed=seed + i) for i in range(lanes)]
+        self.budget = hbm_budget if hbm_budget is not None else 200 * 2 ** 30
+        self.used = 0
+        self.resident = {}  # cid -> (_Resident, lane index)
+        self.queues = {s.cid: deque() for s in specs}
+        self.busy = set()
+        self.cv = threading.Condition()
+        self.stop = False
+        self.completed = []
+        self.threads = [threading.Thread(target=self._worker, args=(i,), daemon=True) for i in range(lanes)]
+        for t in self.threads:
+            t.start()
+
+    # ---------------------------------------------------------------- API
+    def submit(self, req):
+        with self.cv:
+            req.t_submit = time.perf_counter()
+            self.queues[req.cid].append(req)
+            self.cv.notify_all()
+        return req
+
+    def close(self):
+        with self.cv:
+            self.stop = True
+            self.cv.notify_all()
+        for t in self.threads:
+            t.join()
+        for r, _ in list(self.resident.values()):
+            r.free()
+        self.resident.clear()
+        for c in self.lanes:
+            c.close()
+
+    def latencies(self):
+        return np.array([r.t_done - r.t_submit for r in self.completed])
+
+    # ---------------------------------------------------------------- scheduling
+    def _pick(self, lane):
+        """Oldest pending request of a client that is idle and admissible."""
+        best = None
+        for cid, q in self.queues.items():
+            if not q or cid in self.busy:
+                continue
+            if cid in self.resident and self.resident[cid][1] != lane:
+                continue  # resident on another lane's context
+            if best is None or q[0].t_submit < self.queues[best][0].t_submit:
+                best = cid
+        return best
+
+    def _admit(self, cid, lane):
+        spec = self.specs[cid]
+        need = spec.footprint(self.prec)
+        if need > self.budget:
+            raise MemoryError(f"client {cid} needs {need} bytes, more than the HBM budget")
+        while self.used + need > self.budget:
+            idle = [(r.last_used, c) for c, (r, _) in self.resident.items() if c not in self.busy]
+            if not idle:
+                return False
+            _, victim = min(idle)
+            r, _ = self.resident.pop(victim)
+            self.used -= r.spec.footprint(self.prec)
+            r.free()
+        self.used += need
+        self.resident[cid] = (None, lane)  # reserved; built outside the lock
+        return True
+
+    def _worker(self, lane):
+        ctx = self.lanes[lane]
+        while True:
+            with self.cv:
+                while True:
+                    if self.stop:
+                        return
+                    cid = self._pick(lane)
+                    if cid is not None and (cid in self.resident or self._admit(cid, lane)):
+                        break
+                    self.cv.wait(0.01)
+                self.busy.add(cid)
+                req = self.queues[cid].popleft()
+            try:
+                res = self.resident[cid][0]
+                if res is None:
+                    res = _Resident(self.specs[cid], ctx, self.prec, self.tiered)
+                    self.resident[cid] = (res, lane)
+                req.t_start = time.perf_counter()
+                req.value = res.run(req.theta, req.seed)
+                res.last_used = time.perf_counter()
+            except Exception as e:  # reported on the request; the server keeps serving
+                req.error = e
+            req.t_done = time.perf_counter()
+            with self.cv:
+                self.busy.discard(cid)
+                self.completed.append(req)
+                self.cv.notify_all()
+            req.done.set()
+
+
+def plain_request(spec, theta, seed, ctx, prec="c128"):
+    """The plain per-call path: fresh state, one sweep per gate (and one call per
+    channel), <H> at the end; the comparison point of the serving engine."""
+    from .engine import apply
+    n = spec.n
+    if spec.kind == "traj":
+        from .trajectories import run_trajectories
+        st, _ = run_trajectories([_noisy(spec, hea_ops(n, spec.depth, theta))], n, spec.ntraj, prec=prec,
+                                 rng=np.random.default_rng(seed), ctx=ctx)
+        v = _expect_h(st, spec.terms, -1)
+        st.free()
+        return v
+    ops = hea_ops(n, spec.depth, theta)
+    if spec.kind == "dm":
+        st = GPUDensity(n, prec, 1, ctx)
+        apply(_noisy(spec, ops), st)
+    else:
+        st = GPUState(n, prec, 1, ctx)
+        apply(ops, st)
+    v = _expect_h(st, spec.terms)
+    st.free()
+    return v

@@ -318,7 +318,7 @@ struct Offs {
 };
 
 template <typename R, int M, int NB>
-__global__ void __launch_bounds__(BT_TILE_THREADS, 2) k_fused(typename CT<R>::T* __restrict__ psi,
+__global__ void __launch_bounds__(1 << (M - NB), 2) k_fused(typename CT<R>::T* __restrict__ psi,
                                                               const FusedArgs<R> a) {
   typedef typename CT<R>::T C2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -347,17 +347,18 @@ __global__ void __launch_bounds__(BT_TILE_THREADS, 2) k_fused(typename CT<R>::T*
     }
     C2* g = psi + (mem << a.nbits) + base;
     // every 16-byte load of the tile in flight at once (NPT per thread), then to smem
-    constexpr int NPT = NCHUNK / BT_TILE_THREADS;
+    constexpr int T = 1 << (M - NB);
+    constexpr int NPT = NCHUNK / T;
     {
       float4 buf[NPT];
 #pragma unroll
       for (int i = 0; i < NPT; ++i) {
-        const int l = (threadIdx.x + i * BT_TILE_THREADS) * V;
+        const int l = (threadIdx.x + i * T) * V;
         buf[i] = __ldcs(reinterpret_cast<const float4*>(g + runoff[l >> c] + (l & cmask)));
       }
 #pragma unroll
       for (int i = 0; i < NPT; ++i) {
-        const int l = (threadIdx.x + i * BT_TILE_THREADS) * V;
+        const int l = (threadIdx.x + i * T) * V;
         if constexpr (V == 2) {
           tile[swz<R>(l)] = make_float2(buf[i].x, buf[i].y);
           tile[swz<R>(l + 1)] = make_float2(buf[i].z, buf[i].w);
@@ -421,7 +422,7 @@ __global__ void __launch_bounds__(BT_TILE_THREADS, 2) k_fused(typename CT<R>::T*
       float4 buf[NPT];
 #pragma unroll
       for (int i = 0; i < NPT; ++i) {
-        const int l = (threadIdx.x + i * BT_TILE_THREADS) * V;
+        const int l = (threadIdx.x + i * T) * V;
         if constexpr (V == 2) {
           const C2 v0 = tile[swz<R>(l)], v1 = tile[swz<R>(l + 1)];
           buf[i] = make_float4(v0.x, v0.y, v1.x, v1.y);
@@ -431,7 +432,7 @@ __global__ void __launch_bounds__(BT_TILE_THREADS, 2) k_fused(typename CT<R>::T*
       }
 #pragma unroll
       for (int i = 0; i < NPT; ++i) {
-        const int l = (threadIdx.x + i * BT_TILE_THREADS) * V;
+        const int l = (threadIdx.x + i * T) * V;
         __stcs(reinterpret_cast<float4*>(g + runoff[l >> c] + (l & cmask)), buf[i]);
       }
     }
@@ -453,17 +454,28 @@ static int launch_fused(bt_ctx* ctx, void* psi, const FusedArgs<R>& a) {
   int64_t total = (1LL << a.lg_tiles) * a.nmem;
   int64_t grid = (int64_t)ctx->sm_count * 2 * 4;
   if (grid > total) grid = total;
-  k_fused<R, M, NB><<<(unsigned)grid, BT_TILE_THREADS, smem, ctx->stream>>>((C2*)psi, a);
+  k_fused<R, M, NB><<<(unsigned)grid, 1 << (M - NB), smem, ctx->stream>>>((C2*)psi, a);
   ctx->launches++;
   return bt_cuda_check(ctx, cudaGetLastError(), "fused kernel launch");
 }
 
+// tiles smaller than the default hold a whole small state (2^(M-RB) threads per CTA)
 int bt_launch_fused_f(bt_ctx* ctx, void* psi, const FusedArgs<float>& a) {
-  if (a.M != BT_TILE_M_C64) return bt_fail(ctx, BT_ERR_BAD_ARG, "fused pass: unsupported tile size");
-  return launch_fused<float, BT_TILE_M_C64, BT_TILE_RB_C64>(ctx, psi, a);
+  switch (a.M) {
+    case 13: return launch_fused<float, 13, BT_TILE_RB_C64>(ctx, psi, a);
+    case 12: return launch_fused<float, 12, BT_TILE_RB_C64>(ctx, psi, a);
+    case 11: return launch_fused<float, 11, BT_TILE_RB_C64>(ctx, psi, a);
+    case 10: return launch_fused<float, 10, BT_TILE_RB_C64>(ctx, psi, a);
+  }
+  return bt_fail(ctx, BT_ERR_BAD_ARG, "fused pass: unsupported tile size");
 }
 
 int bt_launch_fused_d(bt_ctx* ctx, void* psi, const FusedArgs<double>& a) {
-  if (a.M != BT_TILE_M_C128) return bt_fail(ctx, BT_ERR_BAD_ARG, "fused pass: unsupported tile size");
-  return launch_fused<double, BT_TILE_M_C128, BT_TILE_RB_C128>(ctx, psi, a);
+  switch (a.M) {
+    case 12: return launch_fused<double, 12, BT_TILE_RB_C128>(ctx, psi, a);
+    case 11: return launch_fused<double, 11, BT_TILE_RB_C128>(ctx, psi, a);
+    case 10: return launch_fused<double, 10, BT_TILE_RB_C128>(ctx, psi, a);
+    case 9: return launch_fused<double, 9, BT_TILE_RB_C128>(ctx, psi, a);
+  }
+  return bt_fail(ctx, BT_ERR_BAD_ARG, "fused pass: unsupported tile size");
 }

@@ -16,6 +16,7 @@
 #include <string.h>
 #include <sys/stat.h>
 
+#include <atomic>
 #include <map>
 #include <mutex>
 #include <sstream>
@@ -237,15 +238,16 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
   const int M = a.M, c = a.c, D = 1 << NB;
   const int NM = f ? BT_FUSED_MAX_REALS_F : BT_FUSED_MAX_REALS_D;
   const int V = f ? 2 : 1;
-  const int NPT = (1 << M) / V / BT_TILE_THREADS;
+  const int T = 1 << (M - NB);
+  const int NPT = (1 << M) / V / T;
   const char* T2 = f ? "cf" : "cd";
-  o << "extern \"C\" __global__ void __launch_bounds__(256, 2) " << name << "(" << T2 << "* __restrict__ psi, const "
+  o << "extern \"C\" __global__ void __launch_bounds__(" << T << ", 2) " << name << "(" << T2 << "* __restrict__ psi, const "
     << (f ? "JitArgsF<" : "JitArgsD<") << NM << "> a) {\n";
   o << "  typedef " << (f ? "float" : "double") << " R;\n";
   o << "  extern __shared__ __align__(16) unsigned char smem_raw[];\n";
   o << "  " << T2 << "* tile = reinterpret_cast<" << T2 << "*>(smem_raw);\n";
   o << "  i64* runoff = reinterpret_cast<i64*>(smem_raw + " << ((f ? 8 : 16) << M) << ");\n";
-  o << "  for (int r = threadIdx.x; r < " << (1 << (M - c)) << "; r += 256) { i64 v = 0;";
+  o << "  for (int r = threadIdx.x; r < " << (1 << (M - c)) << "; r += " << T << ") { i64 v = 0;";
   for (int b = 0; b < M - c; ++b) o << " v |= (i64)((r >> " << b << ") & 1) << " << a.tbits[c + b] << ";";
   o << " runoff[r] = v; }\n  __syncthreads();\n";
   o << "  const i64 per = 1LL << a.lg_tiles, total = per * a.nmem;\n";
@@ -259,7 +261,7 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
   // tile load: every 16-byte load in flight, then into the swizzled tile
   o << "    {\n";
   for (int i = 0; i < NPT; ++i)
-    o << "      const int l" << i << " = (threadIdx.x + " << i * BT_TILE_THREADS << ") * " << V << "; const f4 b" << i
+    o << "      const int l" << i << " = (threadIdx.x + " << i * T << ") * " << V << "; const f4 b" << i
       << " = *reinterpret_cast<const f4*>(g + runoff[l" << i << " >> " << c << "] + (l" << i << " & " << ((1 << c) - 1)
       << "));\n";
   for (int i = 0; i < NPT; ++i) {
@@ -300,7 +302,7 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
   }
   o << "    {\n";
   for (int i = 0; i < NPT; ++i) {
-    o << "      const int l" << i << " = (threadIdx.x + " << i * BT_TILE_THREADS << ") * " << V << ";";
+    o << "      const int l" << i << " = (threadIdx.x + " << i * T << ") * " << V << ";";
     if (f)
       o << " const cf u" << i << " = tile[l" << i << " ^ ((l" << i << " >> 4) & 15)], v" << i << " = tile[(l" << i
         << " + 1) ^ (((l" << i << " + 1) >> 4) & 15)]; const f4 b" << i << " = f4{u" << i << ".x, u" << i << ".y, v" << i
@@ -340,8 +342,8 @@ struct JitModule {
 struct JitEntry {
   JitModule* mod = nullptr;
   std::string name;
-  cudaKernel_t kernel = nullptr;
-  bool attr_set[64] = {false};
+  std::atomic<cudaKernel_t> kernel{nullptr};  // resolved at the first launch
+  std::atomic<bool> attr_set[64] = {};         // shared-memory attribute set, per device
 };
 static std::mutex g_jit_mu;
 static std::map<std::string, JitEntry*> g_jit_cache;
@@ -411,16 +413,17 @@ template <typename R>
 static int jit_prepare_t(bt_ctx* ctx, std::vector<const FusedArgs<R>*>& passes, std::vector<void*>& out) {
   out.assign(passes.size(), nullptr);
   if (!nvrtc()) return bt_fail(ctx, BT_ERR_UNSUPPORTED, "NVRTC is not available");
-  std::lock_guard<std::mutex> lk(g_jit_mu);
   std::vector<std::string> keys(passes.size());
   std::vector<std::string> order;                     // new structures in first-seen order
   std::map<std::string, const FusedArgs<R>*> first;
-  for (size_t i = 0; i < passes.size(); ++i) {
-    keys[i] = structure_key(*passes[i]);
-    if (!g_jit_cache.count(keys[i]) && !first.count(keys[i])) {
-      first[keys[i]] = passes[i];
-      order.push_back(keys[i]);
-    }
+  for (size_t i = 0; i < passes.size(); ++i) keys[i] = structure_key(*passes[i]);
+  {
+    std::lock_guard<std::mutex> lk(g_jit_mu);  // held for lookups and inserts, not for compiling
+    for (size_t i = 0; i < passes.size(); ++i)
+      if (!g_jit_cache.count(keys[i]) && !first.count(keys[i])) {
+        first[keys[i]] = passes[i];
+        order.push_back(keys[i]);
+      }
   }
   if (!order.empty()) {
     const int NB = sizeof(R) == 4 ? BT_TILE_RB_C64 : BT_TILE_RB_C128;
@@ -459,14 +462,17 @@ static int jit_prepare_t(bt_ctx* ctx, std::vector<const FusedArgs<R>*>& passes, 
         for (auto* m : mods) delete m;
         return bt_fail(ctx, BT_ERR_DEVICE, errs[b]);
       }
+    std::lock_guard<std::mutex> lk(g_jit_mu);
     for (int b = 0; b < nb; ++b)
       for (size_t i = 0; i < names[b].size(); ++i) {
+        if (g_jit_cache.count(bkeys[b][i])) continue;  // compiled meanwhile by another plan
         JitEntry* je = new JitEntry();
         je->mod = mods[b];
         je->name = names[b][i];
         g_jit_cache[bkeys[b][i]] = je;
       }
   }
+  std::lock_guard<std::mutex> lk(g_jit_mu);
   for (size_t i = 0; i < passes.size(); ++i) out[i] = g_jit_cache[keys[i]];
   return BT_OK;
 }
@@ -492,23 +498,26 @@ static int jit_launch_t(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<R>&
   typedef typename CT<R>::T C2;
   const int M = a.M;
   const size_t smem = (sizeof(C2) << M) + sizeof(int64_t) * (1 << (M - a.c));
-  if (!je->kernel) {  // first launch: load the batch's cubin and resolve the kernel
+  cudaKernel_t kern = je->kernel.load(std::memory_order_acquire);
+  if (!kern) {  // first launch: load the batch's cubin and resolve the kernel
     std::lock_guard<std::mutex> lk(g_jit_mu);
-    if (!je->mod->lib) {
-      cudaError_t e = cudaLibraryLoadData(&je->mod->lib, je->mod->cubin.data(), nullptr, nullptr, 0, nullptr,
-                                          nullptr, 0);
-      if (e != cudaSuccess) return bt_cuda_check(ctx, e, "cudaLibraryLoadData of a plan");
+    kern = je->kernel.load(std::memory_order_acquire);
+    if (!kern) {
+      if (!je->mod->lib) {
+        cudaError_t e = cudaLibraryLoadData(&je->mod->lib, je->mod->cubin.data(), nullptr, nullptr, 0, nullptr,
+                                            nullptr, 0);
+        if (e != cudaSuccess) return bt_cuda_check(ctx, e, "cudaLibraryLoadData of a plan");
+      }
+      cudaError_t e = cudaLibraryGetKernel(&kern, je->mod->lib, je->name.c_str());
+      if (e != cudaSuccess) return bt_cuda_check(ctx, e, "cudaLibraryGetKernel");
+      je->kernel.store(kern, std::memory_order_release);
     }
-    cudaKernel_t k = nullptr;
-    cudaError_t e = cudaLibraryGetKernel(&k, je->mod->lib, je->name.c_str());
-    if (e != cudaSuccess) return bt_cuda_check(ctx, e, "cudaLibraryGetKernel");
-    je->kernel = k;
   }
-  if (ctx->device < 64 && !je->attr_set[ctx->device]) {
-    cudaError_t e = cudaKernelSetAttributeForDevice(je->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                    (int)smem, ctx->device);
+  if (ctx->device < 64 && !je->attr_set[ctx->device].load(std::memory_order_acquire)) {
+    cudaError_t e = cudaKernelSetAttributeForDevice(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem,
+                                                    ctx->device);
     if (e != cudaSuccess) return bt_cuda_check(ctx, e, "jit kernel smem attribute");
-    je->attr_set[ctx->device] = true;
+    je->attr_set[ctx->device].store(true, std::memory_order_release);
   }
   static thread_local JitArgsHost<R> h;
   h.member_lo = a.member_lo;
@@ -520,7 +529,8 @@ static int jit_launch_t(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<R>&
   int64_t total = (1LL << a.lg_tiles) * a.nmem;
   int64_t grid = (int64_t)ctx->sm_count * 2 * 4;
   if (grid > total) grid = total;
-  cudaError_t e = cudaLaunchKernel((const void*)je->kernel, dim3((unsigned)grid), dim3(BT_TILE_THREADS), args, smem,
+  const unsigned threads = 1u << (a.M - (sizeof(R) == 4 ? BT_TILE_RB_C64 : BT_TILE_RB_C128));
+  cudaError_t e = cudaLaunchKernel((const void*)kern, dim3((unsigned)grid), dim3(threads), args, smem,
                                    ctx->stream);
   ctx->launches++;
   return bt_cuda_check(ctx, e, "jit pass launch");

@@ -18,7 +18,10 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
+#include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "bt_fused.cuh"
@@ -29,6 +32,7 @@ struct PGate {
   int bits[2 * BT_MAX_K] = {0};  // bits[0] = most significant bit of the matrix index
   uint64_t cmask = 0;
   std::vector<double> m;  // row-major interleaved 2^k x 2^k
+  int ku = 0, fold_nc = 0;  // the caller's gate size and the controls folded into m
   uint64_t allbits() const {
     uint64_t b = cmask;
     for (int i = 0; i < k; ++i) b |= 1ULL << bits[i];
@@ -41,7 +45,8 @@ struct PPass {
   int gate = -1;
   int ngates = 0;
   std::vector<unsigned char> args;  // FusedArgs<float> or <double>, bytes
-  void* jit = nullptr;              // specialised kernel of this pass (bt_jit.cu), if compiled
+  std::vector<int> op_gate;         // gate of each op, and its register bits before encoding
+  std::vector<uint8_t> op_b0, op_b1;
 };
 
 struct bt_plan {
@@ -49,10 +54,52 @@ struct bt_plan {
   int n = 0, repr = 0, prec = 0, nbits = 0;
   std::vector<PGate> gates;
   std::vector<PPass> passes;
+  std::vector<std::pair<int, int>> adds;  // per bt_plan_add_*: first gate and count (0: not updatable)
   bool compiled = false;
+  int compile_mode = 0;
   int64_t nphases = 0;
-  int64_t njit = 0;
+  // specialised kernel of each pass (bt_jit.cu), published when compiled; the
+  // background compiler of a tiered plan writes them while runs read them
+  std::unique_ptr<std::atomic<void*>[]> jit;
+  std::atomic<int64_t> njit{0};
+  std::thread jit_thread;
 };
+
+static void join_jit(bt_plan* p) {
+  if (p->jit_thread.joinable()) p->jit_thread.join();
+}
+
+// compiles the fused passes' kernels and publishes them pass by pass
+static void specialise(bt_plan* p) {
+  const bool c64 = p->prec == BT_PREC_C64;
+  std::vector<size_t> idx;
+  std::vector<void*> ent;
+  int rc;
+  if (c64) {
+    std::vector<const FusedArgs<float>*> v;
+    for (size_t i = 0; i < p->passes.size(); ++i)
+      if (p->passes[i].kind == 0) {
+        v.push_back(reinterpret_cast<const FusedArgs<float>*>(p->passes[i].args.data()));
+        idx.push_back(i);
+      }
+    rc = bt_jit_prepare_f(p->ctx, v, ent);
+  } else {
+    std::vector<const FusedArgs<double>*> v;
+    for (size_t i = 0; i < p->passes.size(); ++i)
+      if (p->passes[i].kind == 0) {
+        v.push_back(reinterpret_cast<const FusedArgs<double>*>(p->passes[i].args.data()));
+        idx.push_back(i);
+      }
+    rc = bt_jit_prepare_d(p->ctx, v, ent);
+  }
+  if (rc != BT_OK) return;
+  int64_t n = 0;
+  for (size_t j = 0; j < idx.size(); ++j) {
+    p->jit[idx[j]].store(ent[j], std::memory_order_release);
+    n += ent[j] != nullptr;
+  }
+  p->njit.store(n);
+}
 
 static int popc(uint64_t x) { return __builtin_popcountll(x); }
 
@@ -71,7 +118,9 @@ static void kron_ctrl(int k, const double* u_rm, int nc, std::vector<double>& ou
 
 static void add_gate(bt_plan* p, int k, const int* bits, const double* rm, int nc, const int* cbits) {
   PGate g;
+  g.ku = k;
   if (nc > 0 && k + nc <= 2) {
+    g.fold_nc = nc;
     // fold the control into a dense two-bit matrix so the gate can join a tile
     kron_ctrl(k, rm, nc, g.m);
     g.k = k + nc;
@@ -125,9 +174,80 @@ static bool classify_unit(const PGate& g) {
   return true;
 }
 
+// classifies gate g and writes its op type and matrix entries at mat[w...]
+// (o.b0/o.b1 hold the register bits of the gate's first/second bit on entry)
+template <typename R>
+static void encode_op(const PGate& g, FOp& o, R* mat, int& w) {
+  int perm[4] = {0, 1, 2, 3};
+  const int cls = classify(g, perm);
+  o.moff = (uint16_t)w;
+  const double* m = g.m.data();
+  if (g.k == 1) {
+    // m = [m00r m00i m01r m01i m10r m10i m11r m11i]
+    const bool real = m[1] == 0 && m[3] == 0 && m[5] == 0 && m[7] == 0;
+    if (cls == 2) {
+      o.type = FOP_D1;
+      mat[w++] = (R)m[0];
+      mat[w++] = (R)m[1];
+      mat[w++] = (R)m[6];
+      mat[w++] = (R)m[7];
+    } else if (cls == 1) {  // anti-diagonal
+      o.type = FOP_X1;
+      o.unit = (m[2] == 1 && m[3] == 0 && m[4] == 1 && m[5] == 0) ? 1 : 0;
+      mat[w++] = (R)m[2];
+      mat[w++] = (R)m[3];
+      mat[w++] = (R)m[4];
+      mat[w++] = (R)m[5];
+    } else if (real) {
+      o.type = FOP_R1;
+      mat[w++] = (R)m[0];
+      mat[w++] = (R)m[2];
+      mat[w++] = (R)m[4];
+      mat[w++] = (R)m[6];
+    } else if (m[0] == m[6] && m[1] == 0 && m[7] == 0 && m[2] == 0 && m[4] == 0 && m[3] == m[5]) {
+      o.type = FOP_RX1;
+      mat[w++] = (R)m[0];
+      mat[w++] = (R)m[3];
+    } else {
+      o.type = FOP_G1;
+      for (int e = 0; e < 8; ++e) mat[w++] = (R)m[e];
+    }
+  } else if (cls == 1 && classify_unit(g) && perm[0] == 0 && perm[1] == 1 && perm[2] == 3 && perm[3] == 2) {
+    o.type = FOP_CX;  // control = matrix MSB (register b0), target = LSB (b1)
+  } else if (cls == 1 && classify_unit(g) && perm[0] == 0 && perm[1] == 3 && perm[2] == 2 && perm[3] == 1) {
+    o.type = FOP_CX;  // control = matrix LSB, target = MSB
+    const uint8_t t = o.b0;
+    o.b0 = o.b1;
+    o.b1 = t;
+  } else if (cls == 1 && classify_unit(g) && perm[0] == 0 && perm[1] == 2 && perm[2] == 1 && perm[3] == 3) {
+    o.type = FOP_SW;
+  } else if (cls == 2) {
+    o.type = FOP_D2;
+    for (int r = 0; r < 4; ++r) {
+      mat[w++] = (R)g.m[2 * (r * 4 + r)];
+      mat[w++] = (R)g.m[2 * (r * 4 + r) + 1];
+    }
+  } else if (cls == 1) {
+    o.type = FOP_P2;
+    o.flags = (uint8_t)(perm[0] | (perm[1] << 2) | (perm[2] << 4) | (perm[3] << 6));
+    bool unit = true;
+    for (int r = 0; r < 4; ++r) {
+      double pr = g.m[2 * (r * 4 + perm[r])], pi = g.m[2 * (r * 4 + perm[r]) + 1];
+      if (pr != 1.0 || pi != 0.0) unit = false;
+      mat[w++] = (R)pr;
+      mat[w++] = (R)pi;
+    }
+    o.unit = unit ? 1 : 0;
+  } else {
+    o.type = FOP_G2;
+    for (int e = 0; e < 32; ++e) mat[w++] = (R)g.m[e];
+  }
+}
+
 template <typename R>
 static bool build_fused(bt_plan* p, const std::vector<int>& take, uint64_t tilemask, int M, int NB, int c,
-                        std::vector<int>& kept, FusedArgs<R>& a, int64_t* nph) {
+                        std::vector<int>& kept, FusedArgs<R>& a, int64_t* nph, std::vector<uint8_t>& ob0,
+                        std::vector<uint8_t>& ob1) {
   memset(&a, 0, sizeof(a));
   a.nbits = p->nbits;
   a.M = M;
@@ -193,73 +313,12 @@ static bool build_fused(bt_plan* p, const std::vector<int>& take, uint64_t tilem
   }
   // write matrices compactly in op order
   int w = 0;
+  ob0.clear();
+  ob1.clear();
   for (int i = 0; i < nop; ++i) {
-    const PGate& g = p->gates[kept[i]];
-    FOp& o = a.op[i];
-    int perm[4] = {0, 1, 2, 3};
-    const int cls = classify(g, perm);
-    o.moff = (uint16_t)w;
-    const double* m = g.m.data();
-    if (g.k == 1) {
-      // m = [m00r m00i m01r m01i m10r m10i m11r m11i]
-      const bool real = m[1] == 0 && m[3] == 0 && m[5] == 0 && m[7] == 0;
-      if (cls == 2) {
-        o.type = FOP_D1;
-        a.mat[w++] = (R)m[0];
-        a.mat[w++] = (R)m[1];
-        a.mat[w++] = (R)m[6];
-        a.mat[w++] = (R)m[7];
-      } else if (cls == 1) {  // anti-diagonal
-        o.type = FOP_X1;
-        o.unit = (m[2] == 1 && m[3] == 0 && m[4] == 1 && m[5] == 0) ? 1 : 0;
-        a.mat[w++] = (R)m[2];
-        a.mat[w++] = (R)m[3];
-        a.mat[w++] = (R)m[4];
-        a.mat[w++] = (R)m[5];
-      } else if (real) {
-        o.type = FOP_R1;
-        a.mat[w++] = (R)m[0];
-        a.mat[w++] = (R)m[2];
-        a.mat[w++] = (R)m[4];
-        a.mat[w++] = (R)m[6];
-      } else if (m[0] == m[6] && m[1] == 0 && m[7] == 0 && m[2] == 0 && m[4] == 0 && m[3] == m[5]) {
-        o.type = FOP_RX1;
-        a.mat[w++] = (R)m[0];
-        a.mat[w++] = (R)m[3];
-      } else {
-        o.type = FOP_G1;
-        for (int e = 0; e < 8; ++e) a.mat[w++] = (R)m[e];
-      }
-    } else if (cls == 1 && classify_unit(g) && perm[0] == 0 && perm[1] == 1 && perm[2] == 3 && perm[3] == 2) {
-      o.type = FOP_CX;  // control = matrix MSB (register b0), target = LSB (b1)
-    } else if (cls == 1 && classify_unit(g) && perm[0] == 0 && perm[1] == 3 && perm[2] == 2 && perm[3] == 1) {
-      o.type = FOP_CX;  // control = matrix LSB, target = MSB
-      const uint8_t t = o.b0;
-      o.b0 = o.b1;
-      o.b1 = t;
-    } else if (cls == 1 && classify_unit(g) && perm[0] == 0 && perm[1] == 2 && perm[2] == 1 && perm[3] == 3) {
-      o.type = FOP_SW;
-    } else if (cls == 2) {
-      o.type = FOP_D2;
-      for (int r = 0; r < 4; ++r) {
-        a.mat[w++] = (R)g.m[2 * (r * 4 + r)];
-        a.mat[w++] = (R)g.m[2 * (r * 4 + r) + 1];
-      }
-    } else if (cls == 1) {
-      o.type = FOP_P2;
-      o.flags = (uint8_t)(perm[0] | (perm[1] << 2) | (perm[2] << 4) | (perm[3] << 6));
-      bool unit = true;
-      for (int r = 0; r < 4; ++r) {
-        double pr = g.m[2 * (r * 4 + perm[r])], pi = g.m[2 * (r * 4 + perm[r]) + 1];
-        if (pr != 1.0 || pi != 0.0) unit = false;
-        a.mat[w++] = (R)pr;
-        a.mat[w++] = (R)pi;
-      }
-      o.unit = unit ? 1 : 0;
-    } else {
-      o.type = FOP_G2;
-      for (int e = 0; e < 32; ++e) a.mat[w++] = (R)g.m[e];
-    }
+    ob0.push_back(a.op[i].b0);
+    ob1.push_back(a.op[i].b1);
+    encode_op<R>(p->gates[kept[i]], a.op[i], a.mat, w);
   }
   *nph = a.nphase;
   return !kept.empty();
@@ -285,6 +344,7 @@ int bt_plan_create(bt_ctx* ctx, int n, int repr, int prec, bt_plan** out) {
 }
 
 int bt_plan_free(bt_plan* p) {
+  if (p) join_jit(p);
   delete p;
   return BT_OK;
 }
@@ -312,6 +372,7 @@ int bt_plan_add_matrix(bt_plan* p, int k, const int32_t* qubits, const double* m
   const int n = p->n;
   for (int i = 0; i < k; ++i) bits[i] = n - qubits[i];
   for (int i = 0; i < nctrl; ++i) cb[i] = n - ctrls[i];
+  const int first = (int)p->gates.size();
   add_gate(p, k, bits, rm.data(), nctrl, cb);
   if (p->repr == BT_REPR_DM) {
     for (int i = 0; i < d * d; ++i) rm[2 * i + 1] = -rm[2 * i + 1];
@@ -319,6 +380,7 @@ int bt_plan_add_matrix(bt_plan* p, int k, const int32_t* qubits, const double* m
     for (int i = 0; i < nctrl; ++i) cb[i] = 2 * n - ctrls[i];
     add_gate(p, k, bits, rm.data(), nctrl, cb);
   }
+  p->adds.push_back({first, (int)p->gates.size() - first});
   return BT_OK;
 }
 
@@ -350,19 +412,92 @@ int bt_plan_add_kraus_sum(bt_plan* p, int k, const int32_t* qubits, int nk, cons
     bits[i] = n - qubits[i];
     bits[k + i] = 2 * n - qubits[i];
   }
+  p->adds.push_back({(int)p->gates.size(), 0});  // a channel's matrices are not updatable
   add_gate(p, 2 * k, bits, sup.data(), 0, nullptr);
+  return BT_OK;
+}
+
+}  // extern "C"
+
+template <typename R>
+static bool update_pass(bt_plan* p, PPass& ps, const std::vector<char>& touched) {
+  FusedArgs<R>& a = *reinterpret_cast<FusedArgs<R>*>(ps.args.data());
+  for (size_t i = 0; i < ps.op_gate.size(); ++i) {
+    if (!touched[ps.op_gate[i]]) continue;
+    FOp t = a.op[i];
+    t.b0 = ps.op_b0[i];
+    t.b1 = ps.op_b1[i];
+    t.flags = 0;
+    t.unit = 0;
+    R tmp[32];
+    int tw = 0;
+    encode_op<R>(p->gates[ps.op_gate[i]], t, tmp, tw);
+    const FOp& o = a.op[i];
+    if (t.type != o.type || t.b0 != o.b0 || t.b1 != o.b1 || t.flags != o.flags || t.unit != o.unit) return false;
+    for (int e = 0; e < tw; ++e) a.mat[o.moff + e] = tmp[e];
+  }
+  return true;
+}
+
+extern "C" {
+
+int bt_plan_set_matrices(bt_plan* p, int count, const int64_t* add_index, const double* mats) {
+  if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "plan is NULL");
+  bt_ctx* ctx = p->ctx;
+  if (count < 0 || (count > 0 && (!add_index || !mats))) return bt_fail(ctx, BT_ERR_BAD_ARG, "bad update arrays");
+  std::vector<char> touched(p->gates.size(), 0);
+  size_t off = 0;
+  for (int i = 0; i < count; ++i) {
+    const int64_t ai = add_index[i];
+    if (ai < 0 || ai >= (int64_t)p->adds.size()) return bt_fail(ctx, BT_ERR_BAD_ARG, "add index out of range");
+    const int first = p->adds[ai].first, cnt = p->adds[ai].second;
+    if (cnt == 0) return bt_fail(ctx, BT_ERR_BAD_ARG, "a Kraus sum cannot be updated");
+    const int ku = p->gates[first].ku, d = 1 << ku;
+    std::vector<double> rm(2 * d * d);
+    for (int r = 0; r < d; ++r)
+      for (int c = 0; c < d; ++c) {
+        rm[2 * (r * d + c)] = mats[off + 2 * (r + c * d)];
+        rm[2 * (r * d + c) + 1] = mats[off + 2 * (r + c * d) + 1];
+      }
+    off += 2 * (size_t)d * d;
+    for (int j = 0; j < cnt; ++j) {
+      PGate& g = p->gates[first + j];
+      if (j == 1)  // the column pass of a density-matrix gate applies conj(U)
+        for (int e = 0; e < d * d; ++e) rm[2 * e + 1] = -rm[2 * e + 1];
+      if (g.fold_nc > 0) kron_ctrl(ku, rm.data(), g.fold_nc, g.m);
+      else g.m = rm;
+      touched[first + j] = 1;
+    }
+  }
+  if (!p->compiled) return BT_OK;
+  for (auto& ps : p->passes) {
+    if (ps.kind != 0) continue;
+    const bool ok = p->prec == BT_PREC_C64 ? update_pass<float>(p, ps, touched) : update_pass<double>(p, ps, touched);
+    if (!ok) {  // a gate changed its structural class: recompile at the next run
+      p->compiled = false;
+      break;
+    }
+  }
   return BT_OK;
 }
 
 int bt_plan_compile(bt_plan* p, int mode) {
   if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "plan is NULL");
+  if (mode < 0 || mode > 2) return bt_fail(p->ctx, BT_ERR_BAD_ARG, "compile mode must be 0, 1 or 2");
+  join_jit(p);  // a background compile reads the passes about to be rebuilt
+  p->compile_mode = mode;
   p->passes.clear();
   p->nphases = 0;
   const bool c64 = p->prec == BT_PREC_C64;
-  const int M = c64 ? BT_TILE_M_C64 : BT_TILE_M_C128;
   const int NB = c64 ? BT_TILE_RB_C64 : BT_TILE_RB_C128;
+  // the tile covers the whole state when the state is smaller than the default
+  // tile, down to 2^(M - NB) = 32 threads per CTA
+  const int M = std::min(c64 ? BT_TILE_M_C64 : BT_TILE_M_C128, p->nbits);
   const int c = c64 ? BT_TILE_LOW_C64 : BT_TILE_LOW_C128;
-  const bool fuse = mode == 0 && p->nbits >= M;
+  const bool fuse = (mode == 0 || mode == 2) && M >= NB + 5;
+  // specialised kernels compile in time superlinear in their length: bound the
+  // ops of a pass when they will be specialised
+  const int max_ops = bt_jit_available() ? 64 : BT_FUSED_MAX_OPS;
   std::vector<int> rem(p->gates.size());
   for (size_t i = 0; i < rem.size(); ++i) rem[i] = (int)i;
   const uint64_t lowmask = (1ULL << c) - 1;
@@ -382,7 +517,7 @@ int bt_plan_compile(bt_plan* p, int mode) {
     for (int gi : rem) {
       const PGate& g = p->gates[gi];
       const uint64_t b = g.allbits();
-      if (!eligible(g) || (b & blocked) || popc(Q | b) > M || (int)take.size() >= BT_FUSED_MAX_OPS) {
+      if (!eligible(g) || (b & blocked) || popc(Q | b) > M || (int)take.size() >= max_ops) {
         blocked |= b;
         continue;
       }
@@ -396,11 +531,14 @@ int bt_plan_compile(bt_plan* p, int mode) {
     int64_t nph = 0;
     if (c64) {
       ps.args.resize(sizeof(FusedArgs<float>));
-      build_fused<float>(p, take, Q, M, NB, c, kept, *reinterpret_cast<FusedArgs<float>*>(ps.args.data()), &nph);
+      build_fused<float>(p, take, Q, M, NB, c, kept, *reinterpret_cast<FusedArgs<float>*>(ps.args.data()), &nph,
+                         ps.op_b0, ps.op_b1);
     } else {
       ps.args.resize(sizeof(FusedArgs<double>));
-      build_fused<double>(p, take, Q, M, NB, c, kept, *reinterpret_cast<FusedArgs<double>*>(ps.args.data()), &nph);
+      build_fused<double>(p, take, Q, M, NB, c, kept, *reinterpret_cast<FusedArgs<double>*>(ps.args.data()), &nph,
+                          ps.op_b0, ps.op_b1);
     }
+    ps.op_gate = kept;
     ps.ngates = (int)kept.size();
     p->nphases += nph;
     p->passes.push_back(std::move(ps));
@@ -412,33 +550,17 @@ int bt_plan_compile(bt_plan* p, int mode) {
       if (!done[gi]) nr.push_back(gi);
     rem.swap(nr);
   }
-  // specialise the fused passes (one NVRTC program for every new pass structure);
-  // without NVRTC, or if it fails, the passes run on the generic k_fused kernel
-  p->njit = 0;
-  if (fuse && bt_jit_available()) {
-    std::vector<void*> ent;
-    int rc;
-    if (c64) {
-      std::vector<const FusedArgs<float>*> v;
-      for (auto& ps : p->passes)
-        if (ps.kind == 0) v.push_back(reinterpret_cast<const FusedArgs<float>*>(ps.args.data()));
-      rc = bt_jit_prepare_f(p->ctx, v, ent);
-    } else {
-      std::vector<const FusedArgs<double>*> v;
-      for (auto& ps : p->passes)
-        if (ps.kind == 0) v.push_back(reinterpret_cast<const FusedArgs<double>*>(ps.args.data()));
-      rc = bt_jit_prepare_d(p->ctx, v, ent);
-    }
-    if (rc == BT_OK) {
-      size_t j = 0;
-      for (auto& ps : p->passes)
-        if (ps.kind == 0) {
-          ps.jit = ent[j++];
-          p->njit += ps.jit != nullptr;
-        }
-    }
-  }
+  // specialise the fused passes (one NVRTC program per batch of new pass
+  // structures); until a pass has its kernel, or without NVRTC, it runs on the
+  // generic k_fused kernel.  Mode 2 compiles on a background thread (tiered).
+  p->jit.reset(new std::atomic<void*>[p->passes.size() + 1]);
+  for (size_t i = 0; i <= p->passes.size(); ++i) p->jit[i].store(nullptr);
+  p->njit.store(0);
   p->compiled = true;
+  if (fuse && bt_jit_available()) {
+    if (mode == 2) p->jit_thread = std::thread([p] { specialise(p); });
+    else specialise(p);
+  }
   return BT_OK;
 }
 
@@ -451,7 +573,7 @@ int bt_plan_stats(const bt_plan* p, int64_t* ngates, int64_t* npasses, int64_t* 
   if (npasses) *npasses = (int64_t)p->passes.size();
   if (nfused) *nfused = nf;
   if (nphases) *nphases = p->nphases;
-  if (njit) *njit = p->njit;
+  if (njit) *njit = p->njit.load();
   return BT_OK;
 }
 
@@ -461,7 +583,7 @@ int bt_plan_run(bt_plan* p, bt_state* s, int64_t member) {
   if (s->n != p->n || s->repr != p->repr || s->prec != p->prec)
     return bt_fail(ctx, BT_ERR_BAD_ARG, "plan and state differ in n, repr or prec");
   if (!p->compiled) {
-    int rc = bt_plan_compile(p, 0);
+    int rc = bt_plan_compile(p, p->compile_mode);
     if (rc) return rc;
   }
   int64_t lo = 0, nm = s->batch;
@@ -480,12 +602,14 @@ int bt_plan_run(bt_plan* p, bt_state* s, int64_t member) {
       FusedArgs<float>& a = *reinterpret_cast<FusedArgs<float>*>(ps.args.data());
       a.member_lo = lo;
       a.nmem = nm;
-      rc = ps.jit ? bt_jit_launch_f(ctx, ps.jit, s->d, a) : bt_launch_fused_f(ctx, s->d, a);
+      void* e = p->jit[i].load(std::memory_order_acquire);
+      rc = e ? bt_jit_launch_f(ctx, e, s->d, a) : bt_launch_fused_f(ctx, s->d, a);
     } else {
       FusedArgs<double>& a = *reinterpret_cast<FusedArgs<double>*>(ps.args.data());
       a.member_lo = lo;
       a.nmem = nm;
-      rc = ps.jit ? bt_jit_launch_d(ctx, ps.jit, s->d, a) : bt_launch_fused_d(ctx, s->d, a);
+      void* e = p->jit[i].load(std::memory_order_acquire);
+      rc = e ? bt_jit_launch_d(ctx, e, s->d, a) : bt_launch_fused_d(ctx, s->d, a);
     }
   }
   return rc;

@@ -161,8 +161,18 @@ int bt_plan_add_matrix(bt_plan* p, int k, const int32_t* qubits, const double* m
                        const int32_t* ctrls);
 /* appends rho <- sum_i K_i rho K_i^dagger (density plans, k <= 2; src/struct.jl:58-76) */
 int bt_plan_add_kraus_sum(bt_plan* p, int k, const int32_t* qubits, int nk, const double* kraus);
-/* mode 0: fused passes; mode 1: one sweep per gate (the unfused reference form) */
+/* mode 0: fused passes, kernels specialised before returning;
+ * mode 1: one sweep per gate (the unfused reference form);
+ * mode 2: fused passes that run on the generic kernel at once while their
+ *         specialised kernels compile on a background thread (tiered) */
 int bt_plan_compile(bt_plan* p, int mode);
+/* new matrices for gates already in the plan (variational parameters: the
+ * reference's type "f" ops evaluated at new pars, src/struct.jl:518-528):
+ * add_index[i] counts bt_plan_add_* calls from 0, mats holds the matrices back to
+ * back in the size each gate was added with.  The compiled passes are rewritten
+ * in place; a gate whose structure changes (e.g. an angle making it diagonal)
+ * makes the next run recompile.  Kraus sums cannot be updated. */
+int bt_plan_set_matrices(bt_plan* p, int count, const int64_t* add_index, const double* mats);
 /* njit: fused passes running as kernels specialised for the plan (NVRTC, compiled
  * by bt_plan_compile); the others run on the generic fused kernel */
 int bt_plan_stats(const bt_plan* p, int64_t* ngates, int64_t* npasses, int64_t* nfused, int64_t* nphases,

@@ -15,6 +15,7 @@ the reference's path (the reference is Julia, not runnable here) on the host
 cores for the same metric.
 """
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -430,6 +431,8 @@ def run_serve(args):
     if errs:
         raise errs[0]
     lat = np.array([r.t_done - r.t_submit for r in reqs]) * 1e3
+    service = {k: float(np.mean([(r.t_done - r.t_start) * 1e3 for r in reqs if specs[r.cid].kind == k] or [0]))
+               for k in ("sv", "traj", "dm")}
     served = total / makespan
     # plain per-call complex128 path on a sample: one request per client, serially
     pctx = bt.Context(0, seed=5)
@@ -449,7 +452,10 @@ def run_serve(args):
             p.add(op)
         p.compile(True).run(a)
         b = bt.apply(S.hea_ops(c.n, c.depth, th), bt.zero_state(c.n, "c128", ctx=pctx))
-        infid = max(infid, 1 - bt.fidelity(a, b))
+        # 1 - |<psi64|psi128>|^2 with the complex64 state renormalised in FP64
+        nrm = np.empty(1)
+        a.ctx.check(bt.lib().bt_norm2(a.h, 0, nrm.ctypes.data_as(ctypes.c_void_p)))
+        infid = max(infid, 1 - bt.fidelity(a, b) / nrm[0])
         a.free()
         b.free()
     pctx.close()
@@ -461,6 +467,7 @@ def run_serve(args):
                        "requests": total, "lanes": args.lanes},
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                            "mean": float(lat.mean())},
+            "mean_service_ms_by_kind": service,
             "plain_c128_circuits_per_s": plain_rate, "vs_plain": served / plain_rate,
             "max_rel_dev_vs_c128": dev, "max_infidelity_c64": infid,
             "roofline": None, "cpu_baseline": None, "e2e": None, "gpu_launches": None}

@@ -72,6 +72,14 @@ SIGNATURES = {
     "bt_plan_set_matrices": (i32, [P, i32, P, P]),
     "bt_plan_stats": (i32, [P, P, P, P, P, P]),
     "bt_plan_run": (i32, [P, P, i64]),
+    "bt_program_create": (i32, [P, i32, i32, i32, ctypes.POINTER(P)]),
+    "bt_program_free": (i32, [P]),
+    "bt_program_add_gate": (i32, [P, i32, P, P, i32]),
+    "bt_program_add_channel": (i32, [P, i32, P, i32, P, i32, P]),
+    "bt_program_add_measure": (i32, [P, i32, P]),
+    "bt_program_info": (i32, [P, P, P, P]),
+    "bt_program_set_gate": (i32, [P, i64, P]),
+    "bt_program_run": (i32, [P, P, P, u64, P]),
     "bt_sample": (i32, [P, i64, i64, P, u64, P]),
     "bt_probabilities": (i32, [P, i64, P]),
     "bt_sample_noalloc": (i32, [P, i32, i32, i64, P, u64, u64, P, P]),

@@ -123,6 +123,8 @@ def _noisy(spec, ops):
 
 
 def _expect_h(st, terms, member=-1):
+    """<H> per member divided by the member's norm (trace), accumulated in FP64:
+    removes the complex64 norm drift of long circuits; averaged over members."""
     lib = L.lib()
     xs = np.ascontiguousarray([t[1] for t in terms], dtype=np.uint64)
     zs = np.ascontiguousarray([t[2] for t in terms], dtype=np.uint64)
@@ -130,7 +132,9 @@ def _expect_h(st, terms, member=-1):
     rows = st.batch if member == -1 else 1
     out = np.empty(rows * len(terms), dtype=np.float64)
     st.ctx.check(lib.bt_expect_pauli(st.h, len(terms), _ptr(xs), _ptr(zs), _ptr(cs), member, _ptr(out)))
-    return float(out.reshape(rows, len(terms)).sum(axis=1).mean())
+    nrm = np.empty(rows, dtype=np.float64)
+    st.ctx.check(lib.bt_norm2(st.h, member, _ptr(nrm)))
+    return float((out.reshape(rows, len(terms)).sum(axis=1) / nrm).mean())
 
 
 class _Resident:
@@ -154,11 +158,20 @@ class _Resident:
             self.plan.compile(True, tiered=tiered)
         else:
             self.state = GPUState(n, prec, spec.ntraj, ctx)
+            self.program = None
+            from . import trajectories as T
+            ops = _noisy(spec, hea_ops(n, spec.depth, theta0))
+            slots = T.build_slots(T.member_programs([ops], n, spec.ntraj))
+            if T.program_supported(slots, n, prec):
+                # one slot per op (no ZNE, no twirl): slot i is op i
+                self.program, gate_ops = T.compile_program(slots, n, spec.ntraj, prec, ctx)
+                self.pidx = [gate_ops[i] for i, op in enumerate(ops) if op.name in ("RY", "RZ")]
         self.last_used = time.perf_counter()
 
     def free(self):
         self.state.free()
         self.plan = None
+        self.program = None
 
     def run(self, theta, seed):
         spec = self.spec
@@ -169,6 +182,12 @@ class _Resident:
                 ups.append((ai, _ry(theta[j]) if j % 2 == 0 else _rz(theta[j])))
             self.plan.set_matrices(ups).run(self.state)
             return _expect_h(self.state, spec.terms)
+        if self.program is not None:
+            for j, oi in enumerate(self.pidx):
+                self.program.set_gate(oi, _ry(theta[j]) if j % 2 == 0 else _rz(theta[j]))
+            # draws from the request's seed, in the order the plain path consumes them
+            self.program.run(self.state, rng=np.random.default_rng(seed), records=False)
+            return _expect_h(self.state, spec.terms, -1)
         from .trajectories import run_trajectories
         steps = [_noisy(spec, hea_ops(spec.n, spec.depth, theta))]
         run_trajectories(steps, spec.n, spec.ntraj, prec=self.prec, rng=np.random.default_rng(seed),
@@ -297,7 +316,7 @@ def plain_request(spec, theta, seed, ctx, prec="c128"):
     if spec.kind == "traj":
         from .trajectories import run_trajectories
         st, _ = run_trajectories([_noisy(spec, hea_ops(n, spec.depth, theta))], n, spec.ntraj, prec=prec,
-                                 rng=np.random.default_rng(seed), ctx=ctx)
+                                 rng=np.random.default_rng(seed), ctx=ctx, engine="slots")
         v = _expect_h(st, spec.terms, -1)
         st.free()
         return v

@@ -23,7 +23,8 @@ from .gates import gate
 from .noise import NoiseModel, QuantumChannel, twirl_set
 from .ops import Op, OpQC, ifOp
 
-__all__ = ["Slot", "expand_member", "build_slots", "run_slots", "run_trajectories"]
+__all__ = ["Slot", "expand_member", "build_slots", "run_slots", "run_trajectories", "Program", "compile_program",
+           "program_supported"]
 
 _ID2 = np.eye(2, dtype=np.complex128)
 
@@ -187,6 +188,165 @@ def run_slots(state, slots, rng=None, records=True):
     return recs
 
 
+PROGRAM_MAX_N = {"c64": 14, "c128": 13, "complex64": 14, "complex128": 13}
+
+
+class Program:
+    """A noisy circuit run whole on the GPU, one CTA per member, the member in
+    shared memory (bt_program): every gate, Kraus branch and measurement of a
+    trajectory batch in one launch.  Built from lock-step slots by
+    compile_program; run() fills the records of the measurements."""
+
+    def __init__(self, n, batch, prec="c64", ctx=None):
+        from .engine import Context, _PREC
+        self.ctx = ctx or Context.default()
+        self.n, self.batch, self.prec = n, batch, prec
+        h = ctypes.c_void_p()
+        self.ctx.check(L.lib().bt_program_create(self.ctx.h, n, _PREC[prec], batch, ctypes.byref(h)))
+        self.h = h
+        self.nops = 0
+        self.rec_masks = []  # per record slot: bool per member, True where the member is measured
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                L.lib().bt_program_free(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def add_gate(self, mats, qubits):
+        """mats: one matrix, or a list of batch matrices (per member)."""
+        per = isinstance(mats, (list, tuple))
+        buf = np.ascontiguousarray(np.concatenate([_cm(m).ravel() for m in mats]) if per else _cm(mats).ravel())
+        q = _i32(qubits)
+        self.ctx.check(L.lib().bt_program_add_gate(self.h, len(q), _ptr(q), _ptr(buf), int(per)))
+        self.nops += 1
+        return self.nops - 1
+
+    def set_gate(self, index, mats):
+        per = isinstance(mats, (list, tuple))
+        buf = np.ascontiguousarray(np.concatenate([_cm(m).ravel() for m in mats]) if per else _cm(mats).ravel())
+        self.ctx.check(L.lib().bt_program_set_gate(self.h, int(index), _ptr(buf)))
+
+    def add_channel(self, kraus, qubits, skip=None, unitary_mix=False):
+        K = np.ascontiguousarray(np.concatenate([_cm(k).ravel() for k in kraus]))
+        q = _i32(qubits)
+        flags = L.BT_KRAUS_TRAJ | L.BT_KRAUS_REF_ORDER | (L.BT_KRAUS_UNITARY_MIX if unitary_mix else 0)
+        sk = None if skip is None else _i32(skip)
+        self.ctx.check(L.lib().bt_program_add_channel(self.h, len(q), _ptr(q), len(kraus), _ptr(K), flags, _ptr(sk)))
+        self.nops += 1
+        return self.nops - 1
+
+    def add_measure(self, qubit, skip=None):
+        sk = None if skip is None else _i32(skip)
+        self.ctx.check(L.lib().bt_program_add_measure(self.h, int(qubit), _ptr(sk)))
+        self.rec_masks.append(np.ones(self.batch, bool) if skip is None else ~np.asarray(skip, bool))
+        self.nops += 1
+        return self.nops - 1
+
+    @property
+    def ndraws(self):
+        v = ctypes.c_int64(0)
+        self.ctx.check(L.lib().bt_program_info(self.h, None, ctypes.byref(v), None))
+        return v.value
+
+    def run(self, state, rng=None, seed=0, records=True):
+        """Runs every member of `state` through the program.  rng: numpy Generator
+        whose draws (ndraws x batch, in op order, as run_slots consumes them) decide
+        branches and outcomes, or None for on-device Philox keyed by `seed`.
+        Returns per-member measurement records (lists), or None."""
+        u = None
+        if rng is not None:
+            nd = self.ndraws
+            if nd:
+                u = np.ascontiguousarray(rng.random((nd, self.batch)))
+        nrec = len(self.rec_masks)
+        out = np.empty((self.batch, max(nrec, 1)), dtype=np.int32) if (records and nrec) else None
+        state.ctx.check(L.lib().bt_program_run(self.h, state.h, _ptr(u), int(seed) & (2 ** 64 - 1), _ptr(out)))
+        if not records:
+            return None
+        recs = [[] for _ in range(self.batch)]
+        for r, mask in enumerate(self.rec_masks):
+            for m in np.nonzero(mask)[0]:
+                recs[m].append(int(out[m, r]))
+        return recs
+
+
+def _ctrl_matrix(mat):
+    """|0><0| (x) I + |1><1| (x) U on (control, target), control the matrix MSB."""
+    d = mat.shape[0]
+    M = np.eye(2 * d, dtype=np.complex128)
+    M[d:, d:] = mat
+    return M
+
+
+def program_supported(slots, n, prec):
+    if n < 2 or n > PROGRAM_MAX_N.get(prec, 0):
+        return False
+    for sl in slots:
+        live = [it for it in sl.items if it is not None]
+        if not live:
+            continue
+        if sl.kind == "gate":
+            if any(len(it[1]) + len(it[2]) > 2 or (len(it[1]) == 2 and it[2]) for it in live):
+                return False
+        elif sl.kind == "channel":
+            if len(live[0][1]) > 2:
+                return False
+    return True
+
+
+def compile_program(slots, n, batch, prec="c64", ctx=None, unitary_mix=True):
+    """Lock-step slots -> Program.  unitary_mix: channels whose Kraus operators are
+    multiples of unitaries draw their branch from |c_i|^2 without reducing the
+    state (exact for normalised members; set False for draw-for-draw agreement with
+    run_slots under explicit draws).  Returns (program, gate_ops) with gate_ops[i]
+    the program op index of slot i (gates only, else None)."""
+    prog = Program(n, batch, prec, ctx)
+    gate_ops = []
+    for sl in slots:
+        items = sl.items
+        live = [it for it in items if it is not None]
+        if not live:
+            gate_ops.append(None)
+            continue
+        if sl.kind == "gate":
+            def full(it):
+                mat, qs, ctrls = it
+                return (_ctrl_matrix(np.asarray(mat, np.complex128)), [ctrls[0], qs[0]]) if ctrls else (mat, list(qs))
+            fl = [full(it) if it is not None else None for it in items]
+            qs = fl[items.index(live[0])][1]
+            if any(f is not None and f[1] != qs for f in fl):
+                raise ValueError("members disagree on the qubits of a gate position")
+            if _same_gate(items):
+                gate_ops.append(prog.add_gate(fl[0][0], qs))
+            else:
+                d = 2 ** len(qs)
+                gate_ops.append(prog.add_gate([f[0] if f is not None else np.eye(d) for f in fl], qs))
+        elif sl.kind == "channel":
+            kraus, qs = live[0]
+            if any(it[1] != qs or (it[0] is not kraus and not all(np.array_equal(a, b) for a, b in zip(it[0], kraus)))
+                   for it in live):
+                raise ValueError("members disagree on the channel at one position")
+            skip = None if len(live) == batch else [0 if it is not None else 1 for it in items]
+            prog.add_channel(kraus, list(qs), skip, unitary_mix and _unitary_mix(kraus))
+            gate_ops.append(None)
+        else:
+            name, qubit = live[0]
+            up = name.upper()
+            rot = None if up in ("MZ", "M(Z)") else (gate["H"] if up in ("MX", "M(X)") else gate["HSP"])
+            skip = None if len(live) == batch else [0 if it is not None else 1 for it in items]
+            if rot is not None:
+                prog.add_gate(rot if skip is None else [rot if not s else _ID2 for s in skip], [qubit])
+            prog.add_measure(qubit, skip)
+            if rot is not None:
+                rd = rot.conj().T
+                prog.add_gate(rd if skip is None else [rd if not s else _ID2 for s in skip], [qubit])
+            gate_ops.append(None)
+    return prog, gate_ops
+
+
 def member_programs(steps, n, batch, zne_ids=None, twirl=False, frame_rng=None, measure_prob=0.0,
                     measure_rng=None):
     """Per-member segment lists: each circuit op expanded for the member (ZNE,
@@ -209,18 +369,28 @@ def member_programs(steps, n, batch, zne_ids=None, twirl=False, frame_rng=None, 
 
 
 def run_trajectories(steps, n, batch, noise=False, zne_ids=None, twirl=False, prec="c64", rng=None, frame_rng=None,
-                     measure_prob=0.0, measure_rng=None, ctx=None, state=None):
+                     measure_prob=0.0, measure_rng=None, ctx=None, state=None, engine="auto", seed=0):
     """`batch` trajectories of a circuit given as a list of steps (lists of ops)
     from |0...0> (or the given batched `state`) in one batched state.
 
     zne_ids: per-member ZNE id (None: all 0).  twirl: Pauli-twirl CNOTs per member
     (frames drawn from frame_rng).  measure_prob: after each step every qubit of
     every member is measured in Z with this probability (masks from measure_rng).
+    engine: "program" (the whole batch in one launch, members in shared memory;
+    n <= 14 complex64 / 13 complex128, ops on <= 2 qubits), "slots" (one launch
+    sequence per op over the batch) or "auto" (program when it applies).  rng
+    gives the draws in the same order on both engines; without it the draws come
+    from on-device Philox (`seed` for the program engine).
     Returns (state, records)."""
     if steps and not isinstance(steps[0], (list, tuple)):
         steps = [steps]
     member_ops = member_programs(steps, n, batch, zne_ids, twirl, frame_rng, measure_prob, measure_rng)
     slots = build_slots(member_ops, noise)
     st = state if state is not None else GPUState(n, prec, batch, ctx)
-    recs = run_slots(st, slots, rng=rng)
+    use_prog = engine == "program" or (engine == "auto" and program_supported(slots, n, prec))
+    if use_prog:
+        prog, _ = compile_program(slots, n, batch, prec, st.ctx, unitary_mix=rng is None)
+        recs = prog.run(st, rng=rng, seed=seed)
+    else:
+        recs = run_slots(st, slots, rng=rng)
     return st, recs

@@ -1,0 +1,536 @@
+// Noisy-circuit programs executed whole inside one CTA per member.
+//
+// For members small enough to live in shared memory (2^n complex numbers,
+// n <= 14 for complex64 and 13 for complex128), a trajectory batch runs its whole
+// op sequence -- gates, Monte-Carlo Kraus branches and mid-circuit measurements --
+// in a single launch: CTA m loads member m into shared memory, and for every
+// channel or measurement reduces the reduced density matrix of its qubits in FP64
+// across the block, lets thread 0 draw the branch / outcome with the rules of the
+// reference (first i with u <= cumsum(p), src/hilbert.jl:810-819; u < p0,
+// src/hilbert.jl:693), and applies the renormalised Kraus operator or projector.
+// There is no host round trip and no global synchronisation between ops: this is
+// the per-shot loop of the reference's noisy measure(circuit, shots)
+// (src/ops.jl:617-630: to_state once per shot) with every shot a CTA.  Members whose program is shorter
+// (ZNE repetitions, no measurement at that point) skip ops through per-member
+// flags; per-member gate matrices carry twirl frames.
+#include <string.h>
+
+#include <atomic>
+#include <vector>
+
+#include "bt_internal.cuh"
+
+enum { PG_GATE1 = 1, PG_GATE2 = 2, PG_CHANNEL = 3, PG_MEASURE = 4 };
+
+struct PGOp {
+  int type;
+  int b0, b1;      // bit positions; b0 = most significant bit of the matrix index
+  int k, nk;       // channel: qubits and Kraus operators
+  int flags;       // channel: 1 reference branch order for the pair, 2 unitary mixture
+  int moff;        // gate: offset into gm (reals); channel: offset into km (reals)
+  int mstride;     // gate: per-member stride in gm (0: one matrix for all)
+  int skip_off;    // offset into the skip table (one byte per member), -1: none
+  int rand_idx;    // index of this op's draw, -1: none
+  int rec_idx;     // measurement: record slot
+};
+
+struct bt_program {
+  bt_ctx* ctx = nullptr;
+  int n = 0, prec = 0, batch = 0;
+  std::vector<PGOp> ops;
+  std::vector<double> gm;   // gate matrices, row-major interleaved (converted to the state precision)
+  std::vector<double> km;   // Kraus sets, row-major interleaved FP64
+  std::vector<int8_t> skip;
+  int ndraws = 0, nrec = 0;
+  // device copies
+  bool uploaded = false;
+  bool gm_dirty = false;     // gate matrices rewritten since the upload
+  std::vector<float> gstage; // complex64 copy of gm for uploads
+  void* d_ops = nullptr;
+  void* d_gm = nullptr;
+  void* d_km = nullptr;
+  void* d_skip = nullptr;
+  void* d_rec = nullptr;
+  void* d_u = nullptr;
+  size_t u_bytes = 0;
+};
+
+#define PG_THREADS 256
+#define FULLM 0xffffffffu
+
+template <int W>
+__device__ __forceinline__ void block_reduce(double (&v)[W], double* sh /* 8*W */) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    double x = v[w];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(FULLM, x, o);
+    if (lane == 0) sh[warp * W + w] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < W) {
+    double s = 0;
+    for (int i = 0; i < PG_THREADS / 32; ++i) s += sh[i * W + threadIdx.x];
+    sh[8 * W + threadIdx.x] = s;  // results after the per-warp partials
+  }
+  __syncthreads();
+}
+
+template <typename R>
+__device__ __forceinline__ void apply1(typename CT<R>::T* st, int nbits, int b, const R* m) {
+  const int np = 1 << (nbits - 1);
+  const R m00r = m[0], m00i = m[1], m01r = m[2], m01i = m[3], m10r = m[4], m10i = m[5], m11r = m[6], m11i = m[7];
+  for (int p = threadIdx.x; p < np; p += PG_THREADS) {
+    const int i0 = ((p >> b) << (b + 1)) | (p & ((1 << b) - 1)), i1 = i0 | (1 << b);
+    typename CT<R>::T a = st[i0], c = st[i1];
+    typename CT<R>::T x, y;
+    x.x = m00r * a.x - m00i * a.y + m01r * c.x - m01i * c.y;
+    x.y = m00r * a.y + m00i * a.x + m01r * c.y + m01i * c.x;
+    y.x = m10r * a.x - m10i * a.y + m11r * c.x - m11i * c.y;
+    y.y = m10r * a.y + m10i * a.x + m11r * c.y + m11i * c.x;
+    st[i0] = x;
+    st[i1] = y;
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void apply2(typename CT<R>::T* st, int nbits, int b0, int b1, const R* m) {
+  const int lo = b0 < b1 ? b0 : b1, hi = b0 < b1 ? b1 : b0;
+  const int nq = 1 << (nbits - 2);
+  for (int p = threadIdx.x; p < nq; p += PG_THREADS) {
+    int base = ((p >> lo) << (lo + 1)) | (p & ((1 << lo) - 1));
+    base = ((base >> hi) << (hi + 1)) | (base & ((1 << hi) - 1));
+    const int q[4] = {base, base | (1 << b1), base | (1 << b0), base | (1 << b0) | (1 << b1)};
+    R ar[4], ai[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      typename CT<R>::T v = st[q[c]];
+      ar[c] = v.x;
+      ai[c] = v.y;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      R yr = 0, yi = 0;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const R mr = m[2 * (4 * r + c)], mi = m[2 * (4 * r + c) + 1];
+        yr += mr * ar[c] - mi * ai[c];
+        yi += mr * ai[c] + mi * ar[c];
+      }
+      typename CT<R>::T v;
+      v.x = yr;
+      v.y = yi;
+      st[q[r]] = v;
+    }
+  }
+}
+
+// reduced density matrix of k = 1 / 2 bits (row-major interleaved, FP64) into rho
+template <typename R, int K>
+__device__ void reduce_rho(const typename CT<R>::T* st, int nbits, int b0, int b1, double* sh, double* rho) {
+  constexpr int D = 1 << K, W = 2 * D * D;
+  double acc[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) acc[w] = 0;
+  const int lo = K == 2 ? (b0 < b1 ? b0 : b1) : b0, hi = K == 2 ? (b0 < b1 ? b1 : b0) : b0;
+  const int ng = 1 << (nbits - K);
+  for (int p = threadIdx.x; p < ng; p += PG_THREADS) {
+    int base = ((p >> lo) << (lo + 1)) | (p & ((1 << lo) - 1));
+    if (K == 2) base = ((base >> hi) << (hi + 1)) | (base & ((1 << hi) - 1));
+    double xr[D], xi[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      int idx = base;
+      if (K == 1) idx |= (j & 1) << b0;
+      else idx |= ((j >> 1) & 1) << b0 | (j & 1) << b1;
+      typename CT<R>::T v = st[idx];
+      xr[j] = (double)v.x;
+      xi[j] = (double)v.y;
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+#pragma unroll
+      for (int b = 0; b < D; ++b) {
+        acc[2 * (a * D + b)] += xr[a] * xr[b] + xi[a] * xi[b];
+        acc[2 * (a * D + b) + 1] += xi[a] * xr[b] - xr[a] * xi[b];
+      }
+  }
+  block_reduce<W>(acc, sh);
+  if (threadIdx.x < W) rho[threadIdx.x] = sh[8 * W + threadIdx.x];
+  __syncthreads();
+}
+
+__device__ double tr_krk(const double* K, const double* r, int D, bool diag_rho, bool ref_perm) {
+  const int perm[4] = {0, 2, 1, 3};
+  double p = 0;
+  for (int c = 0; c < D; ++c)
+    for (int a = 0; a < D; ++a) {
+      const double kar = K[2 * (c * D + a)], kai = K[2 * (c * D + a) + 1];
+      for (int b = 0; b < D; ++b) {
+        const int ra = ref_perm ? perm[a] : a, rb = ref_perm ? perm[b] : b;
+        const double rr = diag_rho ? (ra == rb ? 1.0 / D : 0.0) : r[2 * (ra * D + rb)];
+        const double ri = diag_rho ? 0.0 : r[2 * (ra * D + rb) + 1];
+        const double kbr = K[2 * (c * D + b)], kbi = -K[2 * (c * D + b) + 1];
+        const double tr_ = kar * rr - kai * ri, ti = kar * ri + kai * rr;
+        p += tr_ * kbr - ti * kbi;
+      }
+    }
+  return p;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(PG_THREADS) k_program(typename CT<R>::T* __restrict__ states, int nbits,
+                                                        const PGOp* __restrict__ ops, int nops,
+                                                        const R* __restrict__ gm, const double* __restrict__ km,
+                                                        const int8_t* __restrict__ skip, const double* __restrict__ u,
+                                                        uint64_t key, uint64_t stream, int batch,
+                                                        int32_t* __restrict__ rec, int nrec, int* __restrict__ status) {
+  typedef typename CT<R>::T C2;
+  extern __shared__ __align__(16) unsigned char smem[];
+  C2* st = reinterpret_cast<C2*>(smem);
+  double* sh = reinterpret_cast<double*>(smem + (sizeof(C2) << nbits));  // 9 * 32 doubles
+  R* mat = reinterpret_cast<R*>(sh + 9 * 32);                             // 32 reals
+  __shared__ int s_ok;
+  const int m = blockIdx.x;
+  C2* g = states + ((int64_t)m << nbits);
+  const int len = 1 << nbits;
+  for (int i = threadIdx.x; i < len; i += PG_THREADS) st[i] = g[i];
+  __syncthreads();
+  for (int oi = 0; oi < nops; ++oi) {
+    const PGOp op = ops[oi];
+    if (op.skip_off >= 0 && skip[op.skip_off + m]) {  // uniform across the block
+      if (op.type == PG_MEASURE && threadIdx.x == 0) rec[(int64_t)m * nrec + op.rec_idx] = -1;
+      continue;
+    }
+    if (op.type == PG_GATE1) {
+      apply1<R>(st, nbits, op.b0, gm + op.moff + (int64_t)op.mstride * m);
+      __syncthreads();
+    } else if (op.type == PG_GATE2) {
+      apply2<R>(st, nbits, op.b0, op.b1, gm + op.moff + (int64_t)op.mstride * m);
+      __syncthreads();
+    } else if (op.type == PG_CHANNEL) {
+      const int D = 1 << op.k;
+      double* rho = sh + 8 * 32;  // the reduction's result row
+      const bool umix = op.flags & 2;
+      if (!umix) {
+        if (op.k == 1) reduce_rho<R, 1>(st, nbits, op.b0, op.b1, sh, rho);
+        else reduce_rho<R, 2>(st, nbits, op.b0, op.b1, sh, rho);
+      }
+      if (threadIdx.x == 0) {
+        const double uu = u ? u[(int64_t)op.rand_idx * batch + m] : bt_uniform(key, stream ^ (uint64_t)op.rand_idx, m);
+        double cum = 0;
+        int ind = -1;
+        for (int i = 0; i < op.nk; ++i) {
+          cum += tr_krk(km + op.moff + (int64_t)i * 2 * D * D, rho, D, umix, (op.flags & 1) && op.k == 2);
+          if (ind < 0 && uu <= cum) ind = i;
+        }
+        s_ok = 1;
+        double nrm = 0;
+        if (ind >= 0) nrm = tr_krk(km + op.moff + (int64_t)ind * 2 * D * D, rho, D, umix, false);
+        if (ind < 0 || !(nrm > 0)) {
+          atomicExch(status, ind < 0 ? 2 : 3);
+          s_ok = 0;
+        } else {
+          const double sc = 1.0 / sqrt(nrm);
+          const double* K = km + op.moff + (int64_t)ind * 2 * D * D;
+          for (int e = 0; e < 2 * D * D; ++e) mat[e] = (R)(K[e] * sc);
+        }
+      }
+      __syncthreads();
+      if (s_ok) {
+        if (op.k == 1) apply1<R>(st, nbits, op.b0, mat);
+        else apply2<R>(st, nbits, op.b0, op.b1, mat);
+      }
+      __syncthreads();
+    } else if (op.type == PG_MEASURE) {
+      double* rho = sh + 8 * 32;
+      reduce_rho<R, 1>(st, nbits, op.b0, 0, sh, rho);
+      if (threadIdx.x == 0) {
+        const double s0 = rho[0], s1 = rho[6];
+        const double uu = u ? u[(int64_t)op.rand_idx * batch + m] : bt_uniform(key, stream ^ (uint64_t)op.rand_idx, m);
+        const int ind = uu < s0 ? 0 : 1;
+        const double keep = ind ? s1 : s0;
+        s_ok = keep > 0;
+        if (!s_ok) atomicExch(status, 1);
+        rec[(int64_t)m * nrec + op.rec_idx] = s_ok ? ind : -1;
+        mat[0] = s_ok ? (R)(1.0 / sqrt(keep)) : (R)1;
+        mat[1] = (R)ind;
+      }
+      __syncthreads();
+      if (s_ok) {
+        const int ind = (int)mat[1];
+        const R sc = mat[0];
+        for (int i = threadIdx.x; i < len; i += PG_THREADS) {
+          C2 v = st[i];
+          if (((i >> op.b0) & 1) == ind) {
+            v.x *= sc;
+            v.y *= sc;
+          } else {
+            v.x = 0;
+            v.y = 0;
+          }
+          st[i] = v;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int i = threadIdx.x; i < len; i += PG_THREADS) g[i] = st[i];
+}
+
+// ------------------------------------------------------------------ host API
+static int prog_qubits(bt_program* p, int k, const int32_t* q) {
+  if (k < 1 || k > 2 || !q) return bt_fail(p->ctx, BT_ERR_UNSUPPORTED, "program ops act on 1 or 2 qubits");
+  for (int i = 0; i < k; ++i)
+    if (q[i] < 1 || q[i] > p->n) return bt_fail(p->ctx, BT_ERR_BAD_ARG, "N must be larger than qubits");
+  if (k == 2 && q[0] == q[1]) return bt_fail(p->ctx, BT_ERR_BAD_ARG, "qubits must differ");
+  return BT_OK;
+}
+
+static int prog_skip(bt_program* p, const int32_t* skip) {
+  if (!skip) return -1;
+  const int off = (int)p->skip.size();
+  for (int m = 0; m < p->batch; ++m) p->skip.push_back(skip[m] ? 1 : 0);
+  return off;
+}
+
+extern "C" {
+
+int bt_program_create(bt_ctx* ctx, int n, int prec, int batch, bt_program** out) {
+  if (!ctx || !out) return bt_fail(ctx, BT_ERR_BAD_ARG, "NULL argument");
+  if (prec != BT_PREC_C128 && prec != BT_PREC_C64) return bt_fail(ctx, BT_ERR_BAD_ARG, "prec must be C128 or C64");
+  const int nmax = prec == BT_PREC_C64 ? 14 : 13;
+  if (n < 2 || n > nmax)
+    return bt_fail(ctx, BT_ERR_UNSUPPORTED, "programs hold a member in shared memory: 2 <= n <= 14 (c64) / 13 (c128)");
+  if (batch < 1 || batch > (1 << 30)) return bt_fail(ctx, BT_ERR_BAD_ARG, "bad batch");
+  bt_program* p = new bt_program();
+  p->ctx = ctx;
+  p->n = n;
+  p->prec = prec;
+  p->batch = batch;
+  *out = p;
+  return BT_OK;
+}
+
+int bt_program_free(bt_program* p) {
+  if (!p) return BT_OK;
+  cudaSetDevice(p->ctx->device);
+  cudaStreamSynchronize(p->ctx->stream);
+  for (void* d : {p->d_ops, p->d_gm, p->d_km, p->d_skip, p->d_rec, p->d_u})
+    if (d) cudaFree(d);
+  delete p;
+  return BT_OK;
+}
+
+int bt_program_add_gate(bt_program* p, int k, const int32_t* qubits, const double* mats, int per_member) {
+  if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "program is NULL");
+  int rc = prog_qubits(p, k, qubits);
+  if (rc) return rc;
+  if (!mats) return bt_fail(p->ctx, BT_ERR_BAD_ARG, "matrix is NULL");
+  const int d = 1 << k;
+  const int cnt = per_member ? p->batch : 1;
+  PGOp op = {};
+  op.type = k == 1 ? PG_GATE1 : PG_GATE2;
+  op.b0 = p->n - qubits[0];
+  op.b1 = k == 2 ? p->n - qubits[1] : 0;
+  op.moff = (int)p->gm.size();
+  op.mstride = per_member ? 2 * d * d : 0;
+  op.skip_off = -1;
+  op.rand_idx = -1;
+  for (int m = 0; m < cnt; ++m) {
+    const double* cm = mats + (size_t)m * 2 * d * d;
+    for (int r = 0; r < d; ++r)
+      for (int c = 0; c < d; ++c) {
+        p->gm.push_back(cm[2 * (r + c * d)]);
+        p->gm.push_back(cm[2 * (r + c * d) + 1]);
+      }
+  }
+  p->ops.push_back(op);
+  p->uploaded = false;
+  return BT_OK;
+}
+
+int bt_program_add_channel(bt_program* p, int k, const int32_t* qubits, int nk, const double* kraus, int flags,
+                           const int32_t* skip) {
+  if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "program is NULL");
+  int rc = prog_qubits(p, k, qubits);
+  if (rc) return rc;
+  if (nk < 1 || !kraus) return bt_fail(p->ctx, BT_ERR_BAD_ARG, "need at least one Kraus operator");
+  const int d = 1 << k;
+  PGOp op = {};
+  op.type = PG_CHANNEL;
+  op.k = k;
+  op.nk = nk;
+  op.b0 = p->n - qubits[0];
+  op.b1 = k == 2 ? p->n - qubits[1] : 0;
+  op.flags = ((flags & BT_KRAUS_REF_ORDER) && k == 2 && qubits[0] > qubits[1] ? 1 : 0) |
+             ((flags & BT_KRAUS_UNITARY_MIX) ? 2 : 0);
+  op.moff = (int)p->km.size();
+  op.skip_off = prog_skip(p, skip);
+  op.rand_idx = p->ndraws++;
+  for (int i = 0; i < nk; ++i) {
+    const double* K = kraus + (size_t)i * 2 * d * d;
+    for (int r = 0; r < d; ++r)
+      for (int c = 0; c < d; ++c) {
+        p->km.push_back(K[2 * (r + c * d)]);
+        p->km.push_back(K[2 * (r + c * d) + 1]);
+      }
+  }
+  p->ops.push_back(op);
+  p->uploaded = false;
+  return BT_OK;
+}
+
+int bt_program_add_measure(bt_program* p, int qubit, const int32_t* skip) {
+  if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "program is NULL");
+  int rc = prog_qubits(p, 1, &qubit);
+  if (rc) return rc;
+  PGOp op = {};
+  op.type = PG_MEASURE;
+  op.b0 = p->n - qubit;
+  op.skip_off = prog_skip(p, skip);
+  op.rand_idx = p->ndraws++;
+  op.rec_idx = p->nrec++;
+  p->ops.push_back(op);
+  p->uploaded = false;
+  return BT_OK;
+}
+
+int bt_program_set_gate(bt_program* p, int64_t op_index, const double* mats) {
+  if (!p || !mats) return bt_fail(p ? p->ctx : nullptr, BT_ERR_BAD_ARG, "NULL argument");
+  if (op_index < 0 || op_index >= (int64_t)p->ops.size())
+    return bt_fail(p->ctx, BT_ERR_BAD_ARG, "op index out of range");
+  const PGOp& op = p->ops[op_index];
+  if (op.type != PG_GATE1 && op.type != PG_GATE2) return bt_fail(p->ctx, BT_ERR_BAD_ARG, "op is not a gate");
+  const int d = op.type == PG_GATE1 ? 2 : 4;
+  const int cnt = op.mstride ? p->batch : 1;
+  double* dst = p->gm.data() + op.moff;
+  for (int m = 0; m < cnt; ++m) {
+    const double* cm = mats + (size_t)m * 2 * d * d;
+    for (int r = 0; r < d; ++r)
+      for (int c = 0; c < d; ++c) {
+        *dst++ = cm[2 * (r + c * d)];
+        *dst++ = cm[2 * (r + c * d) + 1];
+      }
+  }
+  if (p->uploaded) p->gm_dirty = true;
+  return BT_OK;
+}
+
+int bt_program_info(const bt_program* p, int64_t* nops, int64_t* ndraws, int64_t* nrecords) {
+  if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "program is NULL");
+  if (nops) *nops = (int64_t)p->ops.size();
+  if (ndraws) *ndraws = p->ndraws;
+  if (nrecords) *nrecords = p->nrec;
+  return BT_OK;
+}
+
+static int upload(bt_program* p) {
+  bt_ctx* ctx = p->ctx;
+  for (void** d : {&p->d_ops, &p->d_gm, &p->d_km, &p->d_skip, &p->d_rec})
+    if (*d) {
+      cudaStreamSynchronize(ctx->stream);
+      cudaFree(*d);
+      *d = nullptr;
+    }
+  const bool f = p->prec == BT_PREC_C64;
+  std::vector<float>& gf = p->gstage;
+  if (f) gf.assign(p->gm.begin(), p->gm.end());
+  const size_t gbytes = f ? gf.size() * 4 : p->gm.size() * 8;
+  struct Buf { void** d; const void* h; size_t bytes; };
+  const Buf bufs[] = {{&p->d_ops, p->ops.data(), p->ops.size() * sizeof(PGOp)},
+                      {&p->d_gm, f ? (const void*)gf.data() : (const void*)p->gm.data(), gbytes},
+                      {&p->d_km, p->km.data(), p->km.size() * 8},
+                      {&p->d_skip, p->skip.data(), p->skip.size()},
+                      {&p->d_rec, nullptr, (size_t)p->batch * (p->nrec ? p->nrec : 1) * 4}};
+  for (const Buf& b : bufs) {
+    int rc = bt_cuda_check(ctx, cudaMalloc(b.d, b.bytes ? b.bytes : 16), "program allocation");
+    if (rc) return rc;
+    if (b.h && b.bytes) {
+      rc = bt_cuda_check(ctx, cudaMemcpy(*b.d, b.h, b.bytes, cudaMemcpyHostToDevice), "program upload");
+      if (rc) return rc;
+    }
+  }
+  p->uploaded = true;
+  p->gm_dirty = false;
+  return BT_OK;
+}
+
+// re-sends the gate matrices after bt_program_set_gate (same size, stream-ordered)
+static int upload_gm(bt_program* p, bt_ctx* ctx) {
+  const bool f = p->prec == BT_PREC_C64;
+  if (f) p->gstage.assign(p->gm.begin(), p->gm.end());
+  const void* h = f ? (const void*)p->gstage.data() : (const void*)p->gm.data();
+  const size_t bytes = f ? p->gstage.size() * 4 : p->gm.size() * 8;
+  p->gm_dirty = false;
+  if (!bytes) return BT_OK;
+  return bt_cuda_check(ctx, cudaMemcpyAsync(p->d_gm, h, bytes, cudaMemcpyHostToDevice, ctx->stream), "gate upload");
+}
+
+int bt_program_run(bt_program* p, bt_state* s, const double* uniforms, uint64_t seed, int32_t* records) {
+  if (!p || !s) return bt_fail(p ? p->ctx : nullptr, BT_ERR_BAD_ARG, "NULL argument");
+  bt_ctx* ctx = s->ctx;
+  if (s->repr != BT_REPR_SV || s->n != p->n || s->prec != p->prec || s->batch != p->batch)
+    return bt_fail(ctx, BT_ERR_BAD_ARG, "program and state differ in n, prec or batch (or the state is a density matrix)");
+  int rc = bt_cuda_check(ctx, cudaSetDevice(ctx->device), "cudaSetDevice");
+  if (rc) return rc;
+  if (!p->uploaded && (rc = upload(p))) return rc;
+  if (p->gm_dirty && (rc = upload_gm(p, ctx))) return rc;
+  const double* du = nullptr;
+  if (uniforms && p->ndraws) {
+    const size_t ub = (size_t)p->ndraws * p->batch * 8;
+    if (p->u_bytes < ub) {
+      if (p->d_u) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(p->d_u);
+      }
+      if ((rc = bt_cuda_check(ctx, cudaMalloc(&p->d_u, ub), "draw buffer"))) return rc;
+      p->u_bytes = ub;
+    }
+    if ((rc = bt_cuda_check(ctx, cudaMemcpyAsync(p->d_u, uniforms, ub, cudaMemcpyHostToDevice, ctx->stream), "draws")))
+      return rc;
+    du = (const double*)p->d_u;
+  }
+  const bool f = p->prec == BT_PREC_C64;
+  const size_t smem = (elem_bytes(p->prec) << p->n) + 9 * 32 * 8 + 32 * 8;
+  static std::atomic<bool> attr[2][64] = {};
+  std::atomic<bool>& done = attr[f][ctx->device & 63];
+  if (!done.load()) {
+    cudaError_t e = f ? cudaFuncSetAttribute(k_program<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)
+                      : cudaFuncSetAttribute(k_program<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if ((rc = bt_cuda_check(ctx, e, "program smem attribute"))) return rc;
+    done.store(true);
+  }
+  const uint64_t stream = (seed * 0x9E3779B97F4A7C15ULL) ^ 0x5052000000000000ULL ^ ctx->rng_calls++;
+  if (f)
+    k_program<float><<<p->batch, PG_THREADS, smem, ctx->stream>>>(
+        (float2*)s->d, s->nbits, (const PGOp*)p->d_ops, (int)p->ops.size(), (const float*)p->d_gm,
+        (const double*)p->d_km, (const int8_t*)p->d_skip, du, ctx->seed, stream, p->batch, (int32_t*)p->d_rec,
+        p->nrec ? p->nrec : 1, ctx->d_status);
+  else
+    k_program<double><<<p->batch, PG_THREADS, smem, ctx->stream>>>(
+        (double2*)s->d, s->nbits, (const PGOp*)p->d_ops, (int)p->ops.size(), (const double*)p->d_gm,
+        (const double*)p->d_km, (const int8_t*)p->d_skip, du, ctx->seed, stream, p->batch, (int32_t*)p->d_rec,
+        p->nrec ? p->nrec : 1, ctx->d_status);
+  ctx->launches++;
+  if ((rc = bt_cuda_check(ctx, cudaGetLastError(), "program launch"))) return rc;
+  if (records && p->nrec)
+    rc = bt_cuda_check(ctx, cudaMemcpyAsync(records, p->d_rec, (size_t)p->batch * p->nrec * 4, cudaMemcpyDeviceToHost,
+                                            ctx->stream), "records");
+  if (rc) return rc;
+  rc = bt_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "program sync");
+  if (rc) return rc;
+  int st = 0;
+  rc = bt_cuda_check(ctx, cudaMemcpy(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost), "status read");
+  if (rc) return rc;
+  if (st) {
+    cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    return bt_fail(ctx, st == 1 ? BT_ERR_BAD_ARG : (st == 2 ? BT_ERR_NO_BRANCH : BT_ERR_BAD_ARG),
+                   "a program branch or outcome had zero probability; that member kept its state");
+  }
+  return BT_OK;
+}
+
+}  // extern "C"

@@ -180,6 +180,39 @@ int bt_plan_stats(const bt_plan* p, int64_t* ngates, int64_t* npasses, int64_t* 
 /* runs the plan on member `member` (-1: every member) of a state of the same n/repr/prec */
 int bt_plan_run(bt_plan* p, bt_state* s, int64_t member);
 
+/* ---------------------------------------------------------------- programs */
+/* A program is a noisy circuit run whole, one CTA per member, with the member
+ * held in shared memory (2 <= n <= 14 qubits complex64, 13 complex128; state
+ * vectors only): the per-shot loop of the noisy measure(circuit, shots)
+ * (src/ops.jl:617-630) as one launch.  Ops act on 1 or 2 qubits:
+ *   gate     op.expand(N)*state; mats is one column-major matrix, or batch of them
+ *            back to back when per_member (twirl frames, per-client angles);
+ *   channel  apply_kraus (src/struct.jl:58-76, branch rule src/hilbert.jl:810-819)
+ *            with flags BT_KRAUS_REF_ORDER / BT_KRAUS_UNITARY_MIX as in bt_apply_kraus;
+ *   measure  _born_measure (src/hilbert.jl:682-703): outcome u < p0 ? 0 : 1, the
+ *            other half set to zero, the kept half renormalised; the outcome goes to
+ *            the next record slot.
+ * skip (batch flags, or NULL) makes members pass over a channel or measurement
+ * (their record slot reads -1).  Draw i of member m is uniforms[i*batch + m] when
+ * uniforms is given to bt_program_run, else on-device Philox keyed by the ctx seed
+ * and `seed`.  A branch or outcome of zero probability leaves that member as it
+ * was at that op (record -1) and the run reports BT_ERR_NO_BRANCH / BT_ERR_BAD_ARG
+ * after every member has finished. */
+typedef struct bt_program bt_program;
+int bt_program_create(bt_ctx* ctx, int n, int prec, int batch, bt_program** out);
+int bt_program_free(bt_program* p);
+int bt_program_add_gate(bt_program* p, int k, const int32_t* qubits, const double* mats, int per_member);
+int bt_program_add_channel(bt_program* p, int k, const int32_t* qubits, int nk, const double* kraus, int flags,
+                           const int32_t* skip);
+int bt_program_add_measure(bt_program* p, int qubit, const int32_t* skip);
+int bt_program_info(const bt_program* p, int64_t* nops, int64_t* ndraws, int64_t* nrecords);
+/* new matrices for gate op `op_index` (counting every bt_program_add_* call from
+ * 0), in the count it was added with (variational angles between runs) */
+int bt_program_set_gate(bt_program* p, int64_t op_index, const double* mats);
+/* runs on every member of s (n, prec and batch as created); records: batch x
+ * nrecords int32, member-major (may be NULL) */
+int bt_program_run(bt_program* p, bt_state* s, const double* uniforms, uint64_t seed, int32_t* records);
+
 /* ---------------------------------------------------------------- sampling */
 /* sample(psi, shots) (src/ops.jl:46-62): per shot t = u*sum|psi|^2, outcome =
  * first index with cumsum >= t.  uniforms (shots values) or NULL for on-device

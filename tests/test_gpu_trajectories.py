@@ -75,7 +75,111 @@ def test_trajectories_uneven_programs_match_oracle(ctx, oracle, kref, twirl):
     assert sum(len(r) for r in recs) > 0  # some members were measured
 
 
-def test_trajectories_device_rng_statistics(ctx, oracle):
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-12), ("c64", 2e-5)])
+@pytest.mark.parametrize("twirl", [False, True])
+def test_program_uneven_programs_match_oracle(ctx, oracle, kref, prec, tol, twirl):
+    """The whole-program kernel (one CTA per member) against the oracle replaying
+    each member with the same draws: ZNE repetitions, twirl frames, random
+    mid-circuit measurements, Kraus branches.  complex64 tolerance: float32
+    rounding over ~150 ops of a 5-qubit member."""
+    import bluetangle_gpu as bt
+    import bluetangle_gpu.trajectories as T
+    n, B = 5, 6
+    h = np.random.default_rng(3).uniform(0.5, 1.5, n)
+    steps = tfim_cnot_steps(n, 2, 0.3, h)
+    member_ops = T.member_programs(steps, n, B, zne_ids=[0, 1, 2, 0, 1, 2], twirl=twirl,
+                                   frame_rng=np.random.default_rng(7), measure_prob=0.3,
+                                   measure_rng=np.random.default_rng(8))
+    slots = T.build_slots(member_ops)
+    assert T.program_supported(slots, n, prec)
+    st = bt.zero_state(n, prec, batch=B)
+    prog, _ = T.compile_program(slots, n, B, prec, unitary_mix=False)
+    recs = prog.run(st, rng=np.random.default_rng(11))
+    ref, rrecs = replay(oracle, slots, B, n, np.random.default_rng(11), kref)
+    for m in range(B):
+        assert recs[m] == rrecs[m]
+        assert np.abs(st.to_numpy(m) - ref[m]).max() < tol
+    assert sum(len(r) for r in recs) > 0
+
+
+def test_program_equals_slots_engine(ctx):
+    """Both trajectory engines with the same explicit draws give the same members
+    and records (8 qubits, 32 members, measurements and 2-qubit channels)."""
+    import bluetangle_gpu.trajectories as T
+    n, B = 8, 32
+    h = np.random.default_rng(4).uniform(0.5, 1.5, n)
+    steps = tfim_cnot_steps(n, 2, 0.2, h)
+    kw = dict(zne_ids=[i % 3 for i in range(B)], twirl=True, measure_prob=0.1, prec="c128")
+    a, ra = T.run_trajectories(steps, n, B, rng=np.random.default_rng(5), frame_rng=np.random.default_rng(6),
+                               measure_rng=np.random.default_rng(7), engine="program", **kw)
+    b, rb = T.run_trajectories(steps, n, B, rng=np.random.default_rng(5), frame_rng=np.random.default_rng(6),
+                               measure_rng=np.random.default_rng(7), engine="slots", **kw)
+    assert ra == rb
+    for m in range(B):
+        assert np.abs(a.to_numpy(m) - b.to_numpy(m)).max() < 1e-12
+
+
+def test_program_set_gate_matches_fresh_compile(ctx):
+    """New gate matrices between runs (variational angles) give what a program
+    compiled with those matrices gives."""
+    import bluetangle_gpu as bt
+    import bluetangle_gpu.trajectories as T
+    n, B = 6, 4
+    rng = np.random.default_rng(1)
+
+    def ops(theta):
+        out = []
+        for q in range(1, n + 1):
+            out += [bt.Op(f"RY({float(theta[q - 1])!r})", q), bt.OpQC("amplitude_damping", 0.05, q)]
+        for q in range(1, n):
+            out += [bt.Op("CNOT", q, q + 1), bt.OpQC("depolarizing", 0.02, q, q + 1)]
+        return out
+
+    t0, t1 = rng.uniform(0, 3, n), rng.uniform(0, 3, n)
+    slots0 = T.build_slots(T.member_programs([ops(t0)], n, B))
+    slots1 = T.build_slots(T.member_programs([ops(t1)], n, B))
+    prog, gate_ops = T.compile_program(slots0, n, B, "c128", unitary_mix=False)
+    st = bt.zero_state(n, "c128", batch=B)
+    prog.run(st, rng=np.random.default_rng(2))
+    for i, sl in enumerate(slots1):
+        if gate_ops[i] is not None and sl.items[0][0].shape[0] == 2:
+            prog.set_gate(gate_ops[i], sl.items[0][0])
+    st.set_zero()
+    prog.run(st, rng=np.random.default_rng(3))
+    fresh, _ = T.compile_program(slots1, n, B, "c128", unitary_mix=False)
+    st2 = bt.zero_state(n, "c128", batch=B)
+    fresh.run(st2, rng=np.random.default_rng(3))
+    for m in range(B):
+        assert np.abs(st.to_numpy(m) - st2.to_numpy(m)).max() < 1e-14
+
+
+def test_program_no_branch_leaves_member(ctx):
+    """A Kraus set whose probabilities sum below u selects no branch (the
+    reference's _weighted_sample returns nothing): the run reports it and that
+    member keeps its state; the other members proceed."""
+    import bluetangle_gpu as bt
+    import bluetangle_gpu.trajectories as T
+    n, B = 3, 2
+    prog = T.Program(n, B, "c128")
+    prog.add_gate(np.array([[1, 1], [1, -1]]) / np.sqrt(2), [1])
+    prog.add_channel([np.sqrt(0.5) * np.eye(2)], [2])  # probabilities sum to 0.5
+    st = bt.zero_state(n, "c128", batch=B)
+
+    class Draws:
+        def random(self, shape):
+            return np.array([[0.25, 0.75]]).reshape(shape)
+
+    with pytest.raises(bt.BTError) as e:
+        prog.run(st, rng=Draws())
+    assert e.value.code == -7
+    plus = np.zeros(2 ** n, complex)
+    plus[0] = plus[4] = 1 / np.sqrt(2)
+    assert np.abs(st.to_numpy(1) - plus).max() < 1e-15      # untouched
+    assert np.abs(st.to_numpy(0) - plus).max() < 1e-15      # K/sqrt(p) = I on a normalised member
+
+
+@pytest.mark.parametrize("engine", ["program", "slots"])
+def test_trajectories_device_rng_statistics(ctx, oracle, engine):
     """On-device Philox draws (with the unitary-mixture shortcut for depolarizing
     channels): the mean over trajectories of <Z_1> matches the density matrix."""
     import bluetangle_gpu as bt
@@ -83,7 +187,7 @@ def test_trajectories_device_rng_statistics(ctx, oracle):
     n, B = 4, 2000
     h = [1.0, 0.8, 1.2, 0.9]
     steps = tfim_cnot_steps(n, 2, 0.25, h, p1=0.05, p2=0.1, gamma=0.05)
-    st, _ = T.run_trajectories(steps, n, B, prec="c128")
+    st, _ = T.run_trajectories(steps, n, B, prec="c128", engine=engine, seed=17)
     zs = bt.expect(st, "Z", member=-1)[:, 0]
     rho = bt.zero_rho(n)
     for step in steps:

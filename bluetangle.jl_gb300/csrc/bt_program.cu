@@ -56,6 +56,7 @@ struct bt_program {
 };
 
 #define PG_THREADS 256
+#define PG_MAX_KRAUS 64
 #define FULLM 0xffffffffu
 
 template <int W>
@@ -190,7 +191,9 @@ __global__ void __launch_bounds__(PG_THREADS) k_program(typename CT<R>::T* __res
   extern __shared__ __align__(16) unsigned char smem[];
   C2* st = reinterpret_cast<C2*>(smem);
   double* sh = reinterpret_cast<double*>(smem + (sizeof(C2) << nbits));  // 9 * 32 doubles
-  R* mat = reinterpret_cast<R*>(sh + 9 * 32);                             // 32 reals
+  double* pk = sh + 9 * 32;                                               // PG_MAX_KRAUS branch probabilities
+  double* nk = pk + PG_MAX_KRAUS;                                         // PG_MAX_KRAUS branch norms
+  R* mat = reinterpret_cast<R*>(nk + PG_MAX_KRAUS);                       // 32 reals
   __shared__ int s_ok;
   const int m = blockIdx.x;
   C2* g = states + ((int64_t)m << nbits);
@@ -217,17 +220,28 @@ __global__ void __launch_bounds__(PG_THREADS) k_program(typename CT<R>::T* __res
         if (op.k == 1) reduce_rho<R, 1>(st, nbits, op.b0, op.b1, sh, rho);
         else reduce_rho<R, 2>(st, nbits, op.b0, op.b1, sh, rho);
       }
+      // branch probabilities (reference order) and norms (application order), one
+      // Kraus operator per lane of warp 0
+      if (threadIdx.x < 32) {
+        const bool perm = (op.flags & 1) && op.k == 2;
+        for (int i = threadIdx.x; i < op.nk; i += 32) {
+          const double* Ki = km + op.moff + (int64_t)i * 2 * D * D;
+          const double pi = tr_krk(Ki, rho, D, umix, perm);
+          pk[i] = pi;
+          nk[i] = perm ? tr_krk(Ki, rho, D, umix, false) : pi;
+        }
+      }
+      __syncthreads();
       if (threadIdx.x == 0) {
         const double uu = u ? u[(int64_t)op.rand_idx * batch + m] : bt_uniform(key, stream ^ (uint64_t)op.rand_idx, m);
         double cum = 0;
         int ind = -1;
         for (int i = 0; i < op.nk; ++i) {
-          cum += tr_krk(km + op.moff + (int64_t)i * 2 * D * D, rho, D, umix, (op.flags & 1) && op.k == 2);
+          cum += pk[i];
           if (ind < 0 && uu <= cum) ind = i;
         }
         s_ok = 1;
-        double nrm = 0;
-        if (ind >= 0) nrm = tr_krk(km + op.moff + (int64_t)ind * 2 * D * D, rho, D, umix, false);
+        const double nrm = ind >= 0 ? nk[ind] : 0.0;
         if (ind < 0 || !(nrm > 0)) {
           atomicExch(status, ind < 0 ? 2 : 3);
           s_ok = 0;
@@ -357,6 +371,7 @@ int bt_program_add_channel(bt_program* p, int k, const int32_t* qubits, int nk, 
   int rc = prog_qubits(p, k, qubits);
   if (rc) return rc;
   if (nk < 1 || !kraus) return bt_fail(p->ctx, BT_ERR_BAD_ARG, "need at least one Kraus operator");
+  if (nk > PG_MAX_KRAUS) return bt_fail(p->ctx, BT_ERR_UNSUPPORTED, "programs take at most 64 Kraus operators per channel");
   const int d = 1 << k;
   PGOp op = {};
   op.type = PG_CHANNEL;
@@ -493,7 +508,7 @@ int bt_program_run(bt_program* p, bt_state* s, const double* uniforms, uint64_t 
     du = (const double*)p->d_u;
   }
   const bool f = p->prec == BT_PREC_C64;
-  const size_t smem = (elem_bytes(p->prec) << p->n) + 9 * 32 * 8 + 32 * 8;
+  const size_t smem = (elem_bytes(p->prec) << p->n) + (9 * 32 + 2 * PG_MAX_KRAUS) * 8 + 32 * 8;
   static std::atomic<bool> attr[2][64] = {};
   std::atomic<bool>& done = attr[f][ctx->device & 63];
   if (!done.load()) {

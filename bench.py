@@ -55,7 +55,12 @@ def parse():
     ap.add_argument("--cpu-n", type=int, default=24, help="qubits of the CPU baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="brickwork", choices=["brickwork", "serve"])
+    ap.add_argument("--workload", default="brickwork", choices=["brickwork", "serve", "c1", "c2", "c3"],
+                    help="brickwork: 33q c64 depth-30 (default); serve: the serving stream; c1: 12q c128 "
+                         "brickwork + <Z> + shots; c2: 10q noisy density matrix; c3: 20q trajectories")
+    ap.add_argument("--c3-n", type=int, default=20)
+    ap.add_argument("--c3-members", type=int, default=4096)
+    ap.add_argument("--c3-twirl", type=int, default=64, help="twirl instances (x3 ZNE scales)")
     ap.add_argument("--rate", type=float, default=2000.0, help="serving: Poisson arrival rate (req/s)")
     ap.add_argument("--lanes", type=int, default=8, help="serving: concurrent lanes (contexts/streams)")
     return ap.parse_args()
@@ -474,11 +479,343 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ the other configurations
+def _oracle():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    return O
+
+
+def _op_qubits(op):
+    return [op.qubit] if op.q == 1 else [op.qubit, op.target_qubit]
+
+
+def _op_ctrls(op):
+    return [op.control] if op.control != -2 else []
+
+
+def _events(ctx):
+    import torch
+    s = torch.cuda.ExternalStream(ctx.stream)
+    return s, torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def _timed(ctx, fn, steps, warmup):
+    """Runs fn(i) warmup + steps times; CUDA-event ms and host seconds of the timed steps."""
+    for i in range(warmup):
+        fn(i)
+    ctx.synchronize()
+    stream, e0, e1 = _events(ctx)
+    clocks = ClockSampler(0)
+    clocks.start()
+    time.sleep(0.3)
+    l0 = ctx.launch_count
+    e0.record(stream)
+    t0 = time.perf_counter()
+    for i in range(warmup, warmup + steps):
+        fn(i)
+    e1.record(stream)
+    e1.synchronize()
+    host = time.perf_counter() - t0
+    return e0.elapsed_time(e1), host, ctx.launch_count - l0, clocks.stop()
+
+
+def run_c1(args):
+    """12-qubit complex128 brickwork of depth 20 from |0...0>, outputs the state,
+    <Z_i> for every qubit and 10^4 shots (the configuration the reference runs as
+    is on CPU).  A step is one circuit: reset, the circuit as a compiled plan,
+    <Z_i> and the shots returned to the host; e2e adds the state download."""
+    import bluetangle_gpu as bt
+    from bluetangle_gpu.circuits import brickwork
+    n, depth, shots = 12, 20, 10_000
+    ctx = bt.Context(0, seed=args.seed)
+    bt.Context._default = ctx
+    ops = brickwork(n, depth, np.random.default_rng(args.seed))
+    plan = bt.Plan(n, "sv", "c128", ctx)
+    for op in ops:
+        plan.add(op)
+    plan.compile(True)
+    st = bt.zero_state(n, "c128", ctx=ctx)
+    out = {}
+
+    def circuit(i, download=False):
+        st.set_zero()
+        plan.run(st)
+        out["z"] = bt.expect(st, "Z")
+        out["s"] = bt.sample(st, shots, seed=i)
+        if download:
+            out["psi"] = st.to_numpy()
+
+    ms, host, launches, clk = _timed(ctx, circuit, args.steps, args.warmup)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        circuit(i, True)
+    e2e_s = time.perf_counter() - t0
+    # parity against the oracle on the same circuit
+    O = _oracle()
+    psi = np.zeros(2 ** n, complex)
+    psi[0] = 1
+    for op in ops:
+        psi = O.apply_k(psi, op.mat, _op_qubits(op), _op_ctrls(op))
+    circuit(0, True)
+    dev = float(np.abs(out["psi"] - psi).max())
+    p = np.abs(psi) ** 2
+    bits = (np.arange(2 ** n)[:, None] >> (n - np.arange(1, n + 1))[None, :]) & 1
+    zref = (p[:, None] * (1 - 2 * bits)).sum(0)
+    zdev = float(np.abs(np.asarray(out["z"]) - zref).max())
+    # CPU: the oracle runs the same circuit with the same outputs, single thread
+    cpu_n = 0
+    t0 = time.perf_counter()
+    urng = np.random.default_rng(1)
+    while time.perf_counter() - t0 < min(args.cpu_seconds, 10.0) or cpu_n < 3:
+        q = np.zeros(2 ** n, complex)
+        q[0] = 1
+        for op in ops:
+            q = O.apply_k(q, op.mat, _op_qubits(op), _op_ctrls(op))
+        pq = np.abs(q) ** 2
+        _ = (pq[:, None] * (1 - 2 * bits)).sum(0)
+        _ = O.sample(q, urng.random(shots))
+        cpu_n += 1
+    cpu_rate = cpu_n / (time.perf_counter() - t0)
+    value = args.steps / (ms / 1e3)
+    line = {"metric": "circuits/s", "value": value, "unit": "circuits/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": "brickwork-12q-c128-depth20+Z+1e4shots", "gates": len(ops),
+                       "plan": plan.stats(), "l2": "state (64 KiB) is L2/shared-memory resident"},
+            "parity": {"max_abs_state_vs_oracle": dev, "max_abs_z_vs_oracle": zdev},
+            "cpu_baseline": {"value": cpu_rate, "unit": "circuits/s", "cores": 1, "kind": "port",
+                             "sample": f"{cpu_n} circuits through the oracle (same outputs), 1 thread"},
+            "e2e": {"value": args.steps / e2e_s, "unit": "circuits/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": (2 ** n) * 16 + n * 8 + shots * 8},
+            "gpu_launches": launches, "launches_per_circuit": launches / args.steps, "clocks": clk,
+            "host_s": host}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def run_c2(args):
+    """10-qubit density matrix, brickwork of depth 16 with depolarizing and
+    amplitude-damping channels after every gate and a final 2% bit flip per qubit;
+    outputs rho, <Z_i> and <Z_i Z_i+1>.  value: the chosen form (complex64, the
+    circuit compiled into fused passes with every Kraus sum inside the passes);
+    beside it the plain complex128 op-by-op path and the complex128 plan."""
+    import bluetangle_gpu as bt
+    from bluetangle_gpu.circuits import noisy_brickwork_dm
+    n, depth = 10, 16
+    ctx = bt.Context(0, seed=args.seed)
+    bt.Context._default = ctx
+    ops = noisy_brickwork_dm(n, depth, np.random.default_rng(args.seed))
+    ops += [bt.OpQC("bit_flip", 0.02, q) for q in range(1, n + 1)]
+    ngate = sum(1 for op in ops if not isinstance(op, bt.OpQC))
+    plans = {}
+    for prec in ("c64", "c128"):
+        p = bt.Plan(n, "dm", prec, ctx)
+        for op in ops:
+            p.add(op)
+        plans[prec] = p.compile(True)
+    rhos = {prec: bt.zero_rho(n, prec, ctx=ctx) for prec in ("c64", "c128")}
+    res = {}
+
+    def outputs(r):
+        z = bt.expect(r, "Z")
+        zz = [bt.correlation(r, "Z,Z", [q, q + 1]) for q in range(1, n)]
+        return np.asarray(z), np.asarray(zz)
+
+    def chosen(i, prec="c64"):
+        r = rhos[prec]
+        r.set_zero()
+        plans[prec].run(r)
+        res[prec] = outputs(r)
+
+    ms64, host64, launches, clk = _timed(ctx, chosen, args.steps, args.warmup)
+    ms128, _, _, _ = _timed(ctx, lambda i: chosen(i, "c128"), args.steps, args.warmup)
+    # the plain per-call complex128 path: one call per gate and per channel
+    plain = bt.zero_rho(n, "c128", ctx=ctx)
+
+    def plain_run(i):
+        plain.set_zero()
+        bt.apply(ops, plain)
+        res["plain"] = outputs(plain)
+
+    k_plain = max(2, args.steps // 3)
+    msp, _, _, _ = _timed(ctx, plain_run, k_plain, 1)
+    r64, r128, rp = rhos["c64"].to_numpy(), rhos["c128"].to_numpy(), plain.to_numpy()
+    # parity: the oracle's Kraus-sum restatement on the same circuit (complex128)
+    O = _oracle()
+    rho = np.zeros((2 ** n, 2 ** n), complex)
+    rho[0, 0] = 1
+    t0 = time.perf_counter()
+    for op in ops:
+        if isinstance(op, bt.OpQC):
+            qs = _op_qubits(op)
+            rho = O.dm_channel(rho, op.kraus, qs[0], qs[1] if len(qs) == 2 else -1)
+        else:
+            rho = O.dm_gate(rho, op.mat, _op_qubits(op), _op_ctrls(op))
+    cpu_s = time.perf_counter() - t0
+    line = {"metric": "circuits/s", "value": args.steps / (ms64 / 1e3), "unit": "circuits/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms64 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+            "config": {"workload": "noisy-brickwork-dm-10q-depth16", "gates": ngate,
+                       "channels": len(ops) - ngate, "plan_c64": plans["c64"].stats(),
+                       "l2": "rho (8 MiB c64 / 16 MiB c128) is L2-resident"},
+            "c128_plan_circuits_per_s": args.steps / (ms128 / 1e3),
+            "plain_c128_circuits_per_s": k_plain / (msp / 1e3),
+            "vs_plain": (args.steps / (ms64 / 1e3)) / (k_plain / (msp / 1e3)),
+            "errors": {"c64_vs_c128_max_abs_rho": float(np.abs(r64 - r128).max()),
+                       "c64_vs_c128_max_abs_z": float(np.abs(res["c64"][0] - res["c128"][0]).max()),
+                       "c64_vs_c128_max_abs_zz": float(np.abs(res["c64"][1] - res["c128"][1]).max()),
+                       "c128_plan_vs_oracle_max_abs_rho": float(np.abs(r128 - rho).max()),
+                       "plain_c128_vs_oracle_max_abs_rho": float(np.abs(rp - rho).max())},
+            "cpu_baseline": {"value": 1 / cpu_s, "unit": "circuits/s", "cores": O.num_threads(), "kind": "port",
+                             "sample": f"one circuit through the oracle (complex128 Kraus sums) in {cpu_s:.1f} s"},
+            "gpu_launches": launches, "clocks": clk}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def _c3_noise_after(op, p1=1e-3, p2=1e-2, gamma=5e-3):
+    from bluetangle_gpu.ops import OpQC
+    if op.q == 1:
+        return [OpQC("depolarizing", p1, op.qubit), OpQC("amplitude_damping", gamma, op.qubit)]
+    return [OpQC("depolarizing", p2, op.qubit, op.target_qubit), OpQC("amplitude_damping", gamma, op.qubit),
+            OpQC("amplitude_damping", gamma, op.target_qubit)]
+
+
+def run_c3(args):
+    """4096 Monte-Carlo trajectories of a 20-qubit open-chain TFIM (J=1, h_i ~
+    U[0.5,1.5], dt=0.05; RZZ on ascending pairs then RX), depolarizing and
+    amplitude damping after every gate sampled per trajectory, a Z measurement of
+    each qubit with probability 0.1 per step; beside them 64 Pauli-twirled
+    instances at ZNE scales 1, 3, 5 (CNOT.RZ.CNOT form, uneven depth, 192 members
+    with depolarizing noise after every gate including the repetitions).  A step is
+    one Trotter step of every member (40 make the circuit); complex64, on-device
+    Philox draws."""
+    import bluetangle_gpu as bt
+    import bluetangle_gpu.trajectories as T
+    from bluetangle_gpu.noise import NoiseModel
+    n, B, dt = args.c3_n, args.c3_members, 0.05
+    ctx = bt.Context(0, seed=args.seed)
+    bt.Context._default = ctx
+    h = np.random.default_rng(args.seed).uniform(0.5, 1.5, n)
+    step_ops = []
+    for q in range(1, n):
+        op = bt.Op(f"RZZ({2 * dt!r})", q, q + 1)
+        step_ops += [op] + _c3_noise_after(op)
+    for q in range(1, n + 1):
+        op = bt.Op(f"RX({float(2 * h[q - 1] * dt)!r})", q)
+        step_ops += [op] + _c3_noise_after(op)
+    # the shared-payload slots of one step (every member the same ops), then the
+    # measurement slots with this step's per-member masks
+    base = []
+    for op in step_ops:
+        (kind, payload), = T._op_slots(op, False)
+        base.append(T.Slot(kind, [payload] * B))
+    mrng = np.random.default_rng(args.seed + 7)
+    meas_payload = [("MZ", q) for q in range(1, n + 1)]
+
+    def step_slots():
+        sl = list(base)
+        for q in range(1, n + 1):
+            mask = mrng.random(B) < 0.1
+            sl.append(T.Slot("measure", [meas_payload[q - 1] if m else None for m in mask]))
+        return sl
+
+    # twirl / ZNE copies: CNOT.RZ.CNOT form, NoiseModel depolarizing after every gate
+    ncopy = args.c3_twirl * 3
+    copy_step = []
+    for q in range(1, n):
+        copy_step += [bt.Op("CNOT", q, q + 1), bt.Op(f"RZ({2 * dt!r})", q + 1), bt.Op("CNOT", q, q + 1)]
+    copy_step += [bt.Op(f"RX({float(2 * h[q - 1] * dt)!r})", q) for q in range(1, n + 1)]
+    noise = NoiseModel(bt.Noise1("depolarizing", 1e-3), bt.Noise2("depolarizing", 1e-2))
+    frame_rng = np.random.default_rng(args.seed + 11)
+    zne = [k % 3 for k in range(ncopy)]
+
+    st = bt.zero_state(n, "c64", B, ctx)
+    cp = bt.zero_state(n, "c64", ncopy, ctx) if ncopy else None
+    counts = {"ops": 0}
+    pre = [step_slots() for _ in range(args.warmup + args.steps)]
+    pre_c = []
+    if cp is not None:
+        for _ in range(args.warmup + args.steps):
+            mo = T.member_programs([copy_step], n, ncopy, zne_ids=zne, twirl=True, frame_rng=frame_rng,
+                                   measure_prob=0.1, measure_rng=mrng)
+            pre_c.append(T.build_slots(mo, noise))
+
+    def member_ops(slots):
+        return sum(sum(1 for it in s.items if it is not None) for s in slots)
+
+    def step(i):
+        T.run_slots(st, pre[i], records=False)
+        counts["ops"] += member_ops(pre[i])
+        if cp is not None:
+            T.run_slots(cp, pre_c[i], records=False)
+            counts["ops"] += member_ops(pre_c[i])
+
+    ms, host, launches, clk = _timed(ctx, step, args.steps, args.warmup)
+    timed_ops = sum(member_ops(pre[i]) + (member_ops(pre_c[i]) if pre_c else 0)
+                    for i in range(args.warmup, args.warmup + args.steps))
+    # algorithmic HBM bytes of the main batch per step: a gate pass reads and
+    # writes every member; a channel adds a reduction read unless it is a unitary
+    # mixture (depolarizing); a measurement reads once and rewrites (collapse)
+    S = B * (2 ** n) * 8
+    ngates = sum(1 for s in base if s.kind == "gate")
+    nch = sum(1 for s in base if s.kind == "channel")
+    nad = sum(1 for op in step_ops if isinstance(op, bt.OpQC) and op.name == "amplitude_damping")
+    bytes_step = ngates * 2 * S + nch * 2 * S + nad * S + n * (S + 2 * S)
+    zs = bt.expect(st, "Z", member=-1)
+    assert np.all(np.isfinite(zs))
+    # CPU: the oracle on a sample of trajectories (one step each, complex128)
+    O = _oracle()
+    cpu_ops = 0
+    t0 = time.perf_counter()
+    urng = np.random.default_rng(3)
+    traj = 0
+    while time.perf_counter() - t0 < min(args.cpu_seconds, 15.0) or traj < 1:
+        psi = np.zeros(2 ** n, complex)
+        psi[0] = 1
+        for op in step_ops:
+            if isinstance(op, bt.OpQC):
+                qs = _op_qubits(op)
+                psi, _, _ = O.channel_traj(psi, op.kraus, qs[0], qs[1] if len(qs) == 2 else -1, u=urng.random())
+            else:
+                psi = O.apply_k(psi, op.mat, _op_qubits(op), [])
+            cpu_ops += 1
+        for q in range(1, n + 1):
+            if urng.random() < 0.1:
+                psi, _, _ = O.born_measure_z(psi, q, u=urng.random())
+                cpu_ops += 1
+        traj += 1
+    cpu_rate = cpu_ops / (time.perf_counter() - t0)
+    value = timed_ops / (ms / 1e3)
+    achieved = bytes_step * args.steps / (ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    line = {"metric": "trajectory op-apps/s", "value": value, "unit": "member-ops/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+            "config": {"workload": f"tfim-{n}q-{B}traj+{ncopy}twirl/zne-copies", "members": B + ncopy,
+                       "step": "one Trotter step of every member (40 make the circuit)",
+                       "ops_per_member_step": len(step_ops), "l2": f"states ({(B + ncopy) * 2 ** n * 8 / 2**30:.1f} GiB) larger than L2",
+                       "engine": "lock-step slots (one launch sequence per op over the batch)"},
+            "trajectory_steps_per_s": (B + ncopy) * args.steps / (ms / 1e3),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": peak_kind, "traffic": None,
+                         "bytes_per_step_main_batch": bytes_step, "note": "algorithmic bytes of the main batch"},
+            "cpu_baseline": {"value": cpu_rate, "unit": "member-ops/s", "cores": 1, "kind": "port",
+                             "sample": f"{traj} trajectory-steps ({cpu_ops} ops) of the oracle at {n} qubits, 1 thread"},
+            "gpu_launches": launches, "clocks": clk, "host_s": host}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
     elif a.workload == "serve":
         run_serve(a)
+    elif a.workload in ("c1", "c2", "c3"):
+        {"c1": run_c1, "c2": run_c2, "c3": run_c3}[a.workload](a)
     else:
         run_ours(a)

@@ -109,6 +109,9 @@ def build_slots(member_ops, noise=False):
 
 
 def _same_gate(items):
+    first = items[0] if items else None
+    if first is not None and all(it is first for it in items):  # one shared payload
+        return True
     first = None
     for it in items:
         if it is None:

@@ -766,28 +766,32 @@ def run_c3(args):
     bytes_step = ngates * 2 * S + nch * 2 * S + nad * S + n * (S + 2 * S)
     zs = bt.expect(st, "Z", member=-1)
     assert np.all(np.isfinite(zs))
-    # CPU: the oracle on a sample of trajectories (one step each, complex128)
-    O = _oracle()
-    cpu_ops = 0
-    t0 = time.perf_counter()
-    urng = np.random.default_rng(3)
-    traj = 0
-    while time.perf_counter() - t0 < min(args.cpu_seconds, 15.0) or traj < 1:
-        psi = np.zeros(2 ** n, complex)
-        psi[0] = 1
-        for op in step_ops:
-            if isinstance(op, bt.OpQC):
-                qs = _op_qubits(op)
-                psi, _, _ = O.channel_traj(psi, op.kraus, qs[0], qs[1] if len(qs) == 2 else -1, u=urng.random())
-            else:
-                psi = O.apply_k(psi, op.mat, _op_qubits(op), [])
-            cpu_ops += 1
-        for q in range(1, n + 1):
-            if urng.random() < 0.1:
-                psi, _, _ = O.born_measure_z(psi, q, u=urng.random())
+    cpu = None
+    if not args.no_cpu:
+        # CPU: the oracle on a sample of trajectories (one step each, complex128)
+        O = _oracle()
+        cpu_ops = 0
+        t0 = time.perf_counter()
+        urng = np.random.default_rng(3)
+        traj = 0
+        while time.perf_counter() - t0 < min(args.cpu_seconds, 15.0) or traj < 1:
+            psi = np.zeros(2 ** n, complex)
+            psi[0] = 1
+            for op in step_ops:
+                if isinstance(op, bt.OpQC):
+                    qs = _op_qubits(op)
+                    psi, _, _ = O.channel_traj(psi, op.kraus, qs[0], qs[1] if len(qs) == 2 else -1,
+                                               u=urng.random())
+                else:
+                    psi = O.apply_k(psi, op.mat, _op_qubits(op), [])
                 cpu_ops += 1
-        traj += 1
-    cpu_rate = cpu_ops / (time.perf_counter() - t0)
+            for q in range(1, n + 1):
+                if urng.random() < 0.1:
+                    psi, _, _ = O.born_measure_z(psi, q, u=urng.random())
+                    cpu_ops += 1
+            traj += 1
+        cpu = {"value": cpu_ops / (time.perf_counter() - t0), "unit": "member-ops/s", "cores": 1, "kind": "port",
+               "sample": f"{traj} trajectory-steps ({cpu_ops} ops) of the oracle at {n} qubits, 1 thread"}
     value = timed_ops / (ms / 1e3)
     achieved = bytes_step * args.steps / (ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
@@ -802,9 +806,7 @@ def run_c3(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind, "traffic": None,
                          "bytes_per_step_main_batch": bytes_step, "note": "algorithmic bytes of the main batch"},
-            "cpu_baseline": {"value": cpu_rate, "unit": "member-ops/s", "cores": 1, "kind": "port",
-                             "sample": f"{traj} trajectory-steps ({cpu_ops} ops) of the oracle at {n} qubits, 1 thread"},
-            "gpu_launches": launches, "clocks": clk, "host_s": host}
+            "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clk, "host_s": host}
     print(json.dumps(line), flush=True)
     ctx.close()
 

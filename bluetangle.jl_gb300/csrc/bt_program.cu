@@ -16,6 +16,7 @@
 #include <string.h>
 
 #include <atomic>
+#include <type_traits>
 #include <vector>
 
 #include "bt_internal.cuh"
@@ -131,32 +132,60 @@ __device__ __forceinline__ void apply2(typename CT<R>::T* st, int nbits, int b0,
 template <typename R, int K>
 __device__ void reduce_rho(const typename CT<R>::T* st, int nbits, int b0, int b1, double* sh, double* rho) {
   constexpr int D = 1 << K, W = 2 * D * D;
+  // complex64: FP32 products summed over 8 consecutive iterations of a thread,
+  // each group added to FP64 accumulators (GB300's FP64 issue rate would
+  // otherwise bound the reduction); complex128: FP64 throughout
+  typedef typename std::conditional<sizeof(R) == 4, float, double>::type A;
+  constexpr int J = sizeof(R) == 4 ? 8 : 1;
   double acc[W];
 #pragma unroll
   for (int w = 0; w < W; ++w) acc[w] = 0;
   const int lo = K == 2 ? (b0 < b1 ? b0 : b1) : b0, hi = K == 2 ? (b0 < b1 ? b1 : b0) : b0;
   const int ng = 1 << (nbits - K);
-  for (int p = threadIdx.x; p < ng; p += PG_THREADS) {
-    int base = ((p >> lo) << (lo + 1)) | (p & ((1 << lo) - 1));
-    if (K == 2) base = ((base >> hi) << (hi + 1)) | (base & ((1 << hi) - 1));
-    double xr[D], xi[D];
+  for (int p0 = threadIdx.x; p0 < ng; p0 += PG_THREADS * J) {
+    A f[W];
 #pragma unroll
-    for (int j = 0; j < D; ++j) {
-      int idx = base;
-      if (K == 1) idx |= (j & 1) << b0;
-      else idx |= ((j >> 1) & 1) << b0 | (j & 1) << b1;
-      typename CT<R>::T v = st[idx];
-      xr[j] = (double)v.x;
-      xi[j] = (double)v.y;
+    for (int w = 0; w < W; ++w) f[w] = 0;
+#pragma unroll
+    for (int jj = 0; jj < J; ++jj) {
+      const int p = p0 + jj * PG_THREADS;
+      if (p >= ng) break;
+      int base = ((p >> lo) << (lo + 1)) | (p & ((1 << lo) - 1));
+      if (K == 2) base = ((base >> hi) << (hi + 1)) | (base & ((1 << hi) - 1));
+      A xr[D], xi[D];
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        int idx = base;
+        if (K == 1) idx |= (j & 1) << b0;
+        else idx |= ((j >> 1) & 1) << b0 | (j & 1) << b1;
+        typename CT<R>::T v = st[idx];
+        xr[j] = (A)v.x;
+        xi[j] = (A)v.y;
+      }
+#pragma unroll
+      for (int a = 0; a < D; ++a)
+#pragma unroll
+        for (int b = a; b < D; ++b) {
+          f[2 * (a * D + b)] += xr[a] * xr[b] + xi[a] * xi[b];
+          if (b != a) f[2 * (a * D + b) + 1] += xi[a] * xr[b] - xr[a] * xi[b];
+        }
     }
 #pragma unroll
     for (int a = 0; a < D; ++a)
 #pragma unroll
-      for (int b = 0; b < D; ++b) {
-        acc[2 * (a * D + b)] += xr[a] * xr[b] + xi[a] * xi[b];
-        acc[2 * (a * D + b) + 1] += xi[a] * xr[b] - xr[a] * xi[b];
+      for (int b = a; b < D; ++b) {
+        acc[2 * (a * D + b)] += (double)f[2 * (a * D + b)];
+        acc[2 * (a * D + b) + 1] += (double)f[2 * (a * D + b) + 1];
       }
   }
+  // lower triangle from the upper one: rho[b, a] = conj(rho[a, b])
+#pragma unroll
+  for (int a = 0; a < D; ++a)
+#pragma unroll
+    for (int b = 0; b < a; ++b) {
+      acc[2 * (a * D + b)] = acc[2 * (b * D + a)];
+      acc[2 * (a * D + b) + 1] = -acc[2 * (b * D + a) + 1];
+    }
   block_reduce<W>(acc, sh);
   if (threadIdx.x < W) rho[threadIdx.x] = sh[8 * W + threadIdx.x];
   __syncthreads();

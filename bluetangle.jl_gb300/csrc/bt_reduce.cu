@@ -1,5 +1,6 @@
-// Reductions (FP64 accumulation for every precision), measurement collapse,
-// density-matrix dephasing and the device-side branch/outcome decisions.
+// Reductions (FP64 accumulation; complex64 states form 8-term FP32 micro-sums
+// first, see Micro below), measurement collapse, density-matrix dephasing and
+// the device-side branch/outcome decisions.
 //
 // Every reduction writes one partial per (member, block) and a second kernel
 // sums the partials of a member in a fixed order, so results are bit-for-bit
@@ -42,6 +43,28 @@ __global__ void k_finalize(const double* __restrict__ part, int nblk, int W, dou
     for (int b = 0; b < nblk; ++b) s += p[(int64_t)b * W];
     out[mem * W + w] = s;
   }
+}
+
+// Micro-sums.  GB300 issues FP64 at a small fraction of its FP32 rate, so a
+// complex64 reduction that forms every product and every partial sum in FP64 is
+// bound by FP64 issue, far below HBM speed.  For complex64 states each thread
+// forms products and sums MICRO consecutive terms of its grid-stride sequence in
+// FP32 (relative error <= MICRO * 2^-24 per group, below the rounding the
+// complex64 amplitudes already carry) and adds each group to FP64 accumulators;
+// every longer sum -- over groups, threads, blocks -- is FP64, in a fixed order.
+// complex128 states keep FP64 throughout.
+template <typename R> struct Micro { typedef double T; enum { J = 1 }; };
+template <> struct Micro<float> { typedef float T; enum { J = 8 }; };
+
+// Hermitian packing of a D x D reduced matrix: D real diagonal entries, then
+// (re, im) of each a < b; herm_index gives the packed slots of entry (a, b).
+template <int D>
+__device__ __forceinline__ int herm_re(int a, int b) {
+  if (a == b) return a;
+  const int lo = a < b ? a : b, hi = a < b ? b : a;
+  // pairs (lo, hi) in row order: before row lo come sum_{r<lo} (D-1-r) pairs
+  const int pair = lo * (2 * D - lo - 1) / 2 + (hi - lo - 1);
+  return D + 2 * pair;
 }
 
 // blocks per member for a reduction over `units` thread-units per member
@@ -100,33 +123,103 @@ __global__ void __launch_bounds__(BT_THREADS) k_rdm(const typename CT<R>::T* __r
   const int64_t mem = mem_lo + blockIdx.y;
   const typename CT<R>::T* s = psi + (mem << nbits);
   const int64_t ng = 1LL << (nbits - K);
-  double acc[W];
+  const int64_t stride = (int64_t)nblk * blockDim.x;
+  if constexpr (K <= 2) {
+    // Hermitian: accumulate the D*D packed reals, expand to the full matrix at the end
+    typedef typename Micro<R>::T A;
+    constexpr int WH = D * D, J = Micro<R>::J;
+    double acc[WH];
 #pragma unroll
-  for (int w = 0; w < W; ++w) acc[w] = 0;
-  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += (int64_t)nblk * blockDim.x) {
-    uint64_t base = (uint64_t)g;
+    for (int w = 0; w < WH; ++w) acc[w] = 0;
+    for (int64_t g0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g0 < ng; g0 += stride * J) {
+      A f[WH];
 #pragma unroll
-    for (int i = 0; i < K; ++i) {
-      const int p = sorted[i];
-      base = ((base >> p) << (p + 1)) | (base & ((1ULL << p) - 1));
-    }
-    double xr[D], xi[D];
+      for (int w = 0; w < WH; ++w) f[w] = 0;
 #pragma unroll
-    for (int j = 0; j < D; ++j) {
-      typename CT<R>::T v = s[base + off[j]];
-      xr[j] = (double)v.x;
-      xi[j] = (double)v.y;
-    }
-    // rho[a, b] += x_a conj(x_b), row-major interleaved
+      for (int jj = 0; jj < J; ++jj) {
+        const int64_t g = g0 + jj * stride;
+        if (g >= ng) break;
+        uint64_t base = (uint64_t)g;
 #pragma unroll
-    for (int a = 0; a < D; ++a)
+        for (int i = 0; i < K; ++i) {
+          const int p = sorted[i];
+          base = ((base >> p) << (p + 1)) | (base & ((1ULL << p) - 1));
+        }
+        A xr[D], xi[D];
 #pragma unroll
-      for (int b = 0; b < D; ++b) {
-        acc[2 * (a * D + b)] += xr[a] * xr[b] + xi[a] * xi[b];
-        acc[2 * (a * D + b) + 1] += xi[a] * xr[b] - xr[a] * xi[b];
+        for (int j = 0; j < D; ++j) {
+          typename CT<R>::T v = s[base + off[j]];
+          xr[j] = (A)v.x;
+          xi[j] = (A)v.y;
+        }
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+          f[a] += xr[a] * xr[a] + xi[a] * xi[a];
+#pragma unroll
+          for (int b = a + 1; b < D; ++b) {
+            const int r = herm_re<D>(a, b);
+            f[r] += xr[a] * xr[b] + xi[a] * xi[b];      // Re x_a conj(x_b)
+            f[r + 1] += xi[a] * xr[b] - xr[a] * xi[b];  // Im x_a conj(x_b)
+          }
+        }
       }
+#pragma unroll
+      for (int w = 0; w < WH; ++w) acc[w] += (double)f[w];
+    }
+    // block reduction of the packed sums, then the full row-major matrix
+    __shared__ double sh[BT_THREADS / 32][WH];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int w = 0; w < WH; ++w) {
+      double v = acc[w];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+      if (lane == 0) sh[warp][w] = v;
+    }
+    __syncthreads();
+    double* out = part + ((int64_t)blockIdx.y * nblk + blockIdx.x) * W;
+    for (int w = threadIdx.x; w < W; w += blockDim.x) {
+      const int e = w >> 1, a = e / D, b = e % D, im = w & 1;
+      double v = 0;
+      if (a == b) {
+        if (!im)
+          for (int i = 0; i < BT_THREADS / 32; ++i) v += sh[i][a];
+      } else {
+        const int r = herm_re<D>(a, b) + im;
+        for (int i = 0; i < BT_THREADS / 32; ++i) v += sh[i][r];
+        if (im && a > b) v = -v;  // rho[a, b] = conj(rho[b, a])
+      }
+      out[w] = v;
+    }
+  } else {
+    double acc[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) acc[w] = 0;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += stride) {
+      uint64_t base = (uint64_t)g;
+#pragma unroll
+      for (int i = 0; i < K; ++i) {
+        const int p = sorted[i];
+        base = ((base >> p) << (p + 1)) | (base & ((1ULL << p) - 1));
+      }
+      double xr[D], xi[D];
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        typename CT<R>::T v = s[base + off[j]];
+        xr[j] = (double)v.x;
+        xi[j] = (double)v.y;
+      }
+      // rho[a, b] += x_a conj(x_b), row-major interleaved
+#pragma unroll
+      for (int a = 0; a < D; ++a)
+#pragma unroll
+        for (int b = 0; b < D; ++b) {
+          acc[2 * (a * D + b)] += xr[a] * xr[b] + xi[a] * xi[b];
+          acc[2 * (a * D + b) + 1] += xi[a] * xr[b] - xr[a] * xi[b];
+        }
+    }
+    block_sum_store<W>(acc, part + ((int64_t)blockIdx.y * nblk + blockIdx.x) * W, W);
   }
-  block_sum_store<W>(acc, part + ((int64_t)blockIdx.y * nblk + blockIdx.x) * W, W);
 }
 
 template <typename R, int K>
@@ -174,66 +267,100 @@ struct PauliArgs {
   int dm;    // 1: density matrix, element rho[a, a^x] at a + ((a^x) << nsys)
 };
 
-__device__ __forceinline__ void phase_of(uint64_t i, uint64_t x, uint64_t z, double& pr, double& pi) {
+template <typename T>
+__device__ __forceinline__ void phase_of(uint64_t i, uint64_t x, uint64_t z, T& pr, T& pi) {
   // P|i> = i^{popcount(x&z)} (-1)^{popcount(i&z)} |i^x>
   int ny = __popcll(x & z) & 3;
   int sg = __popcll(i & z) & 1;
-  pr = (ny == 0) ? 1.0 : (ny == 2 ? -1.0 : 0.0);
-  pi = (ny == 1) ? 1.0 : (ny == 3 ? -1.0 : 0.0);
+  pr = (ny == 0) ? (T)1 : (ny == 2 ? (T)-1 : (T)0);
+  pi = (ny == 1) ? (T)1 : (ny == 3 ? (T)-1 : (T)0);
   if (sg) { pr = -pr; pi = -pi; }
 }
 
 template <typename R>
 __global__ void __launch_bounds__(BT_THREADS) k_pauli(const typename CT<R>::T* __restrict__ psi, PauliArgs a,
                                                       int64_t mem_lo, int nblk, double* __restrict__ part) {
+  typedef typename Micro<R>::T A;
+  constexpr int J = Micro<R>::J;
   double acc[8];
+  A f[8];
 #pragma unroll
   for (int t = 0; t < 8; ++t) acc[t] = 0;
   const int64_t mem = mem_lo + blockIdx.y;
   const typename CT<R>::T* s = psi + (mem << a.nbits);
+  const int64_t stride = (int64_t)nblk * blockDim.x;
+  const int64_t start = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  // phases are exactly +-1, +-i: computed in double and converted without rounding
   if (a.dm) {
     const int64_t n = 1LL << a.nsys;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)nblk * blockDim.x) {
-      uint64_t j = (uint64_t)i ^ a.x;
-      typename CT<R>::T v = s[(uint64_t)i + (j << a.nsys)];
+    for (int64_t i0 = start; i0 < n; i0 += stride * J) {
 #pragma unroll
-      for (int t = 0; t < 8; ++t) {
-        if (t < a.T) {
-          double pr, pi;
-          phase_of((uint64_t)i, a.x, a.z[t], pr, pi);
-          acc[t] += pr * (double)v.x - pi * (double)v.y;
+      for (int t = 0; t < 8; ++t) f[t] = 0;
+#pragma unroll
+      for (int jj = 0; jj < J; ++jj) {
+        const int64_t i = i0 + jj * stride;
+        if (i >= n) break;
+        uint64_t j = (uint64_t)i ^ a.x;
+        typename CT<R>::T v = s[(uint64_t)i + (j << a.nsys)];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+          if (t < a.T) {
+            A pr, pi;
+            phase_of<A>((uint64_t)i, a.x, a.z[t], pr, pi);
+            f[t] += pr * (A)v.x - pi * (A)v.y;
+          }
         }
       }
+#pragma unroll
+      for (int t = 0; t < 8; ++t) acc[t] += (double)f[t];
     }
   } else if (a.hbit < 0) {
     const int64_t n = 1LL << a.nbits;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)nblk * blockDim.x) {
-      typename CT<R>::T v = s[i];
-      double p = (double)v.x * v.x + (double)v.y * v.y;
+    for (int64_t i0 = start; i0 < n; i0 += stride * J) {
 #pragma unroll
-      for (int t = 0; t < 8; ++t)
-        if (t < a.T) acc[t] += (__popcll((uint64_t)i & a.z[t]) & 1) ? -p : p;
+      for (int t = 0; t < 8; ++t) f[t] = 0;
+#pragma unroll
+      for (int jj = 0; jj < J; ++jj) {
+        const int64_t i = i0 + jj * stride;
+        if (i >= n) break;
+        typename CT<R>::T v = s[i];
+        const A p = (A)v.x * (A)v.x + (A)v.y * (A)v.y;
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+          if (t < a.T) f[t] += (__popcll((uint64_t)i & a.z[t]) & 1) ? -p : p;
+      }
+#pragma unroll
+      for (int t = 0; t < 8; ++t) acc[t] += (double)f[t];
     }
   } else {
     const int64_t n = 1LL << (a.nbits - 1);
     const int h = a.hbit;
-    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (int64_t)nblk * blockDim.x) {
-      uint64_t i = (((uint64_t)g >> h) << (h + 1)) | ((uint64_t)g & ((1ULL << h) - 1));
-      uint64_t j = i ^ a.x;
-      typename CT<R>::T vi = s[i], vj = s[j];
-      // c = conj(psi_j) * psi_i
-      double cr = (double)vj.x * vi.x + (double)vj.y * vi.y;
-      double ci = (double)vj.x * vi.y - (double)vj.y * vi.x;
+    for (int64_t g0 = start; g0 < n; g0 += stride * J) {
 #pragma unroll
-      for (int t = 0; t < 8; ++t) {
-        if (t < a.T) {
-          double p1r, p1i, p2r, p2i;
-          phase_of(i, a.x, a.z[t], p1r, p1i);
-          phase_of(j, a.x, a.z[t], p2r, p2i);
-          // Re(ph_i c) + Re(conj(ph_j) c)
-          acc[t] += (p1r + p2r) * cr - (p1i - p2i) * ci;
+      for (int t = 0; t < 8; ++t) f[t] = 0;
+#pragma unroll
+      for (int jj = 0; jj < J; ++jj) {
+        const int64_t g = g0 + jj * stride;
+        if (g >= n) break;
+        uint64_t i = (((uint64_t)g >> h) << (h + 1)) | ((uint64_t)g & ((1ULL << h) - 1));
+        uint64_t j = i ^ a.x;
+        typename CT<R>::T vi = s[i], vj = s[j];
+        // c = conj(psi_j) * psi_i
+        const A cr = (A)vj.x * (A)vi.x + (A)vj.y * (A)vi.y;
+        const A ci = (A)vj.x * (A)vi.y - (A)vj.y * (A)vi.x;
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+          if (t < a.T) {
+            A p1r, p1i, p2r, p2i;
+            phase_of<A>(i, a.x, a.z[t], p1r, p1i);
+            phase_of<A>(j, a.x, a.z[t], p2r, p2i);
+            // Re(ph_i c) + Re(conj(ph_j) c)
+            f[t] += (p1r + p2r) * cr - (p1i - p2i) * ci;
+          }
         }
       }
+#pragma unroll
+      for (int t = 0; t < 8; ++t) acc[t] += (double)f[t];
     }
   }
   block_sum_store<8>(acc, part + ((int64_t)blockIdx.y * nblk + blockIdx.x) * 8, 8);
@@ -289,18 +416,31 @@ __global__ void __launch_bounds__(BT_THREADS) k_bitsums(const typename CT<R>::T*
   if (nsys >= 10) {
     const int64_t nchunk = nent >> 10;
     double lanetot = 0;
+    typedef typename Micro<R>::T A;
     for (int64_t c = wid; c < nchunk; c += warps_total) {
       double csum = 0;
       double jb[5] = {0, 0, 0, 0, 0};
-#pragma unroll 8
-      for (int j = 0; j < 32; ++j) {
-        uint64_t i = ((uint64_t)c << 10) + ((uint64_t)j << 5) + lane;
-        typename CT<R>::T v = dm ? s[i + (i << nsys)] : s[i];
-        double p = dm ? (double)v.x : (double)v.x * v.x + (double)v.y * v.y;
-        csum += p;
+      // four groups of 8 j's: per group an FP32 (complex64) or FP64 micro-sum and
+      // the sums for j-bits 0-2; j-bits 3-4 are constant within a group
 #pragma unroll
-        for (int b = 0; b < 5; ++b)
-          if ((j >> b) & 1) jb[b] += p;
+      for (int g = 0; g < 4; ++g) {
+        A gs = 0, gb[3] = {0, 0, 0};
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) {
+          const int j = g * 8 + jj;
+          uint64_t i = ((uint64_t)c << 10) + ((uint64_t)j << 5) + lane;
+          typename CT<R>::T v = dm ? s[i + (i << nsys)] : s[i];
+          const A p = dm ? (A)v.x : (A)v.x * (A)v.x + (A)v.y * (A)v.y;
+          gs += p;
+#pragma unroll
+          for (int b = 0; b < 3; ++b)
+            if ((jj >> b) & 1) gb[b] += p;
+        }
+        csum += (double)gs;
+#pragma unroll
+        for (int b = 0; b < 3; ++b) jb[b] += (double)gb[b];
+        if (g & 1) jb[3] += (double)gs;
+        if (g & 2) jb[4] += (double)gs;
       }
       lanetot += csum;
 #pragma unroll
@@ -354,12 +494,24 @@ template <typename Ra, typename Rb>
 __global__ void __launch_bounds__(BT_THREADS) k_inner(const typename CT<Ra>::T* __restrict__ a,
                                                       const typename CT<Rb>::T* __restrict__ b, int64_t n,
                                                       int nblk, double* __restrict__ part) {
+  // FP32 micro-sums only when both states are complex64
+  typedef typename Micro<decltype(Ra() + Rb())>::T A;
+  constexpr int J = Micro<decltype(Ra() + Rb())>::J;
   double acc[2] = {0, 0};
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)nblk * blockDim.x) {
-    typename CT<Ra>::T x = a[i];
-    typename CT<Rb>::T y = b[i];
-    acc[0] += (double)x.x * y.x + (double)x.y * y.y;
-    acc[1] += (double)x.x * y.y - (double)x.y * y.x;
+  const int64_t stride = (int64_t)nblk * blockDim.x;
+  for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += stride * J) {
+    A f0 = 0, f1 = 0;
+#pragma unroll
+    for (int jj = 0; jj < J; ++jj) {
+      const int64_t i = i0 + jj * stride;
+      if (i >= n) break;
+      typename CT<Ra>::T x = a[i];
+      typename CT<Rb>::T y = b[i];
+      f0 += (A)x.x * (A)y.x + (A)x.y * (A)y.y;
+      f1 += (A)x.x * (A)y.y - (A)x.y * (A)y.x;
+    }
+    acc[0] += (double)f0;
+    acc[1] += (double)f1;
   }
   block_sum_store<2>(acc, part + (int64_t)blockIdx.x * 2, 2);
 }

@@ -361,6 +361,8 @@ def run_ours(args):
                                     % (args.depth, sum(lg for _, lg in packed))) if plan is not None else
                                    "one brickwork layer (logical gates: n one-qubit + CNOTs)",
                            "plan": pstats if plan is not None else None,
+                           "tuning": {k: os.environ.get(k) for k in ("BTGPU_JIT_MINB", "BTGPU_PLAN_MAX_OPS")
+                                      if os.environ.get(k)},
                            "passes_per_step": passes / args.steps, "global_batch": 1, "seq_len": None,
                            "parallelism": f"replicas x{ws}", "l2": "state larger than L2, no flush needed",
                            "state_bytes": (2 ** args.n) * esize},

@@ -64,6 +64,24 @@ static Nvrtc* nvrtc() {
 
 bool bt_jit_available() { return nvrtc() != nullptr && getenv("BTGPU_NO_JIT") == nullptr; }
 
+// Tuning knobs of the specialised passes (read once): resident CTAs per SM the
+// kernels are compiled for (register budget 65536 / (threads * blocks)), and the
+// most gates a specialised pass takes.
+static int env_int(const char* name, int dflt, int lo, int hi) {
+  const char* v = getenv(name);
+  if (!v || !*v) return dflt;
+  const int x = atoi(v);
+  return x < lo ? lo : (x > hi ? hi : x);
+}
+int bt_jit_min_blocks() {
+  static const int v = env_int("BTGPU_JIT_MINB", 2, 1, 4);
+  return v;
+}
+int bt_jit_max_ops() {
+  static const int v = env_int("BTGPU_PLAN_MAX_OPS", 64, 8, BT_FUSED_MAX_OPS);
+  return v;
+}
+
 // ------------------------------------------------------------------ generated source
 static const char* kPrelude = R"PRELUDE(
 typedef long long i64;
@@ -241,7 +259,8 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
   const int T = 1 << (M - NB);
   const int NPT = (1 << M) / V / T;
   const char* T2 = f ? "cf" : "cd";
-  o << "extern \"C\" __global__ void __launch_bounds__(" << T << ", 2) " << name << "(" << T2 << "* __restrict__ psi, const "
+  o << "extern \"C\" __global__ void __launch_bounds__(" << T << ", " << bt_jit_min_blocks() << ") " << name << "("
+    << T2 << "* __restrict__ psi, const "
     << (f ? "JitArgsF<" : "JitArgsD<") << NM << "> a) {\n";
   o << "  typedef " << (f ? "float" : "double") << " R;\n";
   o << "  extern __shared__ __align__(16) unsigned char smem_raw[];\n";
@@ -320,7 +339,7 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
 template <typename R>
 static std::string structure_key(const FusedArgs<R>& a) {
   std::ostringstream k;
-  k << (sizeof(R) == 4 ? 'f' : 'd') << a.M << ':' << a.c << ':';
+  k << (sizeof(R) == 4 ? 'f' : 'd') << a.M << ':' << a.c << ':' << bt_jit_min_blocks() << ':';
   for (int i = 0; i < a.M; ++i) k << a.tbits[i] << ',';
   for (int p = 0; p < a.nphase; ++p) {
     const FPhase& ph = a.ph[p];
@@ -527,7 +546,7 @@ static int jit_launch_t(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<R>&
   memcpy(h.mat, a.mat, sizeof(h.mat));
   void* args[] = {&psi, &h};
   int64_t total = (1LL << a.lg_tiles) * a.nmem;
-  int64_t grid = (int64_t)ctx->sm_count * 2 * 4;
+  int64_t grid = (int64_t)ctx->sm_count * bt_jit_min_blocks() * 4;
   if (grid > total) grid = total;
   const unsigned threads = 1u << (a.M - (sizeof(R) == 4 ? BT_TILE_RB_C64 : BT_TILE_RB_C128));
   cudaError_t e = cudaLaunchKernel((const void*)kern, dim3((unsigned)grid), dim3(threads), args, smem,

@@ -6,6 +6,8 @@
 #include "bt_fused.cuh"
 
 bool bt_jit_available();
+int bt_jit_min_blocks();  // CTAs per SM the specialised passes are compiled for (BTGPU_JIT_MINB, default 2)
+int bt_jit_max_ops();     // gates per specialised pass at most (BTGPU_PLAN_MAX_OPS, default 64)
 // compiles (once per distinct pass structure) and returns one kernel entry per pass
 int bt_jit_prepare_f(bt_ctx* ctx, std::vector<const FusedArgs<float>*>& passes, std::vector<void*>& out);
 int bt_jit_prepare_d(bt_ctx* ctx, std::vector<const FusedArgs<double>*>& passes, std::vector<void*>& out);

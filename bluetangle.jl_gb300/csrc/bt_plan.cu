@@ -497,7 +497,7 @@ int bt_plan_compile(bt_plan* p, int mode) {
   const bool fuse = (mode == 0 || mode == 2) && M >= NB + 5;
   // specialised kernels compile in time superlinear in their length: bound the
   // ops of a pass when they will be specialised
-  const int max_ops = bt_jit_available() ? 64 : BT_FUSED_MAX_OPS;
+  const int max_ops = bt_jit_available() ? bt_jit_max_ops() : BT_FUSED_MAX_OPS;
   std::vector<int> rem(p->gates.size());
   for (size_t i = 0; i < rem.size(); ++i) rem[i] = (int)i;
   const uint64_t lowmask = (1ULL << c) - 1;

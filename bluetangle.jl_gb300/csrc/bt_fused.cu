@@ -317,16 +317,6 @@ struct Offs {
   }
 };
 
-// Starts the HBM reads of the CTA's next tile while the current one is computed:
-// each run of 2^c contiguous elements (256 bytes, 256-byte aligned: the low c bits
-// of every tile base are zero) is prefetched into L2 by one bulk prefetch.
-template <typename C2>
-__device__ __forceinline__ void prefetch_tile_l2(const C2* g, const int64_t* runoff, int nruns, int c) {
-  const unsigned bytes = (unsigned)(sizeof(C2) << c);
-  for (int r = threadIdx.x; r < nruns; r += blockDim.x)
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(g + runoff[r]), "r"(bytes) : "memory");
-}
-
 template <typename R, int M, int NB>
 __global__ void __launch_bounds__(1 << (M - NB), 2) k_fused(typename CT<R>::T* __restrict__ psi,
                                                               const FusedArgs<R> a) {
@@ -356,15 +346,6 @@ __global__ void __launch_bounds__(1 << (M - NB), 2) k_fused(typename CT<R>::T* _
       base = ((base >> p) << (p + 1)) | (base & ((1ULL << p) - 1));
     }
     C2* g = psi + (mem << a.nbits) + base;
-    if (tid + gridDim.x < total) {  // the next tile of this CTA into L2
-      const int64_t nt = tid + gridDim.x;
-      uint64_t nb = (uint64_t)(nt & (per - 1));
-      for (int i = 0; i < M; ++i) {
-        const int p = a.tbits[i];
-        nb = ((nb >> p) << (p + 1)) | (nb & ((1ULL << p) - 1));
-      }
-      prefetch_tile_l2(psi + ((a.member_lo + (nt >> a.lg_tiles)) << a.nbits) + nb, runoff, nruns, c);
-    }
     // every 16-byte load of the tile in flight at once (NPT per thread), then to smem
     constexpr int T = 1 << (M - NB);
     constexpr int NPT = NCHUNK / T;

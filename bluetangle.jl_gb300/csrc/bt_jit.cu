@@ -277,17 +277,6 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
     o << "    base = ((base >> " << p << ") << " << (p + 1) << ") | (base & " << fmt_u64((1ULL << p) - 1) << ");\n";
   }
   o << "    " << T2 << "* g = psi + (mem << a.nbits) + base;\n";
-  // the next tile of this CTA into L2 while this one is computed (one bulk
-  // prefetch per 256-byte aligned run of 2^c elements)
-  o << "    if (tid + gridDim.x < total) {\n      const i64 nt = tid + gridDim.x; u64 nb = (u64)(nt & (per - 1));\n";
-  for (int i = 0; i < M; ++i) {
-    const int p = a.tbits[i];
-    o << "      nb = ((nb >> " << p << ") << " << (p + 1) << ") | (nb & " << fmt_u64((1ULL << p) - 1) << ");\n";
-  }
-  o << "      const " << T2 << "* ng = psi + ((a.member_lo + (nt >> a.lg_tiles)) << a.nbits) + nb;\n";
-  o << "      for (int r = threadIdx.x; r < " << (1 << (M - c)) << "; r += " << T
-    << ") asm volatile(\"cp.async.bulk.prefetch.L2.global [%0], " << ((f ? 8 : 16) << c)
-    << ";\" :: \"l\"(ng + runoff[r]) : \"memory\");\n    }\n";
   // tile load: every 16-byte load in flight, then into the swizzled tile
   o << "    {\n";
   for (int i = 0; i < NPT; ++i)

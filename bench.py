@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--c3-twirl", type=int, default=64, help="twirl instances (x3 ZNE scales)")
     ap.add_argument("--rate", type=float, default=2000.0, help="serving: Poisson arrival rate (req/s)")
     ap.add_argument("--lanes", type=int, default=8, help="serving: concurrent lanes (contexts/streams)")
+    ap.add_argument("--python-server", action="store_true",
+                    help="serving: the Python scheduler instead of the library's bt_serve engine")
     return ap.parse_args()
 
 
@@ -383,15 +385,15 @@ def run_ours(args):
 # ------------------------------------------------------------------ serving workload
 def serve_specs(seed, clients=32):
     """The serving mix: 70% state-vector jobs (n ~ U{8..26}), 20% trajectory
-    batches of 64 (n ~ U{8..16}: a 64-member batch then has the footprint of one
-    <= 22-qubit state), 10% density-matrix jobs (n ~ U{8..12}); hardware-efficient
+    batches of 64 (n ~ U{8..14}: each member in one CTA's shared memory, the whole
+    batch one launch), 10% density-matrix jobs (n ~ U{8..12}); hardware-efficient
     ansatz of depth U{4..12}; <H> of 4n random 2-local Pauli terms."""
     import bluetangle_gpu.serving as S
     rng = np.random.default_rng(seed)
     out = []
     for cid in range(clients):
         kind = rng.choice(["sv", "traj", "dm"], p=[0.7, 0.2, 0.1])
-        n = int(rng.integers(8, 27) if kind == "sv" else (rng.integers(8, 17) if kind == "traj" else rng.integers(8, 13)))
+        n = int(rng.integers(8, 27) if kind == "sv" else (rng.integers(8, 15) if kind == "traj" else rng.integers(8, 13)))
         out.append(S.make_client(rng, cid, str(kind), n, int(rng.integers(4, 13))))
     return out
 
@@ -407,19 +409,27 @@ def run_serve(args):
     owners = rng.integers(0, len(specs), total)
     reqs = [S.Request(i, int(owners[i]), rng.normal(0, 0.3, specs[owners[i]].nparams), seed=7000 + i)
             for i in range(total)]
-    srv = S.Server(specs, lanes=args.lanes, prec="c64")
+    native = not args.python_server
+    srv = (S.NativeServer if native else S.Server)(specs, lanes=args.lanes, prec="c64")
+
+    def wait(r):
+        if native:
+            srv.wait(r)
+        else:
+            r.done.wait(600)
+
     try:
         # warm-up: every client admitted once, then wait for the specialised kernels
         warm = [S.Request(-1 - c.cid, c.cid, rng.normal(0, 0.3, c.nparams), seed=c.cid) for c in specs]
         for w in warm:
             srv.submit(w)
         for w in warm:
-            w.done.wait(600)
+            wait(w)
         t0 = time.perf_counter()
         while time.perf_counter() - t0 < 600:
-            ready = all(r.plan is None or r.plan.stats()["jit_passes"] == r.plan.stats()["fused_passes"]
-                        for r, _ in srv.resident.values() if r is not None)
-            if ready:
+            plans = ([p for p in srv.keep if isinstance(p, bt.Plan)] if native else
+                     [r.plan for r, _ in srv.resident.values() if r is not None and r.plan is not None])
+            if all(p.stats()["jit_passes"] == p.stats()["fused_passes"] for p in plans):
                 break
             time.sleep(0.2)
         srv.completed.clear()
@@ -430,7 +440,7 @@ def run_serve(args):
                 time.sleep(dt)
             srv.submit(r)
         for r in reqs:
-            r.done.wait(600)
+            wait(r)
         makespan = max(r.t_done for r in reqs) - start
     finally:
         srv.close()
@@ -438,8 +448,10 @@ def run_serve(args):
     if errs:
         raise errs[0]
     lat = np.array([r.t_done - r.t_submit for r in reqs]) * 1e3
-    service = {k: float(np.mean([(r.t_done - r.t_start) * 1e3 for r in reqs if specs[r.cid].kind == k] or [0]))
-               for k in ("sv", "traj", "dm")}
+    service = None
+    if not native:  # the native engine reports submit-to-done only
+        service = {k: float(np.mean([(r.t_done - r.t_start) * 1e3 for r in reqs if specs[r.cid].kind == k] or [0]))
+                   for k in ("sv", "traj", "dm")}
     served = total / makespan
     # plain per-call complex128 path on a sample: one request per client, serially
     pctx = bt.Context(0, seed=5)
@@ -471,7 +483,8 @@ def run_serve(args):
             "vs_baseline": None, "dtype": "c64", "data": "synthetic",
             "config": {"workload": f"serving-{len(specs)}clients-poisson{args.rate:g}",
                        "mix": {k: sum(1 for c in specs if c.kind == k) for k in ("sv", "traj", "dm")},
-                       "requests": total, "lanes": args.lanes},
+                       "requests": total, "lanes": args.lanes,
+                       "engine": "bt_serve (native lanes)" if native else "python Server"},
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                            "mean": float(lat.mean())},
             "mean_service_ms_by_kind": service,

@@ -80,6 +80,13 @@ SIGNATURES = {
     "bt_program_info": (i32, [P, P, P, P]),
     "bt_program_set_gate": (i32, [P, i64, P]),
     "bt_program_run": (i32, [P, P, P, u64, P]),
+    "bt_serve_create": (i32, [i32, i32, u64, u64, ctypes.POINTER(P)]),
+    "bt_serve_destroy": (i32, [P]),
+    "bt_serve_add_plan_client": (i32, [P, P, i32, P, P, P, P]),
+    "bt_serve_add_program_client": (i32, [P, P, i32, P, P, P, P]),
+    "bt_serve_submit": (i32, [P, i64, i32, P, P, u64, P]),
+    "bt_serve_poll": (i32, [P, i64, i64, P, P]),
+    "bt_serve_stats": (i32, [P, P, P, P, P, P]),
     "bt_sample": (i32, [P, i64, i64, P, u64, P]),
     "bt_probabilities": (i32, [P, i64, P]),
     "bt_sample_noalloc": (i32, [P, i32, i32, i64, P, u64, u64, P, P]),

@@ -33,12 +33,12 @@ from collections import deque
 import numpy as np
 
 from . import _lib as L
-from .engine import Context, GPUDensity, GPUState, Plan, _ptr
+from .engine import Context, GPUDensity, GPUState, Plan, _cm, _ptr
 from .gates import gates
 from .noise import noise_model
 from .ops import Op, OpQC
 
-__all__ = ["ClientSpec", "make_client", "Server", "plain_request", "hea_ops"]
+__all__ = ["ClientSpec", "make_client", "Server", "NativeServer", "plain_request", "hea_ops"]
 
 
 def _ry(t):
@@ -51,6 +51,18 @@ def _rz(t):
 
 
 CNOT = np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 0, 1], [0, 0, 1, 0]], dtype=np.complex128)
+
+
+def _hea_mats(theta):
+    """RY(theta[0]), RZ(theta[1]), RY(theta[2]), ... as column-major 2x2 complex128
+    matrices back to back (the ABI's layout), built in one vectorised step."""
+    th = np.asarray(theta, dtype=np.float64)
+    out = np.zeros((len(th), 4), dtype=np.complex128)
+    ev, od = th[0::2], th[1::2]
+    c, s = np.cos(ev / 2), np.sin(ev / 2)
+    out[0::2, 0], out[0::2, 1], out[0::2, 2], out[0::2, 3] = c, s, -s, c
+    out[1::2, 0], out[1::2, 3] = np.exp(-0.5j * od), np.exp(0.5j * od)
+    return out.ravel()
 
 
 class ClientSpec:
@@ -306,6 +318,97 @@ class Server:
                 self.completed.append(req)
                 self.cv.notify_all()
             req.done.set()
+
+
+class NativeServer:
+    """The library's serving engine (bt_serve_*: C++ lanes, admission and
+    scheduling inside libbtgpu) over the same clients and requests as Server.
+    State-vector and density-matrix clients are compiled plans; trajectory
+    clients are programs (n <= 14 complex64 / 13 complex128), their draws keyed
+    by the request's seed on the device."""
+
+    def __init__(self, specs, lanes=8, prec="c64", hbm_budget=None, device=0, seed=1234, tiered=True):
+        from . import trajectories as T
+        lib = L.lib()
+        h = ctypes.c_void_p()
+        L.check(lib.bt_serve_create(int(device), int(lanes), int(seed), int(hbm_budget or 0), ctypes.byref(h)))
+        self.h = h
+        self.ctx = Context(device, seed=seed + 7919)  # owns the programs' device tables
+        self.specs = {s.cid: s for s in specs}
+        self.prec = prec
+        self.native = {}  # cid -> (client id, gate indices in theta order)
+        self.keep = []    # plans / programs / term arrays the server borrows
+        self.pending = {}
+        self.completed = []
+        for spec in specs:
+            n = spec.n
+            theta0 = np.full(spec.nparams, 0.1)
+            xs = np.ascontiguousarray([t[1] for t in spec.terms], dtype=np.uint64)
+            zs = np.ascontiguousarray([t[2] for t in spec.terms], dtype=np.uint64)
+            cs = np.ascontiguousarray([t[0] for t in spec.terms], dtype=np.float64)
+            cid = ctypes.c_int64()
+            if spec.kind in ("sv", "dm"):
+                dm = spec.kind == "dm"
+                plan = Plan(n, spec.kind, prec, self.ctx)
+                ops = hea_ops(n, spec.depth, theta0)
+                pidx = []
+                for i, op in enumerate(_noisy(spec, ops) if dm else ops):
+                    plan.add(op)
+                    if op.name in ("RY", "RZ"):
+                        pidx.append(i)
+                plan.compile(True, tiered=tiered)
+                L.check(lib.bt_serve_add_plan_client(h, plan.h, len(cs), _ptr(xs), _ptr(zs), _ptr(cs),
+                                                      ctypes.byref(cid)))
+                self.keep.append(plan)
+            else:
+                ops = _noisy(spec, hea_ops(n, spec.depth, theta0))
+                slots = T.build_slots(T.member_programs([ops], n, spec.ntraj))
+                if not T.program_supported(slots, n, prec):
+                    raise ValueError(f"trajectory client {spec.cid} (n={n}) does not fit a program")
+                prog, gate_ops = T.compile_program(slots, n, spec.ntraj, prec, self.ctx)
+                pidx = [gate_ops[i] for i, op in enumerate(ops) if op.name in ("RY", "RZ")]
+                L.check(lib.bt_serve_add_program_client(h, prog.h, len(cs), _ptr(xs), _ptr(zs), _ptr(cs),
+                                                         ctypes.byref(cid)))
+                self.keep.append(prog)
+            self.keep.append((xs, zs, cs))
+            self.native[spec.cid] = (cid.value, np.ascontiguousarray(pidx, dtype=np.int64))
+
+    def submit(self, req):
+        cid, pidx = self.native[req.cid]
+        mats = _hea_mats(req.theta)
+        t = ctypes.c_int64()
+        req.t_submit = time.perf_counter()
+        L.check(L.lib().bt_serve_submit(self.h, cid, len(pidx), _ptr(pidx), _ptr(mats), int(req.seed),
+                                        ctypes.byref(t)))
+        self.pending[t.value] = req
+        return req
+
+    def wait(self, req, timeout=600.0):
+        ticket = next(k for k, v in self.pending.items() if v is req)
+        val, lat = ctypes.c_double(), ctypes.c_double()
+        rc = L.lib().bt_serve_poll(self.h, ticket, int(timeout * 1e3), ctypes.byref(val), ctypes.byref(lat))
+        if rc == L.BT_ERR_TIMEOUT:
+            raise TimeoutError(f"request {req.rid} still pending")
+        del self.pending[ticket]
+        if rc:
+            req.error = L.BTError(rc, L.lib().bt_last_error(None).decode())
+        req.value = val.value
+        req.t_done = req.t_submit + lat.value
+        req.done.set()
+        self.completed.append(req)
+        return req
+
+    def stats(self):
+        v = [ctypes.c_int64(), ctypes.c_double(), ctypes.c_double(), ctypes.c_int64(), ctypes.c_uint64()]
+        L.check(L.lib().bt_serve_stats(self.h, *[ctypes.byref(x) for x in v]))
+        return dict(zip(("completed", "p50_s", "p99_s", "resident", "hbm_used"), (x.value for x in v)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            L.lib().bt_serve_destroy(self.h)
+            self.h = None
+        self.keep = []
+        self.ctx.close()
 
 
 def plain_request(spec, theta, seed, ctx, prec="c128"):

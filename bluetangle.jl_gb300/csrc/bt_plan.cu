@@ -616,3 +616,26 @@ int bt_plan_run(bt_plan* p, bt_state* s, int64_t member) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ serving hooks (bt_serve.cu)
+int bt_plan_shape(const bt_plan* p, int* n, int* repr, int* prec) {
+  if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "plan is NULL");
+  *n = p->n;
+  *repr = p->repr;
+  *prec = p->prec;
+  return BT_OK;
+}
+
+// reals of the matrices that bt_plan_set_matrices reads for these add indices
+int bt_plan_gate_dims(const bt_plan* p, const int64_t* idx, int count, size_t* reals) {
+  size_t r = 0;
+  for (int i = 0; i < count; ++i) {
+    const int64_t ai = idx[i];
+    if (ai < 0 || ai >= (int64_t)p->adds.size()) return bt_fail(nullptr, BT_ERR_BAD_ARG, "add index out of range");
+    if (p->adds[ai].second == 0) return bt_fail(nullptr, BT_ERR_BAD_ARG, "a Kraus sum cannot be updated");
+    const int d = 1 << p->gates[p->adds[ai].first].ku;
+    r += (size_t)2 * d * d;
+  }
+  *reals = r;
+  return BT_OK;
+}

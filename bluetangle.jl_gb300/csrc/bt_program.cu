@@ -546,7 +546,8 @@ int bt_program_run(bt_program* p, bt_state* s, const double* uniforms, uint64_t 
     if ((rc = bt_cuda_check(ctx, e, "program smem attribute"))) return rc;
     done.store(true);
   }
-  const uint64_t stream = (seed * 0x9E3779B97F4A7C15ULL) ^ 0x5052000000000000ULL ^ ctx->rng_calls++;
+  // draws depend on (ctx seed, seed) only, as bt_sample's: a run is reproducible
+  const uint64_t stream = (seed * 0x9E3779B97F4A7C15ULL) ^ 0x5052000000000000ULL;
   if (f)
     k_program<float><<<p->batch, PG_THREADS, smem, ctx->stream>>>(
         (float2*)s->d, s->nbits, (const PGOp*)p->d_ops, (int)p->ops.size(), (const float*)p->d_gm,
@@ -578,3 +579,16 @@ int bt_program_run(bt_program* p, bt_state* s, const double* uniforms, uint64_t 
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ serving hook (bt_serve.cu)
+// matrix dimension of every op (0 where the op is not a gate) and the shape
+int bt_program_gate_dims(const bt_program* p, std::vector<int>& dims, int* n, int* prec, int* batch) {
+  if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "program is NULL");
+  dims.assign(p->ops.size(), 0);
+  for (size_t i = 0; i < p->ops.size(); ++i)
+    dims[i] = p->ops[i].type == PG_GATE1 ? 2 : (p->ops[i].type == PG_GATE2 ? 4 : 0);
+  *n = p->n;
+  *prec = p->prec;
+  *batch = p->batch;
+  return BT_OK;
+}

@@ -1,0 +1,392 @@
+// Serving engine: continuous batching of variational circuit jobs on one GPU.
+//
+// A client is a VQE / Trotter loop of the reference (variational_apply followed
+// by expect(state, H); BlueTangle.jl src/vqa.jl:420-456, src/func.jl:100): a
+// fixed circuit, compiled once (a plan, or a program for trajectory batches),
+// evaluated again and again at new parameters, each time returning <H> of a
+// Pauli sum.  The engine
+//   * keeps each client's state resident between its requests and admits clients
+//     by HBM footprint, evicting idle residents least-recently-used first and
+//     holding a request back while nothing can be evicted;
+//   * runs requests on `lanes` host threads, each with its own context (CUDA
+//     stream), so requests arriving while others are on the GPU start as soon as a
+//     lane is free and their kernels overlap on the device;
+//   * serves a client's requests in arrival order (they share its state), one at
+//     a time, on the lane its state lives on;
+//   * records submit-to-done latency per request for p50/p99.
+// A request carries new matrices for some of the client's gates (plan add
+// indices, or program op indices) and a seed for the program's draws.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "bt_internal.cuh"
+
+namespace {
+
+double now_s() {
+  using namespace std::chrono;
+  return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct Req {
+  int64_t ticket = 0, client = 0;
+  std::vector<int64_t> idx;
+  std::vector<double> mats;
+  uint64_t seed = 0;
+  double t_submit = 0, t_start = 0, t_done = 0;
+  double value = 0;
+  int status = 0;
+  std::string err;
+  bool done = false;
+};
+
+struct Client {
+  int64_t id = 0;
+  bt_plan* plan = nullptr;
+  bt_program* prog = nullptr;
+  int repr = 0, prec = 0, n = 0, batch = 1;
+  std::vector<uint64_t> x, z;
+  std::vector<double> coef;
+  std::vector<int> gate_dim;  // program: matrix dimension of each op (0: not a gate)
+  size_t footprint = 0;
+  bt_state* state = nullptr;  // resident state (nullptr: not resident)
+  bool reserved = false;      // admitted, state being allocated by `lane`
+  int lane = -1;
+  bool busy = false;
+  double last_used = 0;
+  std::deque<Req*> queue;
+};
+
+}  // namespace
+
+struct bt_server {
+  int device = 0;
+  size_t budget = 0, used = 0;
+  std::vector<bt_ctx*> lanes;
+  std::vector<std::thread> threads;
+  std::mutex mu;
+  std::condition_variable cv;
+  bool stop = false;
+  std::map<int64_t, Client*> clients;
+  std::map<int64_t, Req*> reqs;
+  int64_t next_client = 0, next_ticket = 0;
+  std::vector<double> latencies;
+  std::string err;
+};
+
+// program/plan hooks (bt_program.cu, bt_plan.cu)
+int bt_program_gate_dims(const bt_program* p, std::vector<int>& dims, int* n, int* prec, int* batch);
+int bt_plan_shape(const bt_plan* p, int* n, int* repr, int* prec);
+int bt_plan_gate_dims(const bt_plan* p, const int64_t* idx, int count, size_t* reals);
+
+static Client* pick(bt_server* s, int lane) {
+  Client* best = nullptr;
+  for (auto& kv : s->clients) {
+    Client* c = kv.second;
+    if (c->queue.empty() || c->busy) continue;
+    if ((c->state || c->reserved) && c->lane != lane) continue;  // resident on another lane
+    if (!best || c->queue.front()->t_submit < best->queue.front()->t_submit) best = c;
+  }
+  return best;
+}
+
+// reserves HBM for c on `lane`, evicting idle residents LRU-first; false: wait
+static bool admit(bt_server* s, Client* c, int lane, std::vector<bt_state*>& to_free) {
+  if (c->footprint > s->budget) return false;
+  while (s->used + c->footprint > s->budget) {
+    Client* victim = nullptr;
+    for (auto& kv : s->clients) {
+      Client* o = kv.second;
+      if (o->state && !o->busy && (!victim || o->last_used < victim->last_used)) victim = o;
+    }
+    if (!victim) return false;
+    to_free.push_back(victim->state);
+    victim->state = nullptr;
+    victim->lane = -1;
+    s->used -= victim->footprint;
+  }
+  s->used += c->footprint;
+  c->reserved = true;
+  c->lane = lane;
+  return true;
+}
+
+static int run_request(bt_ctx* ctx, Client* c, Req* r, double* value) {
+  int rc = BT_OK;
+  if (c->plan) {
+    if (!r->idx.empty())
+      rc = bt_plan_set_matrices(c->plan, (int)r->idx.size(), r->idx.data(), r->mats.data());
+    if (!rc) rc = bt_state_set_zero(c->state, -1);
+    if (!rc) rc = bt_plan_run(c->plan, c->state, -1);
+  } else {
+    size_t off = 0;
+    for (size_t i = 0; i < r->idx.size() && !rc; ++i) {
+      const int64_t oi = r->idx[i];
+      const int d = oi >= 0 && oi < (int64_t)c->gate_dim.size() ? c->gate_dim[oi] : 0;
+      if (!d) return bt_fail(ctx, BT_ERR_BAD_ARG, "request names an op that is not a gate of the program");
+      rc = bt_program_set_gate(c->prog, oi, r->mats.data() + off);
+      off += (size_t)2 * d * d;
+    }
+    if (!rc) rc = bt_state_set_zero(c->state, -1);
+    if (!rc) rc = bt_program_run(c->prog, c->state, nullptr, r->seed, nullptr);
+  }
+  if (rc) return rc;
+  // <H> per member divided by the member's norm (trace), averaged over members
+  const int nt = (int)c->coef.size();
+  std::vector<double> ev((size_t)c->batch * nt), nrm(c->batch);
+  if (nt) rc = bt_expect_pauli(c->state, nt, c->x.data(), c->z.data(), c->coef.data(), -1, ev.data());
+  if (!rc) rc = bt_norm2(c->state, -1, nrm.data());
+  if (rc) return rc;
+  double acc = 0;
+  for (int m = 0; m < c->batch; ++m) {
+    double h = 0;
+    for (int t = 0; t < nt; ++t) h += ev[(size_t)m * nt + t];
+    acc += h / nrm[m];
+  }
+  *value = acc / c->batch;
+  return BT_OK;
+}
+
+static void worker(bt_server* s, int lane) {
+  bt_ctx* ctx = s->lanes[lane];
+  for (;;) {
+    Client* c = nullptr;
+    Req* r = nullptr;
+    std::vector<bt_state*> to_free;
+    bool alloc = false;
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      for (;;) {
+        if (s->stop) return;
+        c = pick(s, lane);
+        if (c && (c->state || c->reserved || admit(s, c, lane, to_free))) break;
+        c = nullptr;
+        s->cv.wait_for(lk, std::chrono::milliseconds(5));
+      }
+      c->busy = true;
+      alloc = c->state == nullptr;
+      r = c->queue.front();
+      c->queue.pop_front();
+    }
+    for (bt_state* st : to_free) bt_state_free(st);
+    int rc = BT_OK;
+    if (alloc) {
+      bt_state* st = nullptr;
+      rc = bt_state_alloc(ctx, c->n, c->repr, c->prec, c->batch, &st);
+      std::lock_guard<std::mutex> lk(s->mu);
+      c->reserved = false;
+      if (rc) {  // give the reservation back
+        s->used -= c->footprint;
+        c->lane = -1;
+      } else {
+        c->state = st;
+      }
+    }
+    r->t_start = now_s();
+    double v = 0;
+    if (!rc) rc = run_request(ctx, c, r, &v);
+    const double t = now_s();
+    std::lock_guard<std::mutex> lk(s->mu);
+    r->value = v;
+    r->status = rc;
+    if (rc) r->err = bt_last_error(nullptr);  // every failure also lands in this thread's message
+    r->t_done = t;
+    r->done = true;
+    c->busy = false;
+    c->last_used = t;
+    s->latencies.push_back(t - r->t_submit);
+    s->cv.notify_all();
+  }
+}
+
+static int add_client(bt_server* s, Client* c, int nterms, const uint64_t* x, const uint64_t* z, const double* coef,
+                      int64_t* id) {
+  if (nterms < 0 || (nterms > 0 && (!x || !z))) {
+    delete c;
+    return bt_fail(nullptr, BT_ERR_BAD_ARG, "bad Pauli term arrays");
+  }
+  c->x.assign(x, x + nterms);
+  c->z.assign(z, z + nterms);
+  c->coef.resize(nterms);
+  for (int t = 0; t < nterms; ++t) c->coef[t] = coef ? coef[t] : 1.0;
+  const size_t es = c->prec == BT_PREC_C64 ? 8 : 16;
+  c->footprint = ((size_t)1 << (c->repr == BT_REPR_DM ? 2 * c->n : c->n)) * es * c->batch;
+  std::lock_guard<std::mutex> lk(s->mu);
+  c->id = s->next_client++;
+  s->clients[c->id] = c;
+  if (id) *id = c->id;
+  return BT_OK;
+}
+
+extern "C" {
+
+int bt_serve_create(int device, int lanes, uint64_t seed, uint64_t hbm_budget, bt_server** out) {
+  if (!out || lanes < 1 || lanes > 64) return bt_fail(nullptr, BT_ERR_BAD_ARG, "need 1..64 lanes and an out pointer");
+  *out = nullptr;
+  bt_server* s = new bt_server();
+  s->device = device;
+  s->budget = hbm_budget ? hbm_budget : ((uint64_t)200 << 30);
+  for (int i = 0; i < lanes; ++i) {
+    bt_ctx* c = nullptr;
+    // one key for every lane: a request's draws depend on its seed, not on its lane
+    int rc = bt_ctx_create(device, seed, &c);
+    if (rc) {
+      for (bt_ctx* o : s->lanes) bt_ctx_destroy(o);
+      delete s;
+      return rc;
+    }
+    s->lanes.push_back(c);
+  }
+  for (int i = 0; i < lanes; ++i) s->threads.emplace_back(worker, s, i);
+  *out = s;
+  return BT_OK;
+}
+
+int bt_serve_destroy(bt_server* s) {
+  if (!s) return BT_OK;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+    s->cv.notify_all();
+  }
+  for (auto& t : s->threads) t.join();
+  for (auto& kv : s->clients) {
+    if (kv.second->state) bt_state_free(kv.second->state);
+    delete kv.second;
+  }
+  for (auto& kv : s->reqs) delete kv.second;  // queued requests are owned here
+  for (bt_ctx* c : s->lanes) bt_ctx_destroy(c);
+  delete s;
+  return BT_OK;
+}
+
+int bt_serve_add_plan_client(bt_server* s, bt_plan* plan, int nterms, const uint64_t* xmask, const uint64_t* zmask,
+                             const double* coef, int64_t* client) {
+  if (!s || !plan) return bt_fail(nullptr, BT_ERR_BAD_ARG, "NULL server or plan");
+  Client* c = new Client();
+  c->plan = plan;
+  int rc = bt_plan_shape(plan, &c->n, &c->repr, &c->prec);
+  if (rc) {
+    delete c;
+    return rc;
+  }
+  return add_client(s, c, nterms, xmask, zmask, coef, client);
+}
+
+int bt_serve_add_program_client(bt_server* s, bt_program* prog, int nterms, const uint64_t* xmask,
+                                const uint64_t* zmask, const double* coef, int64_t* client) {
+  if (!s || !prog) return bt_fail(nullptr, BT_ERR_BAD_ARG, "NULL server or program");
+  Client* c = new Client();
+  c->prog = prog;
+  c->repr = BT_REPR_SV;
+  int rc = bt_program_gate_dims(prog, c->gate_dim, &c->n, &c->prec, &c->batch);
+  if (rc) {
+    delete c;
+    return rc;
+  }
+  return add_client(s, c, nterms, xmask, zmask, coef, client);
+}
+
+int bt_serve_submit(bt_server* s, int64_t client, int count, const int64_t* index, const double* mats, uint64_t seed,
+                    int64_t* ticket) {
+  if (!s || !ticket) return bt_fail(nullptr, BT_ERR_BAD_ARG, "NULL server or ticket");
+  if (count < 0 || (count > 0 && (!index || !mats))) return bt_fail(nullptr, BT_ERR_BAD_ARG, "bad matrix update arrays");
+  Req* r = new Req();
+  r->client = client;
+  r->seed = seed;
+  r->idx.assign(index, index + count);
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->clients.find(client);
+  if (it == s->clients.end()) {
+    delete r;
+    return bt_fail(nullptr, BT_ERR_BAD_ARG, "unknown client");
+  }
+  Client* c = it->second;
+  if (c->footprint > s->budget) {
+    delete r;
+    return bt_fail(nullptr, BT_ERR_OOM, "the client's state is larger than the server's HBM budget");
+  }
+  // matrices back to back in each gate's size (the size each gate was added with)
+  size_t reals = 0;
+  if (c->plan) {
+    int rc = bt_plan_gate_dims(c->plan, r->idx.data(), count, &reals);
+    if (rc) {
+      delete r;
+      return rc;
+    }
+  } else {
+    for (int i = 0; i < count; ++i) {
+      const int64_t oi = index[i];
+      const int d = oi >= 0 && oi < (int64_t)c->gate_dim.size() ? c->gate_dim[oi] : 0;
+      if (!d) {
+        delete r;
+        return bt_fail(nullptr, BT_ERR_BAD_ARG, "index names an op that is not a gate of the program");
+      }
+      reals += (size_t)2 * d * d;
+    }
+  }
+  r->mats.assign(mats, mats + reals);
+  r->ticket = s->next_ticket++;
+  r->t_submit = now_s();
+  s->reqs[r->ticket] = r;
+  c->queue.push_back(r);
+  *ticket = r->ticket;
+  s->cv.notify_all();
+  return BT_OK;
+}
+
+int bt_serve_poll(bt_server* s, int64_t ticket, int64_t wait_ms, double* value, double* latency_s) {
+  if (!s) return bt_fail(nullptr, BT_ERR_BAD_ARG, "server is NULL");
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(ticket);
+  if (it == s->reqs.end()) return bt_fail(nullptr, BT_ERR_BAD_ARG, "unknown ticket");
+  Req* r = it->second;
+  if (!r->done && wait_ms != 0) {
+    auto pred = [&] { return r->done; };
+    if (wait_ms < 0) s->cv.wait(lk, pred);
+    else s->cv.wait_for(lk, std::chrono::milliseconds(wait_ms), pred);
+  }
+  if (!r->done) return BT_ERR_TIMEOUT;
+  if (value) *value = r->value;
+  if (latency_s) *latency_s = r->t_done - r->t_submit;
+  int st = r->status;
+  if (st) bt_fail(nullptr, st, r->err);
+  s->reqs.erase(it);
+  delete r;
+  return st;
+}
+
+int bt_serve_stats(bt_server* s, int64_t* completed, double* p50_s, double* p99_s, int64_t* resident,
+                   uint64_t* hbm_used) {
+  if (!s) return bt_fail(nullptr, BT_ERR_BAD_ARG, "server is NULL");
+  std::lock_guard<std::mutex> lk(s->mu);
+  std::vector<double> l = s->latencies;
+  std::sort(l.begin(), l.end());
+  auto pct = [&](double q) {
+    if (l.empty()) return 0.0;
+    const double pos = q * (double)(l.size() - 1);
+    const size_t i = (size_t)pos;
+    const double f = pos - (double)i;
+    return i + 1 < l.size() ? l[i] * (1 - f) + l[i + 1] * f : l[i];
+  };
+  if (completed) *completed = (int64_t)l.size();
+  if (p50_s) *p50_s = pct(0.50);
+  if (p99_s) *p99_s = pct(0.99);
+  int64_t res = 0;
+  for (auto& kv : s->clients) res += kv.second->state != nullptr;
+  if (resident) *resident = res;
+  if (hbm_used) *hbm_used = s->used;
+  return BT_OK;
+}
+
+}  // extern "C"

@@ -195,7 +195,8 @@ int bt_plan_run(bt_plan* p, bt_state* s, int64_t member);
  * skip (batch flags, or NULL) makes members pass over a channel or measurement
  * (their record slot reads -1).  Draw i of member m is uniforms[i*batch + m] when
  * uniforms is given to bt_program_run, else on-device Philox keyed by the ctx seed
- * and `seed`.  A branch or outcome of zero probability leaves that member as it
+ * and `seed` (the same pair gives the same draws).  A branch or outcome of zero
+ * probability leaves that member as it
  * was at that op (record -1) and the run reports BT_ERR_NO_BRANCH / BT_ERR_BAD_ARG
  * after every member has finished. */
 typedef struct bt_program bt_program;
@@ -212,6 +213,38 @@ int bt_program_set_gate(bt_program* p, int64_t op_index, const double* mats);
 /* runs on every member of s (n, prec and batch as created); records: batch x
  * nrecords int32, member-major (may be NULL) */
 int bt_program_run(bt_program* p, bt_state* s, const double* uniforms, uint64_t seed, int32_t* records);
+
+/* ----------------------------------------------------------------- serving */
+/* No counterpart in the reference: its VQE / Trotter loops (variational_apply +
+ * expect(state, H), src/vqa.jl:420-456, src/func.jl:100) run one call at a time.
+ * A server owns `lanes` contexts (CUDA streams) with one host thread each and
+ * serves clients: a client is a compiled plan (state vector or density matrix)
+ * or a program (a trajectory batch) plus a Pauli sum H; a request gives new
+ * matrices for some of its gates and returns <H> (per member divided by the
+ * member's norm, averaged over members).  Client states stay resident between
+ * requests; clients are admitted by HBM footprint (state bytes) within
+ * hbm_budget (0: 200 GiB), evicting idle residents least-recently-used first.
+ * A client's requests run in submission order, one at a time; requests of
+ * different clients run concurrently on free lanes.  Plans and programs are
+ * borrowed: keep them alive until the server is destroyed and do not use them
+ * elsewhere meanwhile. */
+typedef struct bt_server bt_server;
+int bt_serve_create(int device, int lanes, uint64_t seed, uint64_t hbm_budget, bt_server** out);
+int bt_serve_destroy(bt_server* s);
+int bt_serve_add_plan_client(bt_server* s, bt_plan* plan, int nterms, const uint64_t* xmask, const uint64_t* zmask,
+                             const double* coef, int64_t* client);
+int bt_serve_add_program_client(bt_server* s, bt_program* prog, int nterms, const uint64_t* xmask,
+                                const uint64_t* zmask, const double* coef, int64_t* client);
+/* index: plan add indices (as bt_plan_set_matrices) or program op indices (as
+ * bt_program_set_gate); mats back to back, column-major, each in its gate's size;
+ * seed keys the program's on-device draws */
+int bt_serve_submit(bt_server* s, int64_t client, int count, const int64_t* index, const double* mats, uint64_t seed,
+                    int64_t* ticket);
+/* waits up to wait_ms (-1: until done, 0: no wait); BT_ERR_TIMEOUT while pending.
+ * A finished ticket is released by the call that reports it. */
+int bt_serve_poll(bt_server* s, int64_t ticket, int64_t wait_ms, double* value, double* latency_s);
+int bt_serve_stats(bt_server* s, int64_t* completed, double* p50_s, double* p99_s, int64_t* resident,
+                   uint64_t* hbm_used);
 
 /* ---------------------------------------------------------------- sampling */
 /* sample(psi, shots) (src/ops.jl:46-62): per shot t = u*sum|psi|^2, outcome =

@@ -115,3 +115,76 @@ def test_admission_evicts_idle_clients(ctx):
             assert abs(match.value - req.value) <= 1e-6 * max(1.0, abs(req.value))
     finally:
         alone.close()
+
+
+def test_native_server_alone_equals_mix_and_python_server(ctx):
+    """The library's serving engine (bt_serve_*): each result is the same served
+    alone (one lane, one request at a time) and in the mix (4 lanes, all requests
+    queued at once), and plan clients agree with the Python server (same passes)."""
+    import bluetangle_gpu.serving as S
+    sp = specs(21)
+    alone = {}
+    srv = S.NativeServer(sp, lanes=1)
+    try:
+        for req in requests(sp, per_client=2, seed=23):
+            srv.submit(req)
+            srv.wait(req)
+            assert req.error is None, req.error
+            alone[req.rid] = req.value
+    finally:
+        srv.close()
+    srv = S.NativeServer(sp, lanes=4)
+    try:
+        reqs = requests(sp, per_client=2, seed=23)
+        for req in reqs:
+            srv.submit(req)
+        for req in reqs:
+            srv.wait(req)
+            assert req.error is None, req.error
+        st = srv.stats()
+        assert st["completed"] == len(reqs) and st["p99_s"] >= st["p50_s"] > 0
+    finally:
+        srv.close()
+    for req in reqs:
+        a = alone[req.rid]
+        assert abs(req.value - a) <= 1e-6 * max(1.0, abs(a)), (req.cid, req.value, a)
+    py = S.Server(sp, lanes=2)
+    try:
+        preqs = [r for r in requests(sp, per_client=2, seed=23) if sp[r.cid].kind != "traj"]
+        for req in preqs:
+            py.submit(req)
+        for req in preqs:
+            req.done.wait(120)
+            assert req.error is None, req.error
+            assert abs(req.value - alone[req.rid]) <= 1e-6 * max(1.0, abs(req.value)), (req.cid, req.value)
+    finally:
+        py.close()
+
+
+def test_native_server_admission_by_footprint(ctx):
+    """With room for about two clients, the engine evicts idle residents and every
+    request still completes with the value it has alone."""
+    import bluetangle_gpu.serving as S
+    sp = specs(29)
+    budget = max(s.footprint("c64") for s in sp) * 2
+    srv = S.NativeServer(sp, lanes=2, hbm_budget=budget)
+    try:
+        reqs = requests(sp, per_client=2, seed=31)
+        for req in reqs:
+            srv.submit(req)
+        for req in reqs:
+            srv.wait(req)
+            assert req.error is None, req.error
+        st = srv.stats()
+        assert st["hbm_used"] <= budget and st["resident"] <= len(sp)
+    finally:
+        srv.close()
+    one = S.NativeServer(sp, lanes=1)
+    try:
+        for req in requests(sp, per_client=2, seed=31):
+            one.submit(req)
+            one.wait(req)
+            match = [r for r in reqs if r.rid == req.rid][0]
+            assert abs(match.value - req.value) <= 1e-6 * max(1.0, abs(req.value))
+    finally:
+        one.close()

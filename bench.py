@@ -459,8 +459,19 @@ def run_serve(args):
     t = time.perf_counter()
     plain_vals = [S.plain_request(specs[r.cid], r.theta, r.seed, pctx, prec="c128") for r in sample]
     plain_rate = len(sample) / (time.perf_counter() - t)
-    dev = max(abs(r.value - v) / max(1e-12, sum(abs(x[0]) for x in specs[r.cid].terms))
-              for r, v in zip(sample, plain_vals))
+    def rel(r, v):
+        return abs(r.value - v) / max(1e-12, sum(abs(x[0]) for x in specs[r.cid].terms))
+
+    if native:
+        # trajectory clients drew on the device (Philox keyed by the request seed):
+        # check them against complex128 runs with the same draws
+        dev = max([rel(r, v) for r, v in zip(sample, plain_vals) if specs[r.cid].kind != "traj"] or [0.0])
+        dctx = bt.Context(0, seed=1234)  # the engine's key (NativeServer's seed)
+        dev = max([dev] + [rel(r, S.program_request(specs[r.cid], r.theta, r.seed, dctx))
+                           for r in sample if specs[r.cid].kind == "traj"])
+        dctx.close()
+    else:
+        dev = max(rel(r, v) for r, v in zip(sample, plain_vals))
     # state infidelity of the served precision (c64 fused plan) against c128 for the sv clients
     infid = 0.0
     for c in [c for c in specs if c.kind == "sv"][:6]:

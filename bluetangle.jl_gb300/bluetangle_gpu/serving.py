@@ -411,6 +411,21 @@ class NativeServer:
         self.ctx.close()
 
 
+def program_request(spec, theta, seed, ctx, prec="c128"):
+    """A trajectory client's request as one program run with the on-device draws
+    of `seed` under ctx's seed: the same draws as the serving engine makes when
+    its seed equals ctx's (for checking a served complex64 value in complex128)."""
+    from . import trajectories as T
+    ops = _noisy(spec, hea_ops(spec.n, spec.depth, theta))
+    slots = T.build_slots(T.member_programs([ops], spec.n, spec.ntraj))
+    prog, _ = T.compile_program(slots, spec.n, spec.ntraj, prec, ctx)
+    st = GPUState(spec.n, prec, spec.ntraj, ctx)
+    prog.run(st, seed=seed, records=False)
+    v = _expect_h(st, spec.terms, -1)
+    st.free()
+    return v
+
+
 def plain_request(spec, theta, seed, ctx, prec="c128"):
     """The plain per-call path: fresh state, one sweep per gate (and one call per
     channel), <H> at the end; the comparison point of the serving engine."""

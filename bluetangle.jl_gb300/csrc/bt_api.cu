@@ -717,9 +717,57 @@ int bt_expect_pauli(const bt_state* s_, int nterms, const uint64_t* xmask, const
   if (rc) return rc;
   if (nterms == 0) return BT_OK;
   if ((rc = set_dev(ctx))) return rc;
-  // group terms by xmask; one read pass per group of <= 8 terms
   std::map<uint64_t, std::vector<int>> groups;
   for (int t = 0; t < nterms; ++t) groups[xmask[t]].push_back(t);
+  if (s->repr == BT_REPR_SV && s->nbits >= 8 && groups.size() >= 3) {
+    // many x-masks: tiles of M bits holding the x-bits of up to
+    // BT_PAULI_TILE_TERMS strings each, one read of the state per tile group
+    const int c = s->prec == BT_PREC_C64 ? 5 : 4;
+    const int M = std::min(s->prec == BT_PREC_C64 ? 13 : 12, s->nbits);
+    std::vector<int> order;
+    for (auto& g : groups)
+      for (int t : g.second) order.push_back(t);  // equal x-masks adjacent: they share products
+    std::vector<std::pair<uint64_t, std::vector<int>>> tg;  // (tile mask, terms)
+    std::vector<char> used(nterms, 0);
+    for (size_t start = 0; start < order.size();) {
+      uint64_t Q = (1ULL << c) - 1;
+      std::vector<int> ts;
+      for (size_t k = start; k < order.size() && (int)ts.size() < BT_PAULI_TILE_TERMS; ++k) {
+        const int t = order[k];
+        if (used[t] || __builtin_popcountll(Q | xmask[t]) > M) continue;
+        Q |= xmask[t];
+        ts.push_back(t);
+        used[t] = 1;
+      }
+      for (int b = 0; b < s->nbits && __builtin_popcountll(Q) < M; ++b) Q |= 1ULL << b;
+      tg.push_back({Q, ts});
+      while (start < order.size() && used[order[start]]) ++start;
+    }
+    Carve cv;
+    const int W = BT_PAULI_TILE_TERMS;
+    int iR = cv.add(tg.size() * nm * W * sizeof(double));
+    if ((rc = cv.commit(ctx))) return rc;
+    double* res = cv.at<double>(iR);
+    for (size_t gi = 0; gi < tg.size() && !rc; ++gi) {
+      uint64_t xs[BT_PAULI_TILE_TERMS], zs[BT_PAULI_TILE_TERMS];
+      const auto& ts = tg[gi].second;
+      for (size_t j = 0; j < ts.size(); ++j) xs[j] = xmask[ts[j]], zs[j] = zmask[ts[j]];
+      rc = bt_launch_pauli_tile(s, M, tg[gi].first, (int)ts.size(), xs, zs, lo, nm, res + gi * nm * W);
+    }
+    if (rc) return rc;
+    std::vector<double> h(tg.size() * nm * W);
+    rc = bt_cuda_check(ctx, cudaMemcpyAsync(h.data(), res, h.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "expect download");
+    if (!rc) rc = bt_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "expect sync");
+    if (rc) return rc;
+    for (size_t gi = 0; gi < tg.size(); ++gi) {
+      const auto& ts = tg[gi].second;
+      for (int64_t m = 0; m < nm; ++m)
+        for (size_t j = 0; j < ts.size(); ++j)
+          out[m * nterms + ts[j]] = (coef ? coef[ts[j]] : 1.0) * h[(gi * nm + m) * W + j];
+    }
+    return BT_OK;
+  }
+  // few x-masks: one read pass per group of <= 8 strings sharing an x-mask
   std::vector<std::pair<uint64_t, std::vector<int>>> batches;
   for (auto& g : groups)
     for (size_t i = 0; i < g.second.size(); i += 8)
@@ -813,15 +861,12 @@ int bt_norm2(const bt_state* s_, int64_t member, double* out) {
   if (rc) return rc;
   if ((rc = set_dev(ctx))) return rc;
   Carve cv;
-  int iR = cv.add(nm * 36 * sizeof(double));
+  int iR = cv.add(nm * sizeof(double));
   if ((rc = cv.commit(ctx))) return rc;
-  if ((rc = bt_launch_bitsums(s, lo, nm, cv.at<double>(iR)))) return rc;
-  std::vector<double> h(nm * 36);
-  rc = bt_cuda_check(ctx, cudaMemcpyAsync(h.data(), cv.at<double>(iR), h.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "norm download");
+  if ((rc = bt_launch_norm2(s, lo, nm, cv.at<double>(iR)))) return rc;
+  rc = bt_cuda_check(ctx, cudaMemcpyAsync(out, cv.at<double>(iR), nm * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "norm download");
   if (!rc) rc = bt_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "norm sync");
-  if (rc) return rc;
-  for (int64_t m = 0; m < nm; ++m) out[m] = h[m * 36];
-  return BT_OK;
+  return rc;
 }
 
 int bt_fidelity(const bt_state* a_, int64_t am, const bt_state* b_, int64_t bm, double* out) {

@@ -109,9 +109,17 @@ int bt_launch_rdm(bt_state* s, int k, const int* bits, int64_t mem_lo, int64_t n
 // Pauli terms sharing one xmask (<= 8 zmasks): out[mem][T] = Re <P_t>
 int bt_launch_pauli(bt_state* s, uint64_t x, int T, const uint64_t* z, int64_t mem_lo, int64_t nmem,
                     double* out);
+// up to BT_PAULI_TILE_TERMS strings whose x-masks lie inside one tile of M bits
+// (tilemask, containing the lowest 5 (c64) / 4 (c128) bits), state vectors only:
+// out[mem][BT_PAULI_TILE_TERMS], term t at index t
+#define BT_PAULI_TILE_TERMS 24
+int bt_launch_pauli_tile(bt_state* s, int M, uint64_t tilemask, int T, const uint64_t* x, const uint64_t* z,
+                         int64_t mem_lo, int64_t nmem, double* out);
 // per-bit weights: out[mem][0] = sum p, out[mem][1 + b] = sum_{bit b set} p (SV: p=|a|^2,
 // DM: p = Re rho[i,i]); b over the n system bits
 int bt_launch_bitsums(bt_state* s, int64_t mem_lo, int64_t nmem, double* out);
+// out[mem] = sum |psi|^2 (state) or Re tr(rho) (density), FP64-accurate for every precision
+int bt_launch_norm2(bt_state* s, int64_t mem_lo, int64_t nmem, double* out);
 // out[mem][0..1] = <a_mem | b_mem'> (complex), one member each
 int bt_launch_inner(bt_state* a, int64_t am, bt_state* b, int64_t bm, double* out);
 // Re <psi| M |psi> for k <= 2 with controls

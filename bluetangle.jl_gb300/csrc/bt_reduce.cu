@@ -8,6 +8,10 @@
 // (BlueTangle.jl src/linalg.jl:83-230), Born probabilities
 // (src/hilbert.jl:682-696), Kraus branch probabilities (src/struct.jl:9-29)
 // and observables (src/func.jl:91-147).
+#include <string.h>
+
+#include <algorithm>
+
 #include "bt_internal.cuh"
 
 #define FULL 0xffffffffu
@@ -394,6 +398,155 @@ int bt_launch_pauli(bt_state* s, uint64_t x, int T, const uint64_t* z, int64_t m
   return finalize(ctx, part, nblk, 8, nmem, out);
 }
 
+// ------------------------------------------------------------ Pauli strings, tiled
+// Many Pauli strings from one read of the state: a CTA stages a tile of 2^M
+// amplitudes (the M tile bits contain the x-mask bits of every string of the
+// group and the lowest c bits, so the tile is 2^(M-c) contiguous runs) in shared
+// memory, and for each amplitude i of the tile adds
+//   Re( phase_t(i) * psi_i * conj(psi_{i ^ x_t}) ),  P_t|i> = phase_t(i)|i ^ x_t>,
+// phase_t(i) = i^{|x_t & z_t|} (-1)^{|i & z_t|}, for every string t of the group;
+// i ^ x_t lies in the same tile.  Strings sharing an x-mask share the product.
+// Sums as in k_pauli: 8-element FP32 micro-sums for complex64, FP64 beyond.
+struct PauliTileArgs {
+  int nbits, M, c, T, lg_tiles;
+  int tbits[16];   // tile bit -> global bit, ascending; tbits[i] = i for i < c
+  uint64_t z[BT_PAULI_TILE_TERMS];
+  uint32_t xl[BT_PAULI_TILE_TERMS];  // x-mask in tile-local bits
+  int ny[BT_PAULI_TILE_TERMS];       // |x & z| mod 4
+};
+
+template <typename R>
+__global__ void __launch_bounds__(BT_THREADS) k_pauli_tile(const typename CT<R>::T* __restrict__ psi,
+                                                           const PauliTileArgs a, int64_t mem_lo, int nblk,
+                                                           double* __restrict__ part) {
+  typedef typename CT<R>::T C2;
+  typedef typename Micro<R>::T A;
+  constexpr int NT = BT_PAULI_TILE_TERMS;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C2* tile = reinterpret_cast<C2*>(smem_raw);
+  int64_t* runoff = reinterpret_cast<int64_t*>(smem_raw + (sizeof(C2) << a.M));
+  const int M = a.M, c = a.c, cmask = (1 << c) - 1;
+  const int nruns = 1 << (M - c);
+  for (int r = threadIdx.x; r < nruns; r += blockDim.x) {
+    int64_t o = 0;
+    for (int b = 0; b < M - c; ++b)
+      if ((r >> b) & 1) o |= 1LL << a.tbits[c + b];
+    runoff[r] = o;
+  }
+  double acc[NT];
+  A f[NT];
+#pragma unroll
+  for (int t = 0; t < NT; ++t) acc[t] = 0, f[t] = 0;
+  const int64_t mem = mem_lo + blockIdx.y;
+  const C2* s = psi + (mem << a.nbits);
+  const int64_t ntiles = 1LL << a.lg_tiles;
+  const int E = (1 << M) / blockDim.x;  // elements per thread per tile (M >= 8)
+  int cnt = 0;
+  for (int64_t tid = blockIdx.x; tid < ntiles; tid += nblk) {
+    uint64_t base = (uint64_t)tid;
+    for (int i = 0; i < M; ++i) {
+      const int p = a.tbits[i];
+      base = ((base >> p) << (p + 1)) | (base & ((1ULL << p) - 1));
+    }
+    __syncthreads();  // the previous tile is no longer read
+    for (int k = 0; k < E; ++k) {
+      const int l = threadIdx.x + k * blockDim.x;
+      tile[l] = s[base + runoff[l >> c] + (l & cmask)];
+    }
+    __syncthreads();
+    for (int k = 0; k < E; ++k) {
+      const int l = threadIdx.x + k * blockDim.x;
+      const uint64_t gi = base + runoff[l >> c] + (l & cmask);
+      const C2 v = tile[l];
+      const A vr = (A)v.x, vi = (A)v.y;
+      uint32_t lastx = 0xffffffffu;
+      A cr = 0, ci = 0;
+#pragma unroll
+      for (int t = 0; t < NT; ++t) {
+        if (t < a.T) {
+          if (a.xl[t] != lastx) {  // psi_i * conj(psi_{i^x})
+            lastx = a.xl[t];
+            const C2 w = tile[l ^ lastx];
+            cr = vr * (A)w.x + vi * (A)w.y;
+            ci = vi * (A)w.x - vr * (A)w.y;
+          }
+          const int ny = a.ny[t];
+          A val = (ny & 1) ? ci : cr;  // Re(i^ny c): cr, -ci, -cr, ci
+          if (ny == 1 || ny == 2) val = -val;
+          f[t] += (__popcll(gi & a.z[t]) & 1) ? -val : val;
+        }
+      }
+      if (++cnt == Micro<R>::J) {
+#pragma unroll
+        for (int t = 0; t < NT; ++t) acc[t] += (double)f[t], f[t] = 0;
+        cnt = 0;
+      }
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < NT; ++t) acc[t] += (double)f[t];
+  __syncthreads();
+  block_sum_store<NT>(acc, part + ((int64_t)blockIdx.y * nblk + blockIdx.x) * NT, NT);
+}
+
+int bt_launch_pauli_tile(bt_state* s, int M, uint64_t tilemask, int T, const uint64_t* x, const uint64_t* z,
+                         int64_t mem_lo, int64_t nmem, double* out) {
+  bt_ctx* ctx = s->ctx;
+  if (T < 1 || T > BT_PAULI_TILE_TERMS) return bt_fail(ctx, BT_ERR_BAD_ARG, "bad tiled Pauli group");
+  if (nmem > 65535) return bt_fail(ctx, BT_ERR_UNSUPPORTED, "at most 65535 members per reduction");
+  PauliTileArgs a;
+  memset(&a, 0, sizeof(a));
+  a.nbits = s->nbits;
+  a.M = M;
+  a.c = s->prec == BT_PREC_C64 ? 5 : 4;
+  a.T = T;
+  a.lg_tiles = s->nbits - M;
+  int local[64], nb = 0;
+  for (int b = 0; b < s->nbits; ++b) {
+    local[b] = -1;
+    if ((tilemask >> b) & 1) {
+      a.tbits[nb] = b;
+      local[b] = nb++;
+    }
+  }
+  if (nb != M || M < 8 || M > 13 || (tilemask & ((1ULL << a.c) - 1)) != ((1ULL << a.c) - 1))
+    return bt_fail(ctx, BT_ERR_BAD_ARG, "bad tile for Pauli strings");
+  for (int t = 0; t < T; ++t) {
+    uint32_t xl = 0;
+    for (int b = 0; b < s->nbits; ++b)
+      if ((x[t] >> b) & 1) {
+        if (local[b] < 0) return bt_fail(ctx, BT_ERR_BAD_ARG, "Pauli x-mask outside the tile");
+        xl |= 1u << local[b];
+      }
+    a.xl[t] = xl;
+    a.z[t] = z[t];
+    a.ny[t] = __builtin_popcountll(x[t] & z[t]) & 3;
+  }
+  const int64_t ntiles = 1LL << a.lg_tiles;
+  const int nblk = (int)std::min<int64_t>(ntiles, std::max<int64_t>(1, (ctx->sm_count * 2 + nmem - 1) / nmem));
+  double* part;
+  int rc = bt_work(ctx, sizeof(double) * (size_t)nmem * nblk * BT_PAULI_TILE_TERMS, &part);
+  if (rc) return rc;
+  const size_t esz = elem_bytes(s->prec);
+  const size_t smem = (esz << M) + sizeof(int64_t) * (1 << (M - a.c));
+  dim3 grid(nblk, (unsigned)nmem);
+  cudaError_t e;
+  if (s->prec == BT_PREC_C64) {
+    e = cudaFuncSetAttribute(k_pauli_tile<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      k_pauli_tile<float><<<grid, BT_THREADS, smem, ctx->stream>>>((const float2*)s->d, a, mem_lo, nblk, part);
+  } else {
+    e = cudaFuncSetAttribute(k_pauli_tile<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      k_pauli_tile<double><<<grid, BT_THREADS, smem, ctx->stream>>>((const double2*)s->d, a, mem_lo, nblk, part);
+  }
+  if ((rc = bt_cuda_check(ctx, e, "pauli tile attribute"))) return rc;
+  ctx->launches++;
+  rc = bt_cuda_check(ctx, cudaGetLastError(), "pauli tile launch");
+  if (rc) return rc;
+  return finalize(ctx, part, nblk, BT_PAULI_TILE_TERMS, nmem, out);
+}
+
 // ------------------------------------------------------------ per-bit sums
 // out[mem][0] = total weight, out[mem][1+b] = weight with bit b set (b < nsys).
 // A warp walks chunks of 1024 consecutive amplitudes, lane l taking entries
@@ -465,6 +618,79 @@ __global__ void __launch_bounds__(BT_THREADS) k_bitsums(const typename CT<R>::T*
     }
   }
   block_sum_store<BS_W>(acc, part + ((int64_t)blockIdx.y * nblk + blockIdx.x) * BS_W, BS_W);
+}
+
+// ------------------------------------------------------------ norms
+// sum |psi|^2 (state) or Re tr(rho) (density matrix) per member.  complex64:
+// every square is split exactly (TwoProduct: p = a*a, e = fma(a, a, -p)) and the
+// terms of a thread's 8-term groups are added with TwoSum into a float-float
+// (hi, lo) pair, so a group carries ~44 significant bits at FP32 issue rate;
+// groups, threads and blocks then sum in FP64.  complex128: FP64 throughout.
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+  const float s = hi + x, bb = s - hi;
+  lo += (hi - (s - bb)) + (x - bb);
+  hi = s;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(BT_THREADS) k_norm2(const typename CT<R>::T* __restrict__ psi, int nbits, int nsys,
+                                                      int dm, int64_t mem_lo, int nblk, double* __restrict__ part) {
+  double acc[1] = {0};
+  const int64_t mem = mem_lo + blockIdx.y;
+  const typename CT<R>::T* s = psi + (mem << nbits);
+  const int64_t n = dm ? (1LL << nsys) : (1LL << nbits);
+  const int64_t stride = (int64_t)nblk * blockDim.x;
+  constexpr int J = 8;
+  for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += stride * J) {
+    if constexpr (sizeof(R) == 4) {
+      float hi = 0, lo = 0;
+#pragma unroll
+      for (int jj = 0; jj < J; ++jj) {
+        const int64_t i = i0 + jj * stride;
+        if (i >= n) break;
+        const typename CT<R>::T v = dm ? s[(uint64_t)i + ((uint64_t)i << nsys)] : s[i];
+        if (dm) {
+          two_sum_acc(hi, lo, v.x);
+        } else {
+          const float p1 = v.x * v.x, e1 = fmaf(v.x, v.x, -p1);
+          const float p2 = v.y * v.y, e2 = fmaf(v.y, v.y, -p2);
+          two_sum_acc(hi, lo, p1);
+          two_sum_acc(hi, lo, p2);
+          lo += e1 + e2;
+        }
+      }
+      acc[0] += (double)hi + (double)lo;
+    } else {
+#pragma unroll
+      for (int jj = 0; jj < J; ++jj) {
+        const int64_t i = i0 + jj * stride;
+        if (i >= n) break;
+        const typename CT<R>::T v = dm ? s[(uint64_t)i + ((uint64_t)i << nsys)] : s[i];
+        acc[0] += dm ? (double)v.x : (double)v.x * v.x + (double)v.y * v.y;
+      }
+    }
+  }
+  block_sum_store<1>(acc, part + ((int64_t)blockIdx.y * nblk + blockIdx.x), 1);
+}
+
+int bt_launch_norm2(bt_state* s, int64_t mem_lo, int64_t nmem, double* out) {
+  bt_ctx* ctx = s->ctx;
+  if (nmem > 65535) return bt_fail(ctx, BT_ERR_UNSUPPORTED, "at most 65535 members per reduction");
+  const int dm = s->repr == BT_REPR_DM;
+  const int64_t units = dm ? (1LL << s->n) : (1LL << s->nbits);
+  const int nblk = blocks_per_member(ctx, units, nmem);
+  double* part;
+  int rc = bt_work(ctx, sizeof(double) * (size_t)nmem * nblk, &part);
+  if (rc) return rc;
+  dim3 grid(nblk, (unsigned)nmem);
+  if (s->prec == BT_PREC_C64)
+    k_norm2<float><<<grid, BT_THREADS, 0, ctx->stream>>>((const float2*)s->d, s->nbits, s->n, dm, mem_lo, nblk, part);
+  else
+    k_norm2<double><<<grid, BT_THREADS, 0, ctx->stream>>>((const double2*)s->d, s->nbits, s->n, dm, mem_lo, nblk, part);
+  ctx->launches++;
+  rc = bt_cuda_check(ctx, cudaGetLastError(), "norm2 launch");
+  if (rc) return rc;
+  return finalize(ctx, part, nblk, 1, nmem, out);
 }
 
 int bt_launch_bitsums(bt_state* s, int64_t mem_lo, int64_t nmem, double* out) {

@@ -12,6 +12,8 @@
 // write of the state however many gates it holds; it replaces that many separate
 // sweeps (each an HBM round trip) of the reference's per-gate operator products
 // (BlueTangle.jl src/hilbert.jl:505, :517-553).
+#include <atomic>
+
 #include "bt_fused.cuh"
 
 template <typename R>
@@ -444,12 +446,14 @@ template <typename R, int M, int NB>
 static int launch_fused(bt_ctx* ctx, void* psi, const FusedArgs<R>& a) {
   typedef typename CT<R>::T C2;
   const size_t smem = (sizeof(C2) << M) + sizeof(int64_t) * (1 << (M - a.c));
-  static bool attr_set[64] = {false};
-  if (ctx->device < 64 && !attr_set[ctx->device]) {
+  // one value per kernel (its largest tile), set once per device; contexts on
+  // other threads may launch meanwhile
+  static std::atomic<bool> attr_set[64] = {};
+  if (ctx->device < 64 && !attr_set[ctx->device].load()) {
     cudaError_t e = cudaFuncSetAttribute(k_fused<R, M, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)((sizeof(C2) << M) + 8 * (1 << M)));
     if (e != cudaSuccess) return bt_cuda_check(ctx, e, "fused smem attribute");
-    attr_set[ctx->device] = true;
+    attr_set[ctx->device].store(true);
   }
   int64_t total = (1LL << a.lg_tiles) * a.nmem;
   int64_t grid = (int64_t)ctx->sm_count * 2 * 4;

@@ -11,6 +11,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "bt_internal.cuh"
 
@@ -530,17 +531,23 @@ int bt_launch_pauli_tile(bt_state* s, int M, uint64_t tilemask, int T, const uin
   const size_t esz = elem_bytes(s->prec);
   const size_t smem = (esz << M) + sizeof(int64_t) * (1 << (M - a.c));
   dim3 grid(nblk, (unsigned)nmem);
-  cudaError_t e;
-  if (s->prec == BT_PREC_C64) {
-    e = cudaFuncSetAttribute(k_pauli_tile<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess)
-      k_pauli_tile<float><<<grid, BT_THREADS, smem, ctx->stream>>>((const float2*)s->d, a, mem_lo, nblk, part);
-  } else {
-    e = cudaFuncSetAttribute(k_pauli_tile<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess)
-      k_pauli_tile<double><<<grid, BT_THREADS, smem, ctx->stream>>>((const double2*)s->d, a, mem_lo, nblk, part);
+  // the largest tile of either precision (2^13 x 8 B or 2^12 x 16 B, plus 256 run
+  // offsets), set once per device: a per-launch setting would race between
+  // contexts launching concurrently from different threads
+  const int kMaxSmem = (1 << 16) + 8 * 256;
+  static std::atomic<bool> attr[2][64] = {};
+  const bool f = s->prec == BT_PREC_C64;
+  std::atomic<bool>& done = attr[f][ctx->device & 63];
+  if (!done.load()) {
+    cudaError_t e = f ? cudaFuncSetAttribute(k_pauli_tile<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem)
+                      : cudaFuncSetAttribute(k_pauli_tile<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
+    if ((rc = bt_cuda_check(ctx, e, "pauli tile attribute"))) return rc;
+    done.store(true);
   }
-  if ((rc = bt_cuda_check(ctx, e, "pauli tile attribute"))) return rc;
+  if (f)
+    k_pauli_tile<float><<<grid, BT_THREADS, smem, ctx->stream>>>((const float2*)s->d, a, mem_lo, nblk, part);
+  else
+    k_pauli_tile<double><<<grid, BT_THREADS, smem, ctx->stream>>>((const double2*)s->d, a, mem_lo, nblk, part);
   ctx->launches++;
   rc = bt_cuda_check(ctx, cudaGetLastError(), "pauli tile launch");
   if (rc) return rc;

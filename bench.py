@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--c3-n", type=int, default=20)
     ap.add_argument("--c3-members", type=int, default=4096)
     ap.add_argument("--c3-twirl", type=int, default=64, help="twirl instances (x3 ZNE scales)")
+    ap.add_argument("--c3-engine", default="program", choices=["program", "slots"])
     ap.add_argument("--rate", type=float, default=2000.0, help="serving: Poisson arrival rate (req/s)")
     ap.add_argument("--lanes", type=int, default=8, help="serving: concurrent lanes (contexts/streams)")
     ap.add_argument("--python-server", action="store_true",
@@ -772,12 +773,22 @@ def run_c3(args):
     def member_ops(slots):
         return sum(sum(1 for it in s.items if it is not None) for s in slots)
 
+    progs = progs_c = None
+    if args.c3_engine == "program":
+        # each step's slots compiled into a program (grouped executor: the members
+        # exceed shared memory), built before the timed region like the slots
+        progs = [T.compile_program(sl, n, B, "c64", ctx)[0] for sl in pre]
+        progs_c = [T.compile_program(sl, n, ncopy, "c64", ctx)[0] for sl in pre_c]
+
     def step(i):
+        if progs is not None:
+            progs[i].run(st, seed=1000 + i, records=False)
+            if cp is not None:
+                progs_c[i].run(cp, seed=5000 + i, records=False)
+            return
         T.run_slots(st, pre[i], records=False)
-        counts["ops"] += member_ops(pre[i])
         if cp is not None:
             T.run_slots(cp, pre_c[i], records=False)
-            counts["ops"] += member_ops(pre_c[i])
 
     ms, host, launches, clk = _timed(ctx, step, args.steps, args.warmup)
     timed_ops = sum(member_ops(pre[i]) + (member_ops(pre_c[i]) if pre_c else 0)
@@ -790,6 +801,9 @@ def run_c3(args):
     nch = sum(1 for s in base if s.kind == "channel")
     nad = sum(1 for op in step_ops if isinstance(op, bt.OpQC) and op.name == "amplitude_damping")
     bytes_step = ngates * 2 * S + nch * 2 * S + nad * S + n * (S + 2 * S)
+    if progs is not None:  # what the grouped executor moves (per group: reduction read + apply)
+        bytes_step = float(np.mean([T.grouped_bytes(pre[i], n, B, "c64")
+                                    for i in range(args.warmup, args.warmup + args.steps)]))
     zs = bt.expect(st, "Z", member=-1)
     assert np.all(np.isfinite(zs))
     cpu = None
@@ -827,7 +841,9 @@ def run_c3(args):
             "config": {"workload": f"tfim-{n}q-{B}traj+{ncopy}twirl/zne-copies", "members": B + ncopy,
                        "step": "one Trotter step of every member (40 make the circuit)",
                        "ops_per_member_step": len(step_ops), "l2": f"states ({(B + ncopy) * 2 ** n * 8 / 2**30:.1f} GiB) larger than L2",
-                       "engine": "lock-step slots (one launch sequence per op over the batch)"},
+                       "engine": ("programs, grouped executor (ops within two qubits decided from one reduced "
+                                  "matrix and applied in one pass)") if progs is not None else
+                                 "lock-step slots (one launch sequence per op over the batch)"},
             "trajectory_steps_per_s": (B + ncopy) * args.steps / (ms / 1e3),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind, "traffic": None,

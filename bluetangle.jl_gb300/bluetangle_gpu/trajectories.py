@@ -191,13 +191,17 @@ def run_slots(state, slots, rng=None, records=True):
     return recs
 
 
-PROGRAM_MAX_N = {"c64": 14, "c128": 13, "complex64": 14, "complex128": 13}
+PROGRAM_MAX_N = 34          # any state the GPU holds
+SHARED_MAX_N = {"c64": 14, "c128": 13, "complex64": 14, "complex128": 13}  # one member per CTA
+EXECUTORS = {"auto": 0, "shared": 1, "grouped": 2}
 
 
 class Program:
-    """A noisy circuit run whole on the GPU, one CTA per member, the member in
-    shared memory (bt_program): every gate, Kraus branch and measurement of a
-    trajectory batch in one launch.  Built from lock-step slots by
+    """A noisy circuit run on every member of a batched state (bt_program): for
+    members of n <= 14 (complex64) / 13 (complex128) qubits one CTA per member in
+    shared memory runs every gate, Kraus branch and measurement in one launch;
+    larger members run group by group (ops within two qubits decided together
+    from one reduced matrix, applied in one pass).  Built from lock-step slots by
     compile_program; run() fills the records of the measurements."""
 
     def __init__(self, n, batch, prec="c64", ctx=None):
@@ -226,6 +230,11 @@ class Program:
         self.ctx.check(L.lib().bt_program_add_gate(self.h, len(q), _ptr(q), _ptr(buf), int(per)))
         self.nops += 1
         return self.nops - 1
+
+    def set_executor(self, name):
+        """"auto", "shared" (one CTA per member) or "grouped"."""
+        self.ctx.check(L.lib().bt_program_set_executor(self.h, EXECUTORS[name]))
+        return self
 
     def set_gate(self, index, mats):
         per = isinstance(mats, (list, tuple))
@@ -284,8 +293,47 @@ def _ctrl_matrix(mat):
     return M
 
 
+def grouped_bytes(slots, n, batch, prec="c64"):
+    """HBM bytes the grouped executor moves for these slots: it groups consecutive
+    ops within two qubits as bt_program does; per group every member that acts in
+    it is read once for the reduced matrix (when a decision needs it) and read and
+    written once by the apply pass.  (Measurement rotations of MX/MY are not
+    counted.)"""
+    member = (2 ** n) * (8 if prec in ("c64", "complex64") else 16)
+    total = 0.0
+    q, need, act = [], False, np.zeros(batch, dtype=bool)
+
+    def close():
+        nonlocal total
+        if q:
+            total += act.sum() * member * (3 if need else 2)
+
+    for sl in slots:
+        live = [it for it in sl.items if it is not None]
+        if not live:
+            continue
+        if sl.kind == "gate":
+            qs = list(live[0][1]) + list(live[0][2])
+        elif sl.kind == "channel":
+            qs = list(live[0][1])
+        else:
+            qs = [live[0][1]]
+        if len(set(q) | set(qs)) > 2:
+            close()
+            q, need, act = [], False, np.zeros(batch, dtype=bool)
+        q = sorted(set(q) | set(qs))
+        if sl.kind == "gate":
+            act[:] = True
+        else:
+            act |= np.array([it is not None for it in sl.items])
+            if sl.kind == "measure" or not _unitary_mix(live[0][0]):
+                need = True
+    close()
+    return total
+
+
 def program_supported(slots, n, prec):
-    if n < 2 or n > PROGRAM_MAX_N.get(prec, 0):
+    if n < 2 or n > PROGRAM_MAX_N:
         return False
     for sl in slots:
         live = [it for it in sl.items if it is not None]

@@ -25,6 +25,7 @@ struct GateArgs {
   int64_t member_lo, nmem;
   const R* per_member;           // optional [member][2*D*D]
   int64_t pm_stride;
+  const int8_t* active;          // optional [member]: 0 = leave the member untouched
 };
 
 template <typename R, int V> struct VecIO;
@@ -75,6 +76,7 @@ __global__ void __launch_bounds__(BT_THREADS) k_gate(typename CT<R>::T* __restri
       base = ((base >> p) << (p + 1)) | (base & ((1ULL << p) - 1));
     }
     if ((base & a.cmask) != a.cmask) continue;
+    if (a.active && !a.active[mem]) continue;
     C2* s = psi + (mem << a.nbits) + base;
     const R* m = a.per_member ? a.per_member + mem * a.pm_stride : a.m;
     R xr[D][V], xi[D][V];
@@ -101,7 +103,7 @@ __global__ void __launch_bounds__(BT_THREADS) k_gate(typename CT<R>::T* __restri
 
 template <typename R, int K, int V>
 static int launch_t(bt_state* s, const int* bits, const double* m, uint64_t cmask, int64_t mem_lo,
-                    int64_t nmem, const void* per_member, int64_t pm_stride) {
+                    int64_t nmem, const void* per_member, int64_t pm_stride, const int8_t* active) {
   constexpr int D = 1 << K;
   GateArgs<R, K> a;
   for (int i = 0; i < 2 * D * D; ++i) a.m[i] = m ? (R)m[i] : (R)0;
@@ -117,6 +119,7 @@ static int launch_t(bt_state* s, const int* bits, const double* m, uint64_t cmas
   a.nmem = nmem;
   a.per_member = (const R*)per_member;
   a.pm_stride = pm_stride;
+  a.active = active;
   int64_t work = (1LL << a.lg_per) * nmem;
   int grid = bt_grid(s->ctx, work, BT_THREADS, 32);
   k_gate<R, K, V><<<grid, BT_THREADS, 0, s->ctx->stream>>>((typename CT<R>::T*)s->d, a);
@@ -126,38 +129,39 @@ static int launch_t(bt_state* s, const int* bits, const double* m, uint64_t cmas
 
 template <typename R>
 static int launch_r(bt_state* s, int k, const int* bits, const double* m, uint64_t cmask, int64_t mem_lo,
-                    int64_t nmem, const void* pm, int64_t pms) {
+                    int64_t nmem, const void* pm, int64_t pms, const int8_t* active) {
   int minbit = 64;
   for (int i = 0; i < k; ++i) minbit = bits[i] < minbit ? bits[i] : minbit;
   bool vec2 = sizeof(R) == 4 && minbit >= 1 && !(cmask & 1ULL) && s->nbits - k >= 1;
   if constexpr (sizeof(R) == 4) {
     if (vec2) {
       switch (k) {
-        case 1: return launch_t<R, 1, 2>(s, bits, m, cmask, mem_lo, nmem, pm, pms);
-        case 2: return launch_t<R, 2, 2>(s, bits, m, cmask, mem_lo, nmem, pm, pms);
-        case 3: return launch_t<R, 3, 2>(s, bits, m, cmask, mem_lo, nmem, pm, pms);
-        case 4: return launch_t<R, 4, 2>(s, bits, m, cmask, mem_lo, nmem, pm, pms);
-        case 5: return launch_t<R, 5, 2>(s, bits, m, cmask, mem_lo, nmem, pm, pms);
+        case 1: return launch_t<R, 1, 2>(s, bits, m, cmask, mem_lo, nmem, pm, pms, active);
+        case 2: return launch_t<R, 2, 2>(s, bits, m, cmask, mem_lo, nmem, pm, pms, active);
+        case 3: return launch_t<R, 3, 2>(s, bits, m, cmask, mem_lo, nmem, pm, pms, active);
+        case 4: return launch_t<R, 4, 2>(s, bits, m, cmask, mem_lo, nmem, pm, pms, active);
+        case 5: return launch_t<R, 5, 2>(s, bits, m, cmask, mem_lo, nmem, pm, pms, active);
       }
     }
   }
   {
     switch (k) {
-      case 1: return launch_t<R, 1, 1>(s, bits, m, cmask, mem_lo, nmem, pm, pms);
-      case 2: return launch_t<R, 2, 1>(s, bits, m, cmask, mem_lo, nmem, pm, pms);
-      case 3: return launch_t<R, 3, 1>(s, bits, m, cmask, mem_lo, nmem, pm, pms);
-      case 4: return launch_t<R, 4, 1>(s, bits, m, cmask, mem_lo, nmem, pm, pms);
-      case 5: return launch_t<R, 5, 1>(s, bits, m, cmask, mem_lo, nmem, pm, pms);
+      case 1: return launch_t<R, 1, 1>(s, bits, m, cmask, mem_lo, nmem, pm, pms, active);
+      case 2: return launch_t<R, 2, 1>(s, bits, m, cmask, mem_lo, nmem, pm, pms, active);
+      case 3: return launch_t<R, 3, 1>(s, bits, m, cmask, mem_lo, nmem, pm, pms, active);
+      case 4: return launch_t<R, 4, 1>(s, bits, m, cmask, mem_lo, nmem, pm, pms, active);
+      case 5: return launch_t<R, 5, 1>(s, bits, m, cmask, mem_lo, nmem, pm, pms, active);
     }
   }
   return bt_fail(s->ctx, BT_ERR_UNSUPPORTED, "gate sweep supports 1 <= k <= 5");
 }
 
 int bt_launch_gate(bt_state* s, int k, const int* bits, const double* m_rowmajor, uint64_t cmask,
-                   int64_t mem_lo, int64_t nmem, const void* per_member, int64_t pm_stride) {
+                   int64_t mem_lo, int64_t nmem, const void* per_member, int64_t pm_stride, const int8_t* active) {
   if (k < 1 || k > BT_MAX_K || k > s->nbits)
     return bt_fail(s->ctx, BT_ERR_UNSUPPORTED, "gate sweep supports 1 <= k <= 5 target qubits");
   if (nmem <= 0) return BT_OK;
-  if (s->prec == BT_PREC_C64) return launch_r<float>(s, k, bits, m_rowmajor, cmask, mem_lo, nmem, per_member, pm_stride);
-  return launch_r<double>(s, k, bits, m_rowmajor, cmask, mem_lo, nmem, per_member, pm_stride);
+  if (s->prec == BT_PREC_C64)
+    return launch_r<float>(s, k, bits, m_rowmajor, cmask, mem_lo, nmem, per_member, pm_stride, active);
+  return launch_r<double>(s, k, bits, m_rowmajor, cmask, mem_lo, nmem, per_member, pm_stride, active);
 }

@@ -100,12 +100,16 @@ __host__ __device__ inline uint64_t bt_insert_zeros(uint64_t g, int k, const int
 // matrix index), all bits of cmask must read 1.  `m` is a row-major interleaved
 // complex128 matrix (host).  per_member (device, precision R, row-major
 // interleaved, pm_stride reals apart) replaces m when not null.
+// active (device, one byte per member, optional): members with 0 are left untouched
 int bt_launch_gate(bt_state* s, int k, const int* bits, const double* m_rowmajor, uint64_t cmask,
-                   int64_t mem_lo, int64_t nmem, const void* per_member, int64_t pm_stride);
+                   int64_t mem_lo, int64_t nmem, const void* per_member, int64_t pm_stride,
+                   const int8_t* active = nullptr);
 
 // Reductions write FP64 results per member into `out` (device), member-major.
 // reduced density matrix (k <= 3) on bits: out[mem][2*D*D] row-major interleaved
-int bt_launch_rdm(bt_state* s, int k, const int* bits, int64_t mem_lo, int64_t nmem, double* out);
+// (active as for bt_launch_gate: members with 0 are not read and get zeros)
+int bt_launch_rdm(bt_state* s, int k, const int* bits, int64_t mem_lo, int64_t nmem, double* out,
+                  const int8_t* active = nullptr);
 // Pauli terms sharing one xmask (<= 8 zmasks): out[mem][T] = Re <P_t>
 int bt_launch_pauli(bt_state* s, uint64_t x, int T, const uint64_t* z, int64_t mem_lo, int64_t nmem,
                     double* out);

@@ -35,9 +35,27 @@ struct PGOp {
   int rec_idx;     // measurement: record slot
 };
 
+// A group of consecutive ops acting inside one set Q of at most two qubits (the
+// grouped executor for members too large for shared memory): one reduction of the
+// member's reduced density matrix on Q, one decision per member (every branch and
+// outcome of the group decided from rho_Q, which each op on Q transforms exactly:
+// rho_Q -> K rho_Q K^dagger / p), one pass applying the product of the chosen
+// matrices.
+struct PGGroup {
+  int nb;        // qubits in Q (1 or 2)
+  int q0, q1;    // bit positions, q0 = most significant bit of the group index
+  int op0, nop;  // ops [op0, op0 + nop)
+  int need_rho;  // some op's decision depends on the state
+};
+
 struct bt_program {
   bt_ctx* ctx = nullptr;
   int n = 0, prec = 0, batch = 0;
+  int executor = 0;  // 0 automatic, 1 shared memory, 2 grouped
+  std::vector<PGGroup> groups;
+  void* d_gact = nullptr;  // [group][member] 1 = the member does something in the group
+  void* d_rho = nullptr;   // [member][32] reduced matrices (FP64)
+  void* d_mat = nullptr;   // [member][32] chosen group matrices (state precision)
   std::vector<PGOp> ops;
   std::vector<double> gm;   // gate matrices, row-major interleaved (converted to the state precision)
   std::vector<double> km;   // Kraus sets, row-major interleaved FP64
@@ -322,6 +340,174 @@ __global__ void __launch_bounds__(PG_THREADS) k_program(typename CT<R>::T* __res
   for (int i = threadIdx.x; i < len; i += PG_THREADS) g[i] = st[i];
 }
 
+// ------------------------------------------------------------------ grouped executor: decisions
+// D x D complex matrices (D <= 4), row-major interleaved, FP64
+__device__ void cm_mul(const double* a, const double* b, double* c, int D) {  // c = a b
+  for (int r = 0; r < D; ++r)
+    for (int k = 0; k < D; ++k) {
+      double sr = 0, si = 0;
+      for (int j = 0; j < D; ++j) {
+        const double ar = a[2 * (r * D + j)], ai = a[2 * (r * D + j) + 1];
+        const double br = b[2 * (j * D + k)], bi = b[2 * (j * D + k) + 1];
+        sr += ar * br - ai * bi;
+        si += ar * bi + ai * br;
+      }
+      c[2 * (r * D + k)] = sr;
+      c[2 * (r * D + k) + 1] = si;
+    }
+}
+
+// c = a b a^dagger
+__device__ void cm_conj(const double* a, const double* b, double* c, int D) {
+  double t[32];
+  cm_mul(a, b, t, D);
+  for (int r = 0; r < D; ++r)
+    for (int k = 0; k < D; ++k) {
+      double sr = 0, si = 0;
+      for (int j = 0; j < D; ++j) {
+        const double tr = t[2 * (r * D + j)], ti = t[2 * (r * D + j) + 1];
+        const double ar = a[2 * (k * D + j)], ai = -a[2 * (k * D + j) + 1];  // conj(a[k][j])
+        sr += tr * ar - ti * ai;
+        si += tr * ai + ti * ar;
+      }
+      c[2 * (r * D + k)] = sr;
+      c[2 * (r * D + k) + 1] = si;
+    }
+}
+
+// op matrix (op bits x[, y], x = most significant) embedded into the group's
+// space (q0 = most significant bit of the group index)
+__device__ void embed(const double* K, int opk, int x, int y, const PGGroup& g, double* E) {
+  const int D = 1 << g.nb;
+  for (int e = 0; e < 2 * D * D; ++e) E[e] = 0;
+  if (g.nb == 1 || (opk == 2 && x == g.q0)) {  // the op spans the group in its order
+    for (int e = 0; e < 2 * D * D; ++e) E[e] = K[e];
+    return;
+  }
+  if (opk == 2) {  // (x, y) = (q1, q0): swap the two index bits
+    const int sw[4] = {0, 2, 1, 3};
+    for (int r = 0; r < 4; ++r)
+      for (int c = 0; c < 4; ++c) {
+        E[2 * (r * 4 + c)] = K[2 * (sw[r] * 4 + sw[c])];
+        E[2 * (r * 4 + c) + 1] = K[2 * (sw[r] * 4 + sw[c]) + 1];
+      }
+    return;
+  }
+  // one-qubit op in a two-qubit group: K (x) I if x = q0, I (x) K if x = q1
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b)
+      for (int c = 0; c < 2; ++c) {
+        const int r = x == g.q0 ? 2 * a + c : 2 * c + a, col = x == g.q0 ? 2 * b + c : 2 * c + b;
+        E[2 * (r * 4 + col)] = K[2 * (a * 2 + b)];
+        E[2 * (r * 4 + col) + 1] = K[2 * (a * 2 + b) + 1];
+      }
+}
+
+// the group's reduced matrix restricted to the op's qubits, in the op's order
+__device__ void restrict_rho(const double* rho, int opk, int x, const PGGroup& g, double* out) {
+  const int D = 1 << g.nb;
+  if (g.nb == 1 || (opk == 2 && x == g.q0)) {
+    for (int e = 0; e < 2 * D * D; ++e) out[e] = rho[e];
+    return;
+  }
+  if (opk == 2) {
+    const int sw[4] = {0, 2, 1, 3};
+    for (int r = 0; r < 4; ++r)
+      for (int c = 0; c < 4; ++c) {
+        out[2 * (r * 4 + c)] = rho[2 * (sw[r] * 4 + sw[c])];
+        out[2 * (r * 4 + c) + 1] = rho[2 * (sw[r] * 4 + sw[c]) + 1];
+      }
+    return;
+  }
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b) {
+      double sr = 0, si = 0;
+      for (int c = 0; c < 2; ++c) {
+        const int r = x == g.q0 ? 2 * a + c : 2 * c + a, col = x == g.q0 ? 2 * b + c : 2 * c + b;
+        sr += rho[2 * (r * 4 + col)];
+        si += rho[2 * (r * 4 + col) + 1];
+      }
+      out[2 * (a * 2 + b)] = sr;
+      out[2 * (a * 2 + b) + 1] = si;
+    }
+}
+
+// One thread per member: every op of group g, decided from rho_Q; writes the
+// product of the chosen (renormalised) matrices in the state precision.  Failure
+// rules as in k_program: an op whose branch or outcome has zero probability is
+// skipped for that member (record -1) and reported through the status word.
+template <typename R>
+__global__ void k_group_decide(const PGGroup g, const PGOp* __restrict__ ops, const R* __restrict__ gm,
+                               const double* __restrict__ km, const int8_t* __restrict__ skip,
+                               const int8_t* __restrict__ act, const double* __restrict__ u, uint64_t key,
+                               uint64_t stream, int batch, const double* __restrict__ rho_in, R* __restrict__ mat_out,
+                               int32_t* __restrict__ rec, int nrec, int* __restrict__ status) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= batch) return;
+  const int D = 1 << g.nb;
+  const bool on = act[m];
+  double M[32], rho[32], E[32], t[32], K[32], rop[32];
+  for (int e = 0; e < 2 * D * D; ++e) {
+    M[e] = (e % (2 * D + 2)) == 0 ? 1.0 : 0.0;
+    rho[e] = g.need_rho && on ? rho_in[(int64_t)m * 32 + e] : 0.0;
+  }
+  for (int oi = g.op0; oi < g.op0 + g.nop; ++oi) {
+    const PGOp op = ops[oi];
+    const bool skipped = !on || (op.skip_off >= 0 && skip[op.skip_off + m]);
+    if (skipped) {
+      if (op.type == PG_MEASURE) rec[(int64_t)m * nrec + op.rec_idx] = -1;
+      continue;
+    }
+    const int opk = op.type == PG_GATE2 ? 2 : (op.type == PG_CHANNEL ? op.k : 1);
+    const int d = 1 << opk;
+    if (op.type == PG_GATE1 || op.type == PG_GATE2) {
+      const R* src = gm + op.moff + (int64_t)op.mstride * m;
+      for (int e = 0; e < 2 * d * d; ++e) K[e] = (double)src[e];
+    } else if (op.type == PG_CHANNEL) {
+      const bool umix = op.flags & 2;
+      if (!umix) restrict_rho(rho, opk, op.b0, g, rop);
+      const double uu = u ? u[(int64_t)op.rand_idx * batch + m] : bt_uniform(key, stream ^ (uint64_t)op.rand_idx, m);
+      double cum = 0;
+      int ind = -1;
+      for (int i = 0; i < op.nk; ++i) {
+        cum += tr_krk(km + op.moff + (int64_t)i * 2 * d * d, rop, d, umix, (op.flags & 1) && opk == 2);
+        if (ind < 0 && uu <= cum) ind = i;
+      }
+      const double* Ki = km + op.moff + (int64_t)(ind < 0 ? 0 : ind) * 2 * d * d;
+      const double nrm = ind >= 0 ? tr_krk(Ki, rop, d, umix, false) : 0.0;
+      if (ind < 0 || !(nrm > 0)) {
+        atomicExch(status, ind < 0 ? 2 : 3);
+        continue;
+      }
+      const double sc = 1.0 / sqrt(nrm);
+      for (int e = 0; e < 2 * d * d; ++e) K[e] = Ki[e] * sc;
+    } else {  // measurement: outcome u < p0 ? 0 : 1 from the qubit's reduced matrix
+      restrict_rho(rho, 1, op.b0, g, rop);
+      const double s0 = rop[0], s1 = rop[6];
+      const double uu = u ? u[(int64_t)op.rand_idx * batch + m] : bt_uniform(key, stream ^ (uint64_t)op.rand_idx, m);
+      const int ind = uu < s0 ? 0 : 1;
+      const double keep = ind ? s1 : s0;
+      if (!(keep > 0)) {
+        atomicExch(status, 1);
+        rec[(int64_t)m * nrec + op.rec_idx] = -1;
+        continue;
+      }
+      rec[(int64_t)m * nrec + op.rec_idx] = ind;
+      for (int e = 0; e < 8; ++e) K[e] = 0;
+      K[ind ? 6 : 0] = 1.0 / sqrt(keep);
+    }
+    embed(K, opk, op.b0, op.b1, g, E);
+    cm_mul(E, M, t, D);
+    for (int e = 0; e < 2 * D * D; ++e) M[e] = t[e];
+    if (g.need_rho) {
+      cm_conj(E, rho, t, D);
+      for (int e = 0; e < 2 * D * D; ++e) rho[e] = t[e];
+    }
+  }
+  R* out = mat_out + (int64_t)m * 32;
+  for (int e = 0; e < 2 * D * D; ++e) out[e] = (R)M[e];
+}
+
 // ------------------------------------------------------------------ host API
 static int prog_qubits(bt_program* p, int k, const int32_t* q) {
   if (k < 1 || k > 2 || !q) return bt_fail(p->ctx, BT_ERR_UNSUPPORTED, "program ops act on 1 or 2 qubits");
@@ -343,9 +529,7 @@ extern "C" {
 int bt_program_create(bt_ctx* ctx, int n, int prec, int batch, bt_program** out) {
   if (!ctx || !out) return bt_fail(ctx, BT_ERR_BAD_ARG, "NULL argument");
   if (prec != BT_PREC_C128 && prec != BT_PREC_C64) return bt_fail(ctx, BT_ERR_BAD_ARG, "prec must be C128 or C64");
-  const int nmax = prec == BT_PREC_C64 ? 14 : 13;
-  if (n < 2 || n > nmax)
-    return bt_fail(ctx, BT_ERR_UNSUPPORTED, "programs hold a member in shared memory: 2 <= n <= 14 (c64) / 13 (c128)");
+  if (n < 2 || n > 34) return bt_fail(ctx, BT_ERR_UNSUPPORTED, "programs take 2 <= n <= 34 qubits");
   if (batch < 1 || batch > (1 << 30)) return bt_fail(ctx, BT_ERR_BAD_ARG, "bad batch");
   bt_program* p = new bt_program();
   p->ctx = ctx;
@@ -360,7 +544,7 @@ int bt_program_free(bt_program* p) {
   if (!p) return BT_OK;
   cudaSetDevice(p->ctx->device);
   cudaStreamSynchronize(p->ctx->stream);
-  for (void* d : {p->d_ops, p->d_gm, p->d_km, p->d_skip, p->d_rec, p->d_u})
+  for (void* d : {p->d_ops, p->d_gm, p->d_km, p->d_skip, p->d_rec, p->d_u, p->d_gact, p->d_rho, p->d_mat})
     if (d) cudaFree(d);
   delete p;
   return BT_OK;
@@ -470,8 +654,91 @@ int bt_program_info(const bt_program* p, int64_t* nops, int64_t* ndraws, int64_t
   return BT_OK;
 }
 
+int bt_program_set_executor(bt_program* p, int executor) {
+  if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "program is NULL");
+  if (executor < 0 || executor > 2) return bt_fail(p->ctx, BT_ERR_BAD_ARG, "executor must be 0, 1 or 2");
+  if (executor == 1 && p->n > (p->prec == BT_PREC_C64 ? 14 : 13))
+    return bt_fail(p->ctx, BT_ERR_UNSUPPORTED, "a member of more than 14 (c64) / 13 (c128) qubits exceeds shared memory");
+  if (p->executor != executor) p->uploaded = false;
+  p->executor = executor;
+  return BT_OK;
+}
+
+static bool use_grouped(const bt_program* p) {
+  return p->executor == 2 || (p->executor == 0 && p->n > (p->prec == BT_PREC_C64 ? 14 : 13));
+}
+
+// groups of consecutive ops within at most two qubits, and per group and member
+// whether the member does anything in it
+static void form_groups(bt_program* p, std::vector<int8_t>& gact) {
+  p->groups.clear();
+  auto bits_of = [](const PGOp& o, int* b) {
+    b[0] = o.b0;
+    const int k = o.type == PG_GATE2 ? 2 : (o.type == PG_CHANNEL ? o.k : 1);
+    if (k == 2) b[1] = o.b1;
+    return k;
+  };
+  for (size_t i = 0; i < p->ops.size();) {
+    PGGroup g = {};
+    int b[2];
+    const int k = bits_of(p->ops[i], b);
+    g.nb = k;
+    g.q0 = b[0];
+    g.q1 = k == 2 ? b[1] : -1;
+    g.op0 = (int)i;
+    size_t j = i;
+    for (; j < p->ops.size(); ++j) {
+      int c[2];
+      const int kc = bits_of(p->ops[j], c);
+      bool fits = true;
+      for (int e = 0; e < kc && fits; ++e) {
+        if (c[e] == g.q0 || c[e] == g.q1) continue;
+        if (g.nb == 1) {  // a one-qubit group takes a second qubit
+          g.nb = 2;
+          g.q1 = c[e];
+        } else {
+          fits = false;
+        }
+      }
+      if (!fits) break;
+      const PGOp& o = p->ops[j];
+      if (o.type == PG_MEASURE || (o.type == PG_CHANNEL && !(o.flags & 2))) g.need_rho = 1;
+    }
+    g.nop = (int)(j - i);
+    p->groups.push_back(g);
+    i = j;
+  }
+  gact.assign(p->groups.size() * (size_t)p->batch, 0);
+  for (size_t gi = 0; gi < p->groups.size(); ++gi) {
+    const PGGroup& g = p->groups[gi];
+    int8_t* row = gact.data() + gi * p->batch;
+    for (int oi = g.op0; oi < g.op0 + g.nop; ++oi) {
+      const PGOp& o = p->ops[oi];
+      for (int m = 0; m < p->batch; ++m)
+        if (o.skip_off < 0 || !p->skip[o.skip_off + m]) row[m] = 1;
+    }
+  }
+}
+
 static int upload(bt_program* p) {
   bt_ctx* ctx = p->ctx;
+  for (void** d : {&p->d_gact, &p->d_rho, &p->d_mat})
+    if (*d) {
+      cudaStreamSynchronize(ctx->stream);
+      cudaFree(*d);
+      *d = nullptr;
+    }
+  if (use_grouped(p)) {
+    std::vector<int8_t> gact;
+    form_groups(p, gact);
+    int rc = bt_cuda_check(ctx, cudaMalloc(&p->d_gact, gact.size() ? gact.size() : 16), "program allocation");
+    if (!rc && gact.size())
+      rc = bt_cuda_check(ctx, cudaMemcpy(p->d_gact, gact.data(), gact.size(), cudaMemcpyHostToDevice), "program upload");
+    if (!rc) rc = bt_cuda_check(ctx, cudaMalloc(&p->d_rho, (size_t)p->batch * 32 * 8), "program allocation");
+    if (!rc) rc = bt_cuda_check(ctx, cudaMalloc(&p->d_mat, (size_t)p->batch * 32 * elem_bytes(p->prec) / 2),
+                                "program allocation");
+    if (rc) return rc;
+  }
   for (void** d : {&p->d_ops, &p->d_gm, &p->d_km, &p->d_skip, &p->d_rec})
     if (*d) {
       cudaStreamSynchronize(ctx->stream);
@@ -512,6 +779,8 @@ static int upload_gm(bt_program* p, bt_ctx* ctx) {
   return bt_cuda_check(ctx, cudaMemcpyAsync(p->d_gm, h, bytes, cudaMemcpyHostToDevice, ctx->stream), "gate upload");
 }
 
+static void launch_program(bt_program* p, bt_state* s, const double* du, uint64_t stream, int nrec);
+
 int bt_program_run(bt_program* p, bt_state* s, const double* uniforms, uint64_t seed, int32_t* records) {
   if (!p || !s) return bt_fail(p ? p->ctx : nullptr, BT_ERR_BAD_ARG, "NULL argument");
   bt_ctx* ctx = s->ctx;
@@ -537,28 +806,48 @@ int bt_program_run(bt_program* p, bt_state* s, const double* uniforms, uint64_t 
     du = (const double*)p->d_u;
   }
   const bool f = p->prec == BT_PREC_C64;
-  const size_t smem = (elem_bytes(p->prec) << p->n) + (9 * 32 + 2 * PG_MAX_KRAUS) * 8 + 32 * 8;
-  static std::atomic<bool> attr[2][64] = {};
-  std::atomic<bool>& done = attr[f][ctx->device & 63];
-  if (!done.load()) {
-    cudaError_t e = f ? cudaFuncSetAttribute(k_program<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)
-                      : cudaFuncSetAttribute(k_program<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if ((rc = bt_cuda_check(ctx, e, "program smem attribute"))) return rc;
-    done.store(true);
-  }
   // draws depend on (ctx seed, seed) only, as bt_sample's: a run is reproducible
   const uint64_t stream = (seed * 0x9E3779B97F4A7C15ULL) ^ 0x5052000000000000ULL;
-  if (f)
-    k_program<float><<<p->batch, PG_THREADS, smem, ctx->stream>>>(
-        (float2*)s->d, s->nbits, (const PGOp*)p->d_ops, (int)p->ops.size(), (const float*)p->d_gm,
-        (const double*)p->d_km, (const int8_t*)p->d_skip, du, ctx->seed, stream, p->batch, (int32_t*)p->d_rec,
-        p->nrec ? p->nrec : 1, ctx->d_status);
-  else
-    k_program<double><<<p->batch, PG_THREADS, smem, ctx->stream>>>(
-        (double2*)s->d, s->nbits, (const PGOp*)p->d_ops, (int)p->ops.size(), (const double*)p->d_gm,
-        (const double*)p->d_km, (const int8_t*)p->d_skip, du, ctx->seed, stream, p->batch, (int32_t*)p->d_rec,
-        p->nrec ? p->nrec : 1, ctx->d_status);
-  ctx->launches++;
+  const int nrec = p->nrec ? p->nrec : 1;
+  if (use_grouped(p)) {
+    // per group: reduce rho_Q (when a decision needs it), decide per member,
+    // apply the chosen matrices; members idle in a group are neither read nor written
+    const int8_t* gact = (const int8_t*)p->d_gact;
+    for (size_t gi = 0; gi < p->groups.size() && !rc; ++gi) {
+      const PGGroup& g = p->groups[gi];
+      const int8_t* act = gact + gi * p->batch;
+      const int bits[2] = {g.q0, g.q1};
+      const int D = 1 << g.nb;
+      if (g.need_rho) rc = bt_launch_rdm(s, g.nb, bits, 0, p->batch, (double*)p->d_rho, act);
+      if (rc) break;
+      const unsigned grid = (unsigned)((p->batch + 127) / 128);
+      if (f)
+        k_group_decide<float><<<grid, 128, 0, ctx->stream>>>(
+            g, (const PGOp*)p->d_ops, (const float*)p->d_gm, (const double*)p->d_km, (const int8_t*)p->d_skip, act,
+            du, ctx->seed, stream, p->batch, (const double*)p->d_rho, (float*)p->d_mat, (int32_t*)p->d_rec, nrec,
+            ctx->d_status);
+      else
+        k_group_decide<double><<<grid, 128, 0, ctx->stream>>>(
+            g, (const PGOp*)p->d_ops, (const double*)p->d_gm, (const double*)p->d_km, (const int8_t*)p->d_skip, act,
+            du, ctx->seed, stream, p->batch, (const double*)p->d_rho, (double*)p->d_mat, (int32_t*)p->d_rec, nrec,
+            ctx->d_status);
+      ctx->launches++;
+      if ((rc = bt_cuda_check(ctx, cudaGetLastError(), "group decide launch"))) break;
+      rc = bt_launch_gate(s, g.nb, bits, nullptr, 0, 0, p->batch, p->d_mat, 32, act);
+      (void)D;
+    }
+    if (rc) return rc;
+  } else {
+    static std::atomic<bool> attr[2][64] = {};
+    std::atomic<bool>& done = attr[f][ctx->device & 63];
+    if (!done.load()) {
+      cudaError_t e = f ? cudaFuncSetAttribute(k_program<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)
+                        : cudaFuncSetAttribute(k_program<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      if ((rc = bt_cuda_check(ctx, e, "program smem attribute"))) return rc;
+      done.store(true);
+    }
+    launch_program(p, s, du, stream, nrec);
+  }
   if ((rc = bt_cuda_check(ctx, cudaGetLastError(), "program launch"))) return rc;
   if (records && p->nrec)
     rc = bt_cuda_check(ctx, cudaMemcpyAsync(records, p->d_rec, (size_t)p->batch * p->nrec * 4, cudaMemcpyDeviceToHost,
@@ -579,6 +868,22 @@ int bt_program_run(bt_program* p, bt_state* s, const double* uniforms, uint64_t 
 }
 
 }  // extern "C"
+
+static void launch_program(bt_program* p, bt_state* s, const double* du, uint64_t stream, int nrec) {
+  bt_ctx* ctx = s->ctx;
+  const size_t smem = (elem_bytes(p->prec) << p->n) + (9 * 32 + 2 * PG_MAX_KRAUS) * 8 + 32 * 8;
+  if (p->prec == BT_PREC_C64)
+    k_program<float><<<p->batch, PG_THREADS, smem, ctx->stream>>>(
+        (float2*)s->d, s->nbits, (const PGOp*)p->d_ops, (int)p->ops.size(), (const float*)p->d_gm,
+        (const double*)p->d_km, (const int8_t*)p->d_skip, du, ctx->seed, stream, p->batch, (int32_t*)p->d_rec,
+        nrec, ctx->d_status);
+  else
+    k_program<double><<<p->batch, PG_THREADS, smem, ctx->stream>>>(
+        (double2*)s->d, s->nbits, (const PGOp*)p->d_ops, (int)p->ops.size(), (const double*)p->d_gm,
+        (const double*)p->d_km, (const int8_t*)p->d_skip, du, ctx->seed, stream, p->batch, (int32_t*)p->d_rec,
+        nrec, ctx->d_status);
+  ctx->launches++;
+}
 
 // ------------------------------------------------------------------ serving hook (bt_serve.cu)
 // matrix dimension of every op (0 where the op is not a gate) and the shape

@@ -112,7 +112,7 @@ int bt_work(bt_ctx* ctx, size_t bytes, double** out) {
 template <typename R, int K>
 __global__ void __launch_bounds__(BT_THREADS) k_rdm(const typename CT<R>::T* __restrict__ psi, int nbits,
                                                     int4 bits4, int4 sorted4, int64_t mem_lo, int nblk,
-                                                    double* __restrict__ part) {
+                                                    double* __restrict__ part, const int8_t* __restrict__ active) {
   constexpr int D = 1 << K, W = 2 * D * D;
   const int bits[4] = {bits4.x, bits4.y, bits4.z, bits4.w};
   const int sorted[4] = {sorted4.x, sorted4.y, sorted4.z, sorted4.w};
@@ -127,7 +127,8 @@ __global__ void __launch_bounds__(BT_THREADS) k_rdm(const typename CT<R>::T* __r
   }
   const int64_t mem = mem_lo + blockIdx.y;
   const typename CT<R>::T* s = psi + (mem << nbits);
-  const int64_t ng = 1LL << (nbits - K);
+  // an inactive member reads nothing and gets a zero matrix
+  const int64_t ng = (!active || active[mem]) ? (1LL << (nbits - K)) : 0;
   const int64_t stride = (int64_t)nblk * blockDim.x;
   if constexpr (K <= 2) {
     // Hermitian: accumulate the D*D packed reals, expand to the full matrix at the end
@@ -228,7 +229,7 @@ __global__ void __launch_bounds__(BT_THREADS) k_rdm(const typename CT<R>::T* __r
 }
 
 template <typename R, int K>
-static int rdm_t(bt_state* s, const int* bits, int64_t mem_lo, int64_t nmem, double* out) {
+static int rdm_t(bt_state* s, const int* bits, int64_t mem_lo, int64_t nmem, double* out, const int8_t* active) {
   bt_ctx* ctx = s->ctx;
   constexpr int W = 2 * (1 << K) * (1 << K);
   int b4[4] = {0, 0, 0, 0}, s4[4] = {0, 0, 0, 0};
@@ -244,20 +245,23 @@ static int rdm_t(bt_state* s, const int* bits, int64_t mem_lo, int64_t nmem, dou
   dim3 grid(nblk, (unsigned)nmem);
   k_rdm<R, K><<<grid, BT_THREADS, 0, ctx->stream>>>((const typename CT<R>::T*)s->d, s->nbits,
                                                     make_int4(b4[0], b4[1], b4[2], b4[3]),
-                                                    make_int4(s4[0], s4[1], s4[2], s4[3]), mem_lo, nblk, part);
+                                                    make_int4(s4[0], s4[1], s4[2], s4[3]), mem_lo, nblk, part,
+                                                    active);
   ctx->launches++;
   rc = bt_cuda_check(ctx, cudaGetLastError(), "rdm launch");
   if (rc) return rc;
   return finalize(ctx, part, nblk, W, nmem, out);
 }
 
-int bt_launch_rdm(bt_state* s, int k, const int* bits, int64_t mem_lo, int64_t nmem, double* out) {
+int bt_launch_rdm(bt_state* s, int k, const int* bits, int64_t mem_lo, int64_t nmem, double* out,
+                  const int8_t* active) {
   if (nmem > 65535) return bt_fail(s->ctx, BT_ERR_UNSUPPORTED, "at most 65535 members per reduction");
   bool c64 = s->prec == BT_PREC_C64;
+  const int8_t* a = active;
   switch (k) {
-    case 1: return c64 ? rdm_t<float, 1>(s, bits, mem_lo, nmem, out) : rdm_t<double, 1>(s, bits, mem_lo, nmem, out);
-    case 2: return c64 ? rdm_t<float, 2>(s, bits, mem_lo, nmem, out) : rdm_t<double, 2>(s, bits, mem_lo, nmem, out);
-    case 3: return c64 ? rdm_t<float, 3>(s, bits, mem_lo, nmem, out) : rdm_t<double, 3>(s, bits, mem_lo, nmem, out);
+    case 1: return c64 ? rdm_t<float, 1>(s, bits, mem_lo, nmem, out, a) : rdm_t<double, 1>(s, bits, mem_lo, nmem, out, a);
+    case 2: return c64 ? rdm_t<float, 2>(s, bits, mem_lo, nmem, out, a) : rdm_t<double, 2>(s, bits, mem_lo, nmem, out, a);
+    case 3: return c64 ? rdm_t<float, 3>(s, bits, mem_lo, nmem, out, a) : rdm_t<double, 3>(s, bits, mem_lo, nmem, out, a);
   }
   return bt_fail(s->ctx, BT_ERR_UNSUPPORTED, "reduced density matrix supports 1 <= k <= 3");
 }

@@ -181,10 +181,19 @@ int bt_plan_stats(const bt_plan* p, int64_t* ngates, int64_t* npasses, int64_t* 
 int bt_plan_run(bt_plan* p, bt_state* s, int64_t member);
 
 /* ---------------------------------------------------------------- programs */
-/* A program is a noisy circuit run whole, one CTA per member, with the member
- * held in shared memory (2 <= n <= 14 qubits complex64, 13 complex128; state
- * vectors only): the per-shot loop of the noisy measure(circuit, shots)
- * (src/ops.jl:617-630) as one launch.  Ops act on 1 or 2 qubits:
+/* A program is a noisy circuit run on every member of a batched state (state
+ * vectors, 2 <= n <= 34): the per-shot loop of the noisy measure(circuit, shots)
+ * (src/ops.jl:617-630) for a whole batch of shots at once.  Two executors:
+ *   shared memory (members of n <= 14 qubits complex64 / 13 complex128): one CTA
+ *     per member runs every op of the program in one launch;
+ *   grouped (any n): consecutive ops inside at most two qubits form a group; per
+ *     group one reduction of the members' reduced matrices on those qubits, one
+ *     decision per member for every branch and outcome of the group (the reduced
+ *     matrix transforms exactly under ops on its qubits), one pass applying the
+ *     product of the chosen matrices; members with nothing to do in a group are
+ *     not touched.
+ * Both make the same decisions from the same draws (up to rounding at a branch
+ * boundary).  Ops act on 1 or 2 qubits:
  *   gate     op.expand(N)*state; mats is one column-major matrix, or batch of them
  *            back to back when per_member (twirl frames, per-client angles);
  *   channel  apply_kraus (src/struct.jl:58-76, branch rule src/hilbert.jl:810-819)
@@ -210,6 +219,9 @@ int bt_program_info(const bt_program* p, int64_t* nops, int64_t* ndraws, int64_t
 /* new matrices for gate op `op_index` (counting every bt_program_add_* call from
  * 0), in the count it was added with (variational angles between runs) */
 int bt_program_set_gate(bt_program* p, int64_t op_index, const double* mats);
+/* 0: shared memory when the member fits, else grouped (default); 1: shared
+ * memory; 2: grouped */
+int bt_program_set_executor(bt_program* p, int executor);
 /* runs on every member of s (n, prec and batch as created); records: batch x
  * nrecords int32, member-major (may be NULL) */
 int bt_program_run(bt_program* p, bt_state* s, const double* uniforms, uint64_t seed, int32_t* records);

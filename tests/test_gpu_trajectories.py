@@ -75,12 +75,14 @@ def test_trajectories_uneven_programs_match_oracle(ctx, oracle, kref, twirl):
     assert sum(len(r) for r in recs) > 0  # some members were measured
 
 
+@pytest.mark.parametrize("executor", ["shared", "grouped"])
 @pytest.mark.parametrize("prec,tol", [("c128", 1e-12), ("c64", 2e-5)])
 @pytest.mark.parametrize("twirl", [False, True])
-def test_program_uneven_programs_match_oracle(ctx, oracle, kref, prec, tol, twirl):
-    """The whole-program kernel (one CTA per member) against the oracle replaying
-    each member with the same draws: ZNE repetitions, twirl frames, random
-    mid-circuit measurements, Kraus branches.  complex64 tolerance: float32
+def test_program_uneven_programs_match_oracle(ctx, oracle, kref, prec, tol, twirl, executor):
+    """Programs on both executors (one CTA per member in shared memory; grouped
+    ops within two qubits decided from one reduced matrix) against the oracle
+    replaying each member with the same draws: ZNE repetitions, twirl frames,
+    random mid-circuit measurements, Kraus branches.  complex64 tolerance: float32
     rounding over ~150 ops of a 5-qubit member."""
     import bluetangle_gpu as bt
     import bluetangle_gpu.trajectories as T
@@ -94,6 +96,7 @@ def test_program_uneven_programs_match_oracle(ctx, oracle, kref, prec, tol, twir
     assert T.program_supported(slots, n, prec)
     st = bt.zero_state(n, prec, batch=B)
     prog, _ = T.compile_program(slots, n, B, prec, unitary_mix=False)
+    prog.set_executor(executor)
     recs = prog.run(st, rng=np.random.default_rng(11))
     ref, rrecs = replay(oracle, slots, B, n, np.random.default_rng(11), kref)
     for m in range(B):
@@ -194,3 +197,22 @@ def test_trajectories_device_rng_statistics(ctx, oracle, engine):
         bt.apply(step, rho)
     z_dm = bt.expect(rho, "Z")[0]
     assert abs(zs.mean() - z_dm) < 4 * zs.std() / np.sqrt(B) + 1e-3
+
+
+def test_grouped_program_large_members_equal_slots_engine(ctx):
+    """Members larger than shared memory (16 qubits, complex64) run grouped; with
+    the same explicit draws they make the slots engine's decisions (records equal)
+    and end in the same states (complex64 rounding)."""
+    import bluetangle_gpu.trajectories as T
+    n, B = 16, 12
+    h = np.random.default_rng(9).uniform(0.5, 1.5, n)
+    steps = tfim_cnot_steps(n, 1, 0.2, h)
+    kw = dict(zne_ids=[i % 3 for i in range(B)], twirl=True, measure_prob=0.1, prec="c64")
+    a, ra = T.run_trajectories(steps, n, B, rng=np.random.default_rng(5), frame_rng=np.random.default_rng(6),
+                               measure_rng=np.random.default_rng(7), engine="program", **kw)
+    b, rb = T.run_trajectories(steps, n, B, rng=np.random.default_rng(5), frame_rng=np.random.default_rng(6),
+                               measure_rng=np.random.default_rng(7), engine="slots", **kw)
+    assert ra == rb
+    assert sum(len(r) for r in ra) > 0
+    for m in range(B):
+        assert np.abs(a.to_numpy(m) - b.to_numpy(m)).max() < 2e-5

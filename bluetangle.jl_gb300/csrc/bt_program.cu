@@ -50,6 +50,7 @@ struct PGGroup {
 
 struct bt_program {
   bt_ctx* ctx = nullptr;
+  int device = 0;  // ctx's device, kept so that freeing needs no live context
   int n = 0, prec = 0, batch = 0;
   int executor = 0;  // 0 automatic, 1 shared memory, 2 grouped
   std::vector<PGGroup> groups;
@@ -533,6 +534,7 @@ int bt_program_create(bt_ctx* ctx, int n, int prec, int batch, bt_program** out)
   if (batch < 1 || batch > (1 << 30)) return bt_fail(ctx, BT_ERR_BAD_ARG, "bad batch");
   bt_program* p = new bt_program();
   p->ctx = ctx;
+  p->device = ctx->device;
   p->n = n;
   p->prec = prec;
   p->batch = batch;
@@ -542,8 +544,8 @@ int bt_program_create(bt_ctx* ctx, int n, int prec, int batch, bt_program** out)
 
 int bt_program_free(bt_program* p) {
   if (!p) return BT_OK;
-  cudaSetDevice(p->ctx->device);
-  cudaStreamSynchronize(p->ctx->stream);
+  // cudaFree waits for the device; the program's context may already be gone
+  cudaSetDevice(p->device);
   for (void* d : {p->d_ops, p->d_gm, p->d_km, p->d_skip, p->d_rec, p->d_u, p->d_gact, p->d_rho, p->d_mat})
     if (d) cudaFree(d);
   delete p;

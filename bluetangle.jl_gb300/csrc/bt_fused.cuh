@@ -1,4 +1,5 @@
-// Shared declarations of the fused tile pass (bt_fused.cu) and its planner (bt_plan.cu).
+// Shared declarations of the fused tile pass (bt_fused_impl.cuh, bt_jit.cu) and its
+// planner (bt_plan.cu).
 #pragma once
 #include "bt_internal.cuh"
 

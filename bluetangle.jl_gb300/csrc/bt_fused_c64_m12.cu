@@ -1,0 +1,6 @@
+// Generic fused tile pass, complex64, tiles of 2^12 amplitudes (bt_fused_impl.cuh).
+#include "bt_fused_impl.cuh"
+
+int bt_fused_f12(bt_ctx* ctx, void* psi, const FusedArgs<float>& a) {
+  return launch_fused<float, 12, BT_TILE_RB_C64>(ctx, psi, a);
+}

@@ -12,6 +12,10 @@
 // write of the state however many gates it holds; it replaces that many separate
 // sweeps (each an HBM round trip) of the reference's per-gate operator products
 // (BlueTangle.jl src/hilbert.jl:505, :517-553).
+//
+// This header holds the kernel templates (the generic pass interprets its op list
+// at run time; plans normally run specialised kernels, bt_jit.cu).
+#pragma once
 #include <atomic>
 
 #include "bt_fused.cuh"
@@ -464,22 +468,5 @@ static int launch_fused(bt_ctx* ctx, void* psi, const FusedArgs<R>& a) {
 }
 
 // tiles smaller than the default hold a whole small state (2^(M-RB) threads per CTA)
-int bt_launch_fused_f(bt_ctx* ctx, void* psi, const FusedArgs<float>& a) {
-  switch (a.M) {
-    case 13: return launch_fused<float, 13, BT_TILE_RB_C64>(ctx, psi, a);
-    case 12: return launch_fused<float, 12, BT_TILE_RB_C64>(ctx, psi, a);
-    case 11: return launch_fused<float, 11, BT_TILE_RB_C64>(ctx, psi, a);
-    case 10: return launch_fused<float, 10, BT_TILE_RB_C64>(ctx, psi, a);
-  }
-  return bt_fail(ctx, BT_ERR_BAD_ARG, "fused pass: unsupported tile size");
-}
-
-int bt_launch_fused_d(bt_ctx* ctx, void* psi, const FusedArgs<double>& a) {
-  switch (a.M) {
-    case 12: return launch_fused<double, 12, BT_TILE_RB_C128>(ctx, psi, a);
-    case 11: return launch_fused<double, 11, BT_TILE_RB_C128>(ctx, psi, a);
-    case 10: return launch_fused<double, 10, BT_TILE_RB_C128>(ctx, psi, a);
-    case 9: return launch_fused<double, 9, BT_TILE_RB_C128>(ctx, psi, a);
-  }
-  return bt_fail(ctx, BT_ERR_BAD_ARG, "fused pass: unsupported tile size");
-}
+// the launchers that instantiate these templates are bt_fused_c64.cu and
+// bt_fused_c128.cu (two translation units, compiled in parallel)

@@ -81,6 +81,10 @@ int bt_jit_max_ops() {
   static const int v = env_int("BTGPU_PLAN_MAX_OPS", 64, 8, BT_FUSED_MAX_OPS);
   return v;
 }
+int bt_tile_rb(bool c64) {
+  static const int v = env_int("BTGPU_TILE_RB", BT_TILE_RB_C64, 4, 5);
+  return c64 ? v : BT_TILE_RB_C128;
+}
 
 // ------------------------------------------------------------------ generated source
 static const char* kPrelude = R"PRELUDE(
@@ -339,7 +343,8 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
 template <typename R>
 static std::string structure_key(const FusedArgs<R>& a) {
   std::ostringstream k;
-  k << (sizeof(R) == 4 ? 'f' : 'd') << a.M << ':' << a.c << ':' << bt_jit_min_blocks() << ':';
+  k << (sizeof(R) == 4 ? 'f' : 'd') << a.M << ':' << a.c << ':' << bt_jit_min_blocks() << ':'
+    << (a.nphase ? (int)a.ph[0].nreg : 0) << ':';
   for (int i = 0; i < a.M; ++i) k << a.tbits[i] << ',';
   for (int p = 0; p < a.nphase; ++p) {
     const FPhase& ph = a.ph[p];
@@ -445,7 +450,6 @@ static int jit_prepare_t(bt_ctx* ctx, std::vector<const FusedArgs<R>*>& passes, 
       }
   }
   if (!order.empty()) {
-    const int NB = sizeof(R) == 4 ? BT_TILE_RB_C64 : BT_TILE_RB_C128;
     // batches of kernels compiled concurrently (NVRTC programs are independent)
     int hw = (int)std::thread::hardware_concurrency();
     if (hw < 1) hw = 1;
@@ -457,7 +461,8 @@ static int jit_prepare_t(bt_ctx* ctx, std::vector<const FusedArgs<R>*>& passes, 
       src << kPrelude;
       for (size_t i = b; i < order.size(); i += nb) {
         const std::string nm = "btk_" + std::to_string(i);
-        gen_kernel<R>(src, *first[order[i]], NB, nm);
+        const FusedArgs<R>& pa = *first[order[i]];
+        gen_kernel<R>(src, pa, pa.nphase ? pa.ph[0].nreg : (sizeof(R) == 4 ? BT_TILE_RB_C64 : BT_TILE_RB_C128), nm);
         names[b].push_back(nm);
         bkeys[b].push_back(order[i]);
       }
@@ -548,7 +553,7 @@ static int jit_launch_t(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<R>&
   int64_t total = (1LL << a.lg_tiles) * a.nmem;
   int64_t grid = (int64_t)ctx->sm_count * bt_jit_min_blocks() * 4;
   if (grid > total) grid = total;
-  const unsigned threads = 1u << (a.M - (sizeof(R) == 4 ? BT_TILE_RB_C64 : BT_TILE_RB_C128));
+  const unsigned threads = 1u << (a.M - (a.nphase ? a.ph[0].nreg : (sizeof(R) == 4 ? BT_TILE_RB_C64 : BT_TILE_RB_C128)));
   cudaError_t e = cudaLaunchKernel((const void*)kern, dim3((unsigned)grid), dim3(threads), args, smem,
                                    ctx->stream);
   ctx->launches++;

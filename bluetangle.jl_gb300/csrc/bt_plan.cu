@@ -9,7 +9,8 @@
 //   * fused passes: a set of at most M bits (always containing the lowest c
 //     bits) and every gate that acts inside it and is not ordered behind a gate
 //     left out; gates inside a pass are grouped into register phases of at most
-//     RB bits.  Each fused pass is one k_fused launch (bt_fused.cu).
+//     RB bits.  Each fused pass is one launch of its specialised kernel (bt_jit.cu)
+//     or of the generic k_fused (bt_fused_impl.cuh).
 //   * sweep passes: gates of more than two bits, or with controls that do not fit
 //     a two-bit matrix, run as one k_gate sweep (bt_gate.cu).
 // Gates are only reordered past gates on disjoint bits, so the plan applies the
@@ -489,7 +490,9 @@ int bt_plan_compile(bt_plan* p, int mode) {
   p->passes.clear();
   p->nphases = 0;
   const bool c64 = p->prec == BT_PREC_C64;
-  const int NB = c64 ? BT_TILE_RB_C64 : BT_TILE_RB_C128;
+  // register bits per thread: a tuned width only where every pass gets its
+  // specialised kernel before the first run (the generic kernel has one width)
+  const int NB = (mode == 0 && bt_jit_available()) ? bt_tile_rb(c64) : (c64 ? BT_TILE_RB_C64 : BT_TILE_RB_C128);
   // the tile covers the whole state when the state is smaller than the default
   // tile, down to 2^(M - NB) = 32 threads per CTA
   const int M = std::min(c64 ? BT_TILE_M_C64 : BT_TILE_M_C128, p->nbits);

@@ -97,6 +97,15 @@ __device__ __forceinline__ float fm(float a, float b, float c) { return __fmaf_r
 __device__ __forceinline__ double fm(double a, double b, double c) { return __fma_rn(a, b, c); }
 template <int NM> struct JitArgsF { i64 member_lo, nmem; int nbits, lg_tiles; float mat[NM]; };
 template <int NM> struct JitArgsD { i64 member_lo, nmem; int nbits, lg_tiles; double mat[NM]; };
+// packed pairs of FP32 values (two amplitudes' real or imaginary parts) and the
+// two-lane FMA / multiply of sm_100-family GPUs
+// (pack / unpack as plain bit operations: register-pair moves the compiler can coalesce)
+__device__ __forceinline__ u64 pk(float a, float b) { return (u64)__float_as_uint(a) | ((u64)__float_as_uint(b) << 32); }
+__device__ __forceinline__ float plo(u64 r) { return __uint_as_float((unsigned)r); }
+__device__ __forceinline__ float phi(u64 r) { return __uint_as_float((unsigned)(r >> 32)); }
+__device__ __forceinline__ u64 ffma2(u64 a, u64 b, u64 c) { u64 d; asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c)); return d; }
+__device__ __forceinline__ u64 fmul2(u64 a, u64 b) { u64 d; asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b)); return d; }
+__device__ __forceinline__ u64 bc(float a) { return pk(a, a); }
 )PRELUDE";
 
 static std::string fmt_u64(uint64_t v) {
@@ -254,6 +263,209 @@ static void emit_op(std::ostringstream& o, const FOp& op, int NB) {
   }
 }
 
+// ------------------------------------------------------------------ packed (complex64)
+// In a packed phase the 2^NB register amplitudes are held as pairs that differ in
+// register bit P: X<j> = (x_j, x_{j|P}), Y<j> = (y_j, y_{j|P}) for j with bit P
+// clear.  An op that does not touch bit P applies the same arithmetic to both
+// lanes, so it runs on the pairs with two-lane FMAs: half the instructions of the
+// scalar code.  Diagonal ops on bit P take per-lane coefficients.  Other ops on
+// bit P fall back to the scalar code (unpack, op, repack).
+
+static bool touches(const FOp& op, int P) {
+  const bool two = op.type == FOP_G2 || op.type == FOP_D2 || op.type == FOP_P2 || op.type == FOP_CX ||
+                   op.type == FOP_SW;
+  return op.b0 == P || (two && op.b1 == P);
+}
+
+// pack bit of a phase: the register bit that the fewest non-diagonal ops touch
+static int choose_pack_bit(const FusedArgs<float>& a, const FPhase& ph, int NB) {
+  int best = NB - 1, bestc = 1 << 30;
+  for (int b = NB - 1; b >= 0; --b) {
+    int cnt = 0;
+    for (int oi = ph.op0; oi < ph.op0 + ph.nop; ++oi) {
+      const FOp& op = a.op[oi];
+      if (op.type != FOP_D1 && op.type != FOP_D2 && touches(op, b)) ++cnt;
+    }
+    if (cnt < bestc) best = b, bestc = cnt;
+  }
+  return best;
+}
+
+// emits op on the pairs; false: the op needs the scalar fallback
+static bool emit_op_packed(std::ostringstream& o, const FOp& op, int NB, int P) {
+  const int D = 1 << NB;
+  auto M = [&](int e) {
+    std::ostringstream s;
+    s << "a.mat[" << (op.moff + e) << "]";
+    return s.str();
+  };
+  auto bcs = [&](const char* name, int e, bool neg) {  // broadcast coefficient pair
+    o << " const u64 " << name << "=bc(" << (neg ? "-" : "") << M(e) << ");";
+  };
+  auto k0 = [&](int j) { return !(j & (1 << P)); };
+  auto pairs = [&](int B, auto&& body) {
+    for (int j = 0; j < D; ++j)
+      if (k0(j) && !(j & (1 << B))) body(j, j | (1 << B));
+  };
+  auto quads = [&](int B0, int B1, auto&& body) {
+    for (int j = 0; j < D; ++j)
+      if (k0(j) && !(j & ((1 << B0) | (1 << B1)))) {
+        const int q[4] = {j, j | (1 << B1), j | (1 << B0), j | (1 << B0) | (1 << B1)};
+        body(q);
+      }
+  };
+  const int b0 = op.b0, b1 = op.b1;
+  if (op.type == FOP_D1 || op.type == FOP_D2) {
+    // diagonal: coefficient index of each lane; per-lane pairs when the index
+    // depends on bit P
+    o << "    {";
+    for (int j = 0; j < D; ++j) {
+      if (!k0(j)) continue;
+      int r[2];
+      for (int l = 0; l < 2; ++l) {
+        const int jj = l ? (j | (1 << P)) : j;
+        r[l] = op.type == FOP_D1 ? ((jj >> b0) & 1) : ((jj >> b0) & 1) * 2 + ((jj >> b1) & 1);
+      }
+      const int base = 0;
+      (void)base;
+      o << "\n      { const u64 er=pk(" << M(2 * r[0]) << "," << M(2 * r[1]) << "), ei=pk(" << M(2 * r[0] + 1) << ","
+        << M(2 * r[1] + 1) << "), nei=pk(-" << M(2 * r[0] + 1) << ",-" << M(2 * r[1] + 1) << "); const u64 ar=X" << j
+        << ", ai=Y" << j << "; X" << j << "=ffma2(er,ar,fmul2(nei,ai)); Y" << j << "=ffma2(er,ai,fmul2(ei,ar)); }";
+    }
+    o << "\n    }\n";
+    return true;
+  }
+  if (touches(op, P)) return false;
+  switch (op.type) {
+    case FOP_G1:
+      o << "    {";
+      bcs("m0", 0, false), bcs("m1", 1, false), bcs("n1", 1, true), bcs("m2", 2, false), bcs("m3", 3, false);
+      bcs("n3", 3, true), bcs("m4", 4, false), bcs("m5", 5, false), bcs("n5", 5, true), bcs("m6", 6, false);
+      bcs("m7", 7, false), bcs("n7", 7, true);
+      o << "\n";
+      pairs(b0, [&](int j, int k) {
+        o << "      { const u64 ar=X" << j << ",ai=Y" << j << ",br=X" << k << ",bi=Y" << k << ";"
+          << " X" << j << "=ffma2(m0,ar,ffma2(n1,ai,ffma2(m2,br,fmul2(n3,bi))));"
+          << " Y" << j << "=ffma2(m0,ai,ffma2(m1,ar,ffma2(m2,bi,fmul2(m3,br))));"
+          << " X" << k << "=ffma2(m4,ar,ffma2(n5,ai,ffma2(m6,br,fmul2(n7,bi))));"
+          << " Y" << k << "=ffma2(m4,ai,ffma2(m5,ar,ffma2(m6,bi,fmul2(m7,br)))); }\n";
+      });
+      o << "    }\n";
+      return true;
+    case FOP_R1:
+      o << "    {";
+      bcs("a0", 0, false), bcs("a1", 1, false), bcs("a2", 2, false), bcs("a3", 3, false);
+      o << "\n";
+      pairs(b0, [&](int j, int k) {
+        o << "      { const u64 ar=X" << j << ",ai=Y" << j << ",br=X" << k << ",bi=Y" << k << "; X" << j
+          << "=ffma2(a0,ar,fmul2(a1,br)); Y" << j << "=ffma2(a0,ai,fmul2(a1,bi)); X" << k << "=ffma2(a2,ar,fmul2(a3,br)); Y" << k
+          << "=ffma2(a2,ai,fmul2(a3,bi)); }\n";
+      });
+      o << "    }\n";
+      return true;
+    case FOP_RX1:
+      o << "    {";
+      bcs("ca", 0, false), bcs("cb", 1, false), bcs("nb", 1, true);
+      o << "\n";
+      pairs(b0, [&](int j, int k) {
+        o << "      { const u64 ar=X" << j << ",ai=Y" << j << ",br=X" << k << ",bi=Y" << k << "; X" << j
+          << "=ffma2(ca,ar,fmul2(nb,bi)); Y" << j << "=ffma2(ca,ai,fmul2(cb,br)); X" << k << "=ffma2(ca,br,fmul2(nb,ai)); Y" << k
+          << "=ffma2(ca,bi,fmul2(cb,ar)); }\n";
+      });
+      o << "    }\n";
+      return true;
+    case FOP_X1:
+      if (op.unit) {
+        pairs(b0, [&](int j, int k) {
+          o << "    { const u64 tr=X" << j << ",ti=Y" << j << "; X" << j << "=X" << k << "; Y" << j << "=Y" << k << "; X" << k
+            << "=tr; Y" << k << "=ti; }\n";
+        });
+      } else {
+        o << "    {";
+        bcs("p0r", 0, false), bcs("p0i", 1, false), bcs("n0i", 1, true);
+        bcs("p1r", 2, false), bcs("p1i", 3, false), bcs("n1i", 3, true);
+        o << "\n";
+        pairs(b0, [&](int j, int k) {
+          o << "      { const u64 ar=X" << j << ",ai=Y" << j << ",br=X" << k << ",bi=Y" << k << "; X" << j
+            << "=ffma2(p0r,br,fmul2(n0i,bi)); Y" << j << "=ffma2(p0r,bi,fmul2(p0i,br)); X" << k << "=ffma2(p1r,ar,fmul2(n1i,ai)); Y" << k
+            << "=ffma2(p1r,ai,fmul2(p1i,ar)); }\n";
+        });
+        o << "    }\n";
+      }
+      return true;
+    case FOP_G2:
+      o << "    {";
+      for (int e = 0; e < 32; ++e) {
+        o << " const u64 g" << e << "=bc(" << M(e) << ");";
+        if (e & 1) o << " const u64 ng" << e << "=bc(-" << M(e) << ");";
+      }
+      o << "\n";
+      quads(b0, b1, [&](const int* q) {
+        o << "      { const u64 ";
+        for (int c = 0; c < 4; ++c) o << (c ? "," : "") << "r" << c << "=X" << q[c] << ",i" << c << "=Y" << q[c];
+        o << ";";
+        for (int r = 0; r < 4; ++r) {
+          std::string re = "fmul2(g" + std::to_string(8 * r) + ",r0)", im = "fmul2(g" + std::to_string(8 * r) + ",i0)";
+          re = "ffma2(ng" + std::to_string(8 * r + 1) + ",i0," + re + ")";
+          im = "ffma2(g" + std::to_string(8 * r + 1) + ",r0," + im + ")";
+          for (int c = 1; c < 4; ++c) {
+            const std::string gr = std::to_string(8 * r + 2 * c), gi = std::to_string(8 * r + 2 * c + 1);
+            const std::string cs = std::to_string(c);
+            re = "ffma2(g" + gr + ",r" + cs + ",ffma2(ng" + gi + ",i" + cs + "," + re + "))";
+            im = "ffma2(g" + gr + ",i" + cs + ",ffma2(g" + gi + ",r" + cs + "," + im + "))";
+          }
+          o << " X" << q[r] << "=" << re << "; Y" << q[r] << "=" << im << ";";
+        }
+        o << " }\n";
+      });
+      o << "    }\n";
+      return true;
+    case FOP_P2:
+    case FOP_CX:
+    case FOP_SW: {
+      int Pm[4];
+      bool unit = true;
+      if (op.type == FOP_CX) {
+        Pm[0] = 0, Pm[1] = 1, Pm[2] = 3, Pm[3] = 2;
+      } else if (op.type == FOP_SW) {
+        Pm[0] = 0, Pm[1] = 2, Pm[2] = 1, Pm[3] = 3;
+      } else {
+        for (int r = 0; r < 4; ++r) Pm[r] = (op.flags >> (2 * r)) & 3;
+        unit = op.unit != 0;
+      }
+      o << "    {";
+      if (!unit)
+        for (int e = 0; e < 8; ++e) {
+          o << " const u64 h" << e << "=bc(" << M(e) << ");";
+          if (e & 1) o << " const u64 nh" << e << "=bc(-" << M(e) << ");";
+        }
+      o << "\n";
+      quads(b0, b1, [&](const int* q) {
+        o << "      { const u64 ";
+        for (int c = 0; c < 4; ++c) o << (c ? "," : "") << "r" << c << "=X" << q[c] << ",i" << c << "=Y" << q[c];
+        o << ";";
+        for (int r = 0; r < 4; ++r) {
+          if (unit)
+            o << " X" << q[r] << "=r" << Pm[r] << "; Y" << q[r] << "=i" << Pm[r] << ";";
+          else
+            o << " X" << q[r] << "=ffma2(h" << 2 * r << ",r" << Pm[r] << ",fmul2(nh" << 2 * r + 1 << ",i" << Pm[r] << ")); Y"
+              << q[r] << "=ffma2(h" << 2 * r << ",i" << Pm[r] << ",fmul2(h" << 2 * r + 1 << ",r" << Pm[r] << "));";
+        }
+        o << " }\n";
+      });
+      o << "    }\n";
+      return true;
+    }
+  }
+  return false;
+}
+
+// complex64 specialised passes run packed (BTGPU_JIT_PACKED=0: scalar code)
+static bool jit_packed() {
+  static const bool v = env_int("BTGPU_JIT_PACKED", 1, 0, 1) != 0;
+  return v;
+}
+
 template <typename R>
 static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, const std::string& name) {
   const bool f = sizeof(R) == 4;
@@ -319,7 +531,43 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
     }
     for (int j = 0; j < D; ++j)
       o << "    { const " << T2 << " v = tile[sb ^ " << offs[j] << "]; x" << j << " = v.x; y" << j << " = v.y; }\n";
-    for (int oi = ph.op0; oi < ph.op0 + ph.nop; ++oi) emit_op(o, a.op[oi], NB);
+    if (f && jit_packed()) {
+      const int P = choose_pack_bit(*reinterpret_cast<const FusedArgs<float>*>(&a), ph, NB);
+      auto pack = [&]() {
+        for (int j = 0; j < D; ++j)
+          if (!(j & (1 << P)))
+            o << "    X" << j << "=pk(x" << j << ",x" << (j | (1 << P)) << "); Y" << j << "=pk(y" << j << ",y"
+              << (j | (1 << P)) << ");\n";
+      };
+      auto unpack = [&]() {
+        for (int j = 0; j < D; ++j)
+          if (!(j & (1 << P)))
+            o << "    x" << j << "=plo(X" << j << "); x" << (j | (1 << P)) << "=phi(X" << j << "); y" << j << "=plo(Y" << j
+              << "); y" << (j | (1 << P)) << "=phi(Y" << j << ");\n";
+      };
+      o << "    u64 ";
+      bool first = true;
+      for (int j = 0; j < D; ++j)
+        if (!(j & (1 << P))) {
+          o << (first ? "" : ", ") << "X" << j << ", Y" << j;
+          first = false;
+        }
+      o << ";\n";
+      pack();
+      for (int oi = ph.op0; oi < ph.op0 + ph.nop; ++oi) {
+        std::ostringstream po;
+        if (emit_op_packed(po, a.op[oi], NB, P)) {
+          o << po.str();
+        } else {  // scalar fallback for an op on the pack bit
+          unpack();
+          emit_op(o, a.op[oi], NB);
+          pack();
+        }
+      }
+      unpack();
+    } else {
+      for (int oi = ph.op0; oi < ph.op0 + ph.nop; ++oi) emit_op(o, a.op[oi], NB);
+    }
     for (int j = 0; j < D; ++j) o << "    tile[sb ^ " << offs[j] << "] = " << T2 << "{x" << j << ", y" << j << "};\n";
     o << "    __syncthreads();\n    }\n";
   }
@@ -344,7 +592,7 @@ template <typename R>
 static std::string structure_key(const FusedArgs<R>& a) {
   std::ostringstream k;
   k << (sizeof(R) == 4 ? 'f' : 'd') << a.M << ':' << a.c << ':' << bt_jit_min_blocks() << ':'
-    << (a.nphase ? (int)a.ph[0].nreg : 0) << ':';
+    << (a.nphase ? (int)a.ph[0].nreg : 0) << ':' << (sizeof(R) == 4 && jit_packed() ? 'p' : 's') << ':';
   for (int i = 0; i < a.M; ++i) k << a.tbits[i] << ',';
   for (int p = 0; p < a.nphase; ++p) {
     const FPhase& ph = a.ph[p];

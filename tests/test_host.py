@@ -82,3 +82,25 @@ def test_twirl_frames_preserve_cnot():
             tot = after @ Gq @ before
             ph = tot[np.nonzero(np.abs(tot) > 1e-12)][0] / Gq[np.nonzero(np.abs(Gq) > 1e-12)][0]
             assert np.allclose(tot, ph * Gq, atol=1e-12), f
+
+
+def test_variational_parameter_binding():
+    """Parameters are consumed in op order, as many per op as its matrix function
+    takes (_find_argument_number, src/vqa.jl:224-235); a wrong count is an error."""
+    import bluetangle_gpu as bt
+    import bluetangle_gpu.vqa as V
+
+    def u2(a, b):
+        return np.array([[1, -np.exp(1j * b)], [np.exp(1j * a), np.exp(1j * (a + b))]]) / np.sqrt(2)
+
+    def ry(t):
+        return np.array([[np.cos(t / 2), -np.sin(t / 2)], [np.sin(t / 2), np.cos(t / 2)]])
+
+    ops = [bt.Op("RY", ry, 1), bt.Op("H", 2), bt.Op("U2", u2, 2), bt.Op("CNOT", 1, 2), bt.Op("RY", ry, 2)]
+    assert V.arg_counts(ops) == [1, 0, 2, 0, 1]
+    p = np.array([0.1, 0.2, 0.3, 0.4])
+    b = V._bound(ops, V.arg_counts(ops), p)
+    assert np.allclose(b[0][1], ry(0.1)) and b[1][1] is None and np.allclose(b[2][1], u2(0.2, 0.3))
+    assert np.allclose(b[4][1], ry(0.4))
+    with pytest.raises(ValueError):
+        V._bound(ops, V.arg_counts(ops), p[:3])

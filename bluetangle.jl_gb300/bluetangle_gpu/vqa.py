@@ -41,6 +41,8 @@ def arg_counts(ops):
 
 def _bound(ops, counts, p):
     """(op, matrix) per op with the parametrised ops evaluated at p, in order."""
+    if sum(counts) != len(p):
+        raise ValueError(f"the ansatz takes {sum(counts)} parameters, {len(p)} given")
     out, c = [], 0
     for op, k in zip(ops, counts):
         if k:

@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--cpu-n", type=int, default=24, help="qubits of the CPU baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="brickwork", choices=["brickwork", "serve", "c1", "c2", "c3"],
+    ap.add_argument("--workload", default="brickwork", choices=["brickwork", "serve", "c1", "c2", "c3", "vqa"],
                     help="brickwork: 33q c64 depth-30 (default); serve: the serving stream; c1: 12q c128 "
                          "brickwork + <Z> + shots; c2: 10q noisy density matrix; c3: 20q trajectories")
     ap.add_argument("--c3-n", type=int, default=20)
@@ -853,13 +853,94 @@ def run_c3(args):
     ctx.close()
 
 
+def run_vqa(args):
+    """Parameter-shift gradients of a hardware-efficient ansatz (parametrised RY, RZ
+    on every qubit, CNOT ladder) for <H> of 3n random 2-local Pauli terms: the
+    2P + 1 shifted evaluations of loss_and_grad_paramshift as one batch.  A step is
+    one gradient; 12 qubits depth 6 (P = 144: one CTA per evaluation) and 20 qubits
+    depth 4 (P = 160: fused plan, angles rewritten per evaluation)."""
+    import bluetangle_gpu as bt
+    import bluetangle_gpu.vqa as V
+    from bluetangle_gpu.serving import random_terms
+
+    def ry(t):
+        c, s = math.cos(t / 2), math.sin(t / 2)
+        return np.array([[c, -s], [s, c]], dtype=np.complex128)
+
+    def rz(t):
+        return np.array([[np.exp(-0.5j * t), 0], [0, np.exp(0.5j * t)]], dtype=np.complex128)
+
+    def hea(n, depth):
+        ops = []
+        for _ in range(depth):
+            for q in range(1, n + 1):
+                ops += [bt.Op("RY", ry, q), bt.Op("RZ", rz, q)]
+            ops += [bt.Op("CNOT", q, q + 1) for q in range(1, n)]
+        return ops
+
+    ctx = bt.Context(0, seed=args.seed)
+    bt.Context._default = ctx
+    out = {}
+    for n, depth in ((12, 6), (20, 4)):
+        ops = hea(n, depth)
+        P = sum(V.arg_counts(ops))
+        terms = random_terms(np.random.default_rng(args.seed + n), n, 3 * n)
+        rng = np.random.default_rng(args.seed)
+        ps = [rng.uniform(0, 2 * np.pi, P) for _ in range(args.warmup + args.steps)]
+        res = {}
+
+        def grad(i):
+            res[i] = V.loss_and_grad_paramshift(ps[i], ops, n, terms, prec=args.prec)
+
+        ms, host, launches, clk = _timed(ctx, grad, args.steps, args.warmup)
+        # plain per-call path: every evaluation gate by gate (engine.apply) + <H>, a sample
+        k = 8
+        t0 = time.perf_counter()
+        for j in range(k):
+            st = V.variational_apply(ps[0], ops, n, prec="c128", ctx=ctx)
+            V._expect_members(st, terms)
+            st.free()
+        plain_eval = k / (time.perf_counter() - t0)
+        out[f"{n}q_depth{depth}"] = {"params": P, "evaluations_per_gradient": 2 * P + 1,
+                                     "gradients_per_s": args.steps / (ms / 1e3),
+                                     "evaluations_per_s": args.steps * (2 * P + 1) / (ms / 1e3),
+                                     "executor": "program (one CTA per evaluation)" if n <= 14 else
+                                                 "fused plan (angles rewritten per evaluation)",
+                                     "plain_c128_evaluations_per_s": plain_eval, "gpu_launches": launches,
+                                     "clocks": clk}
+        if not args.no_cpu:
+            O = _oracle()
+            t0 = time.perf_counter()
+            cnt = 0
+            counts = V.arg_counts(ops)
+            while time.perf_counter() - t0 < min(args.cpu_seconds, 8.0) or cnt < 2:
+                psi = np.zeros(2 ** n, complex)
+                psi[0] = 1
+                for op, mat in V._bound(ops, counts, ps[0]):
+                    qs, cs = V._qubits(op)
+                    psi = O.apply_k(psi, op.mat if mat is None else mat, qs, cs)
+                _ = sum(c * O.expect_pauli_sv(psi, x, z) for c, x, z in terms)
+                cnt += 1
+            rate = cnt / (time.perf_counter() - t0)
+            out[f"{n}q_depth{depth}"]["cpu_baseline"] = {
+                "value": rate / (2 * P + 1), "unit": "gradients/s", "cores": 1, "kind": "port",
+                "sample": f"{cnt} sequential evaluations through the oracle (the reference's loop), 1 thread"}
+    head = out["12q_depth6"]
+    line = {"metric": "parameter-shift gradients/s", "value": head["gradients_per_s"], "unit": "gradients/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": args.prec, "data": "synthetic",
+            "config": {"workload": "paramshift-hea-12q-depth6 (+20q-depth4)", "cases": out}}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
     elif a.workload == "serve":
         run_serve(a)
-    elif a.workload in ("c1", "c2", "c3"):
-        {"c1": run_c1, "c2": run_c2, "c3": run_c3}[a.workload](a)
+    elif a.workload in ("c1", "c2", "c3", "vqa"):
+        {"c1": run_c1, "c2": run_c2, "c3": run_c3, "vqa": run_vqa}[a.workload](a)
     else:
         run_ours(a)

@@ -223,9 +223,14 @@ class Program:
             pass
 
     def add_gate(self, mats, qubits):
-        """mats: one matrix, or a list of batch matrices (per member)."""
-        per = isinstance(mats, (list, tuple))
-        buf = np.ascontiguousarray(np.concatenate([_cm(m).ravel() for m in mats]) if per else _cm(mats).ravel())
+        """mats: one matrix, or batch matrices (per member) as a list or a
+        (batch, d, d) array."""
+        if isinstance(mats, np.ndarray) and mats.ndim == 3:  # column-major per matrix in one step
+            per = True
+            buf = np.ascontiguousarray(np.transpose(mats.astype(np.complex128, copy=False), (0, 2, 1))).ravel()
+        else:
+            per = isinstance(mats, (list, tuple))
+            buf = np.ascontiguousarray(np.concatenate([_cm(m).ravel() for m in mats]) if per else _cm(mats).ravel())
         q = _i32(qubits)
         self.ctx.check(L.lib().bt_program_add_gate(self.h, len(q), _ptr(q), _ptr(buf), int(per)))
         self.nops += 1

@@ -155,15 +155,81 @@ def loss(pars, ops, n, terms, prec="c128", ctx=None):
 def loss_and_grad_paramshift(p, ops, n, terms, prec="c128", ctx=None, executor="auto"):
     """(l, g) of loss_and_grad_paramshift (src/vqa.jl:590-611): the loss at p and,
     for every parameter i, (l(p + pi/2 e_i) - l(p - pi/2 e_i)) / 2; all 2P + 1
-    evaluations in one batch."""
+    evaluations in one batch.  Evaluation 0 is at p, 2i+1 and 2i+2 at p -+ shift of
+    parameter i: every op keeps its matrix at p except in the two evaluations that
+    shift one of its parameters, so each op's matrix is evaluated once at p and
+    twice per parameter it owns."""
+    from . import trajectories as T
+    ctx = ctx or Context.default()
     p = np.asarray(p, dtype=float)
     P = len(p)
-    plist = [p]
+    counts = arg_counts(ops)
+    if sum(counts) != P:
+        raise ValueError(f"the ansatz takes {sum(counts)} parameters, {P} given")
+    base = _bound(ops, counts, p)
+    owner, first = [], []  # op owning each parameter; each op's first parameter
+    c = 0
+    for i, k in enumerate(counts):
+        first.append(c)
+        owner += [i] * k
+        c += k
+    shifted = []  # per parameter: (matrix at p + shift, matrix at p - shift)
     for i in range(P):
+        op = ops[owner[i]]
+        f0, k = first[owner[i]], counts[owner[i]]
+        pair = []
         for s in (SHIFT, -SHIFT):
-            q = p.copy()
-            q[i] = p[i] + s
-            plist.append(q)
-    vals = losses(ops, n, plist, terms, prec, ctx, executor)
+            q = p[f0:f0 + k].copy()
+            q[i - f0] += s
+            pair.append(np.asarray(op.mat(*q), dtype=np.complex128))
+        shifted.append(pair)
+    B = 2 * P + 1
+    fits = n <= T.SHARED_MAX_N[prec]
+    if executor == "program" or (executor == "auto" and fits):
+        prog = T.Program(n, B, prec, ctx)
+        for j, (op, mat) in enumerate(base):
+            qs, cs = _qubits(op)
+            if op.q > 2 or len(qs) + len(cs) > 2:
+                raise ValueError("programs take ops on at most two qubits (control included)")
+            m0 = op.mat if mat is None else mat
+            if counts[j]:
+                stack = np.broadcast_to(m0, (B,) + m0.shape).copy()
+                for i in range(first[j], first[j] + counts[j]):
+                    stack[2 * i + 1], stack[2 * i + 2] = shifted[i]
+                if cs:
+                    stack = np.stack([_ctrl(m) for m in stack])
+                prog.add_gate(stack, cs + qs)
+            else:
+                prog.add_gate(_ctrl(np.asarray(m0)) if cs else m0, cs + qs)
+        st = GPUState(n, prec, B, ctx)
+        prog.run(st, records=False)
+        vals = _expect_members(st, terms)
+        st.free()
+    else:
+        plan = Plan(n, "sv", prec, ctx)
+        for op, mat in base:
+            if mat is None:
+                plan.add(op)
+            else:
+                qs, cs = _qubits(op)
+                plan.add_matrix(mat, qs, cs)
+        plan.compile(True)
+        st = GPUState(n, prec, 1, ctx)
+        vals = np.empty(B)
+
+        def run(m):
+            st.set_zero()
+            plan.run(st)
+            vals[m] = _expect_members(st, terms)[0]
+
+        run(0)
+        for i in range(P):
+            j = owner[i]
+            plan.set_matrices([(j, shifted[i][0])])
+            run(2 * i + 1)
+            plan.set_matrices([(j, shifted[i][1])])
+            run(2 * i + 2)
+            plan.set_matrices([(j, base[j][1])])
+        st.free()
     g = 0.5 * (vals[1::2] - vals[2::2])
     return float(vals[0]), g

@@ -84,6 +84,26 @@ def test_twirl_frames_preserve_cnot():
             assert np.allclose(tot, ph * Gq, atol=1e-12), f
 
 
+@pytest.mark.parametrize("model,p", [("bit_flip", 0.02), ("amplitude_damping", 0.1), ("depolarizing", 0.05)])
+def test_mitigation_matrix_equals_reference_construction(oracle, model, p):
+    """inv(A) from the single-qubit confusion matrix equals the reference's
+    construction (src/ops.jl:472-488): |a><a| through the readout channel on every
+    qubit, diagonals as columns, dense inverse."""
+    import bluetangle_gpu.mitigation as Mi
+    from bluetangle_gpu.noise import noise_model1
+    n = 3
+    kraus = noise_model1(model, p)
+    cols = []
+    for a in range(2 ** n):
+        rho = np.zeros((2 ** n, 2 ** n), complex)
+        rho[a, a] = 1
+        for q in range(1, n + 1):
+            rho = oracle.dm_channel(rho, kraus, q)
+        cols.append(np.real(np.diag(rho)))
+    ref = np.linalg.inv(np.array(cols).T)
+    assert np.abs(Mi.mitigation_matrix(n, kraus) - ref).max() < 1e-12
+
+
 def test_variational_parameter_binding():
     """Parameters are consumed in op order, as many per op as its matrix function
     takes (_find_argument_number, src/vqa.jl:224-235); a wrong count is an error."""

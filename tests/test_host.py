@@ -104,6 +104,41 @@ def test_mitigation_matrix_equals_reference_construction(oracle, model, p):
     assert np.abs(Mi.mitigation_matrix(n, kraus) - ref).max() < 1e-12
 
 
+QASM_SAMPLE = """OPENQASM 2.0;
+include "qelib1.inc";   // boilerplate
+qreg q[4]; creg c[4];
+h q[0]; sdg q[1]; tdg q[2]; sx q[3];
+rx(pi/2) q[0]; u3(0.1,0.2,-pi/4) q[1]; u2(0.3, 0.4) q[2]; u1(0.5) q[3];
+cx q[0],q[1]; cz q[2], q[3]; cp(0.25) q[1],q[2];
+cu3(0.7,0,0) q[0],q[3]; crz(0.9) q[3],q[0];
+swap q[1],q[2]; rzz(0.2) q[0],q[1]; fsim(0.1,0.2) q[2],q[3];
+ccx q[0],q[1],q[2]; cswap q[3],q[0],q[1];
+barrier q;
+reset q[2];
+measure q[1] -> c[1];
+"""
+
+
+def test_qasm_reader_follows_reference_rules():
+    """Statement by statement as from_qasm (src/qasm.jl:285-421): names, 1-based
+    qubits, cx/cz/cp/cu3/crz as controlled one-qubit ops, ccx/cswap with the
+    reference's argument order."""
+    import bluetangle_gpu.qasm as Q
+    ops = Q.from_qasm(QASM_SAMPLE)
+    got = [(type(o).__name__, o.name, o.qubit, getattr(o, "target_qubit", -1), getattr(o, "control", -2))
+           for o in ops]
+    want = [("Op", "H", 1, -1, -2), ("Op", "SD", 2, -1, -2), ("Op", "TD", 3, -1, -2), ("Op", "XSQRT", 4, -1, -2),
+            ("Op", "rx(pi/2)", 1, -1, -2), ("Op", "U3(0.1,0.2,-pi/4)", 2, -1, -2), ("Op", "U2(0.3,0.4)", 3, -1, -2),
+            ("Op", "U1(0.5)", 4, -1, -2), ("Op", "X", 2, -1, 1), ("Op", "Z", 4, -1, 3), ("Op", "U1(0.25)", 3, -1, 2),
+            ("Op", "ry(0.7)", 4, -1, 1), ("Op", "rz(0.9)", 1, -1, 4), ("Op", "SWAP", 2, 3, -2),
+            ("Op", "RZZ(0.2)", 1, 2, -2), ("Op", "FSIM(0.1,0.2)", 3, 4, -2), ("Op", "CX", 1, 3, 2),
+            ("Op", "SWAP", 1, 2, 4)]  # cswap a,b,c -> Op("CSWAP", b, a, c): SWAP(b, c) controlled by a
+    assert got[:len(want)] == want
+    assert type(ops[-2]).__name__ == "OpQC" and ops[-1].name == "MZ" and ops[-1].qubit == 2
+    with pytest.raises(ValueError):
+        Q.from_qasm("qreg q[2]; foo q[0];")
+
+
 def test_variational_parameter_binding():
     """Parameters are consumed in op order, as many per op as its matrix function
     takes (_find_argument_number, src/vqa.jl:224-235); a wrong count is an error."""

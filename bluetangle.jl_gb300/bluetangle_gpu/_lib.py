@@ -81,6 +81,7 @@ SIGNATURES = {
     "bt_program_set_gate": (i32, [P, i64, P]),
     "bt_program_run": (i32, [P, P, P, u64, P]),
     "bt_program_set_executor": (i32, [P, i32]),
+    "bt_shadow_accumulate": (i32, [P, i64, P, P]),
     "bt_serve_create": (i32, [i32, i32, u64, u64, ctypes.POINTER(P)]),
     "bt_serve_destroy": (i32, [P]),
     "bt_serve_add_plan_client": (i32, [P, P, i32, P, P, P, P]),

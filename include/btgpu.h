@@ -226,6 +226,13 @@ int bt_program_set_executor(bt_program* p, int executor);
  * nrecords int32, member-major (may be NULL) */
 int bt_program_run(bt_program* p, bt_state* s, const double* uniforms, uint64_t seed, int32_t* records);
 
+/* ----------------------------------------------------------------- shadows */
+/* rho = (1/nsnap) sum_m (x)_q T[codes[m*n + q]] into a density matrix of n <= 14
+ * qubits (shadow, src/ops.jl:145-185): codes[m*n + q] = 2*basis + outcome of qubit
+ * q+1 in snapshot m, tables holds the 6 single-qubit factors 3 U^dagger|b><b|U - I
+ * as row-major interleaved complex 2x2 matrices (48 doubles) */
+int bt_shadow_accumulate(bt_state* rho, int64_t nsnap, const uint8_t* codes, const double* tables);
+
 /* ----------------------------------------------------------------- serving */
 /* No counterpart in the reference: its VQE / Trotter loops (variational_apply +
  * expect(state, H), src/vqa.jl:420-456, src/func.jl:100) run one call at a time.

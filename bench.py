@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--cpu-n", type=int, default=24, help="qubits of the CPU baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--autotune", action="store_true",
+                    help="plan mode: time the fusion configurations on the state and keep the fastest")
     ap.add_argument("--workload", default="brickwork", choices=["brickwork", "serve", "c1", "c2", "c3", "vqa"],
                     help="brickwork: 33q c64 depth-30 (default); serve: the serving stream; c1: 12q c128 "
                          "brickwork + <Z> + shots; c2: 10q noisy density matrix; c3: 20q trajectories")
@@ -254,6 +256,7 @@ def run_ours(args):
     st = bt.zero_state(args.n, args.prec, 1, ctx)
     lib = bt.lib()
     plan = None
+    tuned = None
     if args.mode == "plan":
         # the whole circuit compiled once into fused tile passes; a step runs all of it
         plan = bt.Plan(args.n, "sv", args.prec, ctx)
@@ -261,6 +264,8 @@ def run_ours(args):
             for m, qs in prog:
                 plan.add_matrix(m, qs)
         plan.compile(True)
+        if args.autotune:  # fusion width / register bits / packed code chosen by timing them here
+            tuned = plan.autotune(st, reps=1)
         pstats = plan.stats()
     # pre-packed column-major matrices and qubit arrays (the circuit is resident on the host)
     packed = []
@@ -364,8 +369,11 @@ def run_ours(args):
                                     % (args.depth, sum(lg for _, lg in packed))) if plan is not None else
                                    "one brickwork layer (logical gates: n one-qubit + CNOTs)",
                            "plan": pstats if plan is not None else None,
-                           "tuning": {k: os.environ.get(k) for k in ("BTGPU_JIT_MINB", "BTGPU_PLAN_MAX_OPS")
+                           "tuning": {k: os.environ.get(k) for k in ("BTGPU_JIT_MINB", "BTGPU_PLAN_MAX_OPS",
+                                                                      "BTGPU_TILE_RB", "BTGPU_JIT_PACKED")
                                       if os.environ.get(k)},
+                           "autotune": ([{"max_ops": c[0], "tile_rb": c[1], "packed": c[2], "s_per_circuit": t}
+                                         for c, t in tuned] if tuned else None),
                            "passes_per_step": passes / args.steps, "global_batch": 1, "seq_len": None,
                            "parallelism": f"replicas x{ws}", "l2": "state larger than L2, no flush needed",
                            "state_bytes": (2 ** args.n) * esize},

@@ -479,6 +479,35 @@ class Plan:
         self.ctx.check(L.lib().bt_plan_set_matrices(self.h, len(updates), _ptr(idx), _ptr(mats)))
         return self
 
+    def set_tuning(self, max_ops=0, tile_rb=0, packed=-1):
+        """Fusion width (gates per pass), register bits per thread (4 or 5) and
+        two-lane arithmetic of the fused passes; 0 / -1 keep the defaults.  Takes
+        effect at the next compile."""
+        self.ctx.check(L.lib().bt_plan_set_tuning(self.h, int(max_ops), int(tile_rb), int(packed)))
+        return self
+
+    def autotune(self, state, configs=None, reps=2):
+        """Times each tuning configuration (max_ops, tile_rb, packed) on `state`
+        (the timing runs overwrite it), keeps the fastest compiled and returns
+        [(config, seconds per run)] in the order tried."""
+        import time
+        if configs is None:
+            configs = ([(64, 5, 1), (64, 5, 0), (32, 5, 1), (128, 5, 1), (64, 4, 1)] if self.prec in ("c64", "complex64")
+                       else [(64, 0, -1), (32, 0, -1), (128, 0, -1)])
+        results = []
+        for cfg in configs:
+            self.set_tuning(*cfg).compile(True)
+            self.run(state)  # loads the specialised kernels
+            self.ctx.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                self.run(state)
+            self.ctx.synchronize()
+            results.append((tuple(cfg), (time.perf_counter() - t0) / reps))
+        best = min(results, key=lambda r: r[1])[0]
+        self.set_tuning(*best).compile(True)
+        return results
+
     def stats(self):
         v = [ctypes.c_int64(0) for _ in range(5)]
         self.ctx.check(L.lib().bt_plan_stats(self.h, *[ctypes.byref(x) for x in v]))

@@ -460,8 +460,9 @@ static bool emit_op_packed(std::ostringstream& o, const FOp& op, int NB, int P) 
   return false;
 }
 
-// complex64 specialised passes run packed (BTGPU_JIT_PACKED=0: scalar code)
-static bool jit_packed() {
+// complex64 specialised passes run packed unless a plan says otherwise
+// (BTGPU_JIT_PACKED=0: scalar code by default)
+bool bt_jit_packed_default() {
   static const bool v = env_int("BTGPU_JIT_PACKED", 1, 0, 1) != 0;
   return v;
 }
@@ -531,7 +532,7 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
     }
     for (int j = 0; j < D; ++j)
       o << "    { const " << T2 << " v = tile[sb ^ " << offs[j] << "]; x" << j << " = v.x; y" << j << " = v.y; }\n";
-    if (f && jit_packed()) {
+    if (f && a.packed) {
       const int P = choose_pack_bit(*reinterpret_cast<const FusedArgs<float>*>(&a), ph, NB);
       auto pack = [&]() {
         for (int j = 0; j < D; ++j)
@@ -592,7 +593,7 @@ template <typename R>
 static std::string structure_key(const FusedArgs<R>& a) {
   std::ostringstream k;
   k << (sizeof(R) == 4 ? 'f' : 'd') << a.M << ':' << a.c << ':' << bt_jit_min_blocks() << ':'
-    << (a.nphase ? (int)a.ph[0].nreg : 0) << ':' << (sizeof(R) == 4 && jit_packed() ? 'p' : 's') << ':';
+    << (a.nphase ? (int)a.ph[0].nreg : 0) << ':' << (sizeof(R) == 4 && a.packed ? 'p' : 's') << ':';
   for (int i = 0; i < a.M; ++i) k << a.tbits[i] << ',';
   for (int p = 0; p < a.nphase; ++p) {
     const FPhase& ph = a.ph[p];

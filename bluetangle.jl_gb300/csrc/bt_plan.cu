@@ -59,6 +59,8 @@ struct bt_plan {
   bool compiled = false;
   int compile_mode = 0;
   int64_t nphases = 0;
+  // tuning (bt_plan_set_tuning; 0 / -1: the library defaults)
+  int tune_max_ops = 0, tune_rb = 0, tune_packed = -1;
   // specialised kernel of each pass (bt_jit.cu), published when compiled; the
   // background compiler of a tiered plan writes them while runs read them
   std::unique_ptr<std::atomic<void*>[]> jit;
@@ -492,7 +494,9 @@ int bt_plan_compile(bt_plan* p, int mode) {
   const bool c64 = p->prec == BT_PREC_C64;
   // register bits per thread: a tuned width only where every pass gets its
   // specialised kernel before the first run (the generic kernel has one width)
-  const int NB = (mode == 0 && bt_jit_available()) ? bt_tile_rb(c64) : (c64 ? BT_TILE_RB_C64 : BT_TILE_RB_C128);
+  const int rb_tuned = c64 ? (p->tune_rb ? p->tune_rb : bt_tile_rb(true)) : BT_TILE_RB_C128;
+  const int NB = (mode == 0 && bt_jit_available()) ? rb_tuned : (c64 ? BT_TILE_RB_C64 : BT_TILE_RB_C128);
+  const int packed = p->tune_packed >= 0 ? p->tune_packed : (int)bt_jit_packed_default();
   // the tile covers the whole state when the state is smaller than the default
   // tile, down to 2^(M - NB) = 32 threads per CTA
   const int M = std::min(c64 ? BT_TILE_M_C64 : BT_TILE_M_C128, p->nbits);
@@ -500,7 +504,7 @@ int bt_plan_compile(bt_plan* p, int mode) {
   const bool fuse = (mode == 0 || mode == 2) && M >= NB + 5;
   // specialised kernels compile in time superlinear in their length: bound the
   // ops of a pass when they will be specialised
-  const int max_ops = bt_jit_available() ? bt_jit_max_ops() : BT_FUSED_MAX_OPS;
+  const int max_ops = bt_jit_available() ? (p->tune_max_ops ? p->tune_max_ops : bt_jit_max_ops()) : BT_FUSED_MAX_OPS;
   std::vector<int> rem(p->gates.size());
   for (size_t i = 0; i < rem.size(); ++i) rem[i] = (int)i;
   const uint64_t lowmask = (1ULL << c) - 1;
@@ -536,6 +540,7 @@ int bt_plan_compile(bt_plan* p, int mode) {
       ps.args.resize(sizeof(FusedArgs<float>));
       build_fused<float>(p, take, Q, M, NB, c, kept, *reinterpret_cast<FusedArgs<float>*>(ps.args.data()), &nph,
                          ps.op_b0, ps.op_b1);
+      reinterpret_cast<FusedArgs<float>*>(ps.args.data())->packed = packed;
     } else {
       ps.args.resize(sizeof(FusedArgs<double>));
       build_fused<double>(p, take, Q, M, NB, c, kept, *reinterpret_cast<FusedArgs<double>*>(ps.args.data()), &nph,
@@ -564,6 +569,19 @@ int bt_plan_compile(bt_plan* p, int mode) {
     if (mode == 2) p->jit_thread = std::thread([p] { specialise(p); });
     else specialise(p);
   }
+  return BT_OK;
+}
+
+int bt_plan_set_tuning(bt_plan* p, int max_ops, int tile_rb, int packed) {
+  if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "plan is NULL");
+  if (max_ops < 0 || max_ops > BT_FUSED_MAX_OPS || (tile_rb != 0 && tile_rb != 4 && tile_rb != 5) || packed < -1 ||
+      packed > 1)
+    return bt_fail(p->ctx, BT_ERR_BAD_ARG, "tuning: 0 <= max_ops <= 192, tile_rb in {0, 4, 5}, packed in {-1, 0, 1}");
+  join_jit(p);
+  p->tune_max_ops = max_ops;
+  p->tune_rb = tile_rb;
+  p->tune_packed = packed;
+  p->compiled = false;
   return BT_OK;
 }
 

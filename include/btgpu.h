@@ -177,6 +177,11 @@ int bt_plan_set_matrices(bt_plan* p, int count, const int64_t* add_index, const 
  * by bt_plan_compile); the others run on the generic fused kernel */
 int bt_plan_stats(const bt_plan* p, int64_t* ngates, int64_t* npasses, int64_t* nfused, int64_t* nphases,
                   int64_t* njit);
+/* tuning of the fused passes (applies at the next bt_plan_compile; 0 / -1 keep
+ * the library default): gates per pass at most (1..192), register bits per
+ * thread of complex64 passes specialised before the first run (4 or 5), and
+ * two-lane FP32 arithmetic in specialised complex64 passes (0 or 1) */
+int bt_plan_set_tuning(bt_plan* p, int max_ops, int tile_rb, int packed);
 /* runs the plan on member `member` (-1: every member) of a state of the same n/repr/prec */
 int bt_plan_run(bt_plan* p, bt_state* s, int64_t member);
 

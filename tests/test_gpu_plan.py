@@ -24,6 +24,34 @@ def oracle_op(oracle, psi, op):
     return oracle.apply_k(psi, op.mat, qs, ctrls)
 
 
+def test_plan_tuning_configurations_and_autotune(ctx, oracle):
+    """Every tuning configuration the autotuner tries (gates per pass, 4 or 5
+    register bits, packed or scalar complex64 code) applies the same map; the
+    autotuner keeps one of them compiled."""
+    import bluetangle_gpu as bt
+    import bluetangle_gpu.circuits as C
+    n = 15
+    rng = np.random.default_rng(7)
+    ops = C.random_ops(n, 8, rng) + C.brickwork(n, 6, rng)
+    psi = rstate(rng, n)
+    ref = psi
+    for op in ops:
+        ref = oracle_op(oracle, ref, op)
+    plan = bt.Plan(n, "sv", "c64")
+    for op in ops:
+        plan.add(op)
+    for cfg in [(64, 5, 1), (64, 5, 0), (16, 5, 1), (64, 4, 1), (128, 4, 0)]:
+        plan.set_tuning(*cfg).compile(True)
+        s = bt.state_from(psi, "c64")
+        plan.run(s)
+        assert np.abs(s.to_numpy() - ref).max() < 5e-5, cfg
+    res = plan.autotune(bt.state_from(psi, "c64"), reps=1)
+    assert len(res) == 5 and all(t > 0 for _, t in res)
+    s = bt.state_from(psi, "c64")
+    plan.run(s)
+    assert np.abs(s.to_numpy() - ref).max() < 5e-5
+
+
 @pytest.mark.parametrize("prec,tol", [("c128", 1e-12), ("c64", 5e-5)])
 @pytest.mark.parametrize("n", [12, 13, 16])
 def test_plan_brickwork_matches_oracle(ctx, oracle, prec, tol, n):

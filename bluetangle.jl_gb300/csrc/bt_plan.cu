@@ -540,7 +540,12 @@ int bt_plan_compile(bt_plan* p, int mode) {
       ps.args.resize(sizeof(FusedArgs<float>));
       build_fused<float>(p, take, Q, M, NB, c, kept, *reinterpret_cast<FusedArgs<float>*>(ps.args.data()), &nph,
                          ps.op_b0, ps.op_b1);
-      reinterpret_cast<FusedArgs<float>*>(ps.args.data())->packed = packed;
+      // two-lane code where the pass has no dense two-qubit op: a dense 4x4 costs as
+      // much either way and its packed form compiles several times slower
+      FusedArgs<float>& fa = *reinterpret_cast<FusedArgs<float>*>(ps.args.data());
+      bool dense2 = false;
+      for (int oi = 0; oi < (int)kept.size(); ++oi) dense2 |= fa.op[oi].type == FOP_G2;
+      fa.packed = packed && !dense2;
     } else {
       ps.args.resize(sizeof(FusedArgs<double>));
       build_fused<double>(p, take, Q, M, NB, c, kept, *reinterpret_cast<FusedArgs<double>*>(ps.args.data()), &nph,

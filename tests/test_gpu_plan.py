@@ -30,9 +30,9 @@ def test_plan_tuning_configurations_and_autotune(ctx, oracle):
     autotuner keeps one of them compiled."""
     import bluetangle_gpu as bt
     import bluetangle_gpu.circuits as C
-    n = 15
+    n = 14
     rng = np.random.default_rng(7)
-    ops = C.random_ops(n, 8, rng) + C.brickwork(n, 6, rng)
+    ops = C.random_ops(n, 3, rng) + C.brickwork(n, 5, rng)
     psi = rstate(rng, n)
     ref = psi
     for op in ops:
@@ -40,13 +40,13 @@ def test_plan_tuning_configurations_and_autotune(ctx, oracle):
     plan = bt.Plan(n, "sv", "c64")
     for op in ops:
         plan.add(op)
-    for cfg in [(64, 5, 1), (64, 5, 0), (16, 5, 1), (64, 4, 1), (128, 4, 0)]:
+    for cfg in [(64, 5, 1), (64, 5, 0), (16, 5, 1), (64, 4, 1)]:
         plan.set_tuning(*cfg).compile(True)
         s = bt.state_from(psi, "c64")
         plan.run(s)
         assert np.abs(s.to_numpy() - ref).max() < 5e-5, cfg
-    res = plan.autotune(bt.state_from(psi, "c64"), reps=1)
-    assert len(res) == 5 and all(t > 0 for _, t in res)
+    res = plan.autotune(bt.state_from(psi, "c64"), configs=[(64, 5, 1), (32, 5, 0)], reps=1)
+    assert len(res) == 2 and all(t > 0 for _, t in res)
     s = bt.state_from(psi, "c64")
     plan.run(s)
     assert np.abs(s.to_numpy() - ref).max() < 5e-5

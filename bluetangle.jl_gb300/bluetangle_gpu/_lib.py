@@ -72,7 +72,7 @@ SIGNATURES = {
     "bt_plan_set_matrices": (i32, [P, i32, P, P]),
     "bt_plan_stats": (i32, [P, P, P, P, P, P]),
     "bt_plan_run": (i32, [P, P, i64]),
-    "bt_plan_set_tuning": (i32, [P, i32, i32, i32]),
+    "bt_plan_set_tuning": (i32, [P, i32, i32, i32, i32]),
     "bt_program_create": (i32, [P, i32, i32, i32, ctypes.POINTER(P)]),
     "bt_program_free": (i32, [P]),
     "bt_program_add_gate": (i32, [P, i32, P, P, i32]),

@@ -479,21 +479,28 @@ class Plan:
         self.ctx.check(L.lib().bt_plan_set_matrices(self.h, len(updates), _ptr(idx), _ptr(mats)))
         return self
 
-    def set_tuning(self, max_ops=0, tile_rb=0, packed=-1):
-        """Fusion width (gates per pass), register bits per thread (4 or 5) and
-        two-lane arithmetic of the fused passes; 0 / -1 keep the defaults.  Takes
-        effect at the next compile."""
-        self.ctx.check(L.lib().bt_plan_set_tuning(self.h, int(max_ops), int(tile_rb), int(packed)))
+    def set_tuning(self, max_ops=0, tile_rb=0, packed=-1, tile_bits=0):
+        """Fusion width (gates per pass), register bits per thread (4 or 5),
+        two-lane arithmetic and tile bits of the fused passes; 0 / -1 keep the
+        defaults.  Takes effect at the next compile."""
+        self.ctx.check(L.lib().bt_plan_set_tuning(self.h, int(max_ops), int(tile_rb), int(packed), int(tile_bits)))
         return self
 
     def autotune(self, state, configs=None, reps=2):
-        """Times each tuning configuration (max_ops, tile_rb, packed) on `state`
-        (the timing runs overwrite it), keeps the fastest compiled and returns
-        [(config, seconds per run)] in the order tried."""
+        """Times each tuning configuration (max_ops, tile_rb, packed, tile_bits) on
+        `state` (the timing runs overwrite it), keeps the fastest compiled and
+        returns [(config, seconds per run)] in the order tried.  States that fit
+        one default tile also try smaller tiles (more CTAs per pass)."""
         import time
+        c64 = self.prec in ("c64", "complex64")
         if configs is None:
-            configs = ([(64, 5, 1), (64, 5, 0), (32, 5, 1), (128, 5, 1), (64, 4, 1)] if self.prec in ("c64", "complex64")
-                       else [(64, 0, -1), (32, 0, -1), (128, 0, -1)])
+            configs = ([(64, 5, 1, 0), (64, 5, 0, 0), (32, 5, 1, 0), (128, 5, 1, 0), (64, 4, 1, 0)] if c64
+                       else [(64, 0, -1, 0), (32, 0, -1, 0), (128, 0, -1, 0)])
+            nbits = self.n * (2 if self.repr_code == L.BT_REPR_DM else 1)
+            mdef, mmin = (13, 10) if c64 else (12, 9)
+            for m in range(min(mdef, nbits) - 1, mmin - 1, -1)[:3]:
+                configs.append((64, 0, -1, m))
+        configs = [tuple(c) + (0,) * (4 - len(c)) for c in configs]
         results = []
         for cfg in configs:
             self.set_tuning(*cfg).compile(True)

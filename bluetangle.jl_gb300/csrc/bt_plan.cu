@@ -60,7 +60,7 @@ struct bt_plan {
   int compile_mode = 0;
   int64_t nphases = 0;
   // tuning (bt_plan_set_tuning; 0 / -1: the library defaults)
-  int tune_max_ops = 0, tune_rb = 0, tune_packed = -1;
+  int tune_max_ops = 0, tune_rb = 0, tune_packed = -1, tune_m = 0;
   // specialised kernel of each pass (bt_jit.cu), published when compiled; the
   // background compiler of a tiered plan writes them while runs read them
   std::unique_ptr<std::atomic<void*>[]> jit;
@@ -585,8 +585,10 @@ int bt_plan_compile(bt_plan* p, int mode) {
   const int NB = (mode == 0 && bt_jit_available()) ? rb_tuned : (c64 ? BT_TILE_RB_C64 : BT_TILE_RB_C128);
   const int packed = p->tune_packed >= 0 ? p->tune_packed : (int)bt_jit_packed_default();
   // the tile covers the whole state when the state is smaller than the default
-  // tile, down to 2^(M - NB) = 32 threads per CTA
-  const int M = std::min(c64 ? BT_TILE_M_C64 : BT_TILE_M_C128, p->nbits);
+  // tile, down to 2^(M - NB) = 32 threads per CTA; a tuned smaller tile spreads a
+  // small state over more CTAs (more passes, each on more SMs)
+  const int Mdef = c64 ? BT_TILE_M_C64 : BT_TILE_M_C128;
+  const int M = std::min(p->tune_m ? std::min(p->tune_m, Mdef) : Mdef, p->nbits);
   const int c = c64 ? BT_TILE_LOW_C64 : BT_TILE_LOW_C128;
   const bool fuse = (mode == 0 || mode == 2) && M >= NB + 5;
   // specialised kernels compile in time superlinear in their length: bound the
@@ -664,15 +666,19 @@ int bt_plan_compile(bt_plan* p, int mode) {
   return BT_OK;
 }
 
-int bt_plan_set_tuning(bt_plan* p, int max_ops, int tile_rb, int packed) {
+int bt_plan_set_tuning(bt_plan* p, int max_ops, int tile_rb, int packed, int tile_bits) {
   if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "plan is NULL");
+  const int mmin = p->prec == BT_PREC_C64 ? 10 : 9, mmax = p->prec == BT_PREC_C64 ? BT_TILE_M_C64 : BT_TILE_M_C128;
   if (max_ops < 0 || max_ops > BT_FUSED_MAX_OPS || (tile_rb != 0 && tile_rb != 4 && tile_rb != 5) || packed < -1 ||
-      packed > 1)
-    return bt_fail(p->ctx, BT_ERR_BAD_ARG, "tuning: 0 <= max_ops <= 192, tile_rb in {0, 4, 5}, packed in {-1, 0, 1}");
+      packed > 1 || (tile_bits != 0 && (tile_bits < mmin || tile_bits > mmax)))
+    return bt_fail(p->ctx, BT_ERR_BAD_ARG,
+                   "tuning: 0 <= max_ops <= 192, tile_rb in {0, 4, 5}, packed in {-1, 0, 1}, tile_bits 0 or "
+                   "10..13 (complex64) / 9..12 (complex128)");
   join_jit(p);
   p->tune_max_ops = max_ops;
   p->tune_rb = tile_rb;
   p->tune_packed = packed;
+  p->tune_m = tile_bits;
   p->compiled = false;
   return BT_OK;
 }

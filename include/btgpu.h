@@ -180,8 +180,10 @@ int bt_plan_stats(const bt_plan* p, int64_t* ngates, int64_t* npasses, int64_t* 
 /* tuning of the fused passes (applies at the next bt_plan_compile; 0 / -1 keep
  * the library default): gates per pass at most (1..192), register bits per
  * thread of complex64 passes specialised before the first run (4 or 5), and
- * two-lane FP32 arithmetic in specialised complex64 passes (0 or 1) */
-int bt_plan_set_tuning(bt_plan* p, int max_ops, int tile_rb, int packed);
+ * two-lane FP32 arithmetic in specialised complex64 passes (0 or 1), and tile
+ * bits per pass (10..13 complex64 / 9..12 complex128; a smaller tile spreads a
+ * small state over more CTAs) */
+int bt_plan_set_tuning(bt_plan* p, int max_ops, int tile_rb, int packed, int tile_bits);
 /* runs the plan on member `member` (-1: every member) of a state of the same n/repr/prec */
 int bt_plan_run(bt_plan* p, bt_state* s, int64_t member);
 

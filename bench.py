@@ -457,10 +457,11 @@ def run_serve(args):
     if errs:
         raise errs[0]
     lat = np.array([r.t_done - r.t_submit for r in reqs]) * 1e3
-    service = None
-    if not native:  # the native engine reports submit-to-done only
-        service = {k: float(np.mean([(r.t_done - r.t_start) * 1e3 for r in reqs if specs[r.cid].kind == k] or [0]))
-                   for k in ("sv", "traj", "dm")}
+    svc = np.array([r.t_done - r.t_start for r in reqs]) * 1e3
+    service = {k: float(np.mean([s for r, s in zip(reqs, svc) if specs[r.cid].kind == k] or [0]))
+               for k in ("sv", "traj", "dm")}
+    # share of lane time spent running requests over the makespan
+    busy = float(svc.sum() / 1e3 / (args.lanes * (max(r.t_done for r in reqs) - start)))
     served = total / makespan
     # plain per-call complex128 path on a sample: one request per client, serially
     pctx = bt.Context(0, seed=5)
@@ -507,7 +508,8 @@ def run_serve(args):
                        "engine": "bt_serve (native lanes)" if native else "python Server"},
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                            "mean": float(lat.mean())},
-            "mean_service_ms_by_kind": service,
+            "mean_service_ms_by_kind": service, "lane_busy_frac": busy,
+            "mean_queue_ms": float(lat.mean() - svc.mean()),
             "plain_c128_circuits_per_s": plain_rate, "vs_plain": served / plain_rate,
             "max_rel_dev_vs_c128": dev, "max_infidelity_c64": infid,
             "roofline": None, "cpu_baseline": None, "e2e": None, "gpu_launches": None}

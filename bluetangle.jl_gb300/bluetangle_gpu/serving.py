@@ -385,8 +385,9 @@ class NativeServer:
 
     def wait(self, req, timeout=600.0):
         ticket = next(k for k, v in self.pending.items() if v is req)
-        val, lat = ctypes.c_double(), ctypes.c_double()
-        rc = L.lib().bt_serve_poll(self.h, ticket, int(timeout * 1e3), ctypes.byref(val), ctypes.byref(lat))
+        val, lat, svc = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        rc = L.lib().bt_serve_poll(self.h, ticket, int(timeout * 1e3), ctypes.byref(val), ctypes.byref(lat),
+                                   ctypes.byref(svc))
         if rc == L.BT_ERR_TIMEOUT:
             raise TimeoutError(f"request {req.rid} still pending")
         del self.pending[ticket]
@@ -394,6 +395,7 @@ class NativeServer:
             req.error = L.BTError(rc, L.lib().bt_last_error(None).decode())
         req.value = val.value
         req.t_done = req.t_submit + lat.value
+        req.t_start = req.t_done - svc.value
         req.done.set()
         self.completed.append(req)
         return req

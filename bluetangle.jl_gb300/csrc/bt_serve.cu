@@ -345,7 +345,8 @@ int bt_serve_submit(bt_server* s, int64_t client, int count, const int64_t* inde
   return BT_OK;
 }
 
-int bt_serve_poll(bt_server* s, int64_t ticket, int64_t wait_ms, double* value, double* latency_s) {
+int bt_serve_poll(bt_server* s, int64_t ticket, int64_t wait_ms, double* value, double* latency_s,
+                  double* service_s) {
   if (!s) return bt_fail(nullptr, BT_ERR_BAD_ARG, "server is NULL");
   std::unique_lock<std::mutex> lk(s->mu);
   auto it = s->reqs.find(ticket);
@@ -359,6 +360,7 @@ int bt_serve_poll(bt_server* s, int64_t ticket, int64_t wait_ms, double* value, 
   if (!r->done) return BT_ERR_TIMEOUT;
   if (value) *value = r->value;
   if (latency_s) *latency_s = r->t_done - r->t_submit;
+  if (service_s) *service_s = r->t_done - r->t_start;
   int st = r->status;
   if (st) bt_fail(nullptr, st, r->err);
   s->reqs.erase(it);

@@ -267,8 +267,10 @@ int bt_serve_add_program_client(bt_server* s, bt_program* prog, int nterms, cons
 int bt_serve_submit(bt_server* s, int64_t client, int count, const int64_t* index, const double* mats, uint64_t seed,
                     int64_t* ticket);
 /* waits up to wait_ms (-1: until done, 0: no wait); BT_ERR_TIMEOUT while pending.
- * A finished ticket is released by the call that reports it. */
-int bt_serve_poll(bt_server* s, int64_t ticket, int64_t wait_ms, double* value, double* latency_s);
+ * latency_s runs from submit to done, service_s from the lane's start to done
+ * (either may be NULL).  A finished ticket is released by the call that reports it. */
+int bt_serve_poll(bt_server* s, int64_t ticket, int64_t wait_ms, double* value, double* latency_s,
+                  double* service_s);
 int bt_serve_stats(bt_server* s, int64_t* completed, double* p50_s, double* p99_s, int64_t* resident,
                    uint64_t* hbm_used);
 

@@ -16,6 +16,7 @@
 #include <string.h>
 #include <sys/stat.h>
 
+#include <algorithm>
 #include <atomic>
 #include <map>
 #include <mutex>
@@ -467,6 +468,29 @@ bool bt_jit_packed_default() {
   return v;
 }
 
+// Whether a phase may read (first phase) or write (last phase) its register
+// amplitudes straight from / to global memory: a warp's access for one register
+// index spans the lanes' tile bits (the lowest non-register bits), and it is
+// taken when it touches at most twice the 128-byte lines its bytes need.
+// BTGPU_JIT_DIRECT: 0 never, 1 by that rule (default), 2 always.
+static bool direct_ok(const FPhase& ph, int NB, int M, bool f) {
+  static const int mode = env_int("BTGPU_JIT_DIRECT", 1, 0, 2);
+  if (mode != 1) return mode == 2;
+  uint32_t regmask = 0;
+  for (int b = 0; b < NB; ++b) regmask |= 1u << ph.reg[b];
+  const bool pair = f && (regmask & 1);
+  const int bytes = pair ? 16 : (f ? 8 : 16);  // per lane and access
+  const int linebits = f ? 4 : 3;              // tile bits inside a 128-byte line
+  int lanes = 0, outside = 0;
+  for (int bit = 0; bit < M && lanes < 5; ++bit)
+    if (!((regmask >> bit) & 1)) {
+      outside += bit >= linebits;
+      ++lanes;
+    }
+  const int lines = 1 << outside, need = std::max(1, 32 * bytes / 128);
+  return lines <= 2 * need;
+}
+
 template <typename R>
 static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, const std::string& name) {
   const bool f = sizeof(R) == 4;
@@ -480,12 +504,46 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
     << T2 << "* __restrict__ psi, const "
     << (f ? "JitArgsF<" : "JitArgsD<") << NM << "> a) {\n";
   o << "  typedef " << (f ? "float" : "double") << " R;\n";
-  o << "  extern __shared__ __align__(16) unsigned char smem_raw[];\n";
-  o << "  " << T2 << "* tile = reinterpret_cast<" << T2 << "*>(smem_raw);\n";
-  o << "  i64* runoff = reinterpret_cast<i64*>(smem_raw + " << ((f ? 8 : 16) << M) << ");\n";
-  o << "  for (int r = threadIdx.x; r < " << (1 << (M - c)) << "; r += " << T << ") { i64 v = 0;";
-  for (int b = 0; b < M - c; ++b) o << " v |= (i64)((r >> " << b << ") & 1) << " << a.tbits[c + b] << ";";
-  o << " runoff[r] = v; }\n  __syncthreads();\n";
+  const int NP = a.nphase;
+  if (NP == 0) {  // nothing to apply
+    o << "}\n";
+    return;
+  }
+  // The first phase loads its register amplitudes straight from global memory and
+  // the last one stores them straight back, where a warp's accesses stay nearly
+  // coalesced; otherwise the tile is staged through shared memory with 16-byte
+  // accesses.  A one-phase pass with both direct needs no shared memory at all.
+  const bool dfirst = direct_ok(a.ph[0], NB, M, f), dlast = direct_ok(a.ph[NP - 1], NB, M, f);
+  const bool staged = !dfirst || !dlast;
+  const bool use_smem = staged || NP > 1;
+  auto thread_off = [&](const FPhase& ph) {  // global offset of the thread's non-register tile bits
+    uint32_t regmask = 0;
+    for (int b = 0; b < NB; ++b) regmask |= 1u << ph.reg[b];
+    std::ostringstream e;
+    e << "(i64)0";
+    int nb = 0;
+    for (int bit = 0; bit < M; ++bit)
+      if (!((regmask >> bit) & 1)) e << " | ((i64)((threadIdx.x >> " << nb++ << ") & 1) << " << a.tbits[bit] << ")";
+    return e.str();
+  };
+  auto reg_off = [&](const FPhase& ph, int j) {  // global offset of register amplitude j
+    int64_t v = 0;
+    for (int b = 0; b < NB; ++b)
+      if ((j >> b) & 1) v |= (int64_t)1 << a.tbits[ph.reg[b]];
+    return v;
+  };
+  if (use_smem) {
+    o << "  extern __shared__ __align__(16) unsigned char smem_raw[];\n";
+    o << "  " << T2 << "* tile = reinterpret_cast<" << T2 << "*>(smem_raw);\n";
+  }
+  if (staged) {
+    o << "  i64* runoff = reinterpret_cast<i64*>(smem_raw + " << ((f ? 8 : 16) << M) << ");\n";
+    o << "  for (int r = threadIdx.x; r < " << (1 << (M - c)) << "; r += " << T << ") { i64 v = 0;";
+    for (int b = 0; b < M - c; ++b) o << " v |= (i64)((r >> " << b << ") & 1) << " << a.tbits[c + b] << ";";
+    o << " runoff[r] = v; }\n  __syncthreads();\n";
+  }
+  if (dfirst) o << "  const i64 tf = " << thread_off(a.ph[0]) << ";\n";
+  if (dlast) o << "  const i64 tl = " << thread_off(a.ph[NP - 1]) << ";\n";
   o << "  const i64 per = 1LL << a.lg_tiles, total = per * a.nmem;\n";
   o << "  for (i64 tid = blockIdx.x; tid < total; tid += gridDim.x) {\n";
   o << "    const i64 mem = a.member_lo + (tid >> a.lg_tiles);\n    u64 base = (u64)(tid & (per - 1));\n";
@@ -494,33 +552,42 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
     o << "    base = ((base >> " << p << ") << " << (p + 1) << ") | (base & " << fmt_u64((1ULL << p) - 1) << ");\n";
   }
   o << "    " << T2 << "* g = psi + (mem << a.nbits) + base;\n";
-  // tile load: every 16-byte load in flight, then into the swizzled tile
-  o << "    {\n";
-  for (int i = 0; i < NPT; ++i)
-    o << "      const int l" << i << " = (threadIdx.x + " << i * T << ") * " << V << "; const f4 b" << i
-      << " = *reinterpret_cast<const f4*>(g + runoff[l" << i << " >> " << c << "] + (l" << i << " & " << ((1 << c) - 1)
-      << "));\n";
-  for (int i = 0; i < NPT; ++i) {
-    if (f)
-      o << "      { const int s0 = l" << i << " ^ ((l" << i << " >> 4) & 15), s1 = (l" << i << " + 1) ^ (((l" << i
-        << " + 1) >> 4) & 15); tile[s0] = cf{b" << i << ".x, b" << i << ".y}; tile[s1] = cf{b" << i << ".z, b" << i
-        << ".w}; }\n";
-    else
-      o << "      *reinterpret_cast<f4*>(&tile[l" << i << " ^ ((l" << i << " >> 3) & 7)]) = b" << i << ";\n";
+  if (!dfirst) {
+    // tile load: every 16-byte load in flight, then into the swizzled tile
+    o << "    {\n";
+    for (int i = 0; i < NPT; ++i)
+      o << "      const int l" << i << " = (threadIdx.x + " << i * T << ") * " << V << "; const f4 b" << i
+        << " = *reinterpret_cast<const f4*>(g + runoff[l" << i << " >> " << c << "] + (l" << i << " & "
+        << ((1 << c) - 1) << "));\n";
+    for (int i = 0; i < NPT; ++i) {
+      if (f)
+        o << "      { const int s0 = l" << i << " ^ ((l" << i << " >> 4) & 15), s1 = (l" << i << " + 1) ^ (((l" << i
+          << " + 1) >> 4) & 15); tile[s0] = cf{b" << i << ".x, b" << i << ".y}; tile[s1] = cf{b" << i << ".z, b" << i
+          << ".w}; }\n";
+      else
+        o << "      *reinterpret_cast<f4*>(&tile[l" << i << " ^ ((l" << i << " >> 3) & 7)]) = b" << i << ";\n";
+    }
+    o << "    }\n    __syncthreads();\n";
   }
-  o << "    }\n    __syncthreads();\n";
-  for (int p = 0; p < a.nphase; ++p) {
+  for (int p = 0; p < NP; ++p) {
     const FPhase& ph = a.ph[p];
+    const bool rd_direct = p == 0 && dfirst, wr_direct = p == NP - 1 && dlast;
+    // complex64 amplitude pairs that differ in tile bit 0 (register bit 0) move as 16 bytes
+    const bool pair = f && ph.reg[0] == 0;
     uint32_t regmask = 0;
     for (int b = 0; b < NB; ++b) regmask |= 1u << ph.reg[b];
-    o << "    { // phase " << p << "\n    const int t = threadIdx.x; const int lb = 0";
-    int nb = 0;
-    for (int bit = 0; bit < M; ++bit)
-      if (!((regmask >> bit) & 1)) {
-        o << " | (((t >> " << nb << ") & 1) << " << bit << ")";
-        ++nb;
-      }
-    o << ";\n    const int sb = " << (f ? "lb ^ ((lb >> 4) & 15)" : "lb ^ ((lb >> 3) & 7)") << ";\n    R ";
+    o << "    { // phase " << p << "\n";
+    if (!rd_direct || !wr_direct) {
+      o << "    const int t = threadIdx.x; const int lb = 0";
+      int nb = 0;
+      for (int bit = 0; bit < M; ++bit)
+        if (!((regmask >> bit) & 1)) {
+          o << " | (((t >> " << nb << ") & 1) << " << bit << ")";
+          ++nb;
+        }
+      o << ";\n    const int sb = " << (f ? "lb ^ ((lb >> 4) & 15)" : "lb ^ ((lb >> 3) & 7)") << ";\n";
+    }
+    o << "    R ";
     for (int j = 0; j < D; ++j) o << (j ? ", " : "") << "x" << j << ", y" << j;
     o << ";\n";
     std::vector<int> offs(D);
@@ -530,8 +597,23 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
         if ((j >> b) & 1) l |= 1 << ph.reg[b];
       offs[j] = swz_host(f, l);  // the swizzle is XOR-linear: swz(lb | l) = swz(lb) ^ swz(l)
     }
-    for (int j = 0; j < D; ++j)
-      o << "    { const " << T2 << " v = tile[sb ^ " << offs[j] << "]; x" << j << " = v.x; y" << j << " = v.y; }\n";
+    if (rd_direct) {
+      o << "    { const " << T2 << "* gp = g + tf;\n";
+      for (int j = 0; j < D; ++j) {
+        if (pair && (j & 1)) continue;
+        if (pair)
+          o << "    { const f4 v = *reinterpret_cast<const f4*>(gp + " << reg_off(ph, j) << "LL); x" << j << " = v.x; y"
+            << j << " = v.y; x" << (j | 1) << " = v.z; y" << (j | 1) << " = v.w; }\n";
+        else
+          o << "    { const " << T2 << " v = gp[" << reg_off(ph, j) << "LL]; x" << j << " = v.x; y" << j << " = v.y; }\n";
+      }
+      o << "    }\n";
+    } else {
+      for (int j = 0; j < D; ++j)
+        o << "    { const " << T2 << " v = tile[sb ^ " << offs[j] << "]; x" << j << " = v.x; y" << j << " = v.y; }\n";
+      // the tile's last shared-memory reads: the next tile may overwrite it once every warp is past them
+      if (wr_direct) o << "    __syncthreads();\n";
+    }
     if (f && a.packed) {
       const int P = choose_pack_bit(*reinterpret_cast<const FusedArgs<float>*>(&a), ph, NB);
       auto pack = [&]() {
@@ -569,23 +651,39 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
     } else {
       for (int oi = ph.op0; oi < ph.op0 + ph.nop; ++oi) emit_op(o, a.op[oi], NB);
     }
-    for (int j = 0; j < D; ++j) o << "    tile[sb ^ " << offs[j] << "] = " << T2 << "{x" << j << ", y" << j << "};\n";
-    o << "    __syncthreads();\n    }\n";
+    if (wr_direct) {
+      o << "    { " << T2 << "* gp = g + tl;\n";
+      for (int j = 0; j < D; ++j) {
+        if (pair && (j & 1)) continue;
+        if (pair)
+          o << "    *reinterpret_cast<f4*>(gp + " << reg_off(ph, j) << "LL) = f4{x" << j << ", y" << j << ", x"
+            << (j | 1) << ", y" << (j | 1) << "};\n";
+        else
+          o << "    gp[" << reg_off(ph, j) << "LL] = " << T2 << "{x" << j << ", y" << j << "};\n";
+      }
+      o << "    }\n    }\n";
+    } else {
+      for (int j = 0; j < D; ++j) o << "    tile[sb ^ " << offs[j] << "] = " << T2 << "{x" << j << ", y" << j << "};\n";
+      o << "    __syncthreads();\n    }\n";
+    }
   }
-  o << "    {\n";
-  for (int i = 0; i < NPT; ++i) {
-    o << "      const int l" << i << " = (threadIdx.x + " << i * T << ") * " << V << ";";
-    if (f)
-      o << " const cf u" << i << " = tile[l" << i << " ^ ((l" << i << " >> 4) & 15)], v" << i << " = tile[(l" << i
-        << " + 1) ^ (((l" << i << " + 1) >> 4) & 15)]; const f4 b" << i << " = f4{u" << i << ".x, u" << i << ".y, v" << i
-        << ".x, v" << i << ".y};\n";
-    else
-      o << " const f4 b" << i << " = *reinterpret_cast<const f4*>(&tile[l" << i << " ^ ((l" << i << " >> 3) & 7)]);\n";
+  if (!dlast) {
+    o << "    {\n";
+    for (int i = 0; i < NPT; ++i) {
+      o << "      const int l" << i << " = (threadIdx.x + " << i * T << ") * " << V << ";";
+      if (f)
+        o << " const cf u" << i << " = tile[l" << i << " ^ ((l" << i << " >> 4) & 15)], v" << i << " = tile[(l" << i
+          << " + 1) ^ (((l" << i << " + 1) >> 4) & 15)]; const f4 b" << i << " = f4{u" << i << ".x, u" << i << ".y, v"
+          << i << ".x, v" << i << ".y};\n";
+      else
+        o << " const f4 b" << i << " = *reinterpret_cast<const f4*>(&tile[l" << i << " ^ ((l" << i << " >> 3) & 7)]);\n";
+    }
+    for (int i = 0; i < NPT; ++i)
+      o << "      *reinterpret_cast<f4*>(g + runoff[l" << i << " >> " << c << "] + (l" << i << " & " << ((1 << c) - 1)
+        << ")) = b" << i << ";\n";
+    o << "    }\n    __syncthreads();\n";
   }
-  for (int i = 0; i < NPT; ++i)
-    o << "      *reinterpret_cast<f4*>(g + runoff[l" << i << " >> " << c << "] + (l" << i << " & " << ((1 << c) - 1)
-      << ")) = b" << i << ";\n";
-  o << "    }\n    __syncthreads();\n  }\n}\n";
+  o << "  }\n}\n";
 }
 
 // structure key: everything that shapes the code (not the matrix values)

@@ -52,6 +52,52 @@ def test_plan_tuning_configurations_and_autotune(ctx, oracle):
     assert np.abs(s.to_numpy() - ref).max() < 5e-5
 
 
+_DIRECT_SCRIPT = r"""
+import sys, numpy as np
+sys.path[:0] = sys.argv[2:4]
+import bluetangle_gpu as bt
+import bluetangle_gpu.circuits as C
+out = {}
+for prec, n in (("c64", 17), ("c128", 16)):
+    rng = np.random.default_rng(23)
+    ops = C.random_ops(n, 2, rng) + C.brickwork(n, 8, rng)
+    plan = bt.plan_from_ops(ops, n, prec=prec)
+    psi = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
+    s = bt.state_from(psi / np.linalg.norm(psi), prec)
+    plan.run(s)
+    out[prec] = s.to_numpy()
+    out[prec + "_in"] = psi / np.linalg.norm(psi)
+np.savez(sys.argv[1], **out)
+"""
+
+
+def test_plan_direct_and_staged_phases_identical(oracle, tmp_path):
+    """The first/last phase of a specialised pass reads/writes its registers
+    straight from/to global memory (BTGPU_JIT_DIRECT=1: where coalesced, 2:
+    always) or through the shared-memory tile (0): the same arithmetic, so the
+    states are bit-identical; the staged run is checked against the oracle."""
+    import os
+    import subprocess
+    import sys
+    import bluetangle_gpu.circuits as C
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    res = {}
+    for mode in ("0", "1", "2"):
+        f = str(tmp_path / f"d{mode}.npz")
+        env = dict(os.environ, BTGPU_JIT_DIRECT=mode)
+        subprocess.run([sys.executable, "-c", _DIRECT_SCRIPT, f, root, os.path.join(root, "bluetangle.jl_gb300")],
+                       env=env, check=True, timeout=600)
+        res[mode] = np.load(f)
+    for prec in ("c64", "c128"):
+        assert np.array_equal(res["0"][prec], res["1"][prec]) and np.array_equal(res["0"][prec], res["2"][prec])
+    rng = np.random.default_rng(23)
+    ops = C.random_ops(16, 2, rng) + C.brickwork(16, 8, rng)
+    ref = res["0"]["c128_in"]
+    for op in ops:
+        ref = oracle_op(oracle, ref, op)
+    assert np.abs(res["0"]["c128"] - ref).max() < 1e-12
+
+
 @pytest.mark.parametrize("prec,tol", [("c128", 1e-12), ("c64", 5e-5)])
 @pytest.mark.parametrize("n", [12, 13, 16])
 def test_plan_brickwork_matches_oracle(ctx, oracle, prec, tol, n):

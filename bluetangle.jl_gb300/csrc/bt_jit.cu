@@ -491,6 +491,14 @@ static bool direct_ok(const FPhase& ph, int NB, int M, bool f) {
   return lines <= 2 * need;
 }
 
+// next-tile prefetch into shared memory during a direct last phase
+// (BTGPU_JIT_PREFETCH=1; off by default: on the 28- and 33-qubit brickwork the
+// extra shared-memory copies cost more than the hidden load latency saves)
+static bool prefetch_on() {
+  static const bool v = env_int("BTGPU_JIT_PREFETCH", 0, 0, 1) != 0;
+  return v;
+}
+
 template <typename R>
 static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, const std::string& name) {
   const bool f = sizeof(R) == 4;
@@ -513,8 +521,14 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
   // the last one stores them straight back, where a warp's accesses stay nearly
   // coalesced; otherwise the tile is staged through shared memory with 16-byte
   // accesses.  A one-phase pass with both direct needs no shared memory at all.
-  const bool dfirst = direct_ok(a.ph[0], NB, M, f), dlast = direct_ok(a.ph[NP - 1], NB, M, f);
-  const bool staged = !dfirst || !dlast;
+  // With prefetch (the last phase direct), the next tile is instead copied into
+  // the shared-memory tile with cp.async as soon as the last phase has read the
+  // current one, so its load latency hides behind that phase's arithmetic and
+  // stores.
+  const bool dlast = direct_ok(a.ph[NP - 1], NB, M, f);
+  const bool pf = dlast && prefetch_on();
+  const bool dfirst = !pf && direct_ok(a.ph[0], NB, M, f);
+  const bool staged = pf || !dfirst || !dlast;
   const bool use_smem = staged || NP > 1;
   auto thread_off = [&](const FPhase& ph) {  // global offset of the thread's non-register tile bits
     uint32_t regmask = 0;
@@ -545,14 +559,33 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
   if (dfirst) o << "  const i64 tf = " << thread_off(a.ph[0]) << ";\n";
   if (dlast) o << "  const i64 tl = " << thread_off(a.ph[NP - 1]) << ";\n";
   o << "  const i64 per = 1LL << a.lg_tiles, total = per * a.nmem;\n";
-  o << "  for (i64 tid = blockIdx.x; tid < total; tid += gridDim.x) {\n";
+  // first amplitude of tile `tid`: the tile bits inserted as zeros into the tile index
+  o << "  auto tile_ptr = [&](i64 tid) -> " << T2 << "* {\n";
   o << "    const i64 mem = a.member_lo + (tid >> a.lg_tiles);\n    u64 base = (u64)(tid & (per - 1));\n";
   for (int i = 0; i < M; ++i) {
     const int p = a.tbits[i];
     o << "    base = ((base >> " << p << ") << " << (p + 1) << ") | (base & " << fmt_u64((1ULL << p) - 1) << ");\n";
   }
-  o << "    " << T2 << "* g = psi + (mem << a.nbits) + base;\n";
-  if (!dfirst) {
+  o << "    return psi + (mem << a.nbits) + base;\n  };\n";
+  if (pf) {
+    // one amplitude per copy, straight into its swizzled slot; one commit group
+    // per tile (empty past the end)
+    o << "  auto fetch = [&](i64 tid) {\n    if (tid < total) {\n      const " << T2 << "* g = tile_ptr(tid);\n";
+    o << "      const unsigned sb = (unsigned)__cvta_generic_to_shared(tile);\n";
+    for (int i = 0; i < (1 << M) / T; ++i) {
+      o << "      { const int l = threadIdx.x + " << i * T << "; const " << T2 << "* src = g + runoff[l >> " << c
+        << "] + (l & " << ((1 << c) - 1) << "); const unsigned dst = sb + "
+        << (f ? "8u * (unsigned)(l ^ ((l >> 4) & 15))" : "16u * (unsigned)(l ^ ((l >> 3) & 7))") << ";";
+      o << (f ? " asm volatile(\"cp.async.ca.shared.global [%0], [%1], 8;\" :: \"r\"(dst), \"l\"(src) : \"memory\"); }\n"
+              : " asm volatile(\"cp.async.cg.shared.global [%0], [%1], 16;\" :: \"r\"(dst), \"l\"(src) : \"memory\"); }\n");
+    }
+    o << "    }\n    asm volatile(\"cp.async.commit_group;\" ::: \"memory\");\n  };\n";
+    o << "  fetch(blockIdx.x);\n";
+  }
+  o << "  for (i64 tid = blockIdx.x; tid < total; tid += gridDim.x) {\n";
+  o << "    " << T2 << "* g = tile_ptr(tid);\n";
+  if (pf) o << "    asm volatile(\"cp.async.wait_group 0;\" ::: \"memory\");\n    __syncthreads();\n";
+  if (!dfirst && !pf) {
     // tile load: every 16-byte load in flight, then into the swizzled tile
     o << "    {\n";
     for (int i = 0; i < NPT; ++i)
@@ -613,6 +646,7 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
         o << "    { const " << T2 << " v = tile[sb ^ " << offs[j] << "]; x" << j << " = v.x; y" << j << " = v.y; }\n";
       // the tile's last shared-memory reads: the next tile may overwrite it once every warp is past them
       if (wr_direct) o << "    __syncthreads();\n";
+      if (wr_direct && pf) o << "    fetch(tid + gridDim.x);\n";
     }
     if (f && a.packed) {
       const int P = choose_pack_bit(*reinterpret_cast<const FusedArgs<float>*>(&a), ph, NB);
@@ -683,7 +717,9 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
         << ")) = b" << i << ";\n";
     o << "    }\n    __syncthreads();\n";
   }
-  o << "  }\n}\n";
+  o << "  }\n";
+  if (pf) o << "  asm volatile(\"cp.async.wait_group 0;\" ::: \"memory\");\n";
+  o << "}\n";
 }
 
 // structure key: everything that shapes the code (not the matrix values)

@@ -74,22 +74,26 @@ np.savez(sys.argv[1], **out)
 def test_plan_direct_and_staged_phases_identical(oracle, tmp_path):
     """The first/last phase of a specialised pass reads/writes its registers
     straight from/to global memory (BTGPU_JIT_DIRECT=1: where coalesced, 2:
-    always) or through the shared-memory tile (0): the same arithmetic, so the
-    states are bit-identical; the staged run is checked against the oracle."""
+    always) or through the shared-memory tile (0), with or without the next
+    tile copied in by cp.async during a direct last phase (BTGPU_JIT_PREFETCH):
+    the same arithmetic, so the states are bit-identical; the staged run is
+    checked against the oracle."""
     import os
     import subprocess
     import sys
     import bluetangle_gpu.circuits as C
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     res = {}
-    for mode in ("0", "1", "2"):
-        f = str(tmp_path / f"d{mode}.npz")
-        env = dict(os.environ, BTGPU_JIT_DIRECT=mode)
+    modes = {"0": ("0", "1"), "1": ("1", "1"), "2": ("2", "1"), "1np": ("1", "0"), "2np": ("2", "0")}
+    for key, (direct, prefetch) in modes.items():
+        f = str(tmp_path / f"d{key}.npz")
+        env = dict(os.environ, BTGPU_JIT_DIRECT=direct, BTGPU_JIT_PREFETCH=prefetch)
         subprocess.run([sys.executable, "-c", _DIRECT_SCRIPT, f, root, os.path.join(root, "bluetangle.jl_gb300")],
                        env=env, check=True, timeout=600)
-        res[mode] = np.load(f)
+        res[key] = np.load(f)
     for prec in ("c64", "c128"):
-        assert np.array_equal(res["0"][prec], res["1"][prec]) and np.array_equal(res["0"][prec], res["2"][prec])
+        for key in modes:
+            assert np.array_equal(res["0"][prec], res[key][prec]), (prec, key)
     rng = np.random.default_rng(23)
     ops = C.random_ops(16, 2, rng) + C.brickwork(16, 8, rng)
     ref = res["0"]["c128_in"]

@@ -370,7 +370,9 @@ def run_ours(args):
                                    "one brickwork layer (logical gates: n one-qubit + CNOTs)",
                            "plan": pstats if plan is not None else None,
                            "tuning": {k: os.environ.get(k) for k in ("BTGPU_JIT_MINB", "BTGPU_PLAN_MAX_OPS",
-                                                                      "BTGPU_TILE_RB", "BTGPU_JIT_PACKED")
+                                                                      "BTGPU_TILE_RB", "BTGPU_JIT_PACKED",
+                                                                      "BTGPU_JIT_DIRECT", "BTGPU_JIT_PREFETCH",
+                                                                      "BTGPU_PLAN_FACTOR")
                                       if os.environ.get(k)},
                            "autotune": ([{"max_ops": c[0], "tile_rb": c[1], "packed": c[2], "tile_bits": c[3],
                                           "s_per_circuit": t} for c, t in tuned] if tuned else None),

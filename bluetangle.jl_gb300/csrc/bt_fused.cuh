@@ -28,6 +28,8 @@ enum {
   FOP_X1 = 8,  // anti-diagonal 2x2: out0 = p0*in1, out1 = p1*in0 (4 reals); unit: plain swap
   FOP_R1 = 9,  // real 2x2 (4 reals): H, RY, ...
   FOP_RX1 = 10,  // [[a, ib], [ib, a]] with a, b real (2 reals): RX
+  FOP_DH = 11,   // diag(1, q) (2 reals); unit 2: q = -1, 3: q = i, 4: q = -i (no arithmetic)
+  FOP_HB = 12,   // butterfly [[1, s01], [s10, s11]], signs -1 where flags bits 0, 1, 2 are set (no reals)
 };
 
 struct FOp {

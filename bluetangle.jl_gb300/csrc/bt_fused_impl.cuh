@@ -233,6 +233,48 @@ __device__ __forceinline__ void op_rx1(R (&xr)[1 << NB], R (&xi)[1 << NB], const
   }
 }
 
+// diag(1, q) (the scalar d0 of diag(d0, d1) is folded elsewhere in the pass);
+// code 2: q = -1, 3: q = i, 4: q = -i
+template <typename R, int NB, int B>
+__device__ __forceinline__ void op_dh(R (&xr)[1 << NB], R (&xi)[1 << NB], const R* __restrict__ m, int code) {
+  if constexpr (B < NB) {
+    const R qr = m[0], qi = m[1];
+#pragma unroll
+    for (int j = 0; j < (1 << NB); ++j) {
+      if (!(j & (1 << B))) continue;
+      const R ar = xr[j], ai = xi[j];
+      if (code == 2) {
+        xr[j] = -ar; xi[j] = -ai;
+      } else if (code == 3) {
+        xr[j] = -ai; xi[j] = ar;
+      } else if (code == 4) {
+        xr[j] = ai; xi[j] = -ar;
+      } else {
+        xr[j] = fma(qr, ar, -qi * ai);
+        xi[j] = fma(qr, ai, qi * ar);
+      }
+    }
+  }
+}
+
+// butterfly [[1, s01], [s10, s11]] with s = -1 where bits 0, 1, 2 of fl are set
+template <typename R, int NB, int B>
+__device__ __forceinline__ void op_hb(R (&xr)[1 << NB], R (&xi)[1 << NB], int fl) {
+  if constexpr (B < NB) {
+    const R s01 = (fl & 1) ? R(-1) : R(1), s10 = (fl & 2) ? R(-1) : R(1), s11 = (fl & 4) ? R(-1) : R(1);
+#pragma unroll
+    for (int j = 0; j < (1 << NB); ++j) {
+      if (j & (1 << B)) continue;
+      const int k = j | (1 << B);
+      const R ar = xr[j], ai = xi[j], br = xr[k], bi = xi[k];
+      xr[j] = fma(s01, br, ar);
+      xi[j] = fma(s01, bi, ai);
+      xr[k] = fma(s11, br, s10 * ar);
+      xi[k] = fma(s11, bi, s10 * ai);
+    }
+  }
+}
+
 #define BT_PAIRS(X)                                                                                     \
   X(0, 1) X(0, 2) X(0, 3) X(0, 4) X(1, 0) X(1, 2) X(1, 3) X(1, 4) X(2, 0) X(2, 1) X(2, 3) X(2, 4) X(3, 0) \
   X(3, 1) X(3, 2) X(3, 4) X(4, 0) X(4, 1) X(4, 2) X(4, 3)
@@ -305,6 +347,8 @@ __device__ __forceinline__ void apply_op(R (&xr)[1 << NB], R (&xi)[1 << NB], con
     case FOP_X1: ONE(op_x1, m, o.unit) break;
     case FOP_R1: ONE(op_r1, m) break;
     case FOP_RX1: ONE(op_rx1, m) break;
+    case FOP_DH: ONE(op_dh, m, o.unit) break;
+    case FOP_HB: ONE(op_hb, o.flags) break;
 #undef ONE
   }
 }

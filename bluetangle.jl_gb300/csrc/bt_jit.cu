@@ -168,6 +168,29 @@ static void emit_op(std::ostringstream& o, const FOp& op, int NB) {
       });
       o << "    }\n";
       break;
+    case FOP_DH:  // diag(1, q): the bit-1 half only
+      if (op.unit == 0) o << "    { const R qr=" << M(0) << ",qi=" << M(1) << ";\n";
+      for (int j = 0; j < D; ++j) {
+        if (!(j & (1 << b0))) continue;
+        o << "      { const R ar=x" << j << ",ai=y" << j << ";";
+        if (op.unit == 2) o << " x" << j << "=-ar; y" << j << "=-ai; }\n";
+        else if (op.unit == 3) o << " x" << j << "=-ai; y" << j << "=ar; }\n";
+        else if (op.unit == 4) o << " x" << j << "=ai; y" << j << "=-ar; }\n";
+        else o << " x" << j << "=fm(qr,ar,-qi*ai); y" << j << "=fm(qr,ai,qi*ar); }\n";
+      }
+      if (op.unit == 0) o << "    }\n";
+      break;
+    case FOP_HB: {  // [[1, s01], [s10, s11]]: adds and subtracts
+      const char* s01 = (op.flags & 1) ? "-" : "+";
+      const char* s10 = (op.flags & 2) ? "-" : "";
+      const char* s11 = (op.flags & 4) ? "-" : "+";
+      pairs(b0, [&](int j, int k) {
+        o << "    { const R ar=x" << j << ",ai=y" << j << ",br=x" << k << ",bi=y" << k << "; x" << j << "=ar" << s01
+          << "br; y" << j << "=ai" << s01 << "bi; x" << k << "=" << s10 << "ar" << s11 << "br; y" << k << "=" << s10
+          << "ai" << s11 << "bi; }\n";
+      });
+      break;
+    }
     case FOP_RX1:
       o << "    { const R ca=" << M(0) << ",cb=" << M(1) << ";\n";
       pairs(b0, [&](int j, int k) {
@@ -285,7 +308,7 @@ static int choose_pack_bit(const FusedArgs<float>& a, const FPhase& ph, int NB) 
     int cnt = 0;
     for (int oi = ph.op0; oi < ph.op0 + ph.nop; ++oi) {
       const FOp& op = a.op[oi];
-      if (op.type != FOP_D1 && op.type != FOP_D2 && touches(op, b)) ++cnt;
+      if (op.type != FOP_D1 && op.type != FOP_D2 && op.type != FOP_DH && touches(op, b)) ++cnt;
     }
     if (cnt < bestc) best = b, bestc = cnt;
   }
@@ -336,8 +359,58 @@ static bool emit_op_packed(std::ostringstream& o, const FOp& op, int NB, int P) 
     o << "\n    }\n";
     return true;
   }
+  if (op.type == FOP_DH) {
+    // diag(1, q) on bit b0: on the pack bit only the high lanes change
+    const bool onp = b0 == P;
+    const char* SG = onp ? "0x8000000000000000ULL" : "0x8000000080000000ULL";
+    if (op.unit == 0) {
+      o << "    { const float qr=" << M(0) << ", qi=" << M(1) << ";";
+      if (onp)
+        o << " const u64 er=pk(1.0f,qr), ei=pk(0.0f,qi), nei=pk(-0.0f,-qi);";
+      else
+        o << " const u64 er=bc(qr), ei=bc(qi), nei=bc(-qi);";
+      o << "\n";
+    }
+    for (int j = 0; j < D; ++j) {
+      if (!k0(j) || (!onp && !(j & (1 << b0)))) continue;
+      const std::string X = "X" + std::to_string(j), Y = "Y" + std::to_string(j);
+      if (op.unit == 0)
+        o << "      { const u64 ar=" << X << ", ai=" << Y << "; " << X << "=ffma2(er,ar,fmul2(nei,ai)); " << Y
+          << "=ffma2(er,ai,fmul2(ei,ar)); }\n";
+      else if (op.unit == 2)
+        o << "    " << X << "^=" << SG << "; " << Y << "^=" << SG << ";\n";
+      else if (!onp && op.unit == 3)
+        o << "    { const u64 ar=" << X << "; " << X << "=" << Y << "^" << SG << "; " << Y << "=ar; }\n";
+      else if (!onp)  // unit 4
+        o << "    { const u64 ar=" << X << "; " << X << "=" << Y << "; " << Y << "=ar^" << SG << "; }\n";
+      else if (op.unit == 3)  // high lane (x, y) -> (-y, x)
+        o << "    { const u64 ar=" << X << ", ai=" << Y << "; " << X << "=(ar&0xFFFFFFFFULL)|((ai^" << SG
+          << ")&0xFFFFFFFF00000000ULL); " << Y << "=(ai&0xFFFFFFFFULL)|(ar&0xFFFFFFFF00000000ULL); }\n";
+      else  // high lane (x, y) -> (y, -x)
+        o << "    { const u64 ar=" << X << ", ai=" << Y << "; " << X << "=(ar&0xFFFFFFFFULL)|(ai&0xFFFFFFFF00000000ULL); "
+          << Y << "=(ai&0xFFFFFFFFULL)|((ar^" << SG << ")&0xFFFFFFFF00000000ULL); }\n";
+    }
+    if (op.unit == 0) o << "    }\n";
+    return true;
+  }
   if (touches(op, P)) return false;
   switch (op.type) {
+    case FOP_HB: {  // [[1, s01], [s10, s11]] as two-lane fma(+-1, a, b): one rounding, = add / subtract
+      const bool n01 = op.flags & 1, n10 = op.flags & 2, n11 = op.flags & 4;
+      o << "    { const u64 P1=bc(1.0f), N1=bc(-1.0f);\n";
+      pairs(b0, [&](int j, int k) {
+        for (int c = 0; c < 2; ++c) {
+          const std::string A = (c ? "Y" : "X") + std::to_string(j), B = (c ? "Y" : "X") + std::to_string(k);
+          o << "      { const u64 ua=" << A << ", ub=" << B << "; " << A << "=ffma2(" << (n01 ? "N1" : "P1") << ",ub,ua); "
+            << B << "=";
+          if (!n11) o << "ffma2(" << (n10 ? "N1" : "P1") << ",ua,ub); }\n";
+          else if (!n10) o << "ffma2(N1,ub,ua); }\n";
+          else o << "ffma2(N1,ua,ub^0x8000000080000000ULL); }\n";
+        }
+      });
+      o << "    }\n";
+      return true;
+    }
     case FOP_G1:
       o << "    {";
       bcs("m0", 0, false), bcs("m1", 1, false), bcs("n1", 1, true), bcs("m2", 2, false), bcs("m3", 3, false);

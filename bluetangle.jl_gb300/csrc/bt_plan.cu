@@ -177,43 +177,73 @@ static bool classify_unit(const PGate& g) {
   return true;
 }
 
-// classifies gate g and writes its op type and matrix entries at mat[w...]
+// Scalar factors taken out of one-qubit ops (BTGPU_PLAN_FACTOR=0 turns it off):
+// diag(d0, d1) = d0 diag(1, d1/d0) touches half the amplitudes, and a real
+// matrix with entries of one magnitude (H) is that magnitude times an add/sub
+// butterfly.  The factors of a pass multiply into one scalar that is folded
+// back into one op of the pass (encode_pass), so the pass applies the same map.
+static bool factor_on() {
+  static const bool v = [] {
+    const char* e = getenv("BTGPU_PLAN_FACTOR");
+    return !(e && *e == '0');
+  }();
+  return v;
+}
+
+// classifies gate g and writes its op type and matrix entries at mat[0..nre)
+// in double; fac receives the complex scalar taken out of the op (1 if none).
 // (o.b0/o.b1 hold the register bits of the gate's first/second bit on entry)
-template <typename R>
-static void encode_op(const PGate& g, FOp& o, R* mat, int& w) {
+static void encode_op(const PGate& g, FOp& o, double* mat, int& nre, double* fac, bool factor) {
   int perm[4] = {0, 1, 2, 3};
   const int cls = classify(g, perm);
-  o.moff = (uint16_t)w;
   const double* m = g.m.data();
+  int w = 0;
+  fac[0] = 1.0, fac[1] = 0.0;
   if (g.k == 1) {
     // m = [m00r m00i m01r m01i m10r m10i m11r m11i]
     const bool real = m[1] == 0 && m[3] == 0 && m[5] == 0 && m[7] == 0;
-    if (cls == 2) {
+    const double a0 = fabs(m[0]);
+    if (cls == 2 && factor && (m[0] != 0 || m[1] != 0)) {
+      // d1 / d0 on the bit-1 half; exact -1, i, -i become sign flips and swaps
+      const double n = m[0] * m[0] + m[1] * m[1];
+      const double qr = (m[6] * m[0] + m[7] * m[1]) / n, qi = (m[7] * m[0] - m[6] * m[1]) / n;
+      o.type = FOP_DH;
+      o.unit = (qr == -1 && qi == 0) ? 2 : (qr == 0 && qi == 1) ? 3 : (qr == 0 && qi == -1) ? 4 : 0;
+      mat[w++] = qr;
+      mat[w++] = qi;
+      fac[0] = m[0], fac[1] = m[1];
+    } else if (cls == 2) {
       o.type = FOP_D1;
-      mat[w++] = (R)m[0];
-      mat[w++] = (R)m[1];
-      mat[w++] = (R)m[6];
-      mat[w++] = (R)m[7];
+      mat[w++] = m[0];
+      mat[w++] = m[1];
+      mat[w++] = m[6];
+      mat[w++] = m[7];
     } else if (cls == 1) {  // anti-diagonal
       o.type = FOP_X1;
       o.unit = (m[2] == 1 && m[3] == 0 && m[4] == 1 && m[5] == 0) ? 1 : 0;
-      mat[w++] = (R)m[2];
-      mat[w++] = (R)m[3];
-      mat[w++] = (R)m[4];
-      mat[w++] = (R)m[5];
+      mat[w++] = m[2];
+      mat[w++] = m[3];
+      mat[w++] = m[4];
+      mat[w++] = m[5];
+    } else if (real && factor && a0 != 0 && fabs(m[2]) == a0 && fabs(m[4]) == a0 && fabs(m[6]) == a0) {
+      // m00 * [[1, s01], [s10, s11]], signs relative to m00
+      o.type = FOP_HB;
+      o.flags = (uint8_t)(((m[2] < 0) != (m[0] < 0)) | (((m[4] < 0) != (m[0] < 0)) << 1) |
+                          (((m[6] < 0) != (m[0] < 0)) << 2));
+      fac[0] = m[0];
     } else if (real) {
       o.type = FOP_R1;
-      mat[w++] = (R)m[0];
-      mat[w++] = (R)m[2];
-      mat[w++] = (R)m[4];
-      mat[w++] = (R)m[6];
+      mat[w++] = m[0];
+      mat[w++] = m[2];
+      mat[w++] = m[4];
+      mat[w++] = m[6];
     } else if (m[0] == m[6] && m[1] == 0 && m[7] == 0 && m[2] == 0 && m[4] == 0 && m[3] == m[5]) {
       o.type = FOP_RX1;
-      mat[w++] = (R)m[0];
-      mat[w++] = (R)m[3];
+      mat[w++] = m[0];
+      mat[w++] = m[3];
     } else {
       o.type = FOP_G1;
-      for (int e = 0; e < 8; ++e) mat[w++] = (R)m[e];
+      for (int e = 0; e < 8; ++e) mat[w++] = m[e];
     }
   } else if (cls == 1 && classify_unit(g) && perm[0] == 0 && perm[1] == 1 && perm[2] == 3 && perm[3] == 2) {
     o.type = FOP_CX;  // control = matrix MSB (register b0), target = LSB (b1)
@@ -227,8 +257,8 @@ static void encode_op(const PGate& g, FOp& o, R* mat, int& w) {
   } else if (cls == 2) {
     o.type = FOP_D2;
     for (int r = 0; r < 4; ++r) {
-      mat[w++] = (R)g.m[2 * (r * 4 + r)];
-      mat[w++] = (R)g.m[2 * (r * 4 + r) + 1];
+      mat[w++] = g.m[2 * (r * 4 + r)];
+      mat[w++] = g.m[2 * (r * 4 + r) + 1];
     }
   } else if (cls == 1) {
     o.type = FOP_P2;
@@ -237,14 +267,97 @@ static void encode_op(const PGate& g, FOp& o, R* mat, int& w) {
     for (int r = 0; r < 4; ++r) {
       double pr = g.m[2 * (r * 4 + perm[r])], pi = g.m[2 * (r * 4 + perm[r]) + 1];
       if (pr != 1.0 || pi != 0.0) unit = false;
-      mat[w++] = (R)pr;
-      mat[w++] = (R)pi;
+      mat[w++] = pr;
+      mat[w++] = pi;
     }
     o.unit = unit ? 1 : 0;
   } else {
     o.type = FOP_G2;
-    for (int e = 0; e < 32; ++e) mat[w++] = (R)g.m[e];
+    for (int e = 0; e < 32; ++e) mat[w++] = g.m[e];
   }
+  nre = w;
+}
+
+// Encodes the ops of a fused pass (kept: their gates; ob0/ob1: their register
+// bits) with the scalar factors folded into one op: a general op (complex
+// entries scaled), a real op when the scalar is real, else one factored
+// diagonal / butterfly turned back into its full form.  update: the pass
+// exists and only its matrices are rewritten; false when an op's structure
+// (type, bits, flags) would change, which needs a recompile.
+template <typename R>
+static bool encode_pass(bt_plan* p, const std::vector<int>& kept, const std::vector<uint8_t>& ob0,
+                        const std::vector<uint8_t>& ob1, FusedArgs<R>& a, bool update) {
+  const int nop = (int)kept.size();
+  std::vector<FOp> ops(nop);
+  std::vector<double> mats((size_t)nop * 32);
+  std::vector<int> nre(nop);
+  const bool factor = factor_on();
+  double tr = 1.0, ti = 0.0;  // product of the factors
+  for (int i = 0; i < nop; ++i) {
+    FOp& o = ops[i];
+    memset(&o, 0, sizeof(o));
+    o.b0 = ob0[i];
+    o.b1 = ob1[i];
+    double f[2];
+    encode_op(p->gates[kept[i]], o, &mats[(size_t)i * 32], nre[i], f, factor);
+    const double r = tr * f[0] - ti * f[1];
+    ti = tr * f[1] + ti * f[0];
+    tr = r;
+  }
+  if (tr != 1.0 || ti != 0.0) {
+    auto is = [&](int i, std::initializer_list<int> types) {
+      for (int t : types)
+        if (ops[i].type == t) return true;
+      return false;
+    };
+    int t = -1, mode = 0;  // 1 complex scale, 2 real scale, 3 half diagonal -> D1, 4 butterfly -> R1
+    for (int i = 0; i < nop && t < 0; ++i)
+      if (is(i, {FOP_G1, FOP_G2, FOP_D1, FOP_D2}) || (is(i, {FOP_P2, FOP_X1}) && !ops[i].unit)) t = i, mode = 1;
+    for (int i = 0; i < nop && t < 0 && ti == 0; ++i)
+      if (ops[i].type == FOP_R1) t = i, mode = 2;
+    for (int i = 0; i < nop && t < 0; ++i)
+      if (ops[i].type == FOP_DH) t = i, mode = 3;
+    for (int i = 0; i < nop && t < 0 && ti == 0; ++i)
+      if (ops[i].type == FOP_HB) t = i, mode = 4;
+    if (t < 0) return false;  // unreachable: a factor comes from a DH (complex) or HB (real) op
+    double* m = &mats[(size_t)t * 32];
+    if (mode == 1) {
+      for (int e = 0; e + 1 < nre[t]; e += 2) {
+        const double r = m[e] * tr - m[e + 1] * ti;
+        m[e + 1] = m[e] * ti + m[e + 1] * tr;
+        m[e] = r;
+      }
+    } else if (mode == 2) {
+      for (int e = 0; e < nre[t]; ++e) m[e] *= tr;
+    } else if (mode == 3) {  // diag(s, s q)
+      const double qr = m[0], qi = m[1];
+      ops[t].type = FOP_D1;
+      ops[t].unit = 0;
+      m[0] = tr, m[1] = ti, m[2] = tr * qr - ti * qi, m[3] = tr * qi + ti * qr;
+      nre[t] = 4;
+    } else {  // s [[1, s01], [s10, s11]]
+      const int fl = ops[t].flags;
+      ops[t].type = FOP_R1;
+      ops[t].flags = 0;
+      m[0] = tr, m[1] = (fl & 1) ? -tr : tr, m[2] = (fl & 2) ? -tr : tr, m[3] = (fl & 4) ? -tr : tr;
+      nre[t] = 4;
+    }
+  }
+  int w = 0;
+  for (int i = 0; i < nop; ++i) {
+    if (update) {
+      const FOp& o = a.op[i];
+      if (ops[i].type != o.type || ops[i].b0 != o.b0 || ops[i].b1 != o.b1 || ops[i].flags != o.flags ||
+          ops[i].unit != o.unit)
+        return false;
+      w = o.moff;
+    } else {
+      ops[i].moff = (uint16_t)w;
+      a.op[i] = ops[i];
+    }
+    for (int e = 0; e < nre[i]; ++e) a.mat[w++] = (R)mats[(size_t)i * 32 + e];
+  }
+  return true;
 }
 
 template <typename R>
@@ -315,14 +428,13 @@ static bool build_fused(bt_plan* p, const std::vector<int>& take, uint64_t tilem
     rem.swap(rest);
   }
   // write matrices compactly in op order
-  int w = 0;
   ob0.clear();
   ob1.clear();
   for (int i = 0; i < nop; ++i) {
     ob0.push_back(a.op[i].b0);
     ob1.push_back(a.op[i].b1);
-    encode_op<R>(p->gates[kept[i]], a.op[i], a.mat, w);
   }
+  encode_pass<R>(p, kept, ob0, ob1, a, false);
   *nph = a.nphase;
   return !kept.empty();
 }
@@ -512,21 +624,10 @@ int bt_plan_add_kraus_sum(bt_plan* p, int k, const int32_t* qubits, int nk, cons
 template <typename R>
 static bool update_pass(bt_plan* p, PPass& ps, const std::vector<char>& touched) {
   FusedArgs<R>& a = *reinterpret_cast<FusedArgs<R>*>(ps.args.data());
-  for (size_t i = 0; i < ps.op_gate.size(); ++i) {
-    if (!touched[ps.op_gate[i]]) continue;
-    FOp t = a.op[i];
-    t.b0 = ps.op_b0[i];
-    t.b1 = ps.op_b1[i];
-    t.flags = 0;
-    t.unit = 0;
-    R tmp[32];
-    int tw = 0;
-    encode_op<R>(p->gates[ps.op_gate[i]], t, tmp, tw);
-    const FOp& o = a.op[i];
-    if (t.type != o.type || t.b0 != o.b0 || t.b1 != o.b1 || t.flags != o.flags || t.unit != o.unit) return false;
-    for (int e = 0; e < tw; ++e) a.mat[o.moff + e] = tmp[e];
-  }
-  return true;
+  bool any = false;
+  for (int gi : ps.op_gate) any |= touched[gi] != 0;
+  // the whole pass is re-encoded: the folded scalar depends on every op's factor
+  return !any || encode_pass<R>(p, ps.op_gate, ps.op_b0, ps.op_b1, a, true);
 }
 
 extern "C" {

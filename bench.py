@@ -263,7 +263,9 @@ def run_ours(args):
         for prog, _ in [layer_program(l, "unfused") for l in layers]:
             for m, qs in prog:
                 plan.add_matrix(m, qs)
+        t_c = time.perf_counter()
         plan.compile(True)
+        compile_s = time.perf_counter() - t_c
         if args.autotune:  # fusion width / register bits / packed code chosen by timing them here
             tuned = plan.autotune(st, reps=1)
         pstats = plan.stats()
@@ -369,6 +371,7 @@ def run_ours(args):
                                     % (args.depth, sum(lg for _, lg in packed))) if plan is not None else
                                    "one brickwork layer (logical gates: n one-qubit + CNOTs)",
                            "plan": pstats if plan is not None else None,
+                           "plan_compile_s": compile_s if plan is not None else None,
                            "tuning": {k: os.environ.get(k) for k in ("BTGPU_JIT_MINB", "BTGPU_PLAN_MAX_OPS",
                                                                       "BTGPU_TILE_RB", "BTGPU_JIT_PACKED",
                                                                       "BTGPU_JIT_DIRECT", "BTGPU_JIT_PREFETCH",

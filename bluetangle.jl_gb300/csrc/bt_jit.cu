@@ -79,7 +79,7 @@ int bt_jit_min_blocks() {
   return v;
 }
 int bt_jit_max_ops() {
-  static const int v = env_int("BTGPU_PLAN_MAX_OPS", 64, 8, BT_FUSED_MAX_OPS);
+  static const int v = env_int("BTGPU_PLAN_MAX_OPS", 96, 8, BT_FUSED_MAX_OPS);
   return v;
 }
 int bt_tile_rb(bool c64) {

@@ -7,7 +7,7 @@
 
 bool bt_jit_available();
 int bt_jit_min_blocks();  // CTAs per SM the specialised passes are compiled for (BTGPU_JIT_MINB, default 2)
-int bt_jit_max_ops();     // gates per specialised pass at most (BTGPU_PLAN_MAX_OPS, default 64)
+int bt_jit_max_ops();     // gates per specialised pass at most (BTGPU_PLAN_MAX_OPS, default 96)
 int bt_tile_rb(bool c64); // register bits per thread of a fused pass (complex64: BTGPU_TILE_RB, 4 or 5)
 bool bt_jit_packed_default();  // complex64 specialised passes in two-lane arithmetic (BTGPU_JIT_PACKED)
 // compiles (once per distinct pass structure) and returns one kernel entry per pass

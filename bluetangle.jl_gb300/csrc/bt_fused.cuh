@@ -28,8 +28,12 @@ enum {
   FOP_X1 = 8,  // anti-diagonal 2x2: out0 = p0*in1, out1 = p1*in0 (4 reals); unit: plain swap
   FOP_R1 = 9,  // real 2x2 (4 reals): H, RY, ...
   FOP_RX1 = 10,  // [[a, ib], [ib, a]] with a, b real (2 reals): RX
-  FOP_DH = 11,   // diag(1, q) (2 reals); unit 2: q = -1, 3: q = i, 4: q = -i (no arithmetic)
+  FOP_DH = 11,   // diag(1, q), or diag(q, 1) when flags bit 0 is set (2 reals);
+                 // unit 2: q = -1, 3: q = i, 4: q = -i (no arithmetic)
   FOP_HB = 12,   // butterfly [[1, s01], [s10, s11]], signs -1 where flags bits 0, 1, 2 are set (no reals)
+  FOP_RN = 13,   // real [[1, p], [q, s]] (flags bit 1 clear) or [[p, 1], [s, q]] (set); s = -1 if
+                 // flags bit 0 (2 reals p, q): a rotation with its larger entry factored out
+  FOP_RXN = 14,  // [[1, it], [it, 1]] (flags bit 1 clear) or [[-it, 1], [1, -it]] (set) (1 real t)
 };
 
 struct FOp {

@@ -233,15 +233,16 @@ __device__ __forceinline__ void op_rx1(R (&xr)[1 << NB], R (&xi)[1 << NB], const
   }
 }
 
-// diag(1, q) (the scalar d0 of diag(d0, d1) is folded elsewhere in the pass);
-// code 2: q = -1, 3: q = i, 4: q = -i
+// diag(1, q), or diag(q, 1) when lo (the factored scalar is folded elsewhere in
+// the pass); code 2: q = -1, 3: q = i, 4: q = -i
 template <typename R, int NB, int B>
-__device__ __forceinline__ void op_dh(R (&xr)[1 << NB], R (&xi)[1 << NB], const R* __restrict__ m, int code) {
+__device__ __forceinline__ void op_dh(R (&xr)[1 << NB], R (&xi)[1 << NB], const R* __restrict__ m, int code,
+                                      int lo) {
   if constexpr (B < NB) {
     const R qr = m[0], qi = m[1];
 #pragma unroll
     for (int j = 0; j < (1 << NB); ++j) {
-      if (!(j & (1 << B))) continue;
+      if (((j >> B) & 1) == lo) continue;
       const R ar = xr[j], ai = xi[j];
       if (code == 2) {
         xr[j] = -ar; xi[j] = -ai;
@@ -271,6 +272,48 @@ __device__ __forceinline__ void op_hb(R (&xr)[1 << NB], R (&xi)[1 << NB], int fl
       xi[j] = fma(s01, bi, ai);
       xr[k] = fma(s11, br, s10 * ar);
       xi[k] = fma(s11, bi, s10 * ai);
+    }
+  }
+}
+
+// real [[1, p], [q, s]] (flags bit 1 clear) or [[p, 1], [s, q]] (set), s = -1 if flags bit 0
+template <typename R, int NB, int B>
+__device__ __forceinline__ void op_rn(R (&xr)[1 << NB], R (&xi)[1 << NB], const R* __restrict__ m, int fl) {
+  if constexpr (B < NB) {
+    const R p = m[0], q = m[1], sg = (fl & 1) ? R(-1) : R(1);
+#pragma unroll
+    for (int j = 0; j < (1 << NB); ++j) {
+      if (j & (1 << B)) continue;
+      const int k = j | (1 << B);
+      const R ar = xr[j], ai = xi[j], br = xr[k], bi = xi[k];
+      if (!(fl & 2)) {
+        xr[j] = fma(p, br, ar); xi[j] = fma(p, bi, ai);
+        xr[k] = fma(q, ar, sg * br); xi[k] = fma(q, ai, sg * bi);
+      } else {
+        xr[j] = fma(p, ar, br); xi[j] = fma(p, ai, bi);
+        xr[k] = fma(q, br, sg * ar); xi[k] = fma(q, bi, sg * ai);
+      }
+    }
+  }
+}
+
+// [[1, it], [it, 1]] (flags bit 1 clear) or [[-it, 1], [1, -it]] (set)
+template <typename R, int NB, int B>
+__device__ __forceinline__ void op_rxn(R (&xr)[1 << NB], R (&xi)[1 << NB], const R* __restrict__ m, int fl) {
+  if constexpr (B < NB) {
+    const R t = m[0];
+#pragma unroll
+    for (int j = 0; j < (1 << NB); ++j) {
+      if (j & (1 << B)) continue;
+      const int k = j | (1 << B);
+      const R ar = xr[j], ai = xi[j], br = xr[k], bi = xi[k];
+      if (!(fl & 2)) {
+        xr[j] = fma(-t, bi, ar); xi[j] = fma(t, br, ai);
+        xr[k] = fma(-t, ai, br); xi[k] = fma(t, ar, bi);
+      } else {
+        xr[j] = fma(t, ai, br); xi[j] = fma(-t, ar, bi);
+        xr[k] = fma(t, bi, ar); xi[k] = fma(-t, br, ai);
+      }
     }
   }
 }
@@ -347,8 +390,10 @@ __device__ __forceinline__ void apply_op(R (&xr)[1 << NB], R (&xi)[1 << NB], con
     case FOP_X1: ONE(op_x1, m, o.unit) break;
     case FOP_R1: ONE(op_r1, m) break;
     case FOP_RX1: ONE(op_rx1, m) break;
-    case FOP_DH: ONE(op_dh, m, o.unit) break;
+    case FOP_DH: ONE(op_dh, m, o.unit, o.flags & 1) break;
     case FOP_HB: ONE(op_hb, o.flags) break;
+    case FOP_RN: ONE(op_rn, m, o.flags) break;
+    case FOP_RXN: ONE(op_rxn, m, o.flags) break;
 #undef ONE
   }
 }

@@ -168,10 +168,10 @@ static void emit_op(std::ostringstream& o, const FOp& op, int NB) {
       });
       o << "    }\n";
       break;
-    case FOP_DH:  // diag(1, q): the bit-1 half only
+    case FOP_DH:  // diag(1, q) (diag(q, 1) with flags bit 0): one half only
       if (op.unit == 0) o << "    { const R qr=" << M(0) << ",qi=" << M(1) << ";\n";
       for (int j = 0; j < D; ++j) {
-        if (!(j & (1 << b0))) continue;
+        if (((j >> b0) & 1) == (op.flags & 1)) continue;
         o << "      { const R ar=x" << j << ",ai=y" << j << ";";
         if (op.unit == 2) o << " x" << j << "=-ar; y" << j << "=-ai; }\n";
         else if (op.unit == 3) o << " x" << j << "=-ai; y" << j << "=ar; }\n";
@@ -191,6 +191,35 @@ static void emit_op(std::ostringstream& o, const FOp& op, int NB) {
       });
       break;
     }
+    case FOP_RN: {  // [[1, p], [q, s]] or [[p, 1], [s, q]]: one FMA per component
+      const bool B = op.flags & 2;
+      const char* sg = (op.flags & 1) ? "-" : "";
+      o << "    { const R p=" << M(0) << ",q=" << M(1) << ";\n";
+      pairs(b0, [&](int j, int k) {
+        o << "      { const R ar=x" << j << ",ai=y" << j << ",br=x" << k << ",bi=y" << k << ";";
+        if (!B)
+          o << " x" << j << "=fm(p,br,ar); y" << j << "=fm(p,bi,ai); x" << k << "=fm(q,ar," << sg << "br); y" << k
+            << "=fm(q,ai," << sg << "bi); }\n";
+        else
+          o << " x" << j << "=fm(p,ar,br); y" << j << "=fm(p,ai,bi); x" << k << "=fm(q,br," << sg << "ar); y" << k
+            << "=fm(q,bi," << sg << "ai); }\n";
+      });
+      o << "    }\n";
+      break;
+    }
+    case FOP_RXN:  // [[1, it], [it, 1]] or [[-it, 1], [1, -it]]
+      o << "    { const R t=" << M(0) << ";\n";
+      pairs(b0, [&](int j, int k) {
+        o << "      { const R ar=x" << j << ",ai=y" << j << ",br=x" << k << ",bi=y" << k << ";";
+        if (!(op.flags & 2))
+          o << " x" << j << "=fm(-t,bi,ar); y" << j << "=fm(t,br,ai); x" << k << "=fm(-t,ai,br); y" << k
+            << "=fm(t,ar,bi); }\n";
+        else
+          o << " x" << j << "=fm(t,ai,br); y" << j << "=fm(-t,ar,bi); x" << k << "=fm(t,bi,ar); y" << k
+            << "=fm(-t,br,ai); }\n";
+      });
+      o << "    }\n";
+      break;
     case FOP_RX1:
       o << "    { const R ca=" << M(0) << ",cb=" << M(1) << ";\n";
       pairs(b0, [&](int j, int k) {
@@ -360,19 +389,24 @@ static bool emit_op_packed(std::ostringstream& o, const FOp& op, int NB, int P) 
     return true;
   }
   if (op.type == FOP_DH) {
-    // diag(1, q) on bit b0: on the pack bit only the high lanes change
-    const bool onp = b0 == P;
-    const char* SG = onp ? "0x8000000000000000ULL" : "0x8000000080000000ULL";
+    // diag(1, q) (diag(q, 1) with flags bit 0) on bit b0: on the pack bit only the
+    // lanes of the multiplied half change (high lanes for diag(1, q))
+    const bool onp = b0 == P, lo = op.flags & 1;
+    const char* SG = !onp ? "0x8000000080000000ULL" : (lo ? "0x80000000ULL" : "0x8000000000000000ULL");
+    const char* HIT = lo ? "0xFFFFFFFFULL" : "0xFFFFFFFF00000000ULL";   // lane changed on the pack bit
+    const char* KEEP = lo ? "0xFFFFFFFF00000000ULL" : "0xFFFFFFFFULL";
     if (op.unit == 0) {
       o << "    { const float qr=" << M(0) << ", qi=" << M(1) << ";";
-      if (onp)
+      if (onp && !lo)
         o << " const u64 er=pk(1.0f,qr), ei=pk(0.0f,qi), nei=pk(-0.0f,-qi);";
+      else if (onp)
+        o << " const u64 er=pk(qr,1.0f), ei=pk(qi,0.0f), nei=pk(-qi,-0.0f);";
       else
         o << " const u64 er=bc(qr), ei=bc(qi), nei=bc(-qi);";
       o << "\n";
     }
     for (int j = 0; j < D; ++j) {
-      if (!k0(j) || (!onp && !(j & (1 << b0)))) continue;
+      if (!k0(j) || (!onp && ((j >> b0) & 1) == (int)lo)) continue;
       const std::string X = "X" + std::to_string(j), Y = "Y" + std::to_string(j);
       if (op.unit == 0)
         o << "      { const u64 ar=" << X << ", ai=" << Y << "; " << X << "=ffma2(er,ar,fmul2(nei,ai)); " << Y
@@ -383,12 +417,12 @@ static bool emit_op_packed(std::ostringstream& o, const FOp& op, int NB, int P) 
         o << "    { const u64 ar=" << X << "; " << X << "=" << Y << "^" << SG << "; " << Y << "=ar; }\n";
       else if (!onp)  // unit 4
         o << "    { const u64 ar=" << X << "; " << X << "=" << Y << "; " << Y << "=ar^" << SG << "; }\n";
-      else if (op.unit == 3)  // high lane (x, y) -> (-y, x)
-        o << "    { const u64 ar=" << X << ", ai=" << Y << "; " << X << "=(ar&0xFFFFFFFFULL)|((ai^" << SG
-          << ")&0xFFFFFFFF00000000ULL); " << Y << "=(ai&0xFFFFFFFFULL)|(ar&0xFFFFFFFF00000000ULL); }\n";
-      else  // high lane (x, y) -> (y, -x)
-        o << "    { const u64 ar=" << X << ", ai=" << Y << "; " << X << "=(ar&0xFFFFFFFFULL)|(ai&0xFFFFFFFF00000000ULL); "
-          << Y << "=(ai&0xFFFFFFFFULL)|((ar^" << SG << ")&0xFFFFFFFF00000000ULL); }\n";
+      else if (op.unit == 3)  // hit lane (x, y) -> (-y, x)
+        o << "    { const u64 ar=" << X << ", ai=" << Y << "; " << X << "=(ar&" << KEEP << ")|((ai^" << SG << ")&" << HIT
+          << "); " << Y << "=(ai&" << KEEP << ")|(ar&" << HIT << "); }\n";
+      else  // hit lane (x, y) -> (y, -x)
+        o << "    { const u64 ar=" << X << ", ai=" << Y << "; " << X << "=(ar&" << KEEP << ")|(ai&" << HIT << "); " << Y
+          << "=(ai&" << KEEP << ")|((ar^" << SG << ")&" << HIT << "); }\n";
     }
     if (op.unit == 0) o << "    }\n";
     return true;
@@ -411,6 +445,34 @@ static bool emit_op_packed(std::ostringstream& o, const FOp& op, int NB, int P) 
       o << "    }\n";
       return true;
     }
+    case FOP_RN: {  // one two-lane FMA per register; s = -1 flips the addend's signs
+      const bool B = op.flags & 2, neg = op.flags & 1;
+      o << "    { const u64 pp=bc(" << M(0) << "), qq=bc(" << M(1) << ");\n";
+      pairs(b0, [&](int j, int k) {
+        for (int c = 0; c < 2; ++c) {
+          const std::string A = (c ? "Y" : "X") + std::to_string(j), Bk = (c ? "Y" : "X") + std::to_string(k);
+          const std::string sa = neg ? "ua^0x8000000080000000ULL" : "ua", sb = neg ? "ub^0x8000000080000000ULL" : "ub";
+          o << "      { const u64 ua=" << A << ", ub=" << Bk << "; ";
+          if (!B) o << A << "=ffma2(pp,ub,ua); " << Bk << "=ffma2(qq,ua," << sb << "); }\n";
+          else o << A << "=ffma2(pp,ua,ub); " << Bk << "=ffma2(qq,ub," << sa << "); }\n";
+        }
+      });
+      o << "    }\n";
+      return true;
+    }
+    case FOP_RXN:
+      o << "    { const u64 tt=bc(" << M(0) << "), nt=bc(-" << M(0) << ");\n";
+      pairs(b0, [&](int j, int k) {
+        o << "      { const u64 ar=X" << j << ",ai=Y" << j << ",br=X" << k << ",bi=Y" << k << ";";
+        if (!(op.flags & 2))
+          o << " X" << j << "=ffma2(nt,bi,ar); Y" << j << "=ffma2(tt,br,ai); X" << k << "=ffma2(nt,ai,br); Y" << k
+            << "=ffma2(tt,ar,bi); }\n";
+        else
+          o << " X" << j << "=ffma2(tt,ai,br); Y" << j << "=ffma2(nt,ar,bi); X" << k << "=ffma2(tt,bi,ar); Y" << k
+            << "=ffma2(nt,br,ai); }\n";
+      });
+      o << "    }\n";
+      return true;
     case FOP_G1:
       o << "    {";
       bcs("m0", 0, false), bcs("m1", 1, false), bcs("n1", 1, true), bcs("m2", 2, false), bcs("m3", 3, false);

@@ -203,15 +203,21 @@ static void encode_op(const PGate& g, FOp& o, double* mat, int& nre, double* fac
     // m = [m00r m00i m01r m01i m10r m10i m11r m11i]
     const bool real = m[1] == 0 && m[3] == 0 && m[5] == 0 && m[7] == 0;
     const double a0 = fabs(m[0]);
-    if (cls == 2 && factor && (m[0] != 0 || m[1] != 0)) {
-      // d1 / d0 on the bit-1 half; exact -1, i, -i become sign flips and swaps
-      const double n = m[0] * m[0] + m[1] * m[1];
-      const double qr = (m[6] * m[0] + m[7] * m[1]) / n, qi = (m[7] * m[0] - m[6] * m[1]) / n;
+    const double n0 = m[0] * m[0] + m[1] * m[1], n1 = m[6] * m[6] + m[7] * m[7];
+    if (cls == 2 && factor && (n0 != 0 || n1 != 0)) {
+      // the larger entry factored out: d1 / d0 on the bit-1 half (or d0 / d1 on
+      // the bit-0 half); exact -1, i, -i become sign flips and swaps
+      const bool lo = n1 > n0;
+      const double* f = lo ? m + 6 : m;   // factored entry
+      const double* e = lo ? m : m + 6;   // the other
+      const double n = lo ? n1 : n0;
+      const double qr = (e[0] * f[0] + e[1] * f[1]) / n, qi = (e[1] * f[0] - e[0] * f[1]) / n;
       o.type = FOP_DH;
+      o.flags = lo ? 1 : 0;
       o.unit = (qr == -1 && qi == 0) ? 2 : (qr == 0 && qi == 1) ? 3 : (qr == 0 && qi == -1) ? 4 : 0;
       mat[w++] = qr;
       mat[w++] = qi;
-      fac[0] = m[0], fac[1] = m[1];
+      fac[0] = f[0], fac[1] = f[1];
     } else if (cls == 2) {
       o.type = FOP_D1;
       mat[w++] = m[0];
@@ -231,6 +237,21 @@ static void encode_op(const PGate& g, FOp& o, double* mat, int& nre, double* fac
       o.flags = (uint8_t)(((m[2] < 0) != (m[0] < 0)) | (((m[4] < 0) != (m[0] < 0)) << 1) |
                           (((m[6] < 0) != (m[0] < 0)) << 2));
       fac[0] = m[0];
+    } else if (real && factor && m[0] != 0 && fabs(m[6]) == a0 && a0 >= fabs(m[2]) && a0 >= fabs(m[4])) {
+      // [[a, b], [c, d]] with |d| = |a| >= |b|: a [[1, b/a], [c/a, d/a = +-1]]
+      o.type = FOP_RN;
+      o.flags = (uint8_t)((m[6] < 0) != (m[0] < 0));
+      mat[w++] = m[2] / m[0];
+      mat[w++] = m[4] / m[0];
+      fac[0] = m[0];
+    } else if (real && factor && m[2] != 0 && fabs(m[4]) == fabs(m[2]) && fabs(m[2]) >= a0 &&
+               fabs(m[2]) >= fabs(m[6])) {
+      // |c| = |b| >= |a|: b [[a/b, 1], [c/b = +-1, d/b]]
+      o.type = FOP_RN;
+      o.flags = (uint8_t)(2 | ((m[4] < 0) != (m[2] < 0)));
+      mat[w++] = m[0] / m[2];
+      mat[w++] = m[6] / m[2];
+      fac[0] = m[2];
     } else if (real) {
       o.type = FOP_R1;
       mat[w++] = m[0];
@@ -238,9 +259,22 @@ static void encode_op(const PGate& g, FOp& o, double* mat, int& nre, double* fac
       mat[w++] = m[4];
       mat[w++] = m[6];
     } else if (m[0] == m[6] && m[1] == 0 && m[7] == 0 && m[2] == 0 && m[4] == 0 && m[3] == m[5]) {
-      o.type = FOP_RX1;
-      mat[w++] = m[0];
-      mat[w++] = m[3];
+      // [[a, ib], [ib, a]]
+      if (factor && (m[0] != 0 || m[3] != 0)) {
+        o.type = FOP_RXN;
+        if (fabs(m[0]) >= fabs(m[3])) {  // a [[1, i b/a], [i b/a, 1]]
+          mat[w++] = m[3] / m[0];
+          fac[0] = m[0];
+        } else {  // ib [[-i a/b, 1], [1, -i a/b]]
+          o.flags = 2;
+          mat[w++] = m[0] / m[3];
+          fac[0] = 0, fac[1] = m[3];
+        }
+      } else {
+        o.type = FOP_RX1;
+        mat[w++] = m[0];
+        mat[w++] = m[3];
+      }
     } else {
       o.type = FOP_G1;
       for (int e = 0; e < 8; ++e) mat[w++] = m[e];
@@ -286,12 +320,12 @@ static void encode_op(const PGate& g, FOp& o, double* mat, int& nre, double* fac
 // (type, bits, flags) would change, which needs a recompile.
 template <typename R>
 static bool encode_pass(bt_plan* p, const std::vector<int>& kept, const std::vector<uint8_t>& ob0,
-                        const std::vector<uint8_t>& ob1, FusedArgs<R>& a, bool update) {
+                        const std::vector<uint8_t>& ob1, FusedArgs<R>& a, bool update, bool factor = true) {
   const int nop = (int)kept.size();
   std::vector<FOp> ops(nop);
   std::vector<double> mats((size_t)nop * 32);
   std::vector<int> nre(nop);
-  const bool factor = factor_on();
+  factor = factor && factor_on();
   double tr = 1.0, ti = 0.0;  // product of the factors
   for (int i = 0; i < nop; ++i) {
     FOp& o = ops[i];
@@ -304,23 +338,43 @@ static bool encode_pass(bt_plan* p, const std::vector<int>& kept, const std::vec
     ti = tr * f[1] + ti * f[0];
     tr = r;
   }
+  // the factored ops grow amplitudes by at most the inverse of the scalar: keep
+  // it well inside the complex64 range, else encode the pass without factors
+  const double mag = sqrt(tr * tr + ti * ti);
+  if (factor && !(mag > 1e-18 && mag < 1e18)) return encode_pass<R>(p, kept, ob0, ob1, a, update, false);
   if (tr != 1.0 || ti != 0.0) {
-    auto is = [&](int i, std::initializer_list<int> types) {
-      for (int t : types)
-        if (ops[i].type == t) return true;
-      return false;
+    const bool real = ti == 0;
+    int t = -1, mode = 0;
+    auto pick = [&](int m, auto&& ok) {
+      for (int i = 0; i < nop && t < 0; ++i)
+        if (ok(ops[i])) t = i, mode = m;
     };
-    int t = -1, mode = 0;  // 1 complex scale, 2 real scale, 3 half diagonal -> D1, 4 butterfly -> R1
-    for (int i = 0; i < nop && t < 0; ++i)
-      if (is(i, {FOP_G1, FOP_G2, FOP_D1, FOP_D2}) || (is(i, {FOP_P2, FOP_X1}) && !ops[i].unit)) t = i, mode = 1;
-    for (int i = 0; i < nop && t < 0 && ti == 0; ++i)
-      if (ops[i].type == FOP_R1) t = i, mode = 2;
-    for (int i = 0; i < nop && t < 0; ++i)
-      if (ops[i].type == FOP_DH) t = i, mode = 3;
-    for (int i = 0; i < nop && t < 0 && ti == 0; ++i)
-      if (ops[i].type == FOP_HB) t = i, mode = 4;
-    if (t < 0) return false;  // unreachable: a factor comes from a DH (complex) or HB (real) op
+    // in order of the arithmetic the fold adds: none, then the cheapest expansion
+    pick(1, [](const FOp& o) {
+      return o.type == FOP_G1 || o.type == FOP_G2 || o.type == FOP_D1 || o.type == FOP_D2 ||
+             ((o.type == FOP_P2 || o.type == FOP_X1) && !o.unit);
+    });
+    if (real) pick(2, [](const FOp& o) { return o.type == FOP_R1; });
+    pick(3, [](const FOp& o) { return o.type == FOP_DH; });
+    if (real) pick(4, [](const FOp& o) { return o.type == FOP_RN || o.type == FOP_HB; });
+    pick(5, [](const FOp& o) { return o.type == FOP_RXN || o.type == FOP_RN || o.type == FOP_HB; });
+    if (t < 0) return encode_pass<R>(p, kept, ob0, ob1, a, update, false);
     double* m = &mats[(size_t)t * 32];
+    FOp& o = ops[t];
+    // the factored op as a real or complex 2x2 [[e00, e01], [e10, e11]] (RN, HB, RXN)
+    auto full = [&](double (&e)[8]) {
+      for (double& x : e) x = 0;
+      if (o.type == FOP_HB) {
+        e[0] = 1, e[2] = (o.flags & 1) ? -1 : 1, e[4] = (o.flags & 2) ? -1 : 1, e[6] = (o.flags & 4) ? -1 : 1;
+      } else if (o.type == FOP_RN) {
+        const double sg = (o.flags & 1) ? -1 : 1;
+        if (o.flags & 2) e[0] = m[0], e[2] = 1, e[4] = sg, e[6] = m[1];
+        else e[0] = 1, e[2] = m[0], e[4] = m[1], e[6] = sg;
+      } else {  // RXN
+        if (o.flags & 2) e[1] = -m[0], e[2] = 1, e[4] = 1, e[7] = -m[0];
+        else e[0] = 1, e[3] = m[0], e[5] = m[0], e[6] = 1;
+      }
+    };
     if (mode == 1) {
       for (int e = 0; e + 1 < nre[t]; e += 2) {
         const double r = m[e] * tr - m[e + 1] * ti;
@@ -329,18 +383,28 @@ static bool encode_pass(bt_plan* p, const std::vector<int>& kept, const std::vec
       }
     } else if (mode == 2) {
       for (int e = 0; e < nre[t]; ++e) m[e] *= tr;
-    } else if (mode == 3) {  // diag(s, s q)
-      const double qr = m[0], qi = m[1];
-      ops[t].type = FOP_D1;
-      ops[t].unit = 0;
-      m[0] = tr, m[1] = ti, m[2] = tr * qr - ti * qi, m[3] = tr * qi + ti * qr;
+    } else if (mode == 3) {  // diag(s, s q) or diag(s q, s)
+      const double qr = m[0], qi = m[1], sr = tr * qr - ti * qi, si = tr * qi + ti * qr;
+      const bool lo = o.flags & 1;
+      o.type = FOP_D1;
+      o.unit = 0;
+      o.flags = 0;
+      m[0] = lo ? sr : tr, m[1] = lo ? si : ti, m[2] = lo ? tr : sr, m[3] = lo ? ti : si;
       nre[t] = 4;
-    } else {  // s [[1, s01], [s10, s11]]
-      const int fl = ops[t].flags;
-      ops[t].type = FOP_R1;
-      ops[t].flags = 0;
-      m[0] = tr, m[1] = (fl & 1) ? -tr : tr, m[2] = (fl & 2) ? -tr : tr, m[3] = (fl & 4) ? -tr : tr;
-      nre[t] = 4;
+    } else {
+      double e[8];
+      full(e);
+      o.flags = 0;
+      o.unit = 0;
+      if (mode == 4) {  // real scalar: R1
+        o.type = FOP_R1;
+        m[0] = e[0] * tr, m[1] = e[2] * tr, m[2] = e[4] * tr, m[3] = e[6] * tr;
+        nre[t] = 4;
+      } else {  // G1
+        o.type = FOP_G1;
+        for (int k = 0; k < 8; k += 2) m[k] = e[k] * tr - e[k + 1] * ti, m[k + 1] = e[k] * ti + e[k + 1] * tr;
+        nre[t] = 8;
+      }
     }
   }
   int w = 0;

@@ -1,6 +1,8 @@
 """Fused plans (bt_plan_*): the fused tile passes apply the same map as the gates
 one by one.  Checked against the oracle on state vectors and density matrices,
 both precisions, batched members, and mixes with gates the tile cannot hold."""
+import math
+
 import numpy as np
 import pytest
 
@@ -121,6 +123,69 @@ def test_plan_brickwork_matches_oracle(ctx, oracle, prec, tol, n):
     assert np.abs(s.to_numpy() - ref).max() < tol
     if n >= (13 if prec == "c64" else 12):
         assert st["fused_passes"] >= 1 and st["passes"] < len(ops) / 4
+
+
+def _factored_forms(rng):
+    """One-qubit matrices of every factored encoding: half diagonals (upper and
+    lower half, exact -1 / i / -i), butterflies with each sign pattern,
+    rotations with the diagonal or the off-diagonal entry the larger, RX-type in
+    both regimes, non-unitary diagonals, and one diagonal small enough that the
+    pass is encoded without factors."""
+    c, s = math.cos(0.3), math.sin(0.3)
+    h = 1 / math.sqrt(2)
+    mats = [np.diag([1, -1]), np.diag([1, 1j]), np.diag([1, -1j]), np.diag([1, np.exp(0.7j)]),
+            np.diag([0.2, 1.3]), np.diag([1.3j, 0.2]), np.diag([np.exp(-0.4j), np.exp(0.4j)]),
+            h * np.array([[1, 1], [1, -1]]), h * np.array([[1, -1], [1, 1]]), h * np.array([[-1, 1], [1, 1]]),
+            np.array([[c, -s], [s, c]]), np.array([[s, -c], [c, s]]), np.array([[c, s], [s, -c]]),
+            np.array([[c, -1j * s], [-1j * s, c]]), np.array([[s, -1j * c], [-1j * c, s]]),
+            np.array([[0.3, 0.9], [-0.9, 0.3]]), np.diag([1e-19, 1e-19])]
+    return [np.asarray(m, dtype=complex) for m in mats]
+
+
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-12), ("c64", 5e-5)])
+def test_plan_factored_encodings(ctx, oracle, prec, tol):
+    """Plans whose passes hold every factored one-qubit form (the scalar taken out
+    of each op and folded back into one op of the pass) apply the same map as the
+    gates one by one; a dense two-qubit gate and a CNOT ride along."""
+    import bluetangle_gpu as bt
+    rng = np.random.default_rng(31)
+    n = 14
+    mats = _factored_forms(rng)
+    seq = []
+    for rep in range(3):
+        for i, m in enumerate(mats):
+            if i == len(mats) - 1 and rep:
+                continue  # the tiny diagonal once (it scales the state by 1e-19)
+            seq.append((m, [int(rng.integers(1, n + 1))]))
+        a, b = [int(x) for x in rng.choice(np.arange(1, n + 1), 2, replace=False)]
+        seq.append((runitary(rng, 4), [a, b]))
+        seq.append((np.eye(4, dtype=complex)[[0, 1, 3, 2]], [b, a]))
+    psi = rstate(rng, n)
+    ref = psi.copy()
+    plan = bt.Plan(n, prec=prec)
+    for m, qs in seq:
+        plan.add_matrix(m, qs)
+        ref = oracle.apply_k(ref, m, qs, [])
+    plan.compile()
+    s = bt.state_from(psi, prec)
+    plan.run(s)
+    scale = np.abs(ref).max()  # errors relative to the state's scale
+    assert np.abs(s.to_numpy() - ref).max() < tol * scale
+    # in-place angle update of a rotation and a diagonal (the folded scalar changes)
+    ref = psi.copy()
+    upd = []
+    for i, (m, qs) in enumerate(seq):
+        if i in (3, 10):
+            m = np.diag([1, np.exp(1.1j)]) if i == 3 else np.array([[s_, -c_], [c_, s_]])
+            upd.append((i, m))
+        ref = oracle.apply_k(ref, m, qs, [])
+    plan.set_matrices(upd)
+    s2 = bt.state_from(psi, prec)
+    plan.run(s2)
+    assert np.abs(s2.to_numpy() - ref).max() < tol * scale
+
+
+c_, s_ = math.cos(1.2), math.sin(1.2)
 
 
 @pytest.mark.parametrize("prec,tol", [("c128", 1e-12), ("c64", 5e-5)])

@@ -330,6 +330,24 @@ def run_ours(args):
     traffic = None
     if args.prec == "c64":
         traffic = TRAFFIC_BYTES_PER_AMP["plan" if plan is not None else "sweep"] * 2 ** args.n
+    # the arithmetic side: the plan's algorithmic flops (an FMA counts two) against
+    # the CUDA-core peak at the sampled SM clock (FP32: 128 lanes x 2 flops per SM
+    # per cycle; FP64: the nominal 1.25 TFLOP/s of this part)
+    compute = None
+    if plan is not None:
+        cost = plan.cost()
+        flops = cost["flops_per_amp"] * 2 ** args.n * args.steps
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        if args.prec == "c64" and clk.get("sm_mhz"):
+            fpeak, fkind = sms * 128 * 2 * clk["sm_mhz"] * 1e6, "FP32 CUDA cores at the sampled SM clock"
+        else:
+            fpeak, fkind = 1.25e12, "nominal FP64"
+        fach = flops / (ms / 1e3)
+        hbm_floor = cost["bytes_per_amp"] * 2 ** args.n / (peak * 1e9)
+        compute = {"achieved": fach / 1e12, "peak": fpeak / 1e12, "unit": "TFLOP/s", "frac": fach / fpeak,
+                   "peak_kind": fkind, "flops_per_amp": cost["flops_per_amp"],
+                   "bytes_per_amp": cost["bytes_per_amp"],
+                   "floors_ms_per_step": {"hbm": hbm_floor * 1e3, "arith": flops / args.steps / fpeak * 1e3}}
 
     # end to end through the public API: per step the layer's matrices go from host
     # memory into the launches, and <Z_i> for every qubit comes back to the host
@@ -386,7 +404,7 @@ def run_ours(args):
                              "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                              "kernel": "k_fused (tile pass)" if plan is not None else "k_gate (dense sweep)",
                              "bytes_per_launch": bytes_per_launch,
-                             "launches": launches},
+                             "launches": launches, "compute": compute},
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
                 "host_s": host_dt}
         print(json.dumps(line), flush=True)

@@ -520,6 +520,13 @@ class Plan:
         self.ctx.check(L.lib().bt_plan_stats(self.h, *[ctypes.byref(x) for x in v]))
         return dict(zip(("gates", "passes", "fused_passes", "phases", "jit_passes"), (x.value for x in v)))
 
+    def cost(self):
+        """Per amplitude of a member and run: real flops of the compiled passes'
+        arithmetic (an FMA counts two) and HBM bytes moved."""
+        f, b = ctypes.c_double(0), ctypes.c_double(0)
+        self.ctx.check(L.lib().bt_plan_cost(self.h, ctypes.byref(f), ctypes.byref(b)))
+        return {"flops_per_amp": f.value, "bytes_per_amp": b.value}
+
     def run(self, state, member=-1):
         self.ctx.check(L.lib().bt_plan_run(self.h, state.h, member))
         return state

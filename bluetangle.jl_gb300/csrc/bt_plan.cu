@@ -893,6 +893,41 @@ int bt_plan_set_tuning(bt_plan* p, int max_ops, int tile_rb, int packed, int til
   return BT_OK;
 }
 
+// arithmetic of one op per amplitude of the state, in real flops (an FMA counts
+// two), as the specialised code does it
+static double op_flops(const FOp& o) {
+  switch (o.type) {
+    case FOP_G1: return 14;
+    case FOP_G2: return 32;
+    case FOP_D1: case FOP_R1: case FOP_RX1: case FOP_D2: return 6;
+    case FOP_P2: case FOP_X1: return o.unit ? 0 : 6;
+    case FOP_DH: return o.unit ? 0 : 3;
+    case FOP_RN: case FOP_RXN: return 4;
+    case FOP_HB: return 2;
+    default: return 0;  // CX, SW: register renaming
+  }
+}
+
+int bt_plan_cost(const bt_plan* p, double* flops_per_amp, double* bytes_per_amp) {
+  if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "plan is NULL");
+  if (!p->compiled) return bt_fail(p->ctx, BT_ERR_BAD_ARG, "plan is not compiled");
+  const bool c64 = p->prec == BT_PREC_C64;
+  double fl = 0, by = 0;
+  for (const auto& ps : p->passes) {
+    by += 2.0 * (c64 ? 8 : 16);
+    if (ps.kind == 0) {
+      const FOp* ops = c64 ? reinterpret_cast<const FusedArgs<float>*>(ps.args.data())->op
+                           : reinterpret_cast<const FusedArgs<double>*>(ps.args.data())->op;
+      for (int i = 0; i < ps.ngates; ++i) fl += op_flops(ops[i]);
+    } else {
+      fl += 8.0 * (1 << p->gates[ps.gate].k);  // dense sweep: 2^k complex multiply-adds
+    }
+  }
+  if (flops_per_amp) *flops_per_amp = fl;
+  if (bytes_per_amp) *bytes_per_amp = by;
+  return BT_OK;
+}
+
 int bt_plan_stats(const bt_plan* p, int64_t* ngates, int64_t* npasses, int64_t* nfused, int64_t* nphases,
                   int64_t* njit) {
   if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "plan is NULL");

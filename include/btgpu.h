@@ -175,6 +175,10 @@ int bt_plan_compile(bt_plan* p, int mode);
 int bt_plan_set_matrices(bt_plan* p, int count, const int64_t* add_index, const double* mats);
 /* njit: fused passes running as kernels specialised for the plan (NVRTC, compiled
  * by bt_plan_compile); the others run on the generic fused kernel */
+/* algorithmic cost of one run per amplitude of a member: real flops of the
+ * compiled passes' arithmetic (an FMA counts two) and HBM bytes moved (one read
+ * and one write of the state per pass) */
+int bt_plan_cost(const bt_plan* p, double* flops_per_amp, double* bytes_per_amp);
 int bt_plan_stats(const bt_plan* p, int64_t* ngates, int64_t* npasses, int64_t* nfused, int64_t* nphases,
                   int64_t* njit);
 /* tuning of the fused passes (applies at the next bt_plan_compile; 0 / -1 keep

@@ -88,9 +88,10 @@ SIGNATURES = {
     "bt_serve_destroy": (i32, [P]),
     "bt_serve_add_plan_client": (i32, [P, P, i32, P, P, P, P]),
     "bt_serve_add_program_client": (i32, [P, P, i32, P, P, P, P]),
+    "bt_serve_add_packed_client": (i32, [P, P, i32, P, P, P, P]),
     "bt_serve_submit": (i32, [P, i64, i32, P, P, u64, P]),
     "bt_serve_poll": (i32, [P, i64, i64, P, P, P]),
-    "bt_serve_stats": (i32, [P, P, P, P, P, P]),
+    "bt_serve_stats": (i32, [P, P, P, P, P, P, P]),
     "bt_sample": (i32, [P, i64, i64, P, u64, P]),
     "bt_probabilities": (i32, [P, i64, P]),
     "bt_sample_noalloc": (i32, [P, i32, i32, i64, P, u64, u64, P, P]),

@@ -76,13 +76,16 @@ class ClientSpec:
     def nparams(self):
         return 2 * self.n * self.depth
 
-    def footprint(self, prec):
+    def footprint(self, prec, pack=1):
+        """HBM bytes of the client's resident state; pack: members of a packed
+        state-vector client (NativeServer, n small enough for one CTA)."""
         es = 8 if prec == "c64" else 16
         if self.kind == "dm":
             return (4 ** self.n) * es
         if self.kind == "traj":
             return self.ntraj * (2 ** self.n) * es
-        return (2 ** self.n) * es
+        from .trajectories import SHARED_MAX_N
+        return (pack if pack > 1 and self.n <= SHARED_MAX_N[prec] else 1) * (2 ** self.n) * es
 
 
 def random_terms(rng, n, count):
@@ -325,9 +328,12 @@ class NativeServer:
     scheduling inside libbtgpu) over the same clients and requests as Server.
     State-vector and density-matrix clients are compiled plans; trajectory
     clients are programs (n <= 14 complex64 / 13 complex128), their draws keyed
-    by the request's seed on the device."""
+    by the request's seed on the device.  State-vector clients small enough for
+    one CTA are packed: a program of `pack` members, one request per member, so
+    up to `pack` queued requests of the client run as one launch (pack=1: plans
+    for every state-vector client)."""
 
-    def __init__(self, specs, lanes=8, prec="c64", hbm_budget=None, device=0, seed=1234, tiered=True):
+    def __init__(self, specs, lanes=8, prec="c64", hbm_budget=None, device=0, seed=1234, tiered=True, pack=8):
         from . import trajectories as T
         lib = L.lib()
         h = ctypes.c_void_p()
@@ -347,7 +353,19 @@ class NativeServer:
             zs = np.ascontiguousarray([t[2] for t in spec.terms], dtype=np.uint64)
             cs = np.ascontiguousarray([t[0] for t in spec.terms], dtype=np.float64)
             cid = ctypes.c_int64()
-            if spec.kind in ("sv", "dm"):
+            if spec.kind == "sv" and pack > 1 and n <= T.SHARED_MAX_N[prec]:
+                prog = T.Program(n, pack, prec, self.ctx)
+                pidx = []
+                for op in hea_ops(n, spec.depth, theta0):
+                    qs = [op.qubit] if op.q == 1 else [op.qubit, op.target_qubit]
+                    if op.name in ("RY", "RZ"):  # per-member matrices: one request per member
+                        pidx.append(prog.add_gate([op.mat] * pack, qs))
+                    else:
+                        prog.add_gate(op.mat, qs)
+                L.check(lib.bt_serve_add_packed_client(h, prog.h, len(cs), _ptr(xs), _ptr(zs), _ptr(cs),
+                                                        ctypes.byref(cid)))
+                self.keep.append(prog)
+            elif spec.kind in ("sv", "dm"):
                 dm = spec.kind == "dm"
                 plan = Plan(n, spec.kind, prec, self.ctx)
                 ops = hea_ops(n, spec.depth, theta0)
@@ -401,9 +419,10 @@ class NativeServer:
         return req
 
     def stats(self):
-        v = [ctypes.c_int64(), ctypes.c_double(), ctypes.c_double(), ctypes.c_int64(), ctypes.c_uint64()]
+        v = [ctypes.c_int64(), ctypes.c_double(), ctypes.c_double(), ctypes.c_int64(), ctypes.c_uint64(),
+             ctypes.c_int64()]
         L.check(L.lib().bt_serve_stats(self.h, *[ctypes.byref(x) for x in v]))
-        return dict(zip(("completed", "p50_s", "p99_s", "resident", "hbm_used"), (x.value for x in v)))
+        return dict(zip(("completed", "p50_s", "p99_s", "resident", "hbm_used", "runs"), (x.value for x in v)))
 
     def close(self):
         if getattr(self, "h", None):

@@ -889,11 +889,16 @@ static void launch_program(bt_program* p, bt_state* s, const double* du, uint64_
 
 // ------------------------------------------------------------------ serving hook (bt_serve.cu)
 // matrix dimension of every op (0 where the op is not a gate) and the shape
-int bt_program_gate_dims(const bt_program* p, std::vector<int>& dims, int* n, int* prec, int* batch) {
+int bt_program_gate_dims(const bt_program* p, std::vector<int>& dims, int* n, int* prec, int* batch,
+                         std::vector<char>* per_member) {
   if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "program is NULL");
   dims.assign(p->ops.size(), 0);
   for (size_t i = 0; i < p->ops.size(); ++i)
     dims[i] = p->ops[i].type == PG_GATE1 ? 2 : (p->ops[i].type == PG_GATE2 ? 4 : 0);
+  if (per_member) {
+    per_member->assign(p->ops.size(), 0);
+    for (size_t i = 0; i < p->ops.size(); ++i) (*per_member)[i] = dims[i] && p->ops[i].mstride != 0;
+  }
   *n = p->n;
   *prec = p->prec;
   *batch = p->batch;

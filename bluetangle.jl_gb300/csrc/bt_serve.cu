@@ -13,6 +13,9 @@
 //     lane is free and their kernels overlap on the device;
 //   * serves a client's requests in arrival order (they share its state), one at
 //     a time, on the lane its state lives on;
+//   * packs small circuits into one launch: a packed client is a program whose
+//     members are independent requests, so up to its width of queued requests run
+//     as one shared-memory program launch (one CTA per request);
 //   * records submit-to-done latency per request for p50/p99.
 // A request carries new matrices for some of the client's gates (plan add
 // indices, or program op indices) and a seed for the program's draws.
@@ -58,6 +61,11 @@ struct Client {
   std::vector<uint64_t> x, z;
   std::vector<double> coef;
   std::vector<int> gate_dim;  // program: matrix dimension of each op (0: not a gate)
+  // packed client: a program whose members are independent requests (one per
+  // member, its own matrices for the per-member gates); up to `batch` queued
+  // requests naming the same gates run in one launch
+  bool packed = false;
+  std::vector<char> per_member;
   size_t footprint = 0;
   bt_state* state = nullptr;  // resident state (nullptr: not resident)
   bool reserved = false;      // admitted, state being allocated by `lane`
@@ -81,11 +89,13 @@ struct bt_server {
   std::map<int64_t, Req*> reqs;
   int64_t next_client = 0, next_ticket = 0;
   std::vector<double> latencies;
+  int64_t runs = 0;  // request launches (a packed run serves several requests)
   std::string err;
 };
 
 // program/plan hooks (bt_program.cu, bt_plan.cu)
-int bt_program_gate_dims(const bt_program* p, std::vector<int>& dims, int* n, int* prec, int* batch);
+int bt_program_gate_dims(const bt_program* p, std::vector<int>& dims, int* n, int* prec, int* batch,
+                         std::vector<char>* per_member);
 int bt_plan_shape(const bt_plan* p, int* n, int* repr, int* prec);
 int bt_plan_gate_dims(const bt_plan* p, const int64_t* idx, int count, size_t* reals);
 
@@ -157,11 +167,49 @@ static int run_request(bt_ctx* ctx, Client* c, Req* r, double* value) {
   return BT_OK;
 }
 
+// requests rs (1 <= size <= batch, all naming the same gates) of a packed client
+// as the members of one program run: member m takes request m's matrices (the
+// members past the last request repeat it), <H> / norm of member m is request
+// m's value
+static int run_packed(Client* c, const std::vector<Req*>& rs, std::vector<double>& values) {
+  const int K = c->batch, k = (int)rs.size();
+  const std::vector<int64_t>& idx = rs[0]->idx;
+  std::vector<size_t> off(k, 0);
+  std::vector<double> mats;
+  int rc = BT_OK;
+  for (size_t i = 0; i < idx.size() && !rc; ++i) {
+    const int d = c->gate_dim[idx[i]];
+    const size_t sz = (size_t)2 * d * d;
+    mats.resize(sz * K);
+    for (int m = 0; m < K; ++m) {
+      const int r = m < k ? m : k - 1;
+      memcpy(&mats[sz * m], rs[r]->mats.data() + off[r], sz * sizeof(double));
+    }
+    for (int r = 0; r < k; ++r) off[r] += sz;
+    rc = bt_program_set_gate(c->prog, idx[i], mats.data());
+  }
+  if (!rc) rc = bt_state_set_zero(c->state, -1);
+  if (!rc) rc = bt_program_run(c->prog, c->state, nullptr, rs[0]->seed, nullptr);
+  if (rc) return rc;
+  const int nt = (int)c->coef.size();
+  std::vector<double> ev((size_t)K * nt), nrm(K);
+  if (nt) rc = bt_expect_pauli(c->state, nt, c->x.data(), c->z.data(), c->coef.data(), -1, ev.data());
+  if (!rc) rc = bt_norm2(c->state, -1, nrm.data());
+  if (rc) return rc;
+  values.assign(k, 0.0);
+  for (int m = 0; m < k; ++m) {
+    double h = 0;
+    for (int t = 0; t < nt; ++t) h += ev[(size_t)m * nt + t];
+    values[m] = h / nrm[m];
+  }
+  return BT_OK;
+}
+
 static void worker(bt_server* s, int lane) {
   bt_ctx* ctx = s->lanes[lane];
   for (;;) {
     Client* c = nullptr;
-    Req* r = nullptr;
+    std::vector<Req*> rs;
     std::vector<bt_state*> to_free;
     bool alloc = false;
     {
@@ -175,8 +223,13 @@ static void worker(bt_server* s, int lane) {
       }
       c->busy = true;
       alloc = c->state == nullptr;
-      r = c->queue.front();
+      rs.push_back(c->queue.front());
       c->queue.pop_front();
+      // a packed client takes the queued requests that name the same gates, up to its width
+      while (c->packed && (int)rs.size() < c->batch && !c->queue.empty() && c->queue.front()->idx == rs[0]->idx) {
+        rs.push_back(c->queue.front());
+        c->queue.pop_front();
+      }
     }
     for (bt_state* st : to_free) bt_state_free(st);
     int rc = BT_OK;
@@ -192,19 +245,26 @@ static void worker(bt_server* s, int lane) {
         c->state = st;
       }
     }
-    r->t_start = now_s();
-    double v = 0;
-    if (!rc) rc = run_request(ctx, c, r, &v);
+    const double t0 = now_s();
+    std::vector<double> v(rs.size(), 0.0);
+    if (!rc) rc = c->packed ? run_packed(c, rs, v) : run_request(ctx, c, rs[0], &v[0]);
     const double t = now_s();
+    std::string err;
+    if (rc) err = bt_last_error(nullptr);  // every failure also lands in this thread's message
     std::lock_guard<std::mutex> lk(s->mu);
-    r->value = v;
-    r->status = rc;
-    if (rc) r->err = bt_last_error(nullptr);  // every failure also lands in this thread's message
-    r->t_done = t;
-    r->done = true;
+    for (size_t i = 0; i < rs.size(); ++i) {
+      Req* r = rs[i];
+      r->t_start = t0;
+      r->value = v[i];
+      r->status = rc;
+      r->err = err;
+      r->t_done = t;
+      r->done = true;
+      s->latencies.push_back(t - r->t_submit);
+    }
+    ++s->runs;
     c->busy = false;
     c->last_used = t;
-    s->latencies.push_back(t - r->t_submit);
     s->cv.notify_all();
   }
 }
@@ -289,7 +349,22 @@ int bt_serve_add_program_client(bt_server* s, bt_program* prog, int nterms, cons
   Client* c = new Client();
   c->prog = prog;
   c->repr = BT_REPR_SV;
-  int rc = bt_program_gate_dims(prog, c->gate_dim, &c->n, &c->prec, &c->batch);
+  int rc = bt_program_gate_dims(prog, c->gate_dim, &c->n, &c->prec, &c->batch, &c->per_member);
+  if (rc) {
+    delete c;
+    return rc;
+  }
+  return add_client(s, c, nterms, xmask, zmask, coef, client);
+}
+
+int bt_serve_add_packed_client(bt_server* s, bt_program* prog, int nterms, const uint64_t* xmask,
+                               const uint64_t* zmask, const double* coef, int64_t* client) {
+  if (!s || !prog) return bt_fail(nullptr, BT_ERR_BAD_ARG, "NULL server or program");
+  Client* c = new Client();
+  c->prog = prog;
+  c->repr = BT_REPR_SV;
+  c->packed = true;
+  int rc = bt_program_gate_dims(prog, c->gate_dim, &c->n, &c->prec, &c->batch, &c->per_member);
   if (rc) {
     delete c;
     return rc;
@@ -332,6 +407,10 @@ int bt_serve_submit(bt_server* s, int64_t client, int count, const int64_t* inde
         delete r;
         return bt_fail(nullptr, BT_ERR_BAD_ARG, "index names an op that is not a gate of the program");
       }
+      if (c->packed && !c->per_member[oi]) {
+        delete r;
+        return bt_fail(nullptr, BT_ERR_BAD_ARG, "a packed client's request names a gate without per-member matrices");
+      }
       reals += (size_t)2 * d * d;
     }
   }
@@ -369,7 +448,7 @@ int bt_serve_poll(bt_server* s, int64_t ticket, int64_t wait_ms, double* value, 
 }
 
 int bt_serve_stats(bt_server* s, int64_t* completed, double* p50_s, double* p99_s, int64_t* resident,
-                   uint64_t* hbm_used) {
+                   uint64_t* hbm_used, int64_t* runs) {
   if (!s) return bt_fail(nullptr, BT_ERR_BAD_ARG, "server is NULL");
   std::lock_guard<std::mutex> lk(s->mu);
   std::vector<double> l = s->latencies;
@@ -388,6 +467,7 @@ int bt_serve_stats(bt_server* s, int64_t* completed, double* p50_s, double* p99_
   for (auto& kv : s->clients) res += kv.second->state != nullptr;
   if (resident) *resident = res;
   if (hbm_used) *hbm_used = s->used;
+  if (runs) *runs = s->runs;
   return BT_OK;
 }
 

@@ -268,6 +268,13 @@ int bt_serve_add_program_client(bt_server* s, bt_program* prog, int nterms, cons
 /* index: plan add indices (as bt_plan_set_matrices) or program op indices (as
  * bt_program_set_gate); mats back to back, column-major, each in its gate's size;
  * seed keys the program's on-device draws */
+/* a packed client: a program whose `batch` members are independent requests of
+ * one circuit (its parameterised gates added with per-member matrices).  Up to
+ * `batch` queued requests that name the same gates run as one launch, request m
+ * in member m; each request's value is <H> / norm of its member.  Requests may
+ * only name gates with per-member matrices. */
+int bt_serve_add_packed_client(bt_server* s, bt_program* prog, int nterms, const uint64_t* xmask,
+                               const uint64_t* zmask, const double* coef, int64_t* client);
 int bt_serve_submit(bt_server* s, int64_t client, int count, const int64_t* index, const double* mats, uint64_t seed,
                     int64_t* ticket);
 /* waits up to wait_ms (-1: until done, 0: no wait); BT_ERR_TIMEOUT while pending.
@@ -275,8 +282,10 @@ int bt_serve_submit(bt_server* s, int64_t client, int count, const int64_t* inde
  * (either may be NULL).  A finished ticket is released by the call that reports it. */
 int bt_serve_poll(bt_server* s, int64_t ticket, int64_t wait_ms, double* value, double* latency_s,
                   double* service_s);
+/* completed requests, latency percentiles, resident clients, HBM in use, and
+ * runs: launches of requests (a packed run serves several requests) */
 int bt_serve_stats(bt_server* s, int64_t* completed, double* p50_s, double* p99_s, int64_t* resident,
-                   uint64_t* hbm_used);
+                   uint64_t* hbm_used, int64_t* runs);
 
 /* ---------------------------------------------------------------- sampling */
 /* sample(psi, shots) (src/ops.jl:46-62): per shot t = u*sum|psi|^2, outcome =

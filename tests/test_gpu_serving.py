@@ -156,9 +156,49 @@ def test_native_server_alone_equals_mix_and_python_server(ctx):
         for req in preqs:
             req.done.wait(120)
             assert req.error is None, req.error
-            assert abs(req.value - alone[req.rid]) <= 1e-6 * max(1.0, abs(req.value)), (req.cid, req.value)
+            s = sp[req.cid]
+            if s.kind == "sv" and s.footprint("c64", pack=8) > s.footprint("c64"):
+                # packed client: a program (one CTA per request) against the Python
+                # server's fused plan, both complex64: within complex64 accuracy
+                tol = 2e-5 * sum(abs(t[0]) for t in s.terms)
+            else:
+                tol = 1e-6 * max(1.0, abs(req.value))
+            assert abs(req.value - alone[req.rid]) <= tol, (req.cid, req.value)
     finally:
         py.close()
+
+
+def test_native_server_packs_small_circuits_into_one_launch(ctx):
+    """Eight requests of one small state-vector client queued at once run as one
+    packed program launch (they finish together) and each equals its value served
+    alone, and its complex128 plain-path value within complex64 accuracy."""
+    import bluetangle_gpu.serving as S
+    sp = specs(37)[:1]  # sv, 11 qubits
+    reqs = requests(sp, per_client=8, seed=41)
+    srv = S.NativeServer(sp, lanes=1, pack=8)
+    try:
+        for req in reqs:
+            srv.submit(req)
+        for req in reqs:
+            srv.wait(req)
+            assert req.error is None, req.error
+        st = srv.stats()
+    finally:
+        srv.close()
+    assert st["completed"] == len(reqs) and st["runs"] < len(reqs)  # requests shared launches
+    one = S.NativeServer(sp, lanes=1, pack=8)
+    pctx = S.Context(0, seed=3)
+    try:
+        for r in requests(sp, per_client=8, seed=41):
+            one.submit(r)
+            one.wait(r)
+            match = [q for q in reqs if q.rid == r.rid][0]
+            assert abs(match.value - r.value) <= 1e-6 * max(1.0, abs(r.value))
+            ref = S.plain_request(sp[0], r.theta, r.seed, pctx, prec="c128")
+            assert abs(r.value - ref) <= 2e-5 * sum(abs(t[0]) for t in sp[0].terms)
+    finally:
+        one.close()
+        pctx.close()
 
 
 def test_native_server_admission_by_footprint(ctx):
@@ -166,7 +206,7 @@ def test_native_server_admission_by_footprint(ctx):
     request still completes with the value it has alone."""
     import bluetangle_gpu.serving as S
     sp = specs(29)
-    budget = max(s.footprint("c64") for s in sp) * 2
+    budget = max(s.footprint("c64", pack=8) for s in sp) * 2
     srv = S.NativeServer(sp, lanes=2, hbm_budget=budget)
     try:
         reqs = requests(sp, per_client=2, seed=31)

@@ -489,17 +489,18 @@ class Plan:
     def autotune(self, state, configs=None, reps=2):
         """Times each tuning configuration (max_ops, tile_rb, packed, tile_bits) on
         `state` (the timing runs overwrite it), keeps the fastest compiled and
-        returns [(config, seconds per run)] in the order tried.  States that fit
-        one default tile also try smaller tiles (more CTAs per pass)."""
+        returns [(config, seconds per run)] in the order tried.  Smaller tiles are
+        tried too: more CTAs per pass for small states, more CTAs per SM (whose
+        loads and arithmetic overlap) for large ones."""
         import time
         c64 = self.prec in ("c64", "complex64")
         if configs is None:
-            configs = ([(64, 5, 1, 0), (64, 5, 0, 0), (32, 5, 1, 0), (128, 5, 1, 0), (64, 4, 1, 0)] if c64
-                       else [(64, 0, -1, 0), (32, 0, -1, 0), (128, 0, -1, 0)])
+            configs = ([(0, 5, 1, 0), (0, 5, 0, 0), (64, 5, 1, 0), (128, 5, 1, 0), (0, 4, 1, 0)] if c64
+                       else [(0, 0, -1, 0), (64, 0, -1, 0), (128, 0, -1, 0)])
             nbits = self.n * (2 if self.repr_code == L.BT_REPR_DM else 1)
             mdef, mmin = (13, 10) if c64 else (12, 9)
             for m in range(min(mdef, nbits) - 1, mmin - 1, -1)[:3]:
-                configs.append((64, 0, -1, m))
+                configs.append((0, 0, -1, m))
         configs = [tuple(c) + (0,) * (4 - len(c)) for c in configs]
         results = []
         for cfg in configs:

@@ -596,10 +596,13 @@ static bool emit_op_packed(std::ostringstream& o, const FOp& op, int NB, int P) 
   return false;
 }
 
-// complex64 specialised passes run packed unless a plan says otherwise
-// (BTGPU_JIT_PACKED=0: scalar code by default)
+// complex64 specialised passes run scalar FP32 code unless a plan says otherwise
+// (BTGPU_JIT_PACKED=1: two-lane code by default).  With the factored ops (one
+// FMA per component for rotations) the moves that repack amplitude pairs for the
+// two-lane form at every phase boundary cost more than the halved FMA issue saves:
+// 33-qubit brickwork 0.884 s per circuit scalar, 0.963 s two-lane.
 bool bt_jit_packed_default() {
-  static const bool v = env_int("BTGPU_JIT_PACKED", 1, 0, 1) != 0;
+  static const bool v = env_int("BTGPU_JIT_PACKED", 0, 0, 1) != 0;
   return v;
 }
 
@@ -765,6 +768,22 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
         if ((j >> b) & 1) l |= 1 << ph.reg[b];
       offs[j] = swz_host(f, l);  // the swizzle is XOR-linear: swz(lb | l) = swz(lb) ^ swz(l)
     }
+    // Only the swizzled low bits (0-3 complex64, 0-2 complex128) of an offset can
+    // meet the thread's bits: above them offs[j] holds register bits, where sb is
+    // zero, so sb ^ offs[j] = (sb ^ low) + high.  One XOR per distinct low part;
+    // the high part becomes a constant offset of the access.
+    const int lowmask = f ? 15 : 7;
+    std::vector<int> lows;
+    auto saddr = [&](int j) {
+      const int lo = offs[j] & lowmask, hi = offs[j] & ~lowmask;
+      const int k = (int)(std::find(lows.begin(), lows.end(), lo) - lows.begin());
+      return "s" + std::to_string(k) + (hi ? " + " + std::to_string(hi) : std::string());
+    };
+    if (!rd_direct || !wr_direct) {
+      for (int j = 0; j < D; ++j)
+        if (std::find(lows.begin(), lows.end(), offs[j] & lowmask) == lows.end()) lows.push_back(offs[j] & lowmask);
+      for (size_t k = 0; k < lows.size(); ++k) o << "    const int s" << k << " = sb ^ " << lows[k] << ";\n";
+    }
     if (rd_direct) {
       o << "    { const " << T2 << "* gp = g + tf;\n";
       for (int j = 0; j < D; ++j) {
@@ -778,7 +797,7 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
       o << "    }\n";
     } else {
       for (int j = 0; j < D; ++j)
-        o << "    { const " << T2 << " v = tile[sb ^ " << offs[j] << "]; x" << j << " = v.x; y" << j << " = v.y; }\n";
+        o << "    { const " << T2 << " v = tile[" << saddr(j) << "]; x" << j << " = v.x; y" << j << " = v.y; }\n";
       // the tile's last shared-memory reads: the next tile may overwrite it once every warp is past them
       if (wr_direct) o << "    __syncthreads();\n";
       if (wr_direct && pf) o << "    fetch(tid + gridDim.x);\n";
@@ -832,7 +851,7 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
       }
       o << "    }\n    }\n";
     } else {
-      for (int j = 0; j < D; ++j) o << "    tile[sb ^ " << offs[j] << "] = " << T2 << "{x" << j << ", y" << j << "};\n";
+      for (int j = 0; j < D; ++j) o << "    tile[" << saddr(j) << "] = " << T2 << "{x" << j << ", y" << j << "};\n";
       o << "    __syncthreads();\n    }\n";
     }
   }

@@ -632,6 +632,12 @@ static bool direct_ok(const FPhase& ph, int NB, int M, bool f) {
 // next-tile prefetch into shared memory during a direct last phase
 // (BTGPU_JIT_PREFETCH=1; off by default: on the 28- and 33-qubit brickwork the
 // extra shared-memory copies cost more than the hidden load latency saves)
+// L2 prefetch of each CTA's next tile during the current one (BTGPU_JIT_L2PF)
+static bool l2_prefetch_on() {
+  static const bool v = env_int("BTGPU_JIT_L2PF", 1, 0, 1) != 0;
+  return v;
+}
+
 static bool prefetch_on() {
   static const bool v = env_int("BTGPU_JIT_PREFETCH", 0, 0, 1) != 0;
   return v;
@@ -720,8 +726,28 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
     o << "    }\n    asm volatile(\"cp.async.commit_group;\" ::: \"memory\");\n  };\n";
     o << "  fetch(blockIdx.x);\n";
   }
+  // L2 prefetch of the CTA's next tile while this one computes: each thread asks
+  // for whole contiguous runs (2^c amplitudes) of it
+  const int nruns = 1 << (M - c), run_bytes = (f ? 8 : 16) << c;
+  const bool l2pf = l2_prefetch_on() && pf == false;
+  if (l2pf) {
+    o << "  const int pr = threadIdx.x;\n  i64 roff = 0;\n";
+    for (int b = 0; b < M - c; ++b) o << "  roff |= (i64)((pr >> " << b << ") & 1) << " << a.tbits[c + b] << ";\n";
+  }
   o << "  for (i64 tid = blockIdx.x; tid < total; tid += gridDim.x) {\n";
   o << "    " << T2 << "* g = tile_ptr(tid);\n";
+  if (l2pf) {
+    o << "    if (tid + gridDim.x < total" << (T > nruns ? " && threadIdx.x < " + std::to_string(nruns) : std::string())
+      << ") { const " << T2 << "* gn = tile_ptr(tid + gridDim.x) + roff;";
+    o << " asm volatile(\"cp.async.bulk.prefetch.L2.global [%0], " << run_bytes << ";\" :: \"l\"(gn) : \"memory\");";
+    if (T < nruns) {  // fewer threads than runs: the rest by stride
+      o << " for (int q = " << T << "; q < " << nruns << "; q += " << T << ") { i64 ro = 0;";
+      for (int b = 0; b < M - c; ++b) o << " ro |= (i64)(((threadIdx.x + q) >> " << b << ") & 1) << " << a.tbits[c + b] << ";";
+      o << " const " << T2 << "* gq = tile_ptr(tid + gridDim.x) + ro; asm volatile(\"cp.async.bulk.prefetch.L2.global [%0], "
+        << run_bytes << ";\" :: \"l\"(gq) : \"memory\"); }";
+    }
+    o << " }\n";
+  }
   if (pf) o << "    asm volatile(\"cp.async.wait_group 0;\" ::: \"memory\");\n    __syncthreads();\n";
   if (!dfirst && !pf) {
     // tile load: every 16-byte load in flight, then into the swizzled tile

@@ -479,6 +479,14 @@ class Plan:
         self.ctx.check(L.lib().bt_plan_set_matrices(self.h, len(updates), _ptr(idx), _ptr(mats)))
         return self
 
+    def set_variable(self, indices):
+        """Marks the gates of these add indices as variable (updated in place by
+        set_matrices): compiled in entry-independent forms, so updates never
+        recompile.  Call before compile."""
+        idx = np.ascontiguousarray(list(indices), dtype=np.int64)
+        self.ctx.check(L.lib().bt_plan_set_variable(self.h, len(idx), _ptr(idx)))
+        return self
+
     def set_tuning(self, max_ops=0, tile_rb=0, packed=-1, tile_bits=0):
         """Fusion width (gates per pass), register bits per thread (4 or 5),
         two-lane arithmetic and tile bits of the fused passes; 0 / -1 keep the

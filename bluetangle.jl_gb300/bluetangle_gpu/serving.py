@@ -170,7 +170,7 @@ class _Resident:
                 self.plan.add(op)
                 if op.name in ("RY", "RZ"):
                     self.pidx.append(i)
-            self.plan.compile(True, tiered=tiered)
+            self.plan.set_variable(self.pidx).compile(True, tiered=tiered)
         else:
             self.state = GPUState(n, prec, spec.ntraj, ctx)
             self.program = None
@@ -374,7 +374,7 @@ class NativeServer:
                     plan.add(op)
                     if op.name in ("RY", "RZ"):
                         pidx.append(i)
-                plan.compile(True, tiered=tiered)
+                plan.set_variable(pidx).compile(True, tiered=tiered)
                 L.check(lib.bt_serve_add_plan_client(h, plan.h, len(cs), _ptr(xs), _ptr(zs), _ptr(cs),
                                                       ctypes.byref(cid)))
                 self.keep.append(plan)

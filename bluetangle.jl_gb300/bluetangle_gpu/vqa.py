@@ -135,7 +135,7 @@ def losses(ops, n, param_list, terms, prec="c128", ctx=None, executor="auto"):
             qs, cs = _qubits(op)
             plan.add_matrix(mat, qs, cs)
             pidx.append(i)
-    plan.compile(True)
+    plan.set_variable(pidx).compile(True)  # angles are rewritten in place: no recompiles
     st = GPUState(n, prec, 1, ctx)
     vals = np.empty(B)
     for m in range(B):
@@ -207,13 +207,15 @@ def loss_and_grad_paramshift(p, ops, n, terms, prec="c128", ctx=None, executor="
         st.free()
     else:
         plan = Plan(n, "sv", prec, ctx)
-        for op, mat in base:
+        var = []
+        for i, (op, mat) in enumerate(base):
             if mat is None:
                 plan.add(op)
             else:
                 qs, cs = _qubits(op)
                 plan.add_matrix(mat, qs, cs)
-        plan.compile(True)
+                var.append(i)
+        plan.set_variable(var).compile(True)  # shifted angles are rewritten in place: no recompiles
         st = GPUState(n, prec, 1, ctx)
         vals = np.empty(B)
 

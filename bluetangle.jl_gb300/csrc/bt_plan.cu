@@ -34,6 +34,10 @@ struct PGate {
   uint64_t cmask = 0;
   std::vector<double> m;  // row-major interleaved 2^k x 2^k
   int ku = 0, fold_nc = 0;  // the caller's gate size and the controls folded into m
+  // updated in place (bt_plan_set_matrices / bt_plan_set_variable): encoded in
+  // forms whose structure does not depend on the entries, so later updates never
+  // force a recompile
+  bool var = false;
   uint64_t allbits() const {
     uint64_t b = cmask;
     for (int i = 0; i < k; ++i) b |= 1ULL << bits[i];
@@ -194,6 +198,7 @@ static bool factor_on() {
 // in double; fac receives the complex scalar taken out of the op (1 if none).
 // (o.b0/o.b1 hold the register bits of the gate's first/second bit on entry)
 static void encode_op(const PGate& g, FOp& o, double* mat, int& nre, double* fac, bool factor) {
+  factor = factor && !g.var;
   int perm[4] = {0, 1, 2, 3};
   const int cls = classify(g, perm);
   const double* m = g.m.data();
@@ -207,7 +212,7 @@ static void encode_op(const PGate& g, FOp& o, double* mat, int& nre, double* fac
     if (cls == 2 && factor && (n0 != 0 || n1 != 0)) {
       // the larger entry factored out: d1 / d0 on the bit-1 half (or d0 / d1 on
       // the bit-0 half); exact -1, i, -i become sign flips and swaps
-      const bool lo = n1 > n0;
+      const bool lo = n1 > 4 * n0;  // clearly larger only: unitary diagonals always factor d0
       const double* f = lo ? m + 6 : m;   // factored entry
       const double* e = lo ? m : m + 6;   // the other
       const double n = lo ? n1 : n0;
@@ -407,14 +412,24 @@ static bool encode_pass(bt_plan* p, const std::vector<int>& kept, const std::vec
       }
     }
   }
+  if (update) {
+    // a structure that changed needs a recompile; its gates take the
+    // value-independent forms from then on
+    bool same = true;
+    for (int i = 0; i < nop; ++i) {
+      const FOp& o = a.op[i];
+      if (ops[i].type != o.type || ops[i].b0 != o.b0 || ops[i].b1 != o.b1 || ops[i].flags != o.flags ||
+          ops[i].unit != o.unit) {
+        p->gates[kept[i]].var = true;
+        same = false;
+      }
+    }
+    if (!same) return false;
+  }
   int w = 0;
   for (int i = 0; i < nop; ++i) {
     if (update) {
-      const FOp& o = a.op[i];
-      if (ops[i].type != o.type || ops[i].b0 != o.b0 || ops[i].b1 != o.b1 || ops[i].flags != o.flags ||
-          ops[i].unit != o.unit)
-        return false;
-      w = o.moff;
+      w = a.op[i].moff;
     } else {
       ops[i].moff = (uint16_t)w;
       a.op[i] = ops[i];
@@ -721,6 +736,7 @@ int bt_plan_set_matrices(bt_plan* p, int count, const int64_t* add_index, const 
         for (int e = 0; e < d * d; ++e) rm[2 * e + 1] = -rm[2 * e + 1];
       if (g.fold_nc > 0) kron_ctrl(ku, rm.data(), g.fold_nc, g.m);
       else g.m = rm;
+      g.var = true;
       touched[first + j] = 1;
     }
   }
@@ -731,6 +747,21 @@ int bt_plan_set_matrices(bt_plan* p, int count, const int64_t* add_index, const 
     if (!ok) {  // a gate changed its structural class: recompile at the next run
       p->compiled = false;
       break;
+    }
+  }
+  return BT_OK;
+}
+
+int bt_plan_set_variable(bt_plan* p, int count, const int64_t* add_index) {
+  if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "plan is NULL");
+  if (count < 0 || (count > 0 && !add_index)) return bt_fail(p->ctx, BT_ERR_BAD_ARG, "bad index array");
+  for (int i = 0; i < count; ++i) {
+    const int64_t ai = add_index[i];
+    if (ai < 0 || ai >= (int64_t)p->adds.size()) return bt_fail(p->ctx, BT_ERR_BAD_ARG, "add index out of range");
+    const int first = p->adds[ai].first, cnt = p->adds[ai].second;
+    for (int j = 0; j < cnt; ++j) {
+      if (!p->gates[first + j].var) p->compiled = false;
+      p->gates[first + j].var = true;
     }
   }
   return BT_OK;

@@ -173,6 +173,12 @@ int bt_plan_compile(bt_plan* p, int mode);
  * in place; a gate whose structure changes (e.g. an angle making it diagonal)
  * makes the next run recompile.  Kraus sums cannot be updated. */
 int bt_plan_set_matrices(bt_plan* p, int count, const int64_t* add_index, const double* mats);
+/* marks the gates of these adds as variable (parameters updated in place): they
+ * are compiled in forms whose structure does not depend on their entries, so
+ * bt_plan_set_matrices never recompiles for them.  A gate becomes variable at its
+ * first bt_plan_set_matrices anyway (one recompile); marking before
+ * bt_plan_compile avoids that one too. */
+int bt_plan_set_variable(bt_plan* p, int count, const int64_t* add_index);
 /* njit: fused passes running as kernels specialised for the plan (NVRTC, compiled
  * by bt_plan_compile); the others run on the generic fused kernel */
 /* algorithmic cost of one run per amplitude of a member: real flops of the

@@ -159,3 +159,83 @@ def test_variational_parameter_binding():
     assert np.allclose(b[4][1], ry(0.4))
     with pytest.raises(ValueError):
         V._bound(ops, V.arg_counts(ops), p[:3])
+
+
+def _host_plan(lib, n, thetas, variable=()):
+    """A complex64 plan of RY(theta) RZ(theta) on every qubit and a CNOT ladder,
+    planned without a device (the library plans and encodes passes on the host)."""
+    import ctypes
+    from bluetangle_gpu import _lib as L
+    P = ctypes.c_void_p
+    p = P()
+    L.check(lib.bt_plan_create(None, n, L.BT_REPR_SV, L.BT_PREC_C64, ctypes.byref(p)))
+    adds = []
+    for q in range(1, n + 1):
+        for th in thetas:
+            c, s = math.cos(th / 2), math.sin(th / 2)
+            for m in (np.array([[c, -s], [s, c]]), np.diag([np.exp(-0.5j * th), np.exp(0.5j * th)])):
+                mm = np.ascontiguousarray(np.asarray(m, dtype=np.complex128).T)
+                qs = np.array([q], dtype=np.int32)
+                L.check(lib.bt_plan_add_matrix(p, 1, qs.ctypes.data_as(P), mm.ctypes.data_as(P), 0, None))
+                adds.append(len(adds))
+    cx = np.ascontiguousarray(np.eye(4, dtype=np.complex128)[[0, 1, 3, 2]].T)
+    for q in range(1, n):
+        qs = np.array([q, q + 1], dtype=np.int32)
+        L.check(lib.bt_plan_add_matrix(p, 2, qs.ctypes.data_as(P), cx.ctypes.data_as(P), 0, None))
+    if variable:
+        idx = np.ascontiguousarray(variable, dtype=np.int64)
+        L.check(lib.bt_plan_set_variable(p, len(idx), idx.ctypes.data_as(P)))
+    return p, adds
+
+
+def _compiled(lib, p):
+    import ctypes
+    f, b = ctypes.c_double(), ctypes.c_double()
+    return lib.bt_plan_cost(p, ctypes.byref(f), ctypes.byref(b)) == 0
+
+
+def _update(lib, p, adds, th):
+    """every rotation and diagonal rewritten at angle th"""
+    import ctypes
+    P = ctypes.c_void_p
+    c, s = math.cos(th / 2), math.sin(th / 2)
+    mats = []
+    for i in adds:
+        m = np.array([[c, -s], [s, c]]) if i % 2 == 0 else np.diag([np.exp(-0.5j * th), np.exp(0.5j * th)])
+        mats.append(np.asarray(m, dtype=np.complex128).T.ravel())
+    buf = np.ascontiguousarray(np.concatenate(mats))
+    idx = np.ascontiguousarray(adds, dtype=np.int64)
+    from bluetangle_gpu import _lib as L
+    L.check(lib.bt_plan_set_matrices(p, len(idx), idx.ctypes.data_as(P), buf.ctypes.data_as(P)))
+
+
+def test_plan_angle_updates_never_recompile(monkeypatch):
+    """In-place angle updates keep the compiled passes (no recompile per update):
+    a gate's encoding does not depend on its angle once it is variable, which it
+    becomes at its first update (one recompile) or by bt_plan_set_variable before
+    compiling (none).  Planned on the host; the specialised kernels are not built."""
+    monkeypatch.setenv("BTGPU_NO_JIT", "1")
+    from bluetangle_gpu import _lib as L
+    lib = L.lib()
+    n = 15
+    # angles on both sides of |cos| = |sin|: the factored rotation form would flip
+    p, adds = _host_plan(lib, n, [0.4])
+    try:
+        L.check(lib.bt_plan_compile(p, 0))
+        assert _compiled(lib, p)
+        _update(lib, p, adds, 2.9)   # first update: the gates turn variable, one recompile
+        assert not _compiled(lib, p)
+        L.check(lib.bt_plan_compile(p, 0))
+        for th in (0.3, 2.8, 1.1, 3.0, 0.05):
+            _update(lib, p, adds, th)
+            assert _compiled(lib, p), th
+    finally:
+        lib.bt_plan_free(p)
+    p, adds = _host_plan(lib, n, [0.4], variable=list(range(2 * n)))
+    try:
+        L.check(lib.bt_plan_compile(p, 0))
+        for th in (2.9, 0.3, 2.8, 1.1):
+            _update(lib, p, adds, th)
+            assert _compiled(lib, p), th
+    finally:
+        lib.bt_plan_free(p)

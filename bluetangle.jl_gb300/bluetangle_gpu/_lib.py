@@ -73,6 +73,7 @@ SIGNATURES = {
     "bt_plan_set_variable": (i32, [P, i32, P]),
     "bt_plan_stats": (i32, [P, P, P, P, P, P]),
     "bt_plan_cost": (i32, [P, P, P]),
+    "bt_plan_pass_ops": (i32, [P, i64, P, P, P, P, i32, i32]),
     "bt_plan_run": (i32, [P, P, i64]),
     "bt_plan_set_tuning": (i32, [P, i32, i32, i32, i32]),
     "bt_program_create": (i32, [P, i32, i32, i32, ctypes.POINTER(P)]),

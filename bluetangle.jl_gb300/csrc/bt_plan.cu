@@ -959,6 +959,57 @@ int bt_plan_cost(const bt_plan* p, double* flops_per_amp, double* bytes_per_amp)
   return BT_OK;
 }
 
+int bt_plan_pass_ops(const bt_plan* p, int64_t pass, int* kind, int* nops, int32_t* ops, double* mats, int cap_ops,
+                     int cap_reals) {
+  if (!p || !kind || !nops) return bt_fail(nullptr, BT_ERR_BAD_ARG, "NULL argument");
+  if (!p->compiled) return bt_fail(p->ctx, BT_ERR_BAD_ARG, "plan is not compiled");
+  if (pass < 0 || pass >= (int64_t)p->passes.size()) return bt_fail(p->ctx, BT_ERR_BAD_ARG, "pass out of range");
+  const PPass& ps = p->passes[pass];
+  *kind = ps.kind;
+  if (ps.kind != 0) {  // sweep: k, bits[0..4], control mask (low, high 32 bits); the row-major matrix
+    const PGate& g = p->gates[ps.gate];
+    const int d = 1 << g.k;
+    *nops = 1;
+    if (cap_ops < 2 || cap_reals < 2 * d * d || !ops || !mats)
+      return bt_fail(p->ctx, BT_ERR_BAD_ARG, "output arrays too small");
+    ops[0] = g.k;
+    for (int i = 0; i < 5; ++i) ops[1 + i] = i < g.k ? g.bits[i] : -1;
+    ops[6] = (int32_t)(uint32_t)g.cmask;
+    ops[7] = (int32_t)(uint32_t)(g.cmask >> 32);
+    for (int e = 0; e < 2 * d * d; ++e) mats[e] = g.m[e];
+    return BT_OK;
+  }
+  const bool c64 = p->prec == BT_PREC_C64;
+  const void* args = ps.args.data();
+  const FPhase* ph = c64 ? reinterpret_cast<const FusedArgs<float>*>(args)->ph
+                         : reinterpret_cast<const FusedArgs<double>*>(args)->ph;
+  const FOp* op = c64 ? reinterpret_cast<const FusedArgs<float>*>(args)->op
+                      : reinterpret_cast<const FusedArgs<double>*>(args)->op;
+  const int* tbits = c64 ? reinterpret_cast<const FusedArgs<float>*>(args)->tbits
+                         : reinterpret_cast<const FusedArgs<double>*>(args)->tbits;
+  const int nph = c64 ? reinterpret_cast<const FusedArgs<float>*>(args)->nphase
+                      : reinterpret_cast<const FusedArgs<double>*>(args)->nphase;
+  const int nreals = c64 ? BT_FUSED_MAX_REALS_F : BT_FUSED_MAX_REALS_D;
+  *nops = ps.ngates;
+  if (cap_ops < ps.ngates || !ops || !mats || cap_reals < nreals)
+    return bt_fail(p->ctx, BT_ERR_BAD_ARG, "output arrays too small");
+  for (int q = 0; q < nph; ++q)
+    for (int i = ph[q].op0; i < ph[q].op0 + ph[q].nop; ++i) {
+      const FOp& o = op[i];
+      int32_t* r = ops + 6 * i;
+      r[0] = o.type;
+      r[1] = tbits[ph[q].reg[o.b0]];
+      r[2] = tbits[ph[q].reg[o.b1]];
+      r[3] = o.flags;
+      r[4] = o.unit;
+      r[5] = o.moff;
+    }
+  for (int e = 0; e < nreals; ++e)
+    mats[e] = c64 ? reinterpret_cast<const FusedArgs<float>*>(args)->mat[e]
+                  : reinterpret_cast<const FusedArgs<double>*>(args)->mat[e];
+  return BT_OK;
+}
+
 int bt_plan_stats(const bt_plan* p, int64_t* ngates, int64_t* npasses, int64_t* nfused, int64_t* nphases,
                   int64_t* njit) {
   if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "plan is NULL");

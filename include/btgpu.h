@@ -185,6 +185,15 @@ int bt_plan_set_variable(bt_plan* p, int count, const int64_t* add_index);
  * compiled passes' arithmetic (an FMA counts two) and HBM bytes moved (one read
  * and one write of the state per pass) */
 int bt_plan_cost(const bt_plan* p, double* flops_per_amp, double* bytes_per_amp);
+/* introspection of compiled pass `pass` (0 .. npasses-1), for checking plans on
+ * the host.  kind 0 (fused): nops ops in application order, ops[6i..6i+5] =
+ * {type, global bit of b0, global bit of b1, flags, unit, offset of its entries in
+ * mats}, type and entries as the specialised code applies them (FOP_* in
+ * csrc/bt_fused.cuh), mats = the pass's entries (cap_reals >= 4096).  kind 1
+ * (sweep): one gate, ops[0..7] = {k, bits[0..4] (-1 past k), control mask low /
+ * high 32 bits} (cap_ops >= 2), mats = its row-major interleaved 2^k x 2^k matrix. */
+int bt_plan_pass_ops(const bt_plan* p, int64_t pass, int* kind, int* nops, int32_t* ops, double* mats, int cap_ops,
+                     int cap_reals);
 int bt_plan_stats(const bt_plan* p, int64_t* ngates, int64_t* npasses, int64_t* nfused, int64_t* nphases,
                   int64_t* njit);
 /* tuning of the fused passes (applies at the next bt_plan_compile; 0 / -1 keep

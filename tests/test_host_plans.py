@@ -1,0 +1,180 @@
+"""Compiled plans checked on the host: the planner (tile bits among light-cone
+windows, register phases) and the op encoding (classes, factored forms, the
+folded scalar, variable gates) emulated pass by pass from bt_plan_pass_ops and
+compared with the oracle.  No GPU: planning needs none and the specialised
+kernels are not built (BTGPU_NO_JIT)."""
+import math
+
+import numpy as np
+import pytest
+
+import plan_emulator as E
+
+
+@pytest.fixture(autouse=True)
+def _no_jit(monkeypatch):
+    monkeypatch.setenv("BTGPU_NO_JIT", "1")
+
+
+def rstate(rng, n):
+    v = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
+    return v / np.linalg.norm(v)
+
+
+def runitary(rng, d):
+    z = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    q, r = np.linalg.qr(z)
+    return q * (np.diag(r) / np.abs(np.diag(r)))
+
+
+def oracle_op(oracle, psi, op):
+    ctrls = [op.control] if op.control != -2 else []
+    qs = [op.qubit] if op.q == 1 else [op.qubit, op.target_qubit]
+    return oracle.apply_k(psi, op.mat, qs, ctrls)
+
+
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-12), ("c64", 2e-5)])
+def test_host_plan_random_gates_controls_and_wide_gates(oracle, prec, tol):
+    rng = np.random.default_rng(7)
+    n = 15
+    plan = E.host_plan(n, prec=prec)
+    psi = rstate(rng, n)
+    ref = psi.copy()
+    for i in range(200):
+        kind = rng.integers(0, 7)
+        qs = [int(x) for x in rng.choice(np.arange(1, n + 1), size=4, replace=False)]
+        if kind <= 1:
+            U, g = runitary(rng, 2), ([qs[0]], [])
+        elif kind == 2:
+            U, g = np.diag(np.exp(1j * rng.uniform(0, 6, 2))), ([qs[0]], [])
+        elif kind == 3:
+            U, g = runitary(rng, 4), (qs[:2], [])
+        elif kind == 4:
+            U, g = np.eye(4, dtype=complex)[[0, 1, 3, 2]] * np.exp(1j * rng.uniform(0, 6, 4))[:, None], (qs[:2], [])
+        elif kind == 5:
+            U, g = runitary(rng, 2), ([qs[0]], [qs[1]])
+        else:
+            U, g = ((runitary(rng, 8), (qs[:3], [])) if rng.random() < 0.5 else
+                    (np.array([[0, 1], [1, 0]], dtype=complex), ([qs[0]], qs[1:3])))
+        plan.add_matrix(U, g[0], g[1])
+        ref = oracle.apply_k(ref, U, g[0], g[1])
+    plan.compile()
+    assert np.abs(E.run(plan, psi) - ref).max() < tol
+
+
+@pytest.mark.parametrize("prec,n,tol", [("c128", 16, 1e-12), ("c64", 17, 2e-5)])
+def test_host_plan_brickwork_windows(oracle, prec, n, tol):
+    """States wider than a tile: passes take light-cone windows of tile bits."""
+    import bluetangle_gpu.circuits as C
+    rng = np.random.default_rng(100 + n)
+    ops = C.random_ops(n, 2, rng) + C.brickwork(n, 14, rng)
+    plan = E.host_plan(n, prec=prec)
+    for op in ops:
+        plan.add(op)
+    plan.compile()
+    st = plan.stats()
+    assert st["gates"] == len(ops) and st["passes"] < len(ops) / 10
+    psi = rstate(rng, n)
+    ref = psi
+    for op in ops:
+        ref = oracle_op(oracle, ref, op)
+    assert np.abs(E.run(plan, psi) - ref).max() < tol
+
+
+def _forms():
+    c, s = math.cos(0.3), math.sin(0.3)
+    h = 1 / math.sqrt(2)
+    mats = [np.diag([1, -1]), np.diag([1, 1j]), np.diag([1, -1j]), np.diag([1, np.exp(0.7j)]),
+            np.diag([0.2, 1.3]), np.diag([1.3j, 0.2]), np.diag([np.exp(-0.4j), np.exp(0.4j)]),
+            h * np.array([[1, 1], [1, -1]]), h * np.array([[1, -1], [1, 1]]), h * np.array([[-1, 1], [1, 1]]),
+            np.array([[c, -s], [s, c]]), np.array([[s, -c], [c, s]]), np.array([[c, s], [s, -c]]),
+            np.array([[c, -1j * s], [-1j * s, c]]), np.array([[s, -1j * c], [-1j * c, s]]),
+            np.array([[0.3, 0.9], [-0.9, 0.3]]), np.diag([1e-19, 1e-19])]
+    return [np.asarray(m, dtype=complex) for m in mats]
+
+
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-12), ("c64", 2e-5)])
+def test_host_plan_factored_forms_and_updates(oracle, prec, tol):
+    """Every factored one-qubit form with its scalar folded into one op of the
+    pass; then angle updates (the gates turn variable: one recompile, then none)."""
+    rng = np.random.default_rng(31)
+    n = 14
+    seq = []
+    for rep in range(3):
+        for i, m in enumerate(_forms()):
+            if i == 16 and rep:
+                continue
+            seq.append((m, [int(rng.integers(1, n + 1))]))
+        a, b = [int(x) for x in rng.choice(np.arange(1, n + 1), 2, replace=False)]
+        seq.append((runitary(rng, 4), [a, b]))
+        seq.append((np.eye(4, dtype=complex)[[0, 1, 3, 2]], [b, a]))
+    psi = rstate(rng, n)
+    plan = E.host_plan(n, prec=prec)
+    for m, qs in seq:
+        plan.add_matrix(m, qs)
+    plan.compile()
+
+    def check(mats):
+        ref = psi.copy()
+        for m, (_, qs) in zip(mats, seq):
+            ref = oracle.apply_k(ref, m, qs, [])
+        assert np.abs(E.run(plan, psi) - ref).max() < tol * np.abs(ref).max()
+
+    mats = [m for m, _ in seq]
+    check(mats)
+    for th in (2.9, 0.2, 1.9):
+        upd = []
+        for i in (3, 10, 13, 20):
+            c, s = math.cos(th / 2), math.sin(th / 2)
+            m = {3: np.diag([1, np.exp(1j * th)]), 10: np.array([[c, -s], [s, c]]),
+                 13: np.array([[c, -1j * s], [-1j * s, c]]), 20: np.diag([np.exp(-1j * th), 1])}[i]
+            mats[i] = np.asarray(m, dtype=complex)
+            upd.append((i, mats[i]))
+        plan.set_matrices(upd)
+        plan.compile()  # re-encodes only if an update changed a pass's structure
+        check(mats)
+
+
+def test_host_plan_density_matrix_noisy(oracle):
+    """Density-matrix plan over 2n bits: gates as row/column ops, Kraus sums as
+    superoperators (kron-pair channels split into one-qubit ones)."""
+    import bluetangle_gpu as bt
+    import bluetangle_gpu.circuits as C
+    rng = np.random.default_rng(11)
+    n = 6
+    ops = C.noisy_brickwork_dm(n, 5, rng)
+    plan = E.host_plan(n, repr="dm", prec="c128")
+    for op in ops:
+        plan.add(op)
+    plan.compile()
+    rho0 = np.zeros((2 ** n, 2 ** n), complex)
+    rho0[0, 0] = 1
+    ref = rho0
+    for o in ops:
+        if isinstance(o, bt.OpQC):
+            ref = oracle.dm_channel(ref, o.kraus, o.qubit, o.target_qubit if o.q == 2 else -1)
+        elif o.q == 1:
+            ref = oracle.dm_hilbert1(ref, o.mat, o.qubit)
+        else:
+            ref = oracle.dm_hilbert2(ref, o.mat, o.qubit, o.target_qubit)
+    out = E.run(plan, rho0).reshape(2 ** n, 2 ** n, order="F")
+    assert np.abs(out - ref).max() < 1e-12
+
+
+def test_host_plan_headline_pass_count():
+    """The 33-qubit depth-30 brickwork plans into at most 26 passes (tile bits
+    grown in gate order needed 63), and its arithmetic per amplitude stays at the
+    factored forms' cost."""
+    import ctypes
+    import bluetangle_gpu.circuits as C
+    from bluetangle_gpu import _lib as L
+    ops = C.brickwork(33, 30, np.random.default_rng(2024))
+    plan = E.host_plan(33, prec="c64")
+    for op in ops:
+        plan.add(op)
+    plan.compile()
+    st = plan.stats()
+    assert st["gates"] == 1470 and st["passes"] <= 26, st
+    f, b = ctypes.c_double(), ctypes.c_double()
+    L.check(L.lib().bt_plan_cost(plan.h, ctypes.byref(f), ctypes.byref(b)))
+    assert b.value == 16 * st["passes"] and f.value < 2600, (f.value, b.value)

@@ -35,9 +35,9 @@ METRIC = "gate-apps/s"
 # ncu-measured DRAM bytes per amplitude of one pass (read + write) of the dominant
 # kernel, from single-launch captures at 28 qubits (traffic grows in proportion to
 # the state, so it is scaled to the workload's 2^n amplitudes):
-# profiles/btk_fused_pass_c64_brickwork28.md (JIT fused pass, plan mode) and
-# profiles/k_gate_sweep_c64_brickwork28.md (dense sweep, layer modes).
-TRAFFIC_BYTES_PER_AMP = {"plan": (2.147571e9 + 2.086315e9) / 2 ** 28,
+# profiles/btk_fused_pass_windows_c64_brickwork28.md (specialised fused pass, plan
+# mode) and profiles/k_gate_sweep_c64_brickwork28.md (dense sweep, layer modes).
+TRAFFIC_BYTES_PER_AMP = {"plan": (2.15e9 + 2.09e9) / 2 ** 28,
                          "sweep": (2.147591e9 + 2.087163e9) / 2 ** 28}
 
 

@@ -439,6 +439,18 @@ static bool encode_pass(bt_plan* p, const std::vector<int>& kept, const std::vec
   return true;
 }
 
+// register-phase windows (BTGPU_PLAN_PHASE_WINDOWS=1): each register phase of a
+// pass may also take NB consecutive tile bits where they hold more gates than the
+// set grown in gate order (33-qubit brickwork: 90 phases instead of 117; off by
+// default until timed on a GPU)
+static bool phase_windows_on() {
+  static const bool v = [] {
+    const char* e = getenv("BTGPU_PLAN_PHASE_WINDOWS");
+    return e && *e == '1';
+  }();
+  return v;
+}
+
 template <typename R>
 static bool build_fused(bt_plan* p, const std::vector<int>& take, uint64_t tilemask, int M, int NB, int c,
                         std::vector<int>& kept, FusedArgs<R>& a, int64_t* nph, std::vector<uint8_t>& ob0,
@@ -461,26 +473,48 @@ static bool build_fused(bt_plan* p, const std::vector<int>& take, uint64_t tilem
   std::vector<int> rem = take;
   int nop = 0, nreal = 0;
   kept.clear();
-  while (!rem.empty()) {
-    if (a.nphase >= BT_FUSED_MAX_PHASES) break;
-    uint32_t regs = 0, blocked = 0;
-    std::vector<int> ph, rest;
+  // the gates a phase with register set rs takes (in order, a gate left out blocks
+  // its bits): rs grown gate by gate up to NB bits, or given
+  auto scan = [&](uint32_t rs, bool fixed, std::vector<int>& ph, std::vector<int>& rest, uint32_t& regs, int& nr) {
+    regs = fixed ? rs : 0;
+    nr = nreal;
+    uint32_t blocked = 0;
+    ph.clear();
+    rest.clear();
     for (int gi : rem) {
       const PGate& g = p->gates[gi];
       uint32_t lb = 0;
       for (int i = 0; i < g.k; ++i) lb |= 1u << local[g.bits[i]];
       const int need = g.k == 1 ? 8 : 32;
-      if ((lb & blocked) || popc(regs | lb) > NB || nop + (int)ph.size() + 1 > BT_FUSED_MAX_OPS ||
-          nreal + need > maxreals) {
+      if ((lb & blocked) || (fixed ? (lb & ~rs) != 0 : popc(regs | lb) > NB) ||
+          nop + (int)ph.size() + 1 > BT_FUSED_MAX_OPS || nr + need > maxreals) {
         blocked |= lb;
         rest.push_back(gi);
         continue;
       }
-      regs |= lb;
+      if (!fixed) regs |= lb;
       ph.push_back(gi);
-      nreal += need;
+      nr += need;
     }
+  };
+  while (!rem.empty()) {
+    if (a.nphase >= BT_FUSED_MAX_PHASES) break;
+    uint32_t regs = 0, regs2 = 0;
+    int nr = 0, nr2 = 0;
+    std::vector<int> ph, rest, ph2, rest2;
+    scan(0, false, ph, rest, regs, nr);
+    if (phase_windows_on())  // or NB consecutive tile bits, where they take more gates
+      for (int s = 0; s + NB <= M; ++s) {
+        scan(((1u << NB) - 1) << s, true, ph2, rest2, regs2, nr2);
+        if (ph2.size() > ph.size()) {
+          ph.swap(ph2);
+          rest.swap(rest2);
+          regs = regs2;
+          nr = nr2;
+        }
+      }
     if (ph.empty()) break;
+    nreal = nr;
     // pad the register set to NB bits with the highest unused tile bits
     for (int b = M - 1; b >= 0 && popc(regs) < NB; --b) regs |= 1u << b;
     FPhase& P = a.ph[a.nphase++];

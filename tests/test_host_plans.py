@@ -4,6 +4,9 @@ folded scalar, variable gates) emulated pass by pass from bt_plan_pass_ops and
 compared with the oracle.  No GPU: planning needs none and the specialised
 kernels are not built (BTGPU_NO_JIT)."""
 import math
+import os
+import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -175,6 +178,20 @@ def test_host_plan_headline_pass_count():
     plan.compile()
     st = plan.stats()
     assert st["gates"] == 1470 and st["passes"] <= 26, st
+    if os.environ.get("BTGPU_PLAN_PHASE_WINDOWS") == "1":
+        assert st["phases"] <= 100, st  # register-bit windows: 90 phases instead of 117
     f, b = ctypes.c_double(), ctypes.c_double()
     L.check(L.lib().bt_plan_cost(plan.h, ctypes.byref(f), ctypes.byref(b)))
     assert b.value == 16 * st["passes"] and f.value < 2600, (f.value, b.value)
+
+
+def test_host_plans_with_phase_windows():
+    """The same checks with register phases chosen among bit windows as well
+    (BTGPU_PLAN_PHASE_WINDOWS=1, read once per process: run in a child)."""
+    if os.environ.get("BTGPU_PLAN_PHASE_WINDOWS") == "1":
+        pytest.skip("already running with phase windows")
+    env = dict(os.environ, BTGPU_PLAN_PHASE_WINDOWS="1")
+    r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-x", "-p", "no:cacheprovider", __file__],
+                       env=env, cwd=os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]

@@ -195,3 +195,27 @@ def test_host_plans_with_phase_windows():
                        env=env, cwd=os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
                        capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]
+
+
+@pytest.mark.parametrize("cfg", [(16, 5, 0, 0), (0, 4, 0, 0), (0, 5, 0, 12), (0, 5, 0, 11), (0, 5, 0, 10),
+                                 (128, 5, 1, 0)])
+def test_host_plan_tuning_configurations(oracle, cfg, monkeypatch):
+    """Every tuning the autotuner may keep (gates per pass, 4 or 5 register bits,
+    smaller tiles, two-lane code) plans the same map.  A register width other than
+    the default applies to specialised passes only, so that case lets NVRTC build
+    the kernels (on the host; nothing runs)."""
+    import bluetangle_gpu.circuits as C
+    if cfg[1] == 4:
+        monkeypatch.delenv("BTGPU_NO_JIT")
+    rng = np.random.default_rng(55)
+    n = 17
+    ops = C.random_ops(n, 2, rng) + C.brickwork(n, 10, rng)
+    plan = E.host_plan(n, prec="c64")
+    for op in ops:
+        plan.add(op)
+    plan.set_tuning(*cfg).compile()
+    psi = rstate(rng, n)
+    ref = psi
+    for op in ops:
+        ref = oracle_op(oracle, ref, op)
+    assert np.abs(E.run(plan, psi) - ref).max() < 2e-5

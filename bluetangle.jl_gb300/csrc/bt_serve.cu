@@ -88,7 +88,12 @@ struct bt_server {
   std::map<int64_t, Client*> clients;
   std::map<int64_t, Req*> reqs;
   int64_t next_client = 0, next_ticket = 0;
+  // latencies of the most recent requests (a ring of kLatWindow) for p50/p99;
+  // a long-running server keeps a bounded window, not every request
+  static constexpr size_t kLatWindow = 65536;
   std::vector<double> latencies;
+  size_t lat_next = 0;
+  int64_t completed = 0;
   int64_t runs = 0;  // request launches (a packed run serves several requests)
   std::string err;
 };
@@ -260,7 +265,10 @@ static void worker(bt_server* s, int lane) {
       r->err = err;
       r->t_done = t;
       r->done = true;
-      s->latencies.push_back(t - r->t_submit);
+      if (s->latencies.size() < bt_server::kLatWindow) s->latencies.push_back(t - r->t_submit);
+      else s->latencies[s->lat_next] = t - r->t_submit;
+      s->lat_next = (s->lat_next + 1) % bt_server::kLatWindow;
+      ++s->completed;
     }
     ++s->runs;
     c->busy = false;
@@ -460,7 +468,7 @@ int bt_serve_stats(bt_server* s, int64_t* completed, double* p50_s, double* p99_
     const double f = pos - (double)i;
     return i + 1 < l.size() ? l[i] * (1 - f) + l[i + 1] * f : l[i];
   };
-  if (completed) *completed = (int64_t)l.size();
+  if (completed) *completed = s->completed;
   if (p50_s) *p50_s = pct(0.50);
   if (p99_s) *p99_s = pct(0.99);
   int64_t res = 0;

@@ -297,8 +297,9 @@ int bt_serve_submit(bt_server* s, int64_t client, int count, const int64_t* inde
  * (either may be NULL).  A finished ticket is released by the call that reports it. */
 int bt_serve_poll(bt_server* s, int64_t ticket, int64_t wait_ms, double* value, double* latency_s,
                   double* service_s);
-/* completed requests, latency percentiles, resident clients, HBM in use, and
- * runs: launches of requests (a packed run serves several requests) */
+/* completed requests, latency percentiles (over the most recent 65536 requests),
+ * resident clients, HBM in use, and runs: launches of requests (a packed run
+ * serves several requests) */
 int bt_serve_stats(bt_server* s, int64_t* completed, double* p50_s, double* p99_s, int64_t* resident,
                    uint64_t* hbm_used, int64_t* runs);
 

@@ -1004,6 +1004,26 @@ static int jit_prepare_t(bt_ctx* ctx, std::vector<const FusedArgs<R>*>& passes, 
   std::vector<std::string> order;                     // new structures in first-seen order
   std::map<std::string, const FusedArgs<R>*> first;
   for (size_t i = 0; i < passes.size(); ++i) keys[i] = structure_key(*passes[i]);
+  if (const char* dump = getenv("BTGPU_JIT_DUMP")) {
+    // inspection aid: the generated source of every fused pass of this compile,
+    // kernel pass_<i> for the i-th fused pass (whether compiled now or cached)
+    std::ostringstream src;
+    src << kPrelude;
+    for (size_t i = 0; i < passes.size(); ++i) {
+      const FusedArgs<R>& pa = *passes[i];
+      const int nreg = pa.nphase ? pa.ph[0].nreg : (sizeof(R) == 4 ? BT_TILE_RB_C64 : BT_TILE_RB_C128);
+      src << "// pass " << i << ": M=" << pa.M << " threads=" << (1 << (pa.M - nreg)) << "\n";
+      gen_kernel<R>(src, pa, nreg, "pass_" + std::to_string(i));
+    }
+    if (FILE* fd = fopen(dump, "w")) {
+      const std::string t = src.str();
+      fwrite(t.data(), 1, t.size(), fd);
+      fclose(fd);
+    }
+    // BTGPU_JIT_DUMP_ONLY: write the source without building it (the passes keep
+    // the generic kernel)
+    if (getenv("BTGPU_JIT_DUMP_ONLY")) return BT_OK;
+  }
   {
     std::lock_guard<std::mutex> lk(g_jit_mu);  // held for lookups and inserts, not for compiling
     for (size_t i = 0; i < passes.size(); ++i)
@@ -1030,12 +1050,6 @@ static int jit_prepare_t(bt_ctx* ctx, std::vector<const FusedArgs<R>*>& passes, 
         bkeys[b].push_back(order[i]);
       }
       srcs[b] = src.str();
-    }
-    if (const char* dump = getenv("BTGPU_JIT_DUMP")) {  // debugging aid: the generated source of batch 0
-      if (FILE* fd = fopen(dump, "w")) {
-        fwrite(srcs[0].data(), 1, srcs[0].size(), fd);
-        fclose(fd);
-      }
     }
     std::vector<JitModule*> mods(nb);
     std::vector<std::thread> th;

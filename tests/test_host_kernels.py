@@ -1,0 +1,109 @@
+"""The generated fused-pass kernels run on the host (tests/kernel_emulator.py)
+and compared with the oracle: brickworks wide enough for several tiles and the
+window planner, every factored one-qubit form, and random gate mixes, in
+complex64 (scalar and two-lane code) and complex128, with the first/last phases
+direct to memory, staged through shared memory, or as the coalescing rule picks.
+The generator's knobs are read once per process, so each configuration runs in a
+child process, which writes the generated source without building it for the
+device (BTGPU_JIT_DUMP_ONLY); nothing runs on a GPU."""
+import os
+import subprocess
+import sys
+
+import pytest
+
+_CHILD = r"""
+import math, os, sys, tempfile
+import numpy as np
+root = sys.argv[1]
+sys.path[:0] = [os.path.join(root, "tests"), os.path.join(root, "bluetangle.jl_gb300"), os.path.join(root, "oracle")]
+import oracle as O
+import plan_emulator as E
+import kernel_emulator as K
+import bluetangle_gpu.circuits as C
+O.build()
+prec = sys.argv[2]
+tol = 2e-5 if prec == "c64" else 1e-12
+rng = np.random.default_rng(5)
+
+def rstate(n):
+    v = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
+    return v / np.linalg.norm(v)
+
+def check(n, seq, label):
+    plan = E.host_plan(n, prec=prec)
+    for m, qs, cs in seq:
+        plan.add_matrix(m, qs, cs)
+    plan.compile()
+    src = open(os.environ["BTGPU_JIT_DUMP"]).read()
+    psi = rstate(n)
+    ref = psi.copy()
+    for m, qs, cs in seq:
+        ref = O.apply_k(ref, m, qs, cs)
+    with tempfile.TemporaryDirectory() as d:
+        out = K.run(plan, psi, src, d)
+    err = np.abs(out - ref).max() / np.abs(ref).max()
+    assert err < tol, (label, err)
+    print(label, plan.stats()["passes"], "passes, rel err", err)
+
+def ops_seq(ops):
+    out = []
+    for op in ops:
+        qs = [op.qubit] if op.q == 1 else [op.qubit, op.target_qubit]
+        out.append((op.mat, qs, [op.control] if op.control != -2 else []))
+    return out
+
+n = 15 if prec == "c64" else 14
+check(n, ops_seq(C.random_ops(n, 1, rng) + C.brickwork(n, 6, rng)), "brickwork")
+c, s = math.cos(0.3), math.sin(0.3)
+h = 1 / math.sqrt(2)
+forms = [np.diag([1, -1]), np.diag([1, 1j]), np.diag([1, -1j]), np.diag([1, np.exp(0.7j)]),
+         np.diag([0.2, 1.3]), np.diag([1.3j, 0.2]), h * np.array([[1, 1], [1, -1]]),
+         h * np.array([[1, -1], [1, 1]]), h * np.array([[-1, 1], [1, 1]]), np.array([[c, -s], [s, c]]),
+         np.array([[s, -c], [c, s]]), np.array([[c, s], [s, -c]]), np.array([[c, -1j * s], [-1j * s, c]]),
+         np.array([[s, -1j * c], [-1j * c, s]]), np.array([[0.3, 0.9], [-0.9, 0.3]])]
+seq = []
+for rep in range(2):
+    for m in forms:
+        seq.append((np.asarray(m, dtype=complex), [int(rng.integers(1, 14))], []))
+    a, b = [int(x) for x in rng.choice(np.arange(1, 14), 2, replace=False)]
+    z = rng.normal(size=(4, 4)) + 1j * rng.normal(size=(4, 4))
+    q, r = np.linalg.qr(z)
+    seq.append((q, [a, b], []))
+    seq.append((np.eye(4, dtype=complex)[[0, 1, 3, 2]], [b, a], []))
+check(13, seq, "factored forms")
+seq = []
+for i in range(48):
+    qs = [int(x) for x in rng.choice(np.arange(1, 14), size=3, replace=False)]
+    kind = rng.integers(0, 4)
+    if kind == 0:
+        z = rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2)); u, _ = np.linalg.qr(z)
+        seq.append((u, qs[:1], []))
+    elif kind == 1:
+        z = rng.normal(size=(4, 4)) + 1j * rng.normal(size=(4, 4)); u, _ = np.linalg.qr(z)
+        seq.append((u, qs[:2], []))
+    elif kind == 2:
+        z = rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2)); u, _ = np.linalg.qr(z)
+        seq.append((u, qs[:1], qs[1:2]))
+    else:
+        seq.append((np.diag(np.exp(1j * rng.uniform(0, 6, 4))), qs[:2], []))
+check(13, seq, "random gates")
+print("OK")
+"""
+
+
+@pytest.mark.parametrize("prec,env", [
+    ("c64", {}),
+    ("c128", {}),
+    ("c64", {"BTGPU_JIT_PACKED": "1"}),
+    ("c64", {"BTGPU_JIT_DIRECT": "0"}),
+    ("c64", {"BTGPU_JIT_DIRECT": "2", "BTGPU_JIT_PACKED": "1"}),
+    ("c128", {"BTGPU_JIT_DIRECT": "2"}),
+])
+def test_generated_kernels_on_host(prec, env, tmp_path):
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    e = dict(os.environ, BTGPU_JIT_DUMP=str(tmp_path / "kernels.cu"), BTGPU_JIT_L2PF="0", BTGPU_JIT_PREFETCH="0",
+             BTGPU_JIT_DUMP_ONLY="1", **env)
+    e.pop("BTGPU_NO_JIT", None)
+    r = subprocess.run([sys.executable, "-c", _CHILD, root, prec], env=e, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0 and r.stdout.rstrip().endswith("OK"), r.stdout[-2000:] + r.stderr[-4000:]

@@ -2,7 +2,8 @@
 and compared with the oracle: brickworks wide enough for several tiles and the
 window planner, every factored one-qubit form, and random gate mixes, in
 complex64 (scalar and two-lane code) and complex128, with the first/last phases
-direct to memory, staged through shared memory, or as the coalescing rule picks.
+direct to memory, staged through shared memory, or as the coalescing rule picks,
+and with register phases chosen among bit windows.
 The generator's knobs are read once per process, so each configuration runs in a
 child process, which writes the generated source without building it for the
 device (BTGPU_JIT_DUMP_ONLY); nothing runs on a GPU."""
@@ -99,6 +100,7 @@ print("OK")
     ("c64", {"BTGPU_JIT_DIRECT": "0"}),
     ("c64", {"BTGPU_JIT_DIRECT": "2", "BTGPU_JIT_PACKED": "1"}),
     ("c128", {"BTGPU_JIT_DIRECT": "2"}),
+    ("c64", {"BTGPU_PLAN_PHASE_WINDOWS": "1"}),
 ])
 def test_generated_kernels_on_host(prec, env, tmp_path):
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))

@@ -103,9 +103,10 @@ def build(src, workdir, c64):
     return lib, kernels
 
 
-def run(plan, psi, dump_src, workdir):
+def run(plan, psi, dump_src, workdir, members=1):
     """The compiled plan applied to psi by its generated kernels run on the host
-    (sweep passes by the numpy emulation)."""
+    (sweep passes by the numpy emulation).  members > 1: psi holds that many
+    states back to back, run as the members of one batch."""
     import plan_emulator as E
     c64 = plan.prec in ("c64", "complex64")
     lib, kernels = build(dump_src, workdir, c64)
@@ -117,22 +118,23 @@ def run(plan, psi, dump_src, workdir):
                     ("lg_tiles", ctypes.c_int), ("mat", R * nreals)]
 
     x = np.asarray(psi, dtype=np.complex128).ravel(order="F").copy()
-    nbits = int(x.size).bit_length() - 1
+    nbits = int(x.size // members).bit_length() - 1
     state = x.astype(np.complex64 if c64 else np.complex128)
     fused = 0
     for kind, ops, mats in E.passes(plan):
         if kind:
-            y = state.astype(np.complex128)
-            E._sweep(y, nbits, ops, mats)
-            state = y.astype(state.dtype)
+            y = state.astype(np.complex128).reshape(members, -1)
+            for m in range(members):
+                E._sweep(y[m], nbits, ops, mats)
+            state = y.ravel().astype(state.dtype)
             continue
         name, M, threads = kernels[fused]
         assert name == f"pass_{fused}"
         a = Args()
-        a.member_lo, a.nmem, a.nbits, a.lg_tiles = 0, 1, nbits, nbits - M
+        a.member_lo, a.nmem, a.nbits, a.lg_tiles = 0, members, nbits, nbits - M
         for e in range(nreals):
             a.mat[e] = mats[e]
-        grid = min(1 << (nbits - M), 3)  # fewer CTAs than tiles: each loops over several
+        grid = min(members << (nbits - M), 3)  # fewer CTAs than tiles: each loops over several
         rc = lib.run_pass(fused, state.ctypes.data_as(ctypes.c_void_p), ctypes.byref(a), grid, threads)
         assert rc == 0
         fused += 1

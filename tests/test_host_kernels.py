@@ -89,6 +89,48 @@ for i in range(48):
     else:
         seq.append((np.diag(np.exp(1j * rng.uniform(0, 6, 4))), qs[:2], []))
 check(13, seq, "random gates")
+
+# two members of one batch: the tile loop crosses the member boundary
+n = 14
+ops = ops_seq(C.brickwork(n, 4, rng))
+plan = E.host_plan(n, prec=prec)
+for m, qs, cs in ops:
+    plan.add_matrix(m, qs, cs)
+plan.compile()
+src = open(os.environ["BTGPU_JIT_DUMP"]).read()
+psis = [rstate(n), rstate(n)]
+with tempfile.TemporaryDirectory() as d:
+    out = K.run(plan, np.concatenate(psis), src, d, members=2).reshape(2, -1)
+for k in range(2):
+    ref = psis[k]
+    for m, qs, cs in ops:
+        ref = O.apply_k(ref, m, qs, cs)
+    assert np.abs(out[k] - ref).max() < tol, ("members", k)
+print("members ok")
+
+# density matrix over 2n bits: row/column gates and Kraus sums as superoperators
+import bluetangle_gpu as bt
+n = 7
+dops = C.noisy_brickwork_dm(n, 3, rng)
+plan = E.host_plan(n, repr="dm", prec=prec)
+for o in dops:
+    plan.add(o)
+plan.compile()
+src = open(os.environ["BTGPU_JIT_DUMP"]).read()
+rho0 = np.zeros((2 ** n, 2 ** n), complex)
+rho0[0, 0] = 1
+ref = rho0
+for o in dops:
+    if isinstance(o, bt.OpQC):
+        ref = O.dm_channel(ref, o.kraus, o.qubit, o.target_qubit if o.q == 2 else -1)
+    elif o.q == 1:
+        ref = O.dm_hilbert1(ref, o.mat, o.qubit)
+    else:
+        ref = O.dm_hilbert2(ref, o.mat, o.qubit, o.target_qubit)
+with tempfile.TemporaryDirectory() as d:
+    out = K.run(plan, rho0, src, d).reshape(2 ** n, 2 ** n, order="F")
+assert np.abs(out - ref).max() < tol, ("density", np.abs(out - ref).max())
+print("density ok")
 print("OK")
 """
 

@@ -75,6 +75,9 @@ SIGNATURES = {
     "bt_plan_cost": (i32, [P, P, P]),
     "bt_plan_pass_ops": (i32, [P, i64, P, P, P, P, i32, i32]),
     "bt_plan_run": (i32, [P, P, i64]),
+    "bt_plan_run_members": (i32, [P, P, i32, P, P]),
+    "bt_plan_prepare_members": (i32, [P, i32, P]),
+    "bt_plan_member_table": (i32, [P, i64, i64, i32, P, P, P, i64, P]),
     "bt_plan_set_tuning": (i32, [P, i32, i32, i32, i32]),
     "bt_program_create": (i32, [P, i32, i32, i32, ctypes.POINTER(P)]),
     "bt_program_free": (i32, [P]),

@@ -540,6 +540,17 @@ class Plan:
         self.ctx.check(L.lib().bt_plan_run(self.h, state.h, member))
         return state
 
+    def run_members(self, state, indices, member_mats):
+        """Runs the plan on every member of state, member m with member_mats[m]
+        (one matrix per add index in `indices`) for those gates: one launch per
+        pass for the whole batch (bt_plan_run_members)."""
+        idx = np.ascontiguousarray(list(indices), dtype=np.int64)
+        if len(member_mats) != state.batch:
+            raise ValueError("one list of matrices per member")
+        buf = np.ascontiguousarray(np.concatenate([_cm(m).ravel() for mm in member_mats for m in mm]))
+        self.ctx.check(L.lib().bt_plan_run_members(self.h, state.h, len(idx), _ptr(idx), _ptr(buf)))
+        return state
+
 
 def plan_from_ops(ops, n, repr="sv", prec="c128", fused=True, ctx=None):
     p = Plan(n, repr, prec, ctx)

@@ -118,11 +118,12 @@ static std::string fmt_u64(uint64_t v) {
 static int swz_host(bool f, int l) { return f ? (l ^ ((l >> 4) & 15)) : (l ^ ((l >> 3) & 7)); }
 
 // emits one op on the scalar registers x<j> (real) / y<j> (imaginary), j < 2^NB
-static void emit_op(std::ostringstream& o, const FOp& op, int NB) {
+// mref: where the op's entries are read (the kernel parameters, or a per-member table)
+static void emit_op(std::ostringstream& o, const FOp& op, int NB, const char* mref = "a.mat") {
   const int D = 1 << NB;
   auto M = [&](int e) {
     std::ostringstream s;
-    s << "a.mat[" << (op.moff + e) << "]";
+    s << mref << "[" << (op.moff + e) << "]";
     return s.str();
   };
   auto pairs = [&](int B, auto&& body) {
@@ -345,11 +346,11 @@ static int choose_pack_bit(const FusedArgs<float>& a, const FPhase& ph, int NB) 
 }
 
 // emits op on the pairs; false: the op needs the scalar fallback
-static bool emit_op_packed(std::ostringstream& o, const FOp& op, int NB, int P) {
+static bool emit_op_packed(std::ostringstream& o, const FOp& op, int NB, int P, const char* mref = "a.mat") {
   const int D = 1 << NB;
   auto M = [&](int e) {
     std::ostringstream s;
-    s << "a.mat[" << (op.moff + e) << "]";
+    s << mref << "[" << (op.moff + e) << "]";
     return s.str();
   };
   auto bcs = [&](const char* name, int e, bool neg) {  // broadcast coefficient pair
@@ -652,9 +653,14 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
   const int T = 1 << (M - NB);
   const int NPT = (1 << M) / V / T;
   const char* T2 = f ? "cf" : "cd";
+  // per-member entries (a.permem): member m of the launch reads its ops' entries from
+  // row m of the table mm (mstride reals per row) instead of the kernel parameters
+  const char* mref = a.permem ? "cm" : "a.mat";
   o << "extern \"C\" __global__ void __launch_bounds__(" << T << ", " << bt_jit_min_blocks() << ") " << name << "("
     << T2 << "* __restrict__ psi, const "
-    << (f ? "JitArgsF<" : "JitArgsD<") << NM << "> a) {\n";
+    << (f ? "JitArgsF<" : "JitArgsD<") << NM << "> a";
+  if (a.permem) o << ", const " << (f ? "float" : "double") << "* __restrict__ mm, const i64 mstride";
+  o << ") {\n";
   o << "  typedef " << (f ? "float" : "double") << " R;\n";
   const int NP = a.nphase;
   if (NP == 0) {  // nothing to apply
@@ -736,6 +742,7 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
   }
   o << "  for (i64 tid = blockIdx.x; tid < total; tid += gridDim.x) {\n";
   o << "    " << T2 << "* g = tile_ptr(tid);\n";
+  if (a.permem) o << "    const R* cm = mm + (tid >> a.lg_tiles) * mstride;\n";
   if (l2pf) {
     o << "    if (tid + gridDim.x < total" << (T > nruns ? " && threadIdx.x < " + std::to_string(nruns) : std::string())
       << ") { const " << T2 << "* gn = tile_ptr(tid + gridDim.x) + roff;";
@@ -853,17 +860,17 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
       pack();
       for (int oi = ph.op0; oi < ph.op0 + ph.nop; ++oi) {
         std::ostringstream po;
-        if (emit_op_packed(po, a.op[oi], NB, P)) {
+        if (emit_op_packed(po, a.op[oi], NB, P, mref)) {
           o << po.str();
         } else {  // scalar fallback for an op on the pack bit
           unpack();
-          emit_op(o, a.op[oi], NB);
+          emit_op(o, a.op[oi], NB, mref);
           pack();
         }
       }
       unpack();
     } else {
-      for (int oi = ph.op0; oi < ph.op0 + ph.nop; ++oi) emit_op(o, a.op[oi], NB);
+      for (int oi = ph.op0; oi < ph.op0 + ph.nop; ++oi) emit_op(o, a.op[oi], NB, mref);
     }
     if (wr_direct) {
       o << "    { " << T2 << "* gp = g + tl;\n";
@@ -907,7 +914,8 @@ template <typename R>
 static std::string structure_key(const FusedArgs<R>& a) {
   std::ostringstream k;
   k << (sizeof(R) == 4 ? 'f' : 'd') << a.M << ':' << a.c << ':' << bt_jit_min_blocks() << ':'
-    << (a.nphase ? (int)a.ph[0].nreg : 0) << ':' << (sizeof(R) == 4 && a.packed ? 'p' : 's') << ':';
+    << (a.nphase ? (int)a.ph[0].nreg : 0) << ':' << (sizeof(R) == 4 && a.packed ? 'p' : 's') << ':'
+    << (a.permem ? 'm' : 'k') << ':';
   for (int i = 0; i < a.M; ++i) k << a.tbits[i] << ',';
   for (int p = 0; p < a.nphase; ++p) {
     const FPhase& ph = a.ph[p];
@@ -1093,8 +1101,11 @@ struct JitArgsHost {
   R mat[sizeof(R) == 4 ? BT_FUSED_MAX_REALS_F : BT_FUSED_MAX_REALS_D];
 };
 
+// mm / mstride: the per-member table of a kernel compiled with a.permem (row m for
+// member member_lo + m), else unused
 template <typename R>
-static int jit_launch_t(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<R>& a) {
+static int jit_launch_t(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<R>& a, const void* mm = nullptr,
+                        int64_t mstride = 0) {
   JitEntry* je = (JitEntry*)entry;
   typedef typename CT<R>::T C2;
   const int M = a.M;
@@ -1126,7 +1137,7 @@ static int jit_launch_t(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<R>&
   h.nbits = a.nbits;
   h.lg_tiles = a.lg_tiles;
   memcpy(h.mat, a.mat, sizeof(h.mat));
-  void* args[] = {&psi, &h};
+  void* args[] = {&psi, &h, &mm, &mstride};
   int64_t total = (1LL << a.lg_tiles) * a.nmem;
   int64_t grid = (int64_t)ctx->sm_count * bt_jit_min_blocks() * 4;
   if (grid > total) grid = total;
@@ -1139,6 +1150,14 @@ static int jit_launch_t(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<R>&
 
 int bt_jit_launch_f(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<float>& a) {
   return jit_launch_t<float>(ctx, entry, psi, a);
+}
+int bt_jit_launch_members_f(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<float>& a, const float* mm,
+                            int64_t mstride) {
+  return jit_launch_t<float>(ctx, entry, psi, a, mm, mstride);
+}
+int bt_jit_launch_members_d(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<double>& a, const double* mm,
+                            int64_t mstride) {
+  return jit_launch_t<double>(ctx, entry, psi, a, mm, mstride);
 }
 int bt_jit_launch_d(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<double>& a) {
   return jit_launch_t<double>(ctx, entry, psi, a);

@@ -15,3 +15,9 @@ int bt_jit_prepare_f(bt_ctx* ctx, std::vector<const FusedArgs<float>*>& passes, 
 int bt_jit_prepare_d(bt_ctx* ctx, std::vector<const FusedArgs<double>*>& passes, std::vector<void*>& out);
 int bt_jit_launch_f(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<float>& a);
 int bt_jit_launch_d(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<double>& a);
+// kernels compiled with a.permem: member member_lo + m reads row m of the device
+// table mm (mstride reals per row)
+int bt_jit_launch_members_f(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<float>& a, const float* mm,
+                            int64_t mstride);
+int bt_jit_launch_members_d(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<double>& a, const double* mm,
+                            int64_t mstride);

@@ -52,6 +52,10 @@ struct PPass {
   std::vector<unsigned char> args;  // FusedArgs<float> or <double>, bytes
   std::vector<int> op_gate;         // gate of each op, and its register bits before encoding
   std::vector<uint8_t> op_b0, op_b1;
+  // per-member form (bt_plan_run_members): the pass compiled to read its entries
+  // from a per-member table, and its specialised kernel
+  std::vector<unsigned char> pm_args;
+  void* pm_jit = nullptr;
 };
 
 struct bt_plan {
@@ -70,7 +74,14 @@ struct bt_plan {
   std::unique_ptr<std::atomic<void*>[]> jit;
   std::atomic<int64_t> njit{0};
   std::thread jit_thread;
+  // device table of per-member entries (bt_plan_run_members), reused pass by pass
+  void* d_pm = nullptr;
+  size_t d_pm_bytes = 0;
+  int d_pm_device = -1;
 };
+
+// reals of the matrices that bt_plan_set_matrices reads for these add indices
+int bt_plan_gate_dims(const bt_plan* p, const int64_t* idx, int count, size_t* reals);
 
 static void join_jit(bt_plan* p) {
   if (p->jit_thread.joinable()) p->jit_thread.join();
@@ -573,6 +584,10 @@ int bt_plan_create(bt_ctx* ctx, int n, int repr, int prec, bt_plan** out) {
 
 int bt_plan_free(bt_plan* p) {
   if (p) join_jit(p);
+  if (p && p->d_pm) {
+    cudaSetDevice(p->d_pm_device);
+    cudaFree(p->d_pm);
+  }
   delete p;
   return BT_OK;
 }
@@ -745,11 +760,17 @@ static bool update_pass(bt_plan* p, PPass& ps, const std::vector<char>& touched)
 
 extern "C" {
 
-int bt_plan_set_matrices(bt_plan* p, int count, const int64_t* add_index, const double* mats) {
-  if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "plan is NULL");
+}  // extern "C"
+
+// Writes the matrices of these adds (column-major, back to back, in the size each
+// was added with) into their gates: the column pass of a density-matrix gate takes
+// conj(U), folded controls are re-folded.  The gates become variable; touched
+// marks them.
+static int assign_matrices(bt_plan* p, int count, const int64_t* add_index, const double* mats,
+                           std::vector<char>& touched) {
   bt_ctx* ctx = p->ctx;
   if (count < 0 || (count > 0 && (!add_index || !mats))) return bt_fail(ctx, BT_ERR_BAD_ARG, "bad update arrays");
-  std::vector<char> touched(p->gates.size(), 0);
+  touched.assign(p->gates.size(), 0);
   size_t off = 0;
   for (int i = 0; i < count; ++i) {
     const int64_t ai = add_index[i];
@@ -774,6 +795,16 @@ int bt_plan_set_matrices(bt_plan* p, int count, const int64_t* add_index, const 
       touched[first + j] = 1;
     }
   }
+  return BT_OK;
+}
+
+extern "C" {
+
+int bt_plan_set_matrices(bt_plan* p, int count, const int64_t* add_index, const double* mats) {
+  if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "plan is NULL");
+  std::vector<char> touched;
+  int rc = assign_matrices(p, count, add_index, mats, touched);
+  if (rc) return rc;
   if (!p->compiled) return BT_OK;
   for (auto& ps : p->passes) {
     if (ps.kind != 0) continue;
@@ -958,6 +989,147 @@ int bt_plan_set_tuning(bt_plan* p, int max_ops, int tile_rb, int packed, int til
   return BT_OK;
 }
 
+}  // extern "C"
+
+// entries an encoded op reads (from its moff)
+static int op_reals(const FOp& o) {
+  switch (o.type) {
+    case FOP_G1: case FOP_D2: case FOP_P2: return 8;
+    case FOP_G2: return 32;
+    case FOP_D1: case FOP_R1: case FOP_X1: return 4;
+    case FOP_RX1: case FOP_DH: case FOP_RN: return 2;
+    case FOP_RXN: return 1;
+    default: return 0;  // CX, SW, HB
+  }
+}
+
+// Per-member entries of fused pass `pass`: row m holds what the pass reads when the
+// gates of these adds take member m's matrices (mats: `members` blocks of `per`
+// reals, each the matrices of add_index back to back as bt_plan_set_matrices reads
+// them).  The gates must already be variable, so no member changes the pass's
+// structure.  The gates' own matrices are left as they were.
+template <typename R>
+static int member_table(bt_plan* p, size_t pass, int64_t members, int count, const int64_t* add_index,
+                        const double* mats, size_t per, std::vector<R>& table, int* used) {
+  PPass& ps = p->passes[pass];
+  std::vector<unsigned char> scratch(ps.args);
+  FusedArgs<R>& sa = *reinterpret_cast<FusedArgs<R>*>(scratch.data());
+  int u = 0;
+  for (int i = 0; i < ps.ngates; ++i) u = std::max(u, (int)sa.op[i].moff + op_reals(sa.op[i]));
+  std::vector<std::pair<int, std::vector<double>>> saved;
+  for (int i = 0; i < count; ++i)
+    if (add_index[i] >= 0 && add_index[i] < (int64_t)p->adds.size())
+      for (int j = 0; j < p->adds[add_index[i]].second; ++j) {
+        const int gi = p->adds[add_index[i]].first + j;
+        saved.push_back({gi, p->gates[gi].m});
+      }
+  table.assign((size_t)members * (size_t)u, (R)0);
+  std::vector<char> touched;
+  int rc = BT_OK;
+  for (int64_t m = 0; m < members && !rc; ++m) {
+    rc = assign_matrices(p, count, add_index, mats + (size_t)m * per, touched);
+    if (rc) break;
+    if (!encode_pass<R>(p, ps.op_gate, ps.op_b0, ps.op_b1, sa, true)) {
+      rc = bt_fail(p->ctx, BT_ERR_BAD_ARG,
+                   "a member's matrix changes a pass's structure: mark the gates variable and compile first");
+      break;
+    }
+    memcpy(&table[(size_t)m * u], sa.mat, sizeof(R) * u);
+  }
+  for (auto& sv : saved) p->gates[sv.first].m = sv.second;
+  *used = u;
+  return rc;
+}
+
+// the touched gates (of these adds) made variable, the plan compiled with their
+// entry-independent forms, and the per-member kernel of every fused pass that
+// holds one of them built (or written to BTGPU_JIT_DUMP)
+static int prepare_members(bt_plan* p, int count, const int64_t* add_index, std::vector<char>& touched) {
+  size_t per = 0;
+  int rc = bt_plan_gate_dims(p, add_index, count, &per);
+  if (rc) return rc;
+  touched.assign(p->gates.size(), 0);
+  bool changed = false;
+  for (int i = 0; i < count; ++i)
+    for (int j = 0; j < p->adds[add_index[i]].second; ++j) {
+      PGate& g = p->gates[p->adds[add_index[i]].first + j];
+      touched[p->adds[add_index[i]].first + j] = 1;
+      changed |= !g.var;
+      g.var = true;
+    }
+  if (changed || !p->compiled) {
+    rc = bt_plan_compile(p, 0);
+    if (rc) return rc;
+  }
+  join_jit(p);
+  if (!bt_jit_available())
+    return bt_fail(p->ctx, BT_ERR_UNSUPPORTED, "per-member matrices need the specialised kernels (NVRTC)");
+  const bool c64 = p->prec == BT_PREC_C64;
+  std::vector<size_t> idx;
+  for (size_t i = 0; i < p->passes.size(); ++i) {
+    PPass& ps = p->passes[i];
+    bool hit = false;
+    if (ps.kind == 1) {
+      if (touched[ps.gate])
+        return bt_fail(p->ctx, BT_ERR_UNSUPPORTED,
+                       "per-member matrices for a gate outside fused passes (more than two qubits or wide controls)");
+      continue;
+    }
+    for (int gi : ps.op_gate) hit |= touched[gi] != 0;
+    if (!hit || ps.pm_jit) continue;
+    ps.pm_args = ps.args;
+    if (c64) reinterpret_cast<FusedArgs<float>*>(ps.pm_args.data())->permem = 1;
+    else reinterpret_cast<FusedArgs<double>*>(ps.pm_args.data())->permem = 1;
+    idx.push_back(i);
+  }
+  if (idx.empty()) return BT_OK;
+  std::vector<void*> ent;
+  if (c64) {
+    std::vector<const FusedArgs<float>*> v;
+    for (size_t i : idx) v.push_back(reinterpret_cast<const FusedArgs<float>*>(p->passes[i].pm_args.data()));
+    rc = bt_jit_prepare_f(p->ctx, v, ent);
+  } else {
+    std::vector<const FusedArgs<double>*> v;
+    for (size_t i : idx) v.push_back(reinterpret_cast<const FusedArgs<double>*>(p->passes[i].pm_args.data()));
+    rc = bt_jit_prepare_d(p->ctx, v, ent);
+  }
+  if (rc) return rc;
+  for (size_t j = 0; j < idx.size(); ++j) p->passes[idx[j]].pm_jit = ent[j];
+  return BT_OK;
+}
+
+extern "C" {
+
+int bt_plan_prepare_members(bt_plan* p, int count, const int64_t* add_index) {
+  if (!p || count < 1 || !add_index) return bt_fail(p ? p->ctx : nullptr, BT_ERR_BAD_ARG, "bad arguments");
+  std::vector<char> touched;
+  return prepare_members(p, count, add_index, touched);
+}
+
+int bt_plan_member_table(bt_plan* p, int64_t pass, int64_t members, int count, const int64_t* add_index,
+                         const double* mats, double* out, int64_t cap, int* used) {
+  if (!p || !add_index || !mats || !used || members < 1 || count < 1)
+    return bt_fail(p ? p->ctx : nullptr, BT_ERR_BAD_ARG, "bad arguments");
+  if (!p->compiled) return bt_fail(p->ctx, BT_ERR_BAD_ARG, "plan is not compiled");
+  if (pass < 0 || pass >= (int64_t)p->passes.size() || p->passes[pass].kind != 0)
+    return bt_fail(p->ctx, BT_ERR_BAD_ARG, "not a fused pass");
+  size_t per = 0;
+  int rc = bt_plan_gate_dims(p, add_index, count, &per);
+  if (rc) return rc;
+  if (p->prec == BT_PREC_C64) {
+    std::vector<float> t;
+    rc = member_table<float>(p, (size_t)pass, members, count, add_index, mats, per, t, used);
+    if (!rc && out && cap >= (int64_t)t.size())
+      for (size_t e = 0; e < t.size(); ++e) out[e] = t[e];
+  } else {
+    std::vector<double> t;
+    rc = member_table<double>(p, (size_t)pass, members, count, add_index, mats, per, t, used);
+    if (!rc && out && cap >= (int64_t)t.size())
+      for (size_t e = 0; e < t.size(); ++e) out[e] = t[e];
+  }
+  return rc;
+}
+
 // arithmetic of one op per amplitude of the state, in real flops (an FMA counts
 // two), as the specialised code does it
 static double op_flops(const FOp& o) {
@@ -1090,6 +1262,88 @@ int bt_plan_run(bt_plan* p, bt_state* s, int64_t member) {
       a.nmem = nm;
       void* e = p->jit[i].load(std::memory_order_acquire);
       rc = e ? bt_jit_launch_d(ctx, e, s->d, a) : bt_launch_fused_d(ctx, s->d, a);
+    }
+  }
+  return rc;
+}
+
+int bt_plan_run_members(bt_plan* p, bt_state* s, int count, const int64_t* add_index, const double* mats) {
+  if (!p || !s || count < 1 || !add_index || !mats) return bt_fail(p ? p->ctx : nullptr, BT_ERR_BAD_ARG, "bad arguments");
+  bt_ctx* ctx = s->ctx;
+  if (s->n != p->n || s->repr != p->repr || s->prec != p->prec)
+    return bt_fail(ctx, BT_ERR_BAD_ARG, "plan and state differ in n, repr or prec");
+  std::vector<char> touched;
+  int rc = prepare_members(p, count, add_index, touched);
+  if (rc) return rc;
+  size_t per = 0;
+  rc = bt_plan_gate_dims(p, add_index, count, &per);
+  if (rc) return rc;
+  const int64_t B = s->batch;
+  const bool c64 = p->prec == BT_PREC_C64;
+  rc = bt_cuda_check(ctx, cudaSetDevice(ctx->device), "cudaSetDevice");
+  for (size_t i = 0; i < p->passes.size() && !rc; ++i) {
+    PPass& ps = p->passes[i];
+    if (ps.kind == 1) {
+      const PGate& g = p->gates[ps.gate];
+      rc = bt_launch_gate(s, g.k, g.bits, g.m.data(), g.cmask, 0, B, nullptr, 0);
+      continue;
+    }
+    void* e = p->jit[i].load(std::memory_order_acquire);
+    bool hit = false;
+    for (int gi : ps.op_gate) hit |= touched[gi] != 0;
+    if (hit && !ps.pm_jit) {
+      rc = bt_fail(ctx, BT_ERR_DEVICE, "the per-member kernel of a pass was not built");
+      break;
+    }
+    if (!hit) {  // no member-dependent gate in this pass
+      if (c64) {
+        FusedArgs<float>& a = *reinterpret_cast<FusedArgs<float>*>(ps.args.data());
+        a.member_lo = 0;
+        a.nmem = B;
+        rc = e ? bt_jit_launch_f(ctx, e, s->d, a) : bt_launch_fused_f(ctx, s->d, a);
+      } else {
+        FusedArgs<double>& a = *reinterpret_cast<FusedArgs<double>*>(ps.args.data());
+        a.member_lo = 0;
+        a.nmem = B;
+        rc = e ? bt_jit_launch_d(ctx, e, s->d, a) : bt_launch_fused_d(ctx, s->d, a);
+      }
+      continue;
+    }
+    // the pass's entries for every member, uploaded to the plan's table (stream
+    // order keeps the previous pass's reads before this upload)
+    std::vector<float> tf;
+    std::vector<double> td;
+    int used = 0;
+    rc = c64 ? member_table<float>(p, i, B, count, add_index, mats, per, tf, &used)
+             : member_table<double>(p, i, B, count, add_index, mats, per, td, &used);
+    if (rc) break;
+    const size_t bytes = c64 ? tf.size() * sizeof(float) : td.size() * sizeof(double);
+    if (bytes > p->d_pm_bytes || p->d_pm_device != ctx->device) {
+      if (p->d_pm) {
+        cudaSetDevice(p->d_pm_device);
+        cudaFree(p->d_pm);
+        cudaSetDevice(ctx->device);
+        p->d_pm = nullptr;
+      }
+      rc = bt_cuda_check(ctx, cudaMalloc(&p->d_pm, bytes), "per-member table");
+      if (rc) break;
+      p->d_pm_bytes = bytes;
+      p->d_pm_device = ctx->device;
+    }
+    rc = bt_cuda_check(ctx, cudaMemcpyAsync(p->d_pm, c64 ? (const void*)tf.data() : (const void*)td.data(), bytes,
+                                            cudaMemcpyHostToDevice, ctx->stream),
+                       "per-member table upload");
+    if (rc) break;
+    if (c64) {
+      FusedArgs<float>& a = *reinterpret_cast<FusedArgs<float>*>(ps.pm_args.data());
+      a.member_lo = 0;
+      a.nmem = B;
+      rc = bt_jit_launch_members_f(ctx, ps.pm_jit, s->d, a, (const float*)p->d_pm, used);
+    } else {
+      FusedArgs<double>& a = *reinterpret_cast<FusedArgs<double>*>(ps.pm_args.data());
+      a.member_lo = 0;
+      a.nmem = B;
+      rc = bt_jit_launch_members_d(ctx, ps.pm_jit, s->d, a, (const double*)p->d_pm, used);
     }
   }
   return rc;

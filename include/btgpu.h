@@ -203,6 +203,22 @@ int bt_plan_stats(const bt_plan* p, int64_t* ngates, int64_t* npasses, int64_t* 
  * bits per pass (10..13 complex64 / 9..12 complex128; a smaller tile spreads a
  * small state over more CTAs) */
 int bt_plan_set_tuning(bt_plan* p, int max_ops, int tile_rb, int packed, int tile_bits);
+/* Runs the plan on every member of s, member m with its own matrices for the
+ * gates of these adds (mats: s's batch blocks, each the matrices of add_index
+ * back to back as bt_plan_set_matrices reads them): one launch per pass for the
+ * whole batch, the passes that hold those gates reading per-member entries from
+ * a device table (parameter-shift evaluations, served requests of one circuit).
+ * The gates become variable (one recompile if they were not); they must lie in
+ * fused passes (one or two qubits, at most one folded control), and the
+ * specialised kernels are needed (NVRTC).  The plan's own matrices stay as they
+ * were. */
+int bt_plan_run_members(bt_plan* p, bt_state* s, int count, const int64_t* add_index, const double* mats);
+/* host-side parts of bt_plan_run_members, for inspection: building the per-member
+ * kernels (written to BTGPU_JIT_DUMP when set), and the table of fused pass `pass`
+ * (row m: member m's entries, *used reals per row; out, of cap reals, may be NULL) */
+int bt_plan_prepare_members(bt_plan* p, int count, const int64_t* add_index);
+int bt_plan_member_table(bt_plan* p, int64_t pass, int64_t members, int count, const int64_t* add_index,
+                         const double* mats, double* out, int64_t cap, int* used);
 /* runs the plan on member `member` (-1: every member) of a state of the same n/repr/prec */
 int bt_plan_run(bt_plan* p, bt_state* s, int64_t member);
 

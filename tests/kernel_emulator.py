@@ -45,8 +45,8 @@ static inline float __uint_as_float(unsigned u) { float f; std::memcpy(&f, &u, 4
 """
 
 LAUNCH = r"""
-template <typename T2, typename A>
-static void launch(void (*k)(T2*, const A), void* psi, const void* args, int grid, int threads) {
+template <typename F>
+static void grid_run(F body, int grid, int threads) {
   gridDim.x = grid;
   blockDim.x = threads;
   for (int b = 0; b < grid; ++b) {
@@ -57,10 +57,20 @@ static void launch(void (*k)(T2*, const A), void* psi, const void* args, int gri
       ts.emplace_back([&, t, b] {
         threadIdx.x = t;
         blockIdx.x = b;
-        k((T2*)psi, *(const A*)args);
+        body();
       });
     for (auto& th : ts) th.join();
   }
+}
+template <typename T2, typename A>
+static void launch(void (*k)(T2*, const A), void* psi, const void* args, int grid, int threads) {
+  grid_run([&] { k((T2*)psi, *(const A*)args); }, grid, threads);
+}
+// kernels reading per-member entries: row m of mm for member m
+template <typename T2, typename A, typename R>
+static void launch_pm(void (*k)(T2*, const A, const R*, const i64), void* psi, const void* args, const void* mm,
+                      long long mstride, int grid, int threads) {
+  grid_run([&] { k((T2*)psi, *(const A*)args, (const R*)mm, (i64)mstride); }, grid, threads);
 }
 """
 
@@ -84,23 +94,93 @@ def translate(src):
     return HOST_HEADER + code + LAUNCH, kernels
 
 
-def build(src, workdir, c64):
-    """Host library of the generated kernels with run_pass(i, psi, args, grid, threads)."""
+def build(src, workdir, c64, permem=False):
+    """Host library of the generated kernels with run_pass(i, psi, args, grid,
+    threads), or with permem run_pass(i, psi, args, mm, mstride, grid, threads)."""
     code, kernels = translate(src)
-    T2, A = ("cf", "JitArgsF<4096>") if c64 else ("cd", "JitArgsD<2048>")
-    code += 'extern "C" int run_pass(int i, void* psi, const void* args, int grid, int threads) {\n  switch (i) {\n'
-    for name, _, _ in kernels:
-        code += f"    case {int(name[5:])}: launch<{T2}, {A}>({name}, psi, args, grid, threads); return 0;\n"
+    T2, A, R = ("cf", "JitArgsF<4096>", "float") if c64 else ("cd", "JitArgsD<2048>", "double")
+    if permem:
+        code += ('extern "C" int run_pass(int i, void* psi, const void* args, const void* mm, long long mstride, '
+                 'int grid, int threads) {\n  switch (i) {\n')
+        for name, _, _ in kernels:
+            code += (f"    case {int(name[5:])}: launch_pm<{T2}, {A}, {R}>({name}, psi, args, mm, mstride, grid, "
+                     "threads); return 0;\n")
+    else:
+        code += 'extern "C" int run_pass(int i, void* psi, const void* args, int grid, int threads) {\n  switch (i) {\n'
+        for name, _, _ in kernels:
+            code += f"    case {int(name[5:])}: launch<{T2}, {A}>({name}, psi, args, grid, threads); return 0;\n"
     code += "  }\n  return -1;\n}\n"
-    cpp = os.path.join(workdir, "kernels.cpp")
-    so = os.path.join(workdir, "kernels.so")
+    tag = "pm" if permem else "k"
+    cpp = os.path.join(workdir, f"kernels_{tag}.cpp")
+    so = os.path.join(workdir, f"kernels_{tag}.so")
     with open(cpp, "w") as f:
         f.write(code)
     subprocess.run(["g++", "-std=c++20", "-O0", "-shared", "-fPIC", "-pthread", "-w", "-o", so, cpp], check=True)
     lib = ctypes.CDLL(so)
     lib.run_pass.restype = ctypes.c_int
-    lib.run_pass.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+    lib.run_pass.argtypes = ([ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong,
+                              ctypes.c_int, ctypes.c_int] if permem else
+                             [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int])
     return lib, kernels
+
+
+def run_members(plan, psis, src, src_pm, workdir, indices, member_mats):
+    """Member m of psis (a (members, 2^n) array) under the plan with member_mats[m]
+    for the gates of these add indices, as bt_plan_run_members runs it: passes
+    without those gates by their kernels (src), the others by their per-member
+    kernels (src_pm, built by bt_plan_prepare_members) reading the member table."""
+    import plan_emulator as E
+    from bluetangle_gpu import _lib as L
+    from bluetangle_gpu.engine import _cm
+    c64 = plan.prec in ("c64", "complex64")
+    lib, kernels = build(src, workdir, c64)
+    lpm, kpm = build(src_pm, workdir, c64, permem=True)
+    R = ctypes.c_float if c64 else ctypes.c_double
+    nreals = 4096 if c64 else 2048
+
+    class Args(ctypes.Structure):
+        _fields_ = [("member_lo", ctypes.c_int64), ("nmem", ctypes.c_int64), ("nbits", ctypes.c_int),
+                    ("lg_tiles", ctypes.c_int), ("mat", R * nreals)]
+
+    B = len(member_mats)
+    idx = np.ascontiguousarray(list(indices), dtype=np.int64)
+    buf = np.ascontiguousarray(np.concatenate([_cm(m).ravel() for mm in member_mats for m in mm]))
+    x = np.asarray(psis, dtype=np.complex128).reshape(B, -1)
+    nbits = int(x.shape[1]).bit_length() - 1
+    state = x.ravel().astype(np.complex64 if c64 else np.complex128)
+    P = ctypes.c_void_p
+    fused = pm = 0
+    for i, (kind, ops, mats) in enumerate(E.passes(plan)):
+        if kind:
+            y = state.astype(np.complex128).reshape(B, -1)
+            for m in range(B):
+                E._sweep(y[m], nbits, ops, mats)
+            state = y.ravel().astype(state.dtype)
+            continue
+        used = ctypes.c_int()
+        table = np.zeros(B * nreals, dtype=np.float64)
+        rc = L.lib().bt_plan_member_table(plan.h, i, B, len(idx), idx.ctypes.data_as(P), buf.ctypes.data_as(P),
+                                          table.ctypes.data_as(P), table.size, ctypes.byref(used))
+        L.check(rc)
+        a = Args()
+        name, M, threads = kernels[fused]
+        a.member_lo, a.nmem, a.nbits, a.lg_tiles = 0, B, nbits, nbits - M
+        for e in range(nreals):
+            a.mat[e] = mats[e]
+        grid = min(B << (nbits - M), 3)
+        rows = table[:B * used.value].reshape(B, used.value)
+        # a pass without member-dependent gates has equal rows (members here differ in
+        # every such gate's matrix); the count of per-member kernels is checked below
+        if np.all(rows == rows[0]):
+            assert lib.run_pass(fused, state.ctypes.data_as(P), ctypes.byref(a), grid, threads) == 0
+        else:
+            tab = np.ascontiguousarray(rows.astype(np.float32 if c64 else np.float64))
+            assert lpm.run_pass(pm, state.ctypes.data_as(P), ctypes.byref(a), tab.ctypes.data_as(P), used.value,
+                                grid, threads) == 0
+            pm += 1
+        fused += 1
+    assert pm == len(kpm), (pm, len(kpm))
+    return state.astype(np.complex128).reshape(B, -1)
 
 
 def run(plan, psi, dump_src, workdir, members=1):

@@ -151,3 +151,81 @@ def test_generated_kernels_on_host(prec, env, tmp_path):
     e.pop("BTGPU_NO_JIT", None)
     r = subprocess.run([sys.executable, "-c", _CHILD, root, prec], env=e, capture_output=True, text=True, timeout=900)
     assert r.returncode == 0 and r.stdout.rstrip().endswith("OK"), r.stdout[-2000:] + r.stderr[-4000:]
+
+
+_MEMBERS = r"""
+import os, sys, tempfile, shutil
+import numpy as np
+root = sys.argv[1]
+sys.path[:0] = [os.path.join(root, "tests"), os.path.join(root, "bluetangle.jl_gb300"), os.path.join(root, "oracle")]
+import oracle as O
+import plan_emulator as E
+import kernel_emulator as K
+from bluetangle_gpu import _lib as L
+prec = sys.argv[2]
+tol = 2e-5 if prec == "c64" else 1e-12
+rng = np.random.default_rng(9)
+n, B = 14, 3
+
+def ry(t):
+    c, s = np.cos(t / 2), np.sin(t / 2)
+    return np.array([[c, -s], [s, c]], dtype=complex)
+
+def rz(t):
+    return np.diag([np.exp(-0.5j * t), np.exp(0.5j * t)])
+
+# an ansatz: RY RZ on every qubit, a CNOT ladder, three layers; RY/RZ vary per member
+seq, var = [], []
+for layer in range(3):
+    for q in range(1, n + 1):
+        var.append(len(seq)); seq.append(["ry", [q]])
+        var.append(len(seq)); seq.append(["rz", [q]])
+    for q in range(1, n):
+        seq.append(["cx", [q, q + 1]])
+thetas = rng.uniform(0, 2 * np.pi, (B, len(var)))
+cx = np.eye(4, dtype=complex)[[0, 1, 3, 2]]
+
+def mat(kind, t):
+    return ry(t) if kind == "ry" else rz(t)
+
+plan = E.host_plan(n, prec=prec)
+for i, (kind, qs) in enumerate(seq):
+    plan.add_matrix(cx if kind == "cx" else mat(kind, 0.1), qs)
+plan.set_variable(var).compile()
+src = open(os.environ["BTGPU_JIT_DUMP"]).read()
+idx = np.ascontiguousarray(var, dtype=np.int64)
+P = __import__("ctypes").c_void_p
+L.check(L.lib().bt_plan_prepare_members(plan.h, len(idx), idx.ctypes.data_as(P)))
+src_pm = open(os.environ["BTGPU_JIT_DUMP"]).read()
+member_mats = [[mat(seq[j][0], thetas[m, k]) for k, j in enumerate(var)] for m in range(B)]
+psis = np.stack([np.eye(1, 2 ** n, 0).ravel() + 0j for _ in range(B)])
+d = tempfile.mkdtemp()
+out = K.run_members(plan, psis, src, src_pm, d, var, member_mats)
+shutil.rmtree(d)
+for m in range(B):
+    ref = psis[m].copy()
+    k = 0
+    for kind, qs in seq:
+        if kind == "cx":
+            ref = O.apply_k(ref, cx, qs, [])
+        else:
+            ref = O.apply_k(ref, member_mats[m][k], qs, [])
+            k += 1
+    err = np.abs(out[m] - ref).max()
+    assert err < tol, (m, err)
+print("OK")
+"""
+
+
+@pytest.mark.parametrize("prec", ["c64", "c128"])
+def test_per_member_matrices_on_host(prec, tmp_path):
+    """bt_plan_run_members' host side: per-member kernels (entries from a member
+    table) and the tables, run on the host for three members of one ansatz with
+    different angles, each equal to the oracle with its own matrices."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    e = dict(os.environ, BTGPU_JIT_DUMP=str(tmp_path / "kernels.cu"), BTGPU_JIT_L2PF="0", BTGPU_JIT_PREFETCH="0",
+             BTGPU_JIT_DUMP_ONLY="1")
+    e.pop("BTGPU_NO_JIT", None)
+    r = subprocess.run([sys.executable, "-c", _MEMBERS, root, prec], env=e, capture_output=True, text=True,
+                       timeout=900)
+    assert r.returncode == 0 and r.stdout.rstrip().endswith("OK"), r.stdout[-2000:] + r.stderr[-4000:]

@@ -5,7 +5,10 @@
 // then compile-time constants and no register is shuffled between ops (in the
 // generic k_fused the runtime op switch costs several register moves per
 // amplitude per gate).  Matrix entries stay in the kernel parameters at fixed
-// offsets, so passes that differ only in angles share one kernel.
+// offsets (or, for a batch whose members carry their own matrices, in one table
+// row per member), so passes that differ only in angles share one kernel.  The
+// first and last register phases move amplitudes straight between HBM and
+// registers where coalesced, and each CTA asks L2 for its next tile ahead.
 //
 // The generator emits already-expanded code (no templates or loops for the
 // compiler to unroll), kernels are compiled in parallel batches, and cubins are

@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--cpu-n", type=int, default=24, help="qubits of the CPU baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--fidelity", action="store_true",
+                    help="plan mode, complex64: also run the circuit in complex128 and report the infidelity")
     ap.add_argument("--autotune", action="store_true",
                     help="plan mode: time the fusion configurations on the state and keep the fastest")
     ap.add_argument("--workload", default="brickwork", choices=["brickwork", "serve", "c1", "c2", "c3", "vqa"],
@@ -377,6 +379,29 @@ def run_ours(args):
            "d2h_bytes_per_step": zout.nbytes, "readout": "<Z_i> for all qubits each step"}
     assert np.all(np.isfinite(zout))
 
+    precision = None
+    if args.fidelity and plan is not None and args.prec == "c64":
+        # the same circuit in complex128 from |0...0>: infidelity of the complex64
+        # state (renormalised in FP64) and the largest <Z_i> deviation
+        ref = bt.Plan(args.n, "sv", "c128", ctx)
+        for prog, _ in [layer_program(l, "unfused") for l in layers]:
+            for m, qs in prog:
+                ref.add_matrix(m, qs)
+        ref.compile(True)
+        s128 = bt.zero_state(args.n, "c128", 1, ctx)
+        ref.run(s128)
+        st.set_zero()
+        plan.run(st)
+        nrm = np.empty(1)
+        ctx.check(lib.bt_norm2(st.h, 0, nrm.ctypes.data_as(P)))
+        z64, z128 = np.empty(args.n), np.empty(args.n)
+        ctx.check(lib.bt_expect_z_all(st.h, 0, z64.ctypes.data_as(P)))
+        ctx.check(lib.bt_expect_z_all(s128.h, 0, z128.ctypes.data_as(P)))
+        precision = {"infidelity_vs_c128": 1 - bt.fidelity(st, s128) / nrm[0],
+                     "max_abs_z_dev_vs_c128": float(np.abs(z64 / nrm[0] - z128).max())}
+        s128.free()
+        del ref
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_baseline(args, args.cpu_seconds)
@@ -407,6 +432,8 @@ def run_ours(args):
                              "launches": launches, "compute": compute},
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
                 "host_s": host_dt}
+        if precision is not None:
+            line["precision"] = precision
         print(json.dumps(line), flush=True)
     st.free()
     ctx.close()

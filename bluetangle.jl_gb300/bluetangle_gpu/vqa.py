@@ -16,6 +16,7 @@ reference's loss(state) = real(expect(state, H)) for a Hamiltonian matrix H).
 """
 import ctypes
 import inspect
+import os
 
 import numpy as np
 
@@ -152,6 +153,24 @@ def loss(pars, ops, n, terms, prec="c128", ctx=None):
     return float(losses(ops, n, [pars], terms, prec, ctx)[0])
 
 
+# HBM for the members of one batched plan run of parameter-shift evaluations
+_MEMBER_BUDGET = 16 << 30
+
+
+def paramshift_member_mats(base, var, shifted, owner, evals):
+    """The matrices of the variable ops `var` (indices into base) for each
+    evaluation in evals: evaluation 0 is the unshifted circuit, 2i + 1 and 2i + 2
+    shift parameter i (of op owner[i]) by +/- the shift."""
+    out = []
+    for e in evals:
+        mats = {j: base[j][1] for j in var}
+        if e > 0:
+            i = (e - 1) // 2
+            mats[owner[i]] = shifted[i][(e - 1) % 2]
+        out.append([mats[j] for j in var])
+    return out
+
+
 def loss_and_grad_paramshift(p, ops, n, terms, prec="c128", ctx=None, executor="auto"):
     """(l, g) of loss_and_grad_paramshift (src/vqa.jl:590-611): the loss at p and,
     for every parameter i, (l(p + pi/2 e_i) - l(p - pi/2 e_i)) / 2; all 2P + 1
@@ -216,22 +235,34 @@ def loss_and_grad_paramshift(p, ops, n, terms, prec="c128", ctx=None, executor="
                 plan.add_matrix(mat, qs, cs)
                 var.append(i)
         plan.set_variable(var).compile(True)  # shifted angles are rewritten in place: no recompiles
-        st = GPUState(n, prec, 1, ctx)
-        vals = np.empty(B)
+        if os.environ.get("BTGPU_VQA_PLAN_MEMBERS") == "1":
+            # the evaluations as members of batched runs, each with its own matrices
+            vals = np.empty(B)
+            es = 8 if prec in ("c64", "complex64") else 16
+            chunk = max(1, min(B, _MEMBER_BUDGET // ((2 ** n) * es)))
+            for e0 in range(0, B, chunk):
+                evals = list(range(e0, min(B, e0 + chunk)))
+                st = GPUState(n, prec, len(evals), ctx)
+                plan.run_members(st, var, paramshift_member_mats(base, var, shifted, owner, evals))
+                vals[e0:e0 + len(evals)] = _expect_members(st, terms)
+                st.free()
+        else:
+            st = GPUState(n, prec, 1, ctx)
+            vals = np.empty(B)
 
-        def run(m):
-            st.set_zero()
-            plan.run(st)
-            vals[m] = _expect_members(st, terms)[0]
+            def run(m):
+                st.set_zero()
+                plan.run(st)
+                vals[m] = _expect_members(st, terms)[0]
 
-        run(0)
-        for i in range(P):
-            j = owner[i]
-            plan.set_matrices([(j, shifted[i][0])])
-            run(2 * i + 1)
-            plan.set_matrices([(j, shifted[i][1])])
-            run(2 * i + 2)
-            plan.set_matrices([(j, base[j][1])])
-        st.free()
+            run(0)
+            for i in range(P):
+                j = owner[i]
+                plan.set_matrices([(j, shifted[i][0])])
+                run(2 * i + 1)
+                plan.set_matrices([(j, shifted[i][1])])
+                run(2 * i + 2)
+                plan.set_matrices([(j, base[j][1])])
+            st.free()
     g = 0.5 * (vals[1::2] - vals[2::2])
     return float(vals[0]), g

@@ -239,3 +239,18 @@ def test_plan_angle_updates_never_recompile(monkeypatch):
             assert _compiled(lib, p), th
     finally:
         lib.bt_plan_free(p)
+
+
+def test_paramshift_member_matrices():
+    """Per-member matrices of the batched parameter-shift evaluations: member 0
+    is the unshifted circuit, members 2i + 1 / 2i + 2 shift parameter i's op by
+    +/- (its other variable ops keep their base matrices)."""
+    from bluetangle_gpu.vqa import paramshift_member_mats
+    base = [(None, None), ("a", np.full((2, 2), 1.0)), (None, None), ("b", np.full((2, 2), 2.0))]
+    var = [1, 3]
+    shifted = [(np.full((2, 2), 10.0), np.full((2, 2), 11.0)), (np.full((2, 2), 20.0), np.full((2, 2), 21.0)),
+               (np.full((2, 2), 30.0), np.full((2, 2), 31.0))]
+    owner = [1, 3, 3]  # op 3 holds two parameters
+    mm = paramshift_member_mats(base, var, shifted, owner, range(7))
+    firsts = [[float(m[0, 0]) for m in member] for member in mm]
+    assert firsts == [[1, 2], [10, 2], [11, 2], [1, 20], [1, 21], [1, 30], [1, 31]]

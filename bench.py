@@ -34,9 +34,9 @@ import numpy as np  # noqa: E402
 METRIC = "gate-apps/s"
 # ncu-measured DRAM bytes per amplitude of one pass (read + write) of the dominant
 # kernel, from single-launch captures at 28 qubits (traffic grows in proportion to
-# the state, so it is scaled to the workload's 2^n amplitudes):
-# profiles/btk_fused_pass_windows_c64_brickwork28.md (specialised fused pass, plan
-# mode) and profiles/k_gate_sweep_c64_brickwork28.md (dense sweep, layer modes).
+# the state, so it is scaled to the workload's 2^n amplitudes): the specialised
+# fused tile pass (plan mode) moved 2.15 GB read + 2.09 GB written per 2^28
+# amplitudes, the dense k_gate sweep (layer modes) 2.148 + 2.087 GB.
 TRAFFIC_BYTES_PER_AMP = {"plan": (2.15e9 + 2.09e9) / 2 ** 28,
                          "sweep": (2.147591e9 + 2.087163e9) / 2 ** 28}
 
@@ -55,8 +55,9 @@ def parse():
     ap.add_argument("--cpu-n", type=int, default=24, help="qubits of the CPU baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--fidelity", action="store_true",
-                    help="plan mode, complex64: also run the circuit in complex128 and report the infidelity")
+    ap.add_argument("--no-fidelity", dest="fidelity", action="store_false",
+                    help="plan mode, complex64: skip the precision statement (by default the circuit also runs "
+                         "in complex128 and the line reports the infidelity and the <Z_i> deviation)")
     ap.add_argument("--autotune", action="store_true",
                     help="plan mode: time the fusion configurations on the state and keep the fastest")
     ap.add_argument("--workload", default="brickwork", choices=["brickwork", "serve", "c1", "c2", "c3", "vqa"],
@@ -75,7 +76,9 @@ def parse():
 
 # ------------------------------------------------------------------ workload
 def layers_of(n, depth, seed):
-    """Brickwork layers: list of (ones, cnots) with ones[q] = 2x2 matrix, cnots = [(q, q+1)]."""
+    """Brickwork layers: list of (ones, cnots) with ones[q] = 2x2 matrix, cnots = [(q, q+1)].
+    The generator is host-only Python: importing it maps no native library, so the
+    reference arm loads nothing of the engine."""
     import bluetangle_gpu.circuits as C
     ops = C.brickwork(n, depth, np.random.default_rng(seed))
     out, i = [], 0
@@ -218,8 +221,11 @@ def cpu_baseline(args, seconds):
     dt = time.perf_counter() - t0
     rate = gates / dt / 2 ** (args.n - n)
     return {"value": rate, "unit": METRIC, "cores": O.num_threads(), "kind": "port",
-            "sample": f"{li} brickwork layers ({gates} gates) on a {n}-qubit complex128 state in {dt:.1f} s, "
-                      f"OpenMP {O.num_threads()} threads; rate scaled by 2^-{args.n - n} to {args.n} qubits"}
+            "sample": f"{li} brickwork layers ({gates} gates) on a {n}-qubit complex128 state in {dt:.1f} s "
+                      f"through the oracle (the dense C restatement of the reference's gate semantics, not the "
+                      f"reference's own sparse-kron path, which cannot run here), OpenMP {O.num_threads()} "
+                      f"threads; the {args.n}-qubit rate is EXTRAPOLATED from it by 2^-{args.n - n} (work per "
+                      f"gate is proportional to 2^n; a {args.n}-qubit complex128 state does not fit host RAM)"}
 
 
 def run_reference(args):
@@ -237,7 +243,7 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c128", "data": "synthetic",
             "config": {"workload": f"brickwork-{args.n}q-depth{args.depth}", "global_batch": 1, "seq_len": None,
-                       "parallelism": "replicas", "l2": "state larger than L2"},
+                       "parallelism": "replicas", "l2": "state larger than L2", "precision": "complex128"},
             "cpu_baseline": {"value": value, "unit": METRIC, "cores": r["cores"], "kind": "port",
                              "sample": r["sample"]},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -356,11 +362,14 @@ def run_ours(args):
     zout = np.empty(args.n, dtype=np.float64)
     e2e_steps = max(3, args.steps // 2) if plan is None else max(2, args.steps // 3)
     h2d = 0
+    # a plan holds its matrix entries on the host and passes each pass's entries as
+    # kernel parameters: those are the bytes that go host -> device per run
+    param_bytes = 24 + (4 if args.prec == "c64" else 8) * (4096 if args.prec == "c64" else 2048) + 8
     t0 = time.perf_counter()
     for i in range(e2e_steps):
         if plan is not None:
             ctx.check(lib.bt_plan_run(plan.h, st.h, -1))
-            h2d += sum(M.nbytes + Q.nbytes for pk, _ in packed for M, Q in pk)
+            h2d += pstats["passes"] * param_bytes
         else:
             pk, _ = packed[i % len(packed)]
             for M, Q in pk:
@@ -376,7 +385,10 @@ def run_ours(args):
     else:
         e2e_logical = sum(packed[i % len(packed)][1] for i in range(e2e_steps))
     e2e = {"value": e2e_logical * ws / e2e_dt, "unit": METRIC, "h2d_bytes_per_step": h2d // e2e_steps,
-           "d2h_bytes_per_step": zout.nbytes, "readout": "<Z_i> for all qubits each step"}
+           "d2h_bytes_per_step": zout.nbytes, "readout": "<Z_i> for all qubits each step",
+           "inputs": ("compiled plan resident; per step each pass's matrix entries go to the device as kernel "
+                      "parameters (the h2d bytes)") if plan is not None else
+                     "each gate's matrix and qubits from host memory through bt_apply_matrix"}
     assert np.all(np.isfinite(zout))
 
     precision = None
@@ -409,7 +421,9 @@ def run_ours(args):
         line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": args.prec, "data": "synthetic",
-                "config": {"workload": f"brickwork-{args.n}q-{args.prec}-depth{args.depth}", "mode": args.mode,
+                "config": {"workload": f"brickwork-{args.n}q-depth{args.depth}", "mode": args.mode,
+                           "precision": {"c64": "complex64 (FP32 arithmetic; precision statement vs complex128 "
+                                                 "in 'precision')", "c128": "complex128"}[args.prec],
                            "step": ("the whole depth-%d circuit (%d logical gates) as fused tile passes"
                                     % (args.depth, sum(lg for _, lg in packed))) if plan is not None else
                                    "one brickwork layer (logical gates: n one-qubit + CNOTs)",

@@ -3,7 +3,10 @@
 The hot path (gates, channels, measurement, sampling, observables) runs in the
 sm_103a CUDA library libbtgpu.so through its C ABI (include/btgpu.h); this
 package only builds the reference's op descriptors and small host tables and
-calls the library.  Importing it loads the library and fails if it is absent.
+calls the library.  The first engine call (a Context, a state, a plan) loads the
+library and raises ImportError if it is absent: there is no CPU path.  Importing
+the package alone maps no native code, so the pure-host parts (gate tables, op
+descriptors, circuit generators) serve tools that must not load it.
 """
 from ._lib import BTError, lib
 from .engine import (Context, GPUDensity, GPUState, Measurement, Plan, plan_from_ops, apply, apply_channel, apply_matrix, apply_noise,
@@ -13,8 +16,6 @@ from .engine import (Context, GPUDensity, GPUState, Measurement, Plan, plan_from
 from .gates import gate, gates
 from .noise import NoiseModel, Noise1, Noise2, QuantumChannel, apply_twirl, noise_model
 from .ops import Op, OpQC, ifOp
-
-lib()  # load now: no silent fallback exists
 
 __all__ = ["BTError", "Context", "Plan", "plan_from_ops", "GPUState", "GPUDensity", "Measurement", "apply", "apply_channel", "apply_matrix",
            "apply_noise", "born_measure_Z", "channel_probs", "correlation", "expect", "fidelity", "measure",

@@ -1057,8 +1057,13 @@ static int prepare_members(bt_plan* p, int count, const int64_t* add_index, std:
       changed |= !g.var;
       g.var = true;
     }
+  // per-member entries live in fused passes: an unfused plan (mode 1) has none;
+  // a fused or tiered plan keeps its mode (the tiered kernels are joined below)
+  if (p->compile_mode == 1)
+    return bt_fail(p->ctx, BT_ERR_UNSUPPORTED,
+                   "per-member matrices need a fused plan (compile mode 0 or 2), not the unfused mode 1");
   if (changed || !p->compiled) {
-    rc = bt_plan_compile(p, 0);
+    rc = bt_plan_compile(p, p->compile_mode);
     if (rc) return rc;
   }
   join_jit(p);

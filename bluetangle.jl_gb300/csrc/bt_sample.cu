@@ -202,11 +202,16 @@ int bt_launch_convert_out(bt_state* s, int64_t mem, int64_t offset, int64_t len,
 //   size: BT_NOALLOC_CHUNKS doubles (512 KiB), i.e. states of at most
 //         2^(12 + 16) = 2^28 amplitudes (n <= 28); every GPU that loads the
 //         library holds the array until the process exits.
-//   sharing: all calls share the array and it keeps the last call's contents.
-//         Each call overwrites every entry it reads before reading it (chunk
-//         sums, then the in-place scan), so nothing needs clearing, but calls
-//         whose work overlaps on the GPU (different streams, or devices sharing
-//         nothing but the same call sequence) race on it.
+//   sharing: every device holds its own copy of the array; all calls on one
+//         device share that copy, and it keeps the last call's contents.  Each
+//         call overwrites every entry it reads before reading it (chunk sums,
+//         then the in-place scan), so nothing needs clearing, but calls on the
+//         same device whose work overlaps on the GPU (different streams, or
+//         host threads) race on it.  Calls on different devices never race.
+//   address: the array's device address is looked up once per device and kept
+//         for the life of the process; after cudaDeviceReset (or anything else
+//         that destroys the device's primary context) it is stale, so a process
+//         that resets a device must not call this entry point on it again.
 #define BT_NOALLOC_CHUNKS (1 << 16)
 #define BT_NOALLOC_MAX_QUBITS (CHUNK_LG + 16)
 static __device__ __align__(256) double g_noalloc_cum[BT_NOALLOC_CHUNKS];

@@ -341,8 +341,12 @@ int bt_probabilities(const bt_state* s, int64_t member, double* out);
  * memory) and the cudaStream_t `stream` (NULL = the legacy default stream).
  * The call only enqueues work and returns.  The first call on a device looks up
  * the array's device address (cudaGetSymbolAddress) with that device current;
- * make that first call before any stream capture.  All calls share the array:
- * calls that overlap on the GPU race on it. */
+ * make that first call before any stream capture.  The address is kept for the
+ * life of the process: after cudaDeviceReset of a device (or anything else that
+ * destroys its primary context) do not call this entry point on that device
+ * again.  Each device holds its own copy of the array; calls on one device share
+ * it, so calls that overlap on the same GPU race on it (calls on different
+ * devices do not). */
 int bt_sample_noalloc(const void* d_state, int n, int prec, int64_t shots, const double* d_uniforms, uint64_t key,
                       uint64_t seed, int64_t* d_out, void* stream);
 

@@ -13,6 +13,9 @@ from .engine import (Context, GPUDensity, GPUState, Measurement, Plan, plan_from
                      born_measure_Z, channel_probs, correlation, expect, fidelity, measure, partial_trace,
                      pauli_masks, rho_from, run, sample, sample_exact, state_from, to_rho, to_state, zero_rho,
                      zero_state)
+from .circuit import (Circuit, Options, Z3, Z3_s, compile, fidelity_dm, get_stats, measure, minus_state,
+                      neel_state01, neel_state10, neel_state_s, one_state, plus_state, product_state,
+                      random_product_state, random_state)
 from .gates import gate, gates
 from .noise import NoiseModel, Noise1, Noise2, QuantumChannel, apply_twirl, noise_model
 from .ops import Op, OpQC, ifOp
@@ -21,4 +24,6 @@ __all__ = ["BTError", "Context", "Plan", "plan_from_ops", "GPUState", "GPUDensit
            "apply_noise", "born_measure_Z", "channel_probs", "correlation", "expect", "fidelity", "measure",
            "partial_trace", "pauli_masks", "rho_from", "run", "sample", "sample_exact", "state_from", "to_rho",
            "to_state", "zero_rho", "zero_state", "gate", "gates", "NoiseModel", "Noise1", "Noise2",
-           "QuantumChannel", "apply_twirl", "noise_model", "Op", "OpQC", "ifOp"]
+           "QuantumChannel", "apply_twirl", "noise_model", "Op", "OpQC", "ifOp", "Circuit", "Options", "compile",
+           "get_stats", "product_state", "neel_state01", "neel_state10", "neel_state_s", "Z3", "Z3_s", "one_state",
+           "plus_state", "minus_state", "random_product_state", "random_state", "fidelity_dm"]

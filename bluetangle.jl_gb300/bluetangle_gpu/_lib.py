@@ -63,6 +63,7 @@ SIGNATURES = {
     "bt_apply_kraus": (i32, [P, i32, P, i32, P, i32, P, P, P, P]),
     "bt_apply_matrix_members": (i32, [P, i32, P, P, i32, P]),
     "bt_measure_z": (i32, [P, i32, P, P, P, P]),
+    "bt_measure_z2": (i32, [P, i32, i32, P, P, P, P]),
     "bt_reduced_dm": (i32, [P, i32, P, i64, P]),
     "bt_plan_create": (i32, [P, i32, i32, i32, ctypes.POINTER(P)]),
     "bt_plan_free": (i32, [P]),
@@ -98,6 +99,7 @@ SIGNATURES = {
     "bt_serve_poll": (i32, [P, i64, i64, P, P, P]),
     "bt_serve_stats": (i32, [P, P, P, P, P, P, P]),
     "bt_sample": (i32, [P, i64, i64, P, u64, P]),
+    "bt_sample_members": (i32, [P, P, u64, P]),
     "bt_probabilities": (i32, [P, i64, P]),
     "bt_sample_noalloc": (i32, [P, i32, i32, i64, P, u64, u64, P, P]),
     "bt_expect_pauli": (i32, [P, i32, P, P, P, i64, P]),
@@ -105,6 +107,10 @@ SIGNATURES = {
     "bt_expect_matrix": (i32, [P, i32, P, P, i32, P, i64, P]),
     "bt_norm2": (i32, [P, i64, P]),
     "bt_fidelity": (i32, [P, i64, P, i64, P]),
+    "bt_fidelity_dm": (i32, [P, i64, P, i64, P]),
+    "bt_rho_accumulate": (i32, [P, i64, P, dbl]),
+    "bt_state_random": (i32, [P, i64, u64]),
+    "bt_state_clear": (i32, [P, i64]),
 }
 
 _lib = None

@@ -275,10 +275,16 @@ def channel_probs(state, kraus, qubit, target=None, member=0):
     return np.array([np.real(np.trace(K @ rho @ K.conj().T)) for K in kraus])
 
 
-def born_measure_Z(state, qubit, rng=None, forced=None):
+def born_measure_Z(state, qubit, qubit2=None, rng=None, forced=None):
     """born_measure_Z(N, psi, q) (src/hilbert.jl:682-696): returns (state, outcome, p0);
     outcome and p0 are arrays of length batch for a batched state, scalars otherwise.
-    On a density matrix: sum_b P_b rho P_b (src/hilbert.jl:784-796)."""
+    On a density matrix: sum_b P_b rho P_b (src/hilbert.jl:784-796).
+
+    born_measure_Z(N, psi, q1, q2) (src/hilbert.jl:705-721) with qubit2 given:
+    returns (state, outcome, probs) with outcome in 1..4 (the reference's index
+    into [P0 P0, P1 P0, P0 P1, P1 P1] on (q1, q2)) and probs the four weights."""
+    if qubit2 is not None:
+        return _born_measure_Z2(state, qubit, qubit2, rng, forced)
     B = state.batch
     u = _draws(rng, B)
     f = _i32(np.broadcast_to(np.asarray(forced), (B,))) if forced is not None else None
@@ -288,6 +294,20 @@ def born_measure_Z(state, qubit, rng=None, forced=None):
     if B == 1:
         return state, int(out[0]), float(p0[0])
     return state, out, p0
+
+
+def _born_measure_Z2(state, q1, q2, rng, forced):
+    if not isinstance(state, GPUState):
+        raise ValueError("the two-qubit Born measurement acts on state vectors")
+    B = state.batch
+    u = _draws(rng, B)
+    f = _i32(np.broadcast_to(np.asarray(forced), (B,))) if forced is not None else None
+    out = np.empty(B, dtype=np.int32)
+    probs = np.empty((B, 4), dtype=np.float64)
+    state.ctx.check(L.lib().bt_measure_z2(state.h, int(q1), int(q2), _ptr(u), _ptr(f), _ptr(out), _ptr(probs)))
+    if B == 1:
+        return state, int(out[0]), probs[0]
+    return state, out, probs
 
 
 # ------------------------------------------------------------------ apply
@@ -666,9 +686,14 @@ def correlation(state, list_of_operators, qubits_applied, member=0):
 
 
 def fidelity(a, b, amember=0, bmember=0):
-    """fidelity(psi, phi) = |<psi|phi>|^2 (src/tensor.jl:219)."""
+    """fidelity(psi, phi) = |<psi|phi>|^2 (src/tensor.jl:219); for two density
+    matrices fidelity(rho, sigma) = tr(sqrt(sqrt(rho) sigma sqrt(rho)))^2
+    (src/tensor.jl:222-229, bt_fidelity_dm)."""
     out = ctypes.c_double(0)
-    a.ctx.check(L.lib().bt_fidelity(a.h, amember, b.h, bmember, ctypes.byref(out)))
+    if isinstance(a, GPUDensity) or isinstance(b, GPUDensity):
+        a.ctx.check(L.lib().bt_fidelity_dm(a.h, amember, b.h, bmember, ctypes.byref(out)))
+    else:
+        a.ctx.check(L.lib().bt_fidelity(a.h, amember, b.h, bmember, ctypes.byref(out)))
     return out.value
 
 
@@ -734,9 +759,16 @@ def run(ops, shots=1, noise=False, id=0, twirl=False, rng=None, prec="c128", ctx
 
 
 class Measurement:
-    """Measurement record (src/struct.jl:770-815): bitstr, probabilities, <Z_i>, moments."""
+    """Measurement record (src/struct.jl:907-917): bitstr, probabilities (sample),
+    <Z_i> (expect), 12 magnetisation moments, basis, shots, circuit name, qubits
+    and the accumulated density matrix (a GPUDensity when the circuit asked for
+    one, else None: the reference's empty placeholder)."""
 
-    def __init__(self, bitstr, probs, n, shots):
+    def __init__(self, bitstr, probs, n, shots, measurement_basis="0", circuit_name="state to measurement",
+                 density_matrix=None):
+        self.measurement_basis = measurement_basis
+        self.circuit_name = circuit_name
+        self.density_matrix = density_matrix
         self.bitstr = np.asarray(bitstr)
         self.sample = np.asarray(probs)
         self.number_of_qubits = n

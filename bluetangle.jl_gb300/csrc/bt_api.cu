@@ -626,6 +626,44 @@ int bt_measure_z(bt_state* s, int qubit, const double* uniforms, const int32_t* 
   return sync_and_status(ctx, "measure");
 }
 
+int bt_measure_z2(bt_state* s, int q1, int q2, const double* uniforms, const int32_t* forced, int32_t* outcome,
+                  double* probs) {
+  if (!s) return bt_fail(nullptr, BT_ERR_BAD_ARG, "state is NULL");
+  bt_ctx* ctx = s->ctx;
+  const int32_t qs[2] = {q1, q2};
+  int rc = check_qubits(ctx, s->n, 2, qs, 0, nullptr);
+  if (rc) return rc;
+  if (s->repr != BT_REPR_SV)
+    return bt_fail(ctx, BT_ERR_UNSUPPORTED, "the two-qubit Born measurement acts on state vectors");
+  if ((rc = set_dev(ctx))) return rc;
+  const int64_t B = s->batch;
+  const int bits[2] = {s->n - q1, s->n - q2};
+  Carve cv;
+  int iU = uniforms ? cv.add(B * sizeof(double)) : -1;
+  int iF = forced ? cv.add(B * sizeof(int)) : -1;
+  int iR = cv.add(B * 32 * sizeof(double));
+  int iO = cv.add(B * sizeof(int));
+  int iS = cv.add(B * sizeof(double));
+  int iP = cv.add(B * 4 * sizeof(double));
+  if ((rc = cv.commit(ctx))) return rc;
+  if (uniforms) rc = bt_cuda_check(ctx, cudaMemcpyAsync(cv.at<double>(iU), uniforms, B * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "uniform upload");
+  if (!rc && forced) rc = bt_cuda_check(ctx, cudaMemcpyAsync(cv.at<int>(iF), forced, B * sizeof(int), cudaMemcpyHostToDevice, ctx->stream), "forced upload");
+  if (rc) return rc;
+  if ((rc = bt_launch_rdm(s, 2, bits, 0, B, cv.at<double>(iR)))) return rc;
+  uint64_t stream = 0x4d5a320000000000ULL ^ ctx->rng_calls++;
+  rc = bt_launch_decide_measure2(ctx, B, cv.at<double>(iR), uniforms ? cv.at<double>(iU) : nullptr,
+                                 forced ? cv.at<int>(iF) : nullptr, stream, cv.at<int>(iO), cv.at<double>(iS),
+                                 cv.at<double>(iP));
+  if (rc) return rc;
+  if ((rc = bt_launch_collapse2(s, bits[0], bits[1], cv.at<int>(iO), cv.at<double>(iS), 0, B))) return rc;
+  if (outcome)
+    rc = bt_cuda_check(ctx, cudaMemcpyAsync(outcome, cv.at<int>(iO), B * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "outcome download");
+  if (!rc && probs)
+    rc = bt_cuda_check(ctx, cudaMemcpyAsync(probs, cv.at<double>(iP), B * 4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "probs download");
+  if (rc) return rc;
+  return sync_and_status(ctx, "measure2");
+}
+
 int bt_reduced_dm(const bt_state* s_, int k, const int32_t* qubits, int64_t member, double* out) {
   if (!s_) return bt_fail(nullptr, BT_ERR_BAD_ARG, "state is NULL");
   bt_state* s = const_cast<bt_state*>(s_);
@@ -676,6 +714,28 @@ int bt_sample(const bt_state* s_, int64_t member, int64_t shots, const double* u
   uint64_t stream = seed ^ 0x53414d5000000000ULL;
   if ((rc = bt_launch_sample(s, member, shots, uniforms ? cv.at<double>(iU) : nullptr, stream, cv.at<int64_t>(iO)))) return rc;
   rc = bt_cuda_check(ctx, cudaMemcpyAsync(out, cv.at<int64_t>(iO), shots * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream), "shots download");
+  if (rc) return rc;
+  return bt_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "sample sync");
+}
+
+int bt_sample_members(const bt_state* s_, const double* uniforms, uint64_t seed, int64_t* out) {
+  if (!s_) return bt_fail(nullptr, BT_ERR_BAD_ARG, "state is NULL");
+  bt_state* s = const_cast<bt_state*>(s_);
+  bt_ctx* ctx = s->ctx;
+  if (!out) return bt_fail(ctx, BT_ERR_BAD_ARG, "out is NULL");
+  int rc = set_dev(ctx);
+  if (rc) return rc;
+  const int64_t B = s->batch;
+  Carve cv;
+  int iU = uniforms ? cv.add(B * sizeof(double)) : -1;
+  int iO = cv.add(B * sizeof(int64_t));
+  if ((rc = cv.commit(ctx))) return rc;
+  if (uniforms)
+    rc = bt_cuda_check(ctx, cudaMemcpyAsync(cv.at<double>(iU), uniforms, B * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "uniform upload");
+  if (rc) return rc;
+  uint64_t stream = seed ^ 0x53414d4500000000ULL;
+  if ((rc = bt_launch_sample_each(s, uniforms ? cv.at<double>(iU) : nullptr, stream, cv.at<int64_t>(iO)))) return rc;
+  rc = bt_cuda_check(ctx, cudaMemcpyAsync(out, cv.at<int64_t>(iO), B * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream), "shots download");
   if (rc) return rc;
   return bt_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "sample sync");
 }

@@ -133,6 +133,10 @@ int bt_launch_expect_matrix(bt_state* s, int k, const int* bits, const double* m
 // collapse: member m keeps amplitudes whose `bit` equals outcome[m] scaled by scale[m]
 int bt_launch_collapse(bt_state* s, int bit, const int* d_outcome, const double* d_scale, int64_t mem_lo,
                        int64_t nmem);
+// two-qubit collapse: member m keeps amplitudes whose bits (b1, b2) match outcome[m]
+// (1..4: q1 = (o-1)&1, q2 = (o-1)>>1, the reference's order), scaled by scale[m]
+int bt_launch_collapse2(bt_state* s, int b1, int b2, const int* d_outcome, const double* d_scale, int64_t mem_lo,
+                        int64_t nmem);
 // DM dephasing on one qubit: zero rho[i, j] where bit b of i differs from bit b of j
 int bt_launch_dephase(bt_state* s, int b, int64_t mem_lo, int64_t nmem);
 
@@ -140,6 +144,9 @@ int bt_launch_dephase(bt_state* s, int b, int64_t mem_lo, int64_t nmem);
 int bt_launch_decide_measure(bt_ctx* ctx, int64_t nmem, const double* rdm /*[mem][8]*/, const double* u,
                              const int* forced, uint64_t rng_stream, int* outcome, double* scale,
                              double* p0);
+// two-qubit measurement from the 4x4 reduced matrix [mem][32]: outcome 1..4, probs [mem][4]
+int bt_launch_decide_measure2(bt_ctx* ctx, int64_t nmem, const double* rdm, const double* u, const int* forced,
+                              uint64_t rng_stream, int* outcome, double* scale, double* probs);
 struct bt_kraus_desc {
   int k, nk, ref_perm;  // ref_perm: probabilities from the pair permuted to ascending order
 };
@@ -151,6 +158,8 @@ int bt_launch_decide_kraus(bt_state* s, bt_kraus_desc kd, int64_t nmem, const do
 int bt_launch_sample(bt_state* s, int64_t mem, int64_t shots, const double* d_u, uint64_t seed_stream,
                      int64_t* d_out);
 int bt_launch_probs(bt_state* s, int64_t mem, int64_t offset, int64_t len, double* d_out);
+// one shot per member: d_out[m] from member m's weights (d_u[m] or Philox draw m)
+int bt_launch_sample_each(bt_state* s, const double* d_u, uint64_t seed_stream, int64_t* d_out);
 
 // state maintenance
 int bt_launch_set_basis(bt_state* s, int64_t mem_lo, int64_t nmem, uint64_t index);

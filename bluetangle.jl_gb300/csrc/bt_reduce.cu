@@ -970,6 +970,116 @@ int bt_launch_decide_measure(bt_ctx* ctx, int64_t nmem, const double* rdm, const
   return bt_cuda_check(ctx, cudaGetLastError(), "decide_measure launch");
 }
 
+// two-qubit measurement (born_measure_Z(N, psi, q1, q2), src/hilbert.jl:705-721):
+// rdm[mem] is the 4x4 reduced matrix on (q1, q2), q1 the most significant bit
+// (32 doubles, row-major interleaved).  The reference lists the outcomes as
+// [P0 P0, P1 P0, P0 P1, P1 P1] on (q1, q2), i.e. outcome k (1-based) keeps
+// q1 = (k - 1) & 1 and q2 = (k - 1) >> 1, with weights |psi' P_k psi| drawn by
+// _weighted_sample (first k with u <= cumsum(p)[k], no renormalisation).
+__device__ __forceinline__ int meas2_index(int k) {  // reference outcome (0-based) -> reduced index
+  return ((k & 1) << 1) | (k >> 1);
+}
+
+__global__ void k_decide_measure2(int64_t nmem, const double* __restrict__ rdm, const double* __restrict__ u,
+                                  const int* __restrict__ forced, uint64_t key, uint64_t stream,
+                                  int* __restrict__ outcome, double* __restrict__ scale, double* __restrict__ probs,
+                                  int* __restrict__ status) {
+  int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nmem) return;
+  double p[4];
+  for (int k = 0; k < 4; ++k) {
+    const int a = meas2_index(k);
+    p[k] = fabs(rdm[m * 32 + 2 * (a * 4 + a)]);
+    probs[m * 4 + k] = p[k];
+  }
+  const int f = forced ? forced[m] : -1;
+  if (f == -2) {  // this member is not measured
+    outcome[m] = -1;
+    scale[m] = 1.0;
+    return;
+  }
+  int ind = -1;
+  if (f >= 1 && f <= 4) {
+    ind = f - 1;
+  } else {
+    const double uu = u ? u[m] : bt_uniform(key, stream, (uint64_t)m);
+    double cum = 0;
+    for (int k = 0; k < 4 && ind < 0; ++k) {
+      cum += p[k];
+      if (uu <= cum) ind = k;
+    }
+    if (ind < 0) {  // u beyond the cumulative weight: no outcome, as in the reference
+      atomicExch(status, 2);
+      outcome[m] = -1;
+      scale[m] = 1.0;
+      return;
+    }
+  }
+  if (!(p[ind] > 0)) {
+    atomicExch(status, 1);
+    outcome[m] = -1;
+    scale[m] = 1.0;
+    return;
+  }
+  outcome[m] = ind + 1;
+  scale[m] = 1.0 / sqrt(p[ind]);
+}
+
+int bt_launch_decide_measure2(bt_ctx* ctx, int64_t nmem, const double* rdm, const double* u, const int* forced,
+                              uint64_t rng_stream, int* outcome, double* scale, double* probs) {
+  unsigned grid = (unsigned)((nmem + 127) / 128);
+  k_decide_measure2<<<grid, 128, 0, ctx->stream>>>(nmem, rdm, u, forced, ctx->seed, rng_stream, outcome, scale, probs,
+                                                   ctx->d_status);
+  ctx->launches++;
+  return bt_cuda_check(ctx, cudaGetLastError(), "decide_measure2 launch");
+}
+
+// member m keeps the amplitudes whose bits (b1, b2) match its outcome (1..4 in the
+// reference's order) scaled by scale[m]; the rest become zero
+template <typename R>
+__global__ void __launch_bounds__(BT_THREADS) k_collapse2(typename CT<R>::T* __restrict__ psi, int nbits, int b1, int b2,
+                                                          const int* __restrict__ outcome,
+                                                          const double* __restrict__ scale, int64_t mem_lo,
+                                                          int64_t nmem) {
+  const int64_t per = 1LL << nbits;
+  const int64_t total = per * nmem;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t mi = t >> nbits;
+    const int oc = outcome[mi];
+    if (oc < 1) continue;  // member not measured, or whose decision failed: left untouched
+    const int64_t i = t & (per - 1);
+    typename CT<R>::T* p = psi + ((mem_lo + mi) << nbits) + i;
+    const int keep1 = (oc - 1) & 1, keep2 = (oc - 1) >> 1;
+    if ((int)((i >> b1) & 1) == keep1 && (int)((i >> b2) & 1) == keep2) {
+      const R sc = (R)scale[mi];
+      typename CT<R>::T v = *p;
+      v.x *= sc;
+      v.y *= sc;
+      *p = v;
+    } else {
+      typename CT<R>::T z;
+      z.x = 0;
+      z.y = 0;
+      *p = z;
+    }
+  }
+}
+
+int bt_launch_collapse2(bt_state* s, int b1, int b2, const int* d_outcome, const double* d_scale, int64_t mem_lo,
+                        int64_t nmem) {
+  bt_ctx* ctx = s->ctx;
+  int64_t work = (1LL << s->nbits) * nmem;
+  int grid = bt_grid(ctx, work, BT_THREADS, 32);
+  if (s->prec == BT_PREC_C64)
+    k_collapse2<float><<<grid, BT_THREADS, 0, ctx->stream>>>((float2*)s->d, s->nbits, b1, b2, d_outcome, d_scale,
+                                                             mem_lo, nmem);
+  else
+    k_collapse2<double><<<grid, BT_THREADS, 0, ctx->stream>>>((double2*)s->d, s->nbits, b1, b2, d_outcome, d_scale,
+                                                              mem_lo, nmem);
+  ctx->launches++;
+  return bt_cuda_check(ctx, cudaGetLastError(), "collapse2 launch");
+}
+
 // Kraus branch: rdm[mem] is the D x D reduced matrix in application order (q, t);
 // kraus holds nk row-major interleaved D x D matrices (FP64).
 template <typename R>

@@ -123,6 +123,117 @@ int bt_launch_sample(bt_state* s, int64_t mem, int64_t shots, const double* d_u,
   return bt_cuda_check(ctx, cudaGetLastError(), "sample launch");
 }
 
+// One shot from every member of a batch (measure(circuit, shots) draws a single
+// shot from each re-simulated state, src/ops.jl:619-630): the same two-level
+// prefix per member (chunk sums with blockIdx.y = member, one scan block per
+// member), then one warp per member searches its own prefix.
+template <typename R>
+__global__ void __launch_bounds__(BT_THREADS) k_chunk_sums_each(const typename CT<R>::T* __restrict__ s, int dm,
+                                                                int nsys, int nbits, int clg, int64_t nchunk,
+                                                                double* __restrict__ sums) {
+  __shared__ double sh[BT_THREADS / 32];
+  const typename CT<R>::T* sm = s + ((int64_t)blockIdx.y << nbits);
+  const uint64_t c0 = (uint64_t)blockIdx.x << clg;
+  double acc = 0;
+  for (uint64_t i = threadIdx.x; i < (1ULL << clg); i += blockDim.x) acc += weight<R>(sm, dm, nsys, c0 + i);
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(FULL, acc, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int w = 0; w < BT_THREADS / 32; ++w) t += sh[w];
+    sums[(int64_t)blockIdx.y * nchunk + blockIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_each(double* __restrict__ a, int64_t n) {
+  double* am = a + (int64_t)blockIdx.x * n;
+  __shared__ double sh[1024];
+  const int64_t per = (n + 1023) / 1024;
+  const int64_t lo = threadIdx.x * per, hi = lo + per < n ? lo + per : n;
+  double t = 0;
+  for (int64_t i = lo; i < hi; ++i) t += am[i];
+  sh[threadIdx.x] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double run = 0;
+    for (int i = 0; i < 1024; ++i) {
+      double v = sh[i];
+      sh[i] = run;
+      run += v;
+    }
+  }
+  __syncthreads();
+  double run = sh[threadIdx.x];
+  for (int64_t i = lo; i < hi; ++i) {
+    run += am[i];
+    am[i] = run;
+  }
+}
+
+template <typename R>
+__global__ void k_shot_each(const typename CT<R>::T* __restrict__ s, int dm, int nsys, int nbits, int clg,
+                            const double* __restrict__ cum_all, int64_t nchunk, int64_t nmem,
+                            const double* __restrict__ u, uint64_t key, uint64_t stream, int64_t* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t m = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (m >= nmem) return;
+  const typename CT<R>::T* sm = s + (m << nbits);
+  const double* cum = cum_all + m * nchunk;
+  const double total = cum[nchunk - 1];
+  const double uu = u ? u[m] : bt_uniform(key, stream, (uint64_t)m);
+  const double t = uu * total;
+  int64_t lo = 0, hi = nchunk - 1;
+  while (lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    if (cum[mid] < t) lo = mid + 1; else hi = mid;
+  }
+  const uint64_t c0 = (uint64_t)lo << clg;
+  double run = lo > 0 ? cum[lo - 1] : 0.0;
+  int64_t found = -1, lastnz = -1;
+  for (uint64_t b = 0; b < (1ULL << clg) && found < 0; b += 32) {
+    double w = (b + lane < (1ULL << clg)) ? weight<R>(sm, dm, nsys, c0 + b + lane) : 0.0;
+    double incl = w;
+    for (int o = 1; o < 32; o <<= 1) {
+      double v = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += v;
+    }
+    double cw = run + incl;
+    unsigned hit = __ballot_sync(FULL, cw >= t);
+    unsigned nz = __ballot_sync(FULL, w > 0);
+    if (nz) lastnz = (int64_t)(c0 + b + 31 - __clz(nz));
+    if (hit) found = (int64_t)(c0 + b + __ffs(hit) - 1);
+    run = __shfl_sync(FULL, cw, 31);
+  }
+  if (found < 0) found = lastnz >= 0 ? lastnz : (int64_t)c0;
+  if (lane == 0) out[m] = found;
+}
+
+int bt_launch_sample_each(bt_state* s, const double* d_u, uint64_t seed_stream, int64_t* d_out) {
+  bt_ctx* ctx = s->ctx;
+  const int nsys = s->n;
+  const int dm = s->repr == BT_REPR_DM;
+  const int clg = nsys < CHUNK_LG ? nsys : CHUNK_LG;
+  const int64_t nchunk = 1LL << (nsys - clg);
+  const int64_t B = s->batch;
+  if (B > 65535) return bt_fail(ctx, BT_ERR_UNSUPPORTED, "at most 65535 members per call");
+  double* cum = nullptr;
+  int rc = bt_work(ctx, sizeof(double) * nchunk * B, &cum);
+  if (rc) return rc;
+  const bool f = s->prec == BT_PREC_C64;
+  dim3 g1((unsigned)nchunk, (unsigned)B);
+  if (f) k_chunk_sums_each<float><<<g1, BT_THREADS, 0, ctx->stream>>>((const float2*)s->d, dm, nsys, s->nbits, clg, nchunk, cum);
+  else k_chunk_sums_each<double><<<g1, BT_THREADS, 0, ctx->stream>>>((const double2*)s->d, dm, nsys, s->nbits, clg, nchunk, cum);
+  ctx->launches++;
+  k_scan_each<<<(unsigned)B, 1024, 0, ctx->stream>>>(cum, nchunk);
+  ctx->launches++;
+  const unsigned grid = (unsigned)((B * 32 + 255) / 256);
+  if (f) k_shot_each<float><<<grid, 256, 0, ctx->stream>>>((const float2*)s->d, dm, nsys, s->nbits, clg, cum, nchunk, B, d_u, ctx->seed, seed_stream, d_out);
+  else k_shot_each<double><<<grid, 256, 0, ctx->stream>>>((const double2*)s->d, dm, nsys, s->nbits, clg, cum, nchunk, B, d_u, ctx->seed, seed_stream, d_out);
+  ctx->launches++;
+  return bt_cuda_check(ctx, cudaGetLastError(), "sample_each launch");
+}
+
 template <typename R>
 __global__ void k_probs(const typename CT<R>::T* __restrict__ s, int dm, int nsys, int64_t offset, int64_t len,
                         double* __restrict__ out) {

@@ -94,6 +94,13 @@ void* bt_state_device_ptr(bt_state* s);
 int bt_state_set_zero(bt_state* s, int64_t member);
 /* computational basis state |index> (product_state of bits, src/hilbert.jl:835) */
 int bt_state_set_basis(bt_state* s, int64_t member, uint64_t index);
+/* every entry of the member (-1: all members) set to 0: the empty accumulator of
+ * rho_construct (src/ops.jl:603) and the start of superpositions of basis states */
+int bt_state_clear(bt_state* s, int64_t member);
+/* random_state(N) (src/hilbert.jl:882): normalize(rand(ComplexF64, 2^N)), real
+ * and imaginary parts uniform in [0, 1) from on-device Philox keyed by (ctx seed,
+ * seed, member); member = -1 fills every member (each its own draws). */
+int bt_state_random(bt_state* s, int64_t member, uint64_t seed);
 /* copies member `src_member` of src into member `dst_member` of dst (same n/repr/prec);
  * dst_member = -1 broadcasts it to every member of dst */
 int bt_state_copy(bt_state* dst, int64_t dst_member, const bt_state* src, int64_t src_member);
@@ -143,6 +150,15 @@ int bt_apply_kraus(bt_state* s, int k, const int32_t* qubits, int nk, const doub
  * still reported.  forced[m] = -2: member m is not measured (outcome -1). */
 int bt_measure_z(bt_state* s, int qubit, const double* uniforms, const int32_t* forced,
                  int32_t* outcome, double* p0);
+/* born_measure_Z(N, psi, q1, q2) (src/hilbert.jl:705-721) for every member of a
+ * state vector: weights p = |psi' P psi| for P = [P0 P0, P1 P0, P0 P1, P1 P1] on
+ * (q1, q2) in that order, outcome = first k (1..4, the reference's 1-based index)
+ * with u <= cumsum(p)[k] (not renormalised, as _weighted_sample), or forced[m]
+ * (1..4; -2 skips member m, outcome -1); the state keeps the chosen projection,
+ * renormalised, and every other amplitude is set to exactly zero.  probs: 4 per
+ * member (may be NULL).  BT_ERR_NO_BRANCH when u exceeds the total weight. */
+int bt_measure_z2(bt_state* s, int q1, int q2, const double* uniforms, const int32_t* forced, int32_t* outcome,
+                  double* probs);
 /* partial_trace(psi, keep) for k <= 3 kept qubits, in the listed order
  * (src/linalg.jl:83-230); out is a column-major 2^k x 2^k complex matrix */
 int bt_reduced_dm(const bt_state* s, int k, const int32_t* qubits, int64_t member, double* out);
@@ -320,6 +336,11 @@ int bt_serve_stats(bt_server* s, int64_t* completed, double* p50_s, double* p99_
                    uint64_t* hbm_used, int64_t* runs);
 
 /* ---------------------------------------------------------------- sampling */
+/* one shot from every member: out[m] drawn from member m's |psi|^2 (or diag rho)
+ * as bt_sample draws, with uniforms[m] or on-device Philox keyed by (ctx seed,
+ * seed).  The noisy branch of measure(circuit, shots) (src/ops.jl:617-630)
+ * samples one shot from each re-simulated state: members are those states. */
+int bt_sample_members(const bt_state* s, const double* uniforms, uint64_t seed, int64_t* out);
 /* sample(psi, shots) (src/ops.jl:46-62): per shot t = u*sum|psi|^2, outcome =
  * first index with cumsum >= t.  uniforms (shots values) or NULL for on-device
  * Philox keyed by (ctx seed, seed).  On a density matrix samples diag(rho). */
@@ -365,6 +386,16 @@ int bt_expect_matrix(const bt_state* s, int k, const int32_t* qubits, const doub
                      const int32_t* ctrls, int64_t member, double* out);
 /* sum |psi|^2 (or tr rho) per member */
 int bt_norm2(const bt_state* s, int64_t member, double* out);
+/* fidelity(rho, sigma) = real(tr(sqrt(sqrt(rho) sigma sqrt(rho)))^2) for two
+ * density matrices (src/tensor.jl:222-229), n <= 14: on the device from Hermitian
+ * eigendecompositions (cuSOLVER zheevd and cuBLAS zgemm, loaded with dlopen on
+ * first use): (sum_i sqrt(max(mu_i, 0)))^2 over the eigenvalues of
+ * D V' sigma V D, rho = V diag(w) V', D = diag(sqrt(max(w, 0))). */
+int bt_fidelity_dm(const bt_state* rho, int64_t rmember, const bt_state* sigma, int64_t smember, double* out);
+/* rho[:, :] += weight * sum_m |psi_m><psi_m| over every member of the state vector
+ * psi (same n; n <= 14): measure's density_matrix accumulation
+ * (rho_construct += state*state'/shots, src/ops.jl:612, :626). */
+int bt_rho_accumulate(bt_state* rho, int64_t rmember, const bt_state* psi, double weight);
 /* fidelity(psi, phi) = |<psi|phi>|^2 (src/tensor.jl:219) */
 int bt_fidelity(const bt_state* a, int64_t amember, const bt_state* b, int64_t bmember, double* out);
 

@@ -284,6 +284,43 @@ int bto_born_measure_z(int n, double* psi, int q, double u, int forced, int* out
     return 0;
 }
 
+/* born_measure_Z(N, psi, q1, q2) (src/hilbert.jl:705-721): slist = the state
+ * projected by P0 P0, P1 P0, P0 P1, P1 P1 on (q1, q2), weights |psi' slist[k]|,
+ * k = _weighted_sample(weights) (src/hilbert.jl:810-819: first k with
+ * u <= cumsum, not renormalised), result normalize(slist[k]).  outcome is the
+ * reference's 1-based k; forced (1..4) replaces the draw; -1 and no change when
+ * u exceeds the total weight (the reference has no index there). */
+int bto_born_measure_z2(int n, double* psi, int q1, int q2, double u, int forced, int* outcome, double* probs) {
+    if (q1 < 1 || q1 > n || q2 < 1 || q2 > n || q1 == q2) return -1;
+    const int b1 = bitpos(n, q1), b2 = bitpos(n, q2);
+    const int64_t len = 1LL << n;
+    double p[4] = {0, 0, 0, 0};
+    for (int64_t i = 0; i < len; ++i) {
+        /* slot of [P0P0, P1P0, P0P1, P1P1]: q1's bit is the low digit */
+        const int k = (int)((i >> b1) & 1) + 2 * (int)((i >> b2) & 1);
+        p[k] += psi[2 * i] * psi[2 * i] + psi[2 * i + 1] * psi[2 * i + 1];
+    }
+    if (probs)
+        for (int k = 0; k < 4; ++k) probs[k] = p[k];
+    int ind = -1;
+    if (forced >= 1 && forced <= 4) ind = forced - 1;
+    else {
+        double cum = 0;
+        for (int k = 0; k < 4 && ind < 0; ++k) {
+            cum += p[k];
+            if (u <= cum) ind = k;
+        }
+    }
+    if (outcome) *outcome = ind < 0 ? -1 : ind + 1;
+    if (ind < 0) return 0;
+    for (int64_t i = 0; i < len; ++i) {
+        const int k = (int)((i >> b1) & 1) + 2 * (int)((i >> b2) & 1);
+        if (k != ind) { psi[2 * i] = 0.0; psi[2 * i + 1] = 0.0; }
+    }
+    normalize(len, psi);
+    return 0;
+}
+
 /* e_op * rho * e_op': apply E to every column, then conj(E) to every row */
 static int dm_apply_bits(int n, double* rho, int k, const int* bits, const double* m, int nc,
                          const int* cbits) {

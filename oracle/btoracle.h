@@ -36,6 +36,9 @@ int bto_hilbert3(int n, double* psi, const double* m, int first);
 int bto_apply_k(int n, double* psi, int k, const int* qubits, const double* m,
                 int nctrl, const int* ctrls);
 
+/* born_measure_Z(N, psi, q1, q2) (src/hilbert.jl:705-721): outcome 1..4 in the
+ * order [P0 P0, P1 P0, P0 P1, P1 P1] on (q1, q2); probs[4] the weights */
+int bto_born_measure_z2(int n, double* psi, int q1, int q2, double u, int forced, int* outcome, double* probs);
 /* partial_trace(psi, q)      -> 2x2   (src/linalg.jl:167-192) */
 int bto_partial_trace1(int n, const double* psi, int q, double* out);
 /* partial_trace(psi, q, t)   -> 4x4 in (min, max) order (src/linalg.jl:198-230,

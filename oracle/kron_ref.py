@@ -318,6 +318,19 @@ def born_measure_z(psi, qubit, u=None, forced=None):
     return out / np.linalg.norm(out), ind, p0
 
 
+def born_measure_z2(psi, q1, q2, u=None, forced=None):
+    """born_measure_Z(N, psi, q1, q2) (src/hilbert.jl:705-721), literally: the four
+    projections by expand_multi_op, weights |psi' slist[k]|, _weighted_sample,
+    normalize(slist[ind]); outcome 1-based as the reference returns it."""
+    N = int(round(math.log2(len(psi))))
+    slist = [expand_multi_op(names, [q1, q2], N) @ psi
+             for names in (["P0", "P0"], ["P1", "P0"], ["P0", "P1"], ["P1", "P1"])]
+    probs = np.array([abs(np.vdot(psi, s)) for s in slist])
+    ind = (forced - 1) if forced is not None else weighted_sample(probs, u)
+    out = slist[ind]
+    return out / np.linalg.norm(out), ind + 1, probs
+
+
 def dm_channel(rho, kraus, qubit, target=None):
     """__QuantumChannel_new_apply on rho (src/struct.jl:58-76)."""
     N = int(round(math.log2(rho.shape[0])))

@@ -53,6 +53,7 @@ def lib():
             "bto_weighted_sample": (i, [i, P, d]),
             "bto_channel_traj": (i, [i, P, i, i, i, i, P, d, i, P, P]),
             "bto_born_measure_z": (i, [i, P, i, d, i, P, P]),
+            "bto_born_measure_z2": (i, [i, P, i, i, d, i, P, P]),
             "bto_dm_gate": (i, [i, P, i, P, P, i, P]),
             "bto_dm_hilbert1": (i, [i, P, P, i, i]),
             "bto_dm_hilbert2": (i, [i, P, P, i, i, i]),
@@ -181,6 +182,16 @@ def born_measure_z(psi, q, u=0.5, forced=-1):
     _check(lib().bto_born_measure_z(_nq(psi), _ptr(psi), q, float(u), int(forced), ctypes.byref(out),
                                     ctypes.byref(p0)), "born_measure_z")
     return psi, out.value, p0.value
+
+
+def born_measure_z2(psi, q1, q2, u=0.5, forced=-1):
+    """born_measure_Z(N, psi, q1, q2): (state, outcome 1..4 or -1, weights[4])."""
+    psi = np.array(psi, dtype=np.complex128)
+    out = ctypes.c_int(-1)
+    probs = np.zeros(4)
+    _check(lib().bto_born_measure_z2(_nq(psi), _ptr(psi), int(q1), int(q2), float(u), int(forced),
+                                     ctypes.byref(out), _ptr(probs)), "born_measure_z2")
+    return psi, out.value, probs
 
 
 def _dm_buf(rho):

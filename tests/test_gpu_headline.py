@@ -104,15 +104,21 @@ def test_headline_plan_equals_gate_path(ctx, n, prec, amp_tol, rel_tol, z_tol):
     assert 0.5 < share < 2.0, share
     za, zb = _z_all(a), _z_all(b)
     assert float(np.abs(za - zb).max()) <= z_tol, np.abs(za - zb).max()
-    assert abs(_norm2(a) - 1) < (1e-4 if prec == "c64" else 1e-11)
+    # the reference's T (and T-dagger) entries are rounded to 10 significant
+    # digits (src/gates.jl:32-33), so T is not exactly unitary: the norm drifts by
+    # ~2e-11 per T gate (~140 in this circuit) on both paths alike
+    na, nb = _norm2(a), _norm2(b)
+    assert abs(na - nb) < (1e-5 if prec == "c64" else 1e-13), (na, nb)
+    assert abs(nb - 1) < 1e-7, nb
     b.free()
-    # the inverse circuit takes the plan's output back to |0...0>
+    # the inverse circuit (adjoints in reverse order) takes the plan's output back
+    # to |0...0>, up to the same T rounding
     inv = _plan(bt, ops, n, prec, inverse=True)
     inv.run(a)
     x0 = _blocks(a, [0], blk)[0]
     back = float(abs(x0[0]) ** 2)
-    assert back > (1 - 2e-4 if prec == "c64" else 1 - 1e-11), back
-    assert float(np.abs(x0[1:]).max()) < (1e-4 if prec == "c64" else 1e-12)
+    assert abs(back - 1) < (2e-4 if prec == "c64" else 1e-7), back
+    assert float(np.abs(x0[1:]).max()) < (1e-4 if prec == "c64" else 1e-9)
     a.free()
 
 

@@ -224,3 +224,28 @@ def test_ref_channel_cptp_and_sample_semantics(oracle):
     assert oracle.weighted_sample(np.array([0.2, 0.3]), 0.9) is None
     psi = np.sqrt(np.array([0.25, 0, 0.25, 0.5], complex))
     assert list(oracle.sample(psi, [0.0, 0.2, 0.25, 0.26, 0.5, 0.51, 0.999])) == [0, 0, 0, 2, 2, 3, 3]
+
+
+def test_ref_two_qubit_born_measurement(oracle, kref):
+    """born_measure_Z(N, psi, q1, q2) (src/hilbert.jl:705-721): the C restatement
+    equals the literal projection construction (expand_multi_op with P0/P1 on
+    (q1, q2), weights |psi' slist[k]|, _weighted_sample, normalize) for every
+    forced outcome and for drawn ones, with q1 < q2, q1 > q2 and non-adjacent
+    pairs; a Bell pair measured on both qubits gives only outcomes 1 and 4."""
+    rng = np.random.default_rng(44)
+    n = 5
+    for q1, q2 in ((1, 2), (4, 2), (1, 5), (3, 4)):
+        psi = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
+        psi /= np.linalg.norm(psi)
+        for f in (1, 2, 3, 4):
+            a, oa, pa = oracle.born_measure_z2(psi, q1, q2, forced=f)
+            b, ob, pb = kref.born_measure_z2(psi, q1, q2, forced=f)
+            assert oa == ob == f and np.abs(a - b).max() < 1e-13 and np.abs(pa - pb).max() < 1e-14
+        for u in rng.random(6):
+            a, oa, _ = oracle.born_measure_z2(psi, q1, q2, u=u)
+            b, ob, _ = kref.born_measure_z2(psi, q1, q2, u=u)
+            assert oa == ob and np.abs(a - b).max() < 1e-13
+    bell = np.zeros(4, complex)
+    bell[0] = bell[3] = 1 / np.sqrt(2)
+    outs = {oracle.born_measure_z2(bell, 1, 2, u=u)[1] for u in np.linspace(0.01, 0.99, 25)}
+    assert outs == {1, 4}

@@ -450,14 +450,14 @@ static bool encode_pass(bt_plan* p, const std::vector<int>& kept, const std::vec
   return true;
 }
 
-// register-phase windows (BTGPU_PLAN_PHASE_WINDOWS=1): each register phase of a
-// pass may also take NB consecutive tile bits where they hold more gates than the
-// set grown in gate order (33-qubit brickwork: 90 phases instead of 117; off by
-// default until timed on a GPU)
+// register-phase windows (on unless BTGPU_PLAN_PHASE_WINDOWS=0): each register
+// phase of a pass may also take NB consecutive tile bits where they hold more gates
+// than the set grown in gate order (33-qubit brickwork: 90 phases instead of 117,
+// 0.844 -> 0.786 s per circuit on a GB300)
 static bool phase_windows_on() {
   static const bool v = [] {
     const char* e = getenv("BTGPU_PLAN_PHASE_WINDOWS");
-    return e && *e == '1';
+    return !(e && *e == '0');
   }();
   return v;
 }

@@ -123,13 +123,16 @@ def test_fidelity_of_density_matrices(ctx, n):
 
     import bluetangle_gpu as bt
     rng = np.random.default_rng(n)
-    for prec, tol in (("c128", 1e-10), ("c64", 1e-5)):
-        R, S = rdensity(rng, n), rdensity(rng, n, rank=2)
+    # a rank-2 sigma leaves d - 2 eigenvalues of sqrt(rho) sigma sqrt(rho) at
+    # rounding level (~1e-17); every square-root formula, the reference's included,
+    # turns each into a ~3e-9 term of the trace, so that case is compared at 1e-8
+    for prec, rank, tol in (("c128", None, 1e-10), ("c128", 2, 1e-8), ("c64", None, 1e-5)):
+        R, S = rdensity(rng, n), rdensity(rng, n, rank=rank)
         a, b = bt.rho_from(R, prec), bt.rho_from(S, prec)
         sr = sl.sqrtm(R)
         ref = float(np.real(np.trace(sl.sqrtm(sr @ S @ sr)) ** 2))
-        assert abs(bt.fidelity(a, b) - ref) < tol, (prec, bt.fidelity(a, b), ref)
-        assert abs(bt.fidelity(a, a) - 1) < tol
+        assert abs(bt.fidelity(a, b) - ref) < tol, (prec, rank, bt.fidelity(a, b), ref)
+        assert abs(bt.fidelity(a, a) - 1) < max(tol, 1e-10)
     psi, phi = rstate(rng, n), rstate(rng, n)
     a, b = bt.rho_from(np.outer(psi, psi.conj())), bt.rho_from(np.outer(phi, phi.conj()))
     assert abs(bt.fidelity(a, b) - abs(np.vdot(psi, phi)) ** 2) < 1e-10

@@ -142,7 +142,7 @@ print("OK")
     ("c64", {"BTGPU_JIT_DIRECT": "0"}),
     ("c64", {"BTGPU_JIT_DIRECT": "2", "BTGPU_JIT_PACKED": "1"}),
     ("c128", {"BTGPU_JIT_DIRECT": "2"}),
-    ("c64", {"BTGPU_PLAN_PHASE_WINDOWS": "1"}),
+    ("c64", {"BTGPU_PLAN_PHASE_WINDOWS": "0"}),
 ])
 def test_generated_kernels_on_host(prec, env, tmp_path):
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))

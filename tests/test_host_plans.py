@@ -178,19 +178,19 @@ def test_host_plan_headline_pass_count():
     plan.compile()
     st = plan.stats()
     assert st["gates"] == 1470 and st["passes"] <= 26, st
-    if os.environ.get("BTGPU_PLAN_PHASE_WINDOWS") == "1":
+    if os.environ.get("BTGPU_PLAN_PHASE_WINDOWS") != "0":
         assert st["phases"] <= 100, st  # register-bit windows: 90 phases instead of 117
     f, b = ctypes.c_double(), ctypes.c_double()
     L.check(L.lib().bt_plan_cost(plan.h, ctypes.byref(f), ctypes.byref(b)))
     assert b.value == 16 * st["passes"] and f.value < 2600, (f.value, b.value)
 
 
-def test_host_plans_with_phase_windows():
-    """The same checks with register phases chosen among bit windows as well
-    (BTGPU_PLAN_PHASE_WINDOWS=1, read once per process: run in a child)."""
-    if os.environ.get("BTGPU_PLAN_PHASE_WINDOWS") == "1":
-        pytest.skip("already running with phase windows")
-    env = dict(os.environ, BTGPU_PLAN_PHASE_WINDOWS="1")
+def test_host_plans_without_phase_windows():
+    """The same checks with register phases grown in gate order only
+    (BTGPU_PLAN_PHASE_WINDOWS=0, read once per process: run in a child)."""
+    if os.environ.get("BTGPU_PLAN_PHASE_WINDOWS") == "0":
+        pytest.skip("already running without phase windows")
+    env = dict(os.environ, BTGPU_PLAN_PHASE_WINDOWS="0")
     r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-x", "-p", "no:cacheprovider", __file__],
                        env=env, cwd=os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
                        capture_output=True, text=True, timeout=600)

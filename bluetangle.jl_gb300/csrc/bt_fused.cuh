@@ -52,6 +52,8 @@ struct FusedArgs {
   int nbits, M, c, nphase;
   int packed;               // specialised complex64 code in two-lane arithmetic (bt_jit.cu)
   int permem;               // specialised code reading entries from a per-member table (bt_jit.cu)
+  int pbit;                 // lane bit (tile-local) of the pair-lane complex64 form, or -1: every
+                            // phase holds it as its last register bit (bt_plan.cu, bt_jit.cu)
   int tbits[16];            // tile-local bit -> global bit (ascending; tbits[i] = i for i < c)
   int64_t member_lo, nmem;  // members processed
   int lg_tiles;             // log2(tiles per member) = nbits - M

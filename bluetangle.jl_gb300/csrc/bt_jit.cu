@@ -912,13 +912,304 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
   o << "}\n";
 }
 
+// ------------------------------------------------------------------ pair-lane form (complex64)
+// A pass planned with a lane bit P (FusedArgs::pbit, chosen by the planner as the
+// tile bit the fewest non-diagonal gates touch) holds P as register bit 4 of
+// every phase.  A thread's 32 amplitudes are then 16 pairs that differ only in P:
+// X<j> = (x_j, x_{j|16}) and Y<j> = (y_j, y_{j|16}) in 64-bit registers, j < 16,
+// and every op that does not mix the two halves of a pair (all ops not on P, and
+// diagonal ops on P with per-lane coefficients) runs as two-lane FP32 code
+// (fma.rn.f32x2 / mul.rn.f32x2): one instruction for two amplitudes.  The pairs
+// never change between phases: the shared-memory tile holds one 16-byte unit per
+// pair, (re_a, re_b, im_a, im_b) for the amplitudes a (P = 0) and b (P = 1),
+// indexed by the tile index without P and swizzled u ^ ((u >> 3) & 7), so a phase
+// boundary is one 16-byte store and load per pair.  The remaining ops (non-diagonal
+// ops on P, dense two-qubit matrices) run as the scalar code on the unpacked
+// halves.  Global memory keeps its interleaved layout: the direct first/last phase
+// and the staged tile copies regroup the 16-byte accesses into pairs.
+static void gen_kernel_pl(std::ostringstream& o, const FusedArgs<float>& a, const std::string& name) {
+  const int M = a.M, c = a.c, NB = 5, P = a.pbit;
+  const int T = 1 << (M - NB);
+  const int NM = BT_FUSED_MAX_REALS_F;
+  const int NP = a.nphase;
+  const char* mref = a.permem ? "cm" : "a.mat";
+  o << "extern \"C\" __global__ void __launch_bounds__(" << T << ", " << bt_jit_min_blocks() << ") " << name
+    << "(cf* __restrict__ psi, const JitArgsF<" << NM << "> a";
+  if (a.permem) o << ", const float* __restrict__ mm, const i64 mstride";
+  o << ") {\n  typedef float R;\n";
+  if (NP == 0) {
+    o << "}\n";
+    return;
+  }
+  auto qpos = [&](int bit) { return bit < P ? bit : bit - 1; };
+  auto swz16 = [](int u) { return u ^ ((u >> 3) & 7); };
+  const int cmask = (1 << c) - 1;
+  const bool dfirst = direct_ok(a.ph[0], NB, M, true);
+  const bool dlast = direct_ok(a.ph[NP - 1], NB, M, true);
+  const bool staged_in = !dfirst, staged_out = !dlast;
+  const bool use_smem = staged_in || staged_out || NP > 1;
+  auto regmask_of = [&](const FPhase& ph) {
+    uint32_t m = 0;
+    for (int b = 0; b < NB; ++b) m |= 1u << ph.reg[b];
+    return m;
+  };
+  auto thread_off = [&](const FPhase& ph) {  // global offset of the thread's non-register tile bits
+    const uint32_t rm = regmask_of(ph);
+    std::ostringstream e;
+    e << "(i64)0";
+    int nb = 0;
+    for (int bit = 0; bit < M; ++bit)
+      if (!((rm >> bit) & 1)) e << " | ((i64)((threadIdx.x >> " << nb++ << ") & 1) << " << a.tbits[bit] << ")";
+    return e.str();
+  };
+  auto reg_off = [&](const FPhase& ph, int j) {  // global offset of register amplitude j (bit 4: the lane)
+    int64_t v = 0;
+    for (int b = 0; b < NB; ++b)
+      if ((j >> b) & 1) v |= (int64_t)1 << a.tbits[ph.reg[b]];
+    return v;
+  };
+  const int64_t pofs = (int64_t)1 << a.tbits[P];
+  if (use_smem) o << "  extern __shared__ __align__(16) unsigned char smem_raw[];\n  f4* tile4 = reinterpret_cast<f4*>(smem_raw);\n";
+  if (staged_in || staged_out) {
+    o << "  i64* runoff = reinterpret_cast<i64*>(smem_raw + " << (8 << M) << ");\n";
+    o << "  for (int r = threadIdx.x; r < " << (1 << (M - c)) << "; r += " << T << ") { i64 v = 0;";
+    for (int b = 0; b < M - c; ++b) o << " v |= (i64)((r >> " << b << ") & 1) << " << a.tbits[c + b] << ";";
+    o << " runoff[r] = v; }\n  __syncthreads();\n";
+  }
+  if (dfirst) o << "  const i64 tf = " << thread_off(a.ph[0]) << ";\n";
+  if (dlast) o << "  const i64 tl = " << thread_off(a.ph[NP - 1]) << ";\n";
+  o << "  const i64 per = 1LL << a.lg_tiles, total = per * a.nmem;\n";
+  o << "  auto tile_ptr = [&](i64 tid) -> cf* {\n";
+  o << "    const i64 mem = a.member_lo + (tid >> a.lg_tiles);\n    u64 base = (u64)(tid & (per - 1));\n";
+  for (int i = 0; i < M; ++i) {
+    const int p = a.tbits[i];
+    o << "    base = ((base >> " << p << ") << " << (p + 1) << ") | (base & " << fmt_u64((1ULL << p) - 1) << ");\n";
+  }
+  o << "    return psi + (mem << a.nbits) + base;\n  };\n";
+  // global offset (from the tile's first amplitude) of tile index l
+  auto goff = [&](const std::string& l) { return "runoff[(" + l + ") >> " + std::to_string(c) + "] + ((" + l + ") & " + std::to_string(cmask) + ")"; };
+  const int nruns = 1 << (M - c), run_bytes = 8 << c;
+  const bool l2pf = l2_prefetch_on();
+  if (l2pf) {
+    o << "  const int pr = threadIdx.x;\n  i64 roff = 0;\n";
+    for (int b = 0; b < M - c; ++b) o << "  roff |= (i64)((pr >> " << b << ") & 1) << " << a.tbits[c + b] << ";\n";
+  }
+  o << "  for (i64 tid = blockIdx.x; tid < total; tid += gridDim.x) {\n";
+  o << "    cf* g = tile_ptr(tid);\n";
+  if (a.permem) o << "    const R* cm = mm + (tid >> a.lg_tiles) * mstride;\n";
+  if (l2pf) {
+    o << "    if (tid + gridDim.x < total" << (T > nruns ? " && threadIdx.x < " + std::to_string(nruns) : std::string())
+      << ") { const cf* gn = tile_ptr(tid + gridDim.x) + roff;";
+    o << " asm volatile(\"cp.async.bulk.prefetch.L2.global [%0], " << run_bytes << ";\" :: \"l\"(gn) : \"memory\");";
+    if (T < nruns) {
+      o << " for (int q = " << T << "; q < " << nruns << "; q += " << T << ") { i64 ro = 0;";
+      for (int b = 0; b < M - c; ++b) o << " ro |= (i64)(((threadIdx.x + q) >> " << b << ") & 1) << " << a.tbits[c + b] << ";";
+      o << " const cf* gq = tile_ptr(tid + gridDim.x) + ro; asm volatile(\"cp.async.bulk.prefetch.L2.global [%0], "
+        << run_bytes << ";\" :: \"l\"(gq) : \"memory\"); }";
+    }
+    o << " }\n";
+  }
+  const int NU = 1 << (M - 1);  // pair units of the tile
+  // tile index of pair unit u: u with a zero inserted at bit P
+  auto expand = [&](const std::string& u) {
+    return "(((" + u + ") >> " + std::to_string(P) + ") << " + std::to_string(P + 1) + ") | ((" + u + ") & " +
+           std::to_string((1 << P) - 1) + ")";
+  };
+  if (staged_in) {
+    o << "    {\n";
+    if (P == 0) {  // one 16-byte load is one pair (a, a+1)
+      const int UPT = NU / T;
+      for (int i = 0; i < UPT; ++i)
+        o << "      const int u" << i << " = threadIdx.x + " << i * T << "; const f4 b" << i
+          << " = *reinterpret_cast<const f4*>(g + " << goff("u" + std::to_string(i) + " << 1") << ");\n";
+      for (int i = 0; i < UPT; ++i)
+        o << "      tile4[u" << i << " ^ ((u" << i << " >> 3) & 7)] = f4{b" << i << ".x, b" << i << ".z, b" << i
+          << ".y, b" << i << ".w};\n";
+    } else {  // two 16-byte loads (a, a+1) and (a|P, a|P+1) are two pairs
+      const int H = NU / 2 / T;
+      for (int i = 0; i < H; ++i) {
+        o << "      const int u" << i << " = (threadIdx.x + " << i * T << ") << 1; const int l" << i << " = "
+          << expand("u" + std::to_string(i)) << ";\n";
+        o << "      const f4 va" << i << " = *reinterpret_cast<const f4*>(g + " << goff("l" + std::to_string(i))
+          << "), vb" << i << " = *reinterpret_cast<const f4*>(g + "
+          << goff("l" + std::to_string(i) + " | " + std::to_string(1 << P)) << ");\n";
+      }
+      for (int i = 0; i < H; ++i)
+        o << "      tile4[u" << i << " ^ ((u" << i << " >> 3) & 7)] = f4{va" << i << ".x, vb" << i << ".x, va" << i
+          << ".y, vb" << i << ".y}; tile4[(u" << i << " + 1) ^ (((u" << i << " + 1) >> 3) & 7)] = f4{va" << i
+          << ".z, vb" << i << ".z, va" << i << ".w, vb" << i << ".w};\n";
+    }
+    o << "    }\n    __syncthreads();\n";
+  }
+  for (int p = 0; p < NP; ++p) {
+    const FPhase& ph = a.ph[p];
+    const bool rd_direct = p == 0 && dfirst, wr_direct = p == NP - 1 && dlast;
+    const uint32_t rm = regmask_of(ph);
+    // 16-byte global accesses: along the lane bit when it is tile bit 0, else along
+    // tile bit 0 when it is a register bit (reg[0], the register bits ascend)
+    const int gcase = P == 0 ? 0 : (ph.reg[0] == 0 ? 1 : 2);
+    o << "    { // phase " << p << "\n";
+    std::vector<int> offs(16);
+    std::vector<int> lows;
+    if (!rd_direct || !wr_direct) {
+      o << "    const int t = threadIdx.x; const int qb = 0";
+      int nb = 0;
+      for (int bit = 0; bit < M; ++bit)
+        if (!((rm >> bit) & 1)) {
+          o << " | (((t >> " << nb << ") & 1) << " << qpos(bit) << ")";
+          ++nb;
+        }
+      o << ";\n    const int sb = qb ^ ((qb >> 3) & 7);\n";
+      for (int j = 0; j < 16; ++j) {
+        int q = 0;
+        for (int b = 0; b < 4; ++b)
+          if ((j >> b) & 1) q |= 1 << qpos(ph.reg[b]);
+        offs[j] = swz16(q);  // XOR-linear: swz(qb | q) = swz(qb) ^ swz(q); above bit 2 an addition
+        if (std::find(lows.begin(), lows.end(), offs[j] & 7) == lows.end()) lows.push_back(offs[j] & 7);
+      }
+      for (size_t k = 0; k < lows.size(); ++k) o << "    const int s" << k << " = sb ^ " << lows[k] << ";\n";
+    }
+    auto saddr = [&](int j) {
+      const int lo = offs[j] & 7, hi = offs[j] & ~7;
+      const int k = (int)(std::find(lows.begin(), lows.end(), lo) - lows.begin());
+      return "s" + std::to_string(k) + (hi ? " + " + std::to_string(hi) : std::string());
+    };
+    // ops that run as scalar code on the unpacked halves
+    bool scalar = false;
+    std::vector<std::string> packed_src(ph.nop);
+    std::vector<char> is_packed(ph.nop, 0);
+    for (int k = 0; k < ph.nop; ++k) {
+      const FOp& op = a.op[ph.op0 + k];
+      std::ostringstream po;
+      if (op.type != FOP_G2 && emit_op_packed(po, op, NB, 4, mref)) {
+        packed_src[k] = po.str();
+        is_packed[k] = 1;
+      } else {
+        scalar = true;
+      }
+    }
+    o << "    u64 ";
+    for (int j = 0; j < 16; ++j) o << (j ? ", " : "") << "X" << j << ", Y" << j;
+    o << ";\n";
+    if (scalar) {
+      o << "    R ";
+      for (int j = 0; j < 32; ++j) o << (j ? ", " : "") << "x" << j << ", y" << j;
+      o << ";\n";
+    }
+    if (rd_direct) {
+      o << "    { const cf* gp = g + tf;\n";
+      for (int j = 0; j < 16; ++j) {
+        const int64_t r0 = reg_off(ph, j);
+        if (gcase == 0)
+          o << "    { const f4 v = *reinterpret_cast<const f4*>(gp + " << r0 << "LL); X" << j << " = pk(v.x, v.z); Y" << j
+            << " = pk(v.y, v.w); }\n";
+        else if (gcase == 1) {
+          if (j & 1) continue;
+          o << "    { const f4 v0 = *reinterpret_cast<const f4*>(gp + " << r0 << "LL), v1 = *reinterpret_cast<const f4*>(gp + "
+            << (r0 + pofs) << "LL); X" << j << " = pk(v0.x, v1.x); Y" << j << " = pk(v0.y, v1.y); X" << (j | 1)
+            << " = pk(v0.z, v1.z); Y" << (j | 1) << " = pk(v0.w, v1.w); }\n";
+        } else
+          o << "    { const cf va = gp[" << r0 << "LL], vb = gp[" << (r0 + pofs) << "LL]; X" << j << " = pk(va.x, vb.x); Y"
+            << j << " = pk(va.y, vb.y); }\n";
+      }
+      o << "    }\n";
+    } else {
+      for (int j = 0; j < 16; ++j)
+        o << "    { const f4 v = tile4[" << saddr(j) << "]; X" << j << " = pk(v.x, v.y); Y" << j << " = pk(v.z, v.w); }\n";
+      // the tile's last shared-memory reads: the next tile may overwrite it once every warp is past them
+      if (wr_direct) o << "    __syncthreads();\n";
+    }
+    auto unpack = [&]() {
+      for (int j = 0; j < 16; ++j)
+        o << "    x" << j << "=plo(X" << j << "); x" << (j | 16) << "=phi(X" << j << "); y" << j << "=plo(Y" << j << "); y"
+          << (j | 16) << "=phi(Y" << j << ");\n";
+    };
+    auto pack = [&]() {
+      for (int j = 0; j < 16; ++j)
+        o << "    X" << j << "=pk(x" << j << ",x" << (j | 16) << "); Y" << j << "=pk(y" << j << ",y" << (j | 16) << ");\n";
+    };
+    for (int k = 0; k < ph.nop; ++k) {
+      if (is_packed[k]) {
+        o << packed_src[k];
+        continue;
+      }
+      unpack();
+      emit_op(o, a.op[ph.op0 + k], NB, mref);
+      pack();
+    }
+    if (wr_direct) {
+      o << "    { cf* gp = g + tl;\n";
+      for (int j = 0; j < 16; ++j) {
+        const int64_t r0 = reg_off(ph, j);
+        if (gcase == 0)
+          o << "    *reinterpret_cast<f4*>(gp + " << r0 << "LL) = f4{plo(X" << j << "), plo(Y" << j << "), phi(X" << j
+            << "), phi(Y" << j << ")};\n";
+        else if (gcase == 1) {
+          if (j & 1) continue;
+          o << "    *reinterpret_cast<f4*>(gp + " << r0 << "LL) = f4{plo(X" << j << "), plo(Y" << j << "), plo(X"
+            << (j | 1) << "), plo(Y" << (j | 1) << ")};\n";
+          o << "    *reinterpret_cast<f4*>(gp + " << (r0 + pofs) << "LL) = f4{phi(X" << j << "), phi(Y" << j << "), phi(X"
+            << (j | 1) << "), phi(Y" << (j | 1) << ")};\n";
+        } else
+          o << "    gp[" << r0 << "LL] = cf{plo(X" << j << "), plo(Y" << j << ")}; gp[" << (r0 + pofs) << "LL] = cf{phi(X"
+            << j << "), phi(Y" << j << ")};\n";
+      }
+      o << "    }\n    }\n";
+    } else {
+      for (int j = 0; j < 16; ++j)
+        o << "    tile4[" << saddr(j) << "] = f4{plo(X" << j << "), phi(X" << j << "), plo(Y" << j << "), phi(Y" << j
+          << ")};\n";
+      o << "    __syncthreads();\n    }\n";
+    }
+  }
+  if (staged_out) {
+    o << "    {\n";
+    if (P == 0) {
+      const int UPT = NU / T;
+      for (int i = 0; i < UPT; ++i)
+        o << "      const int u" << i << " = threadIdx.x + " << i * T << "; const f4 b" << i << " = tile4[u" << i
+          << " ^ ((u" << i << " >> 3) & 7)];\n";
+      for (int i = 0; i < UPT; ++i)
+        o << "      *reinterpret_cast<f4*>(g + " << goff("u" + std::to_string(i) + " << 1") << ") = f4{b" << i << ".x, b"
+          << i << ".z, b" << i << ".y, b" << i << ".w};\n";
+    } else {
+      const int H = NU / 2 / T;
+      for (int i = 0; i < H; ++i)
+        o << "      const int u" << i << " = (threadIdx.x + " << i * T << ") << 1; const int l" << i << " = "
+          << expand("u" + std::to_string(i)) << "; const f4 va" << i << " = tile4[u" << i << " ^ ((u" << i
+          << " >> 3) & 7)], vb" << i << " = tile4[(u" << i << " + 1) ^ (((u" << i << " + 1) >> 3) & 7)];\n";
+      for (int i = 0; i < H; ++i) {
+        o << "      *reinterpret_cast<f4*>(g + " << goff("l" + std::to_string(i)) << ") = f4{va" << i << ".x, va" << i
+          << ".z, vb" << i << ".x, vb" << i << ".z};\n";
+        o << "      *reinterpret_cast<f4*>(g + " << goff("l" + std::to_string(i) + " | " + std::to_string(1 << P))
+          << ") = f4{va" << i << ".y, va" << i << ".w, vb" << i << ".y, vb" << i << ".w};\n";
+      }
+    }
+    o << "    }\n    __syncthreads();\n";
+  }
+  o << "  }\n}\n";
+}
+
+// the kernel of one fused pass: the pair-lane form where the pass was planned with
+// a lane bit (complex64), else the scalar / two-lane-per-phase form
+template <typename R>
+static void gen_pass(std::ostringstream& o, const FusedArgs<R>& a, int NB, const std::string& name) {
+  if constexpr (sizeof(R) == 4) {
+    if (a.pbit >= 0 && NB == 5) {
+      gen_kernel_pl(o, a, name);
+      return;
+    }
+  }
+  gen_kernel<R>(o, a, NB, name);
+}
+
 // structure key: everything that shapes the code (not the matrix values)
 template <typename R>
 static std::string structure_key(const FusedArgs<R>& a) {
   std::ostringstream k;
   k << (sizeof(R) == 4 ? 'f' : 'd') << a.M << ':' << a.c << ':' << bt_jit_min_blocks() << ':'
     << (a.nphase ? (int)a.ph[0].nreg : 0) << ':' << (sizeof(R) == 4 && a.packed ? 'p' : 's') << ':'
-    << (a.permem ? 'm' : 'k') << ':';
+    << (a.permem ? 'm' : 'k') << ':' << a.pbit << ':';
   for (int i = 0; i < a.M; ++i) k << a.tbits[i] << ',';
   for (int p = 0; p < a.nphase; ++p) {
     const FPhase& ph = a.ph[p];
@@ -1024,7 +1315,7 @@ static int jit_prepare_t(bt_ctx* ctx, std::vector<const FusedArgs<R>*>& passes, 
       const FusedArgs<R>& pa = *passes[i];
       const int nreg = pa.nphase ? pa.ph[0].nreg : (sizeof(R) == 4 ? BT_TILE_RB_C64 : BT_TILE_RB_C128);
       src << "// pass " << i << ": M=" << pa.M << " threads=" << (1 << (pa.M - nreg)) << "\n";
-      gen_kernel<R>(src, pa, nreg, "pass_" + std::to_string(i));
+      gen_pass<R>(src, pa, nreg, "pass_" + std::to_string(i));
     }
     if (FILE* fd = fopen(dump, "w")) {
       const std::string t = src.str();
@@ -1056,7 +1347,7 @@ static int jit_prepare_t(bt_ctx* ctx, std::vector<const FusedArgs<R>*>& passes, 
       for (size_t i = b; i < order.size(); i += nb) {
         const std::string nm = "btk_" + std::to_string(i);
         const FusedArgs<R>& pa = *first[order[i]];
-        gen_kernel<R>(src, pa, pa.nphase ? pa.ph[0].nreg : (sizeof(R) == 4 ? BT_TILE_RB_C64 : BT_TILE_RB_C128), nm);
+        gen_pass<R>(src, pa, pa.nphase ? pa.ph[0].nreg : (sizeof(R) == 4 ? BT_TILE_RB_C64 : BT_TILE_RB_C128), nm);
         names[b].push_back(nm);
         bkeys[b].push_back(order[i]);
       }

@@ -462,14 +462,31 @@ static bool phase_windows_on() {
   return v;
 }
 
+// Pair-lane form (complex64 specialised passes, bt_jit.cu): one tile bit of the
+// pass, the lane bit, is a register bit of every phase, so each thread holds its
+// amplitudes as pairs that differ only in that bit and applies every op that
+// does not mix the two halves with two-lane FP32 instructions (fma.rn.f32x2) on
+// the pair.  The lane bit is the tile bit the fewest non-diagonal gates of the
+// pass touch (on the window planner's passes usually one of the low bits that no
+// gate of the pass acts on); a phase then chooses NB - 1 register bits.
+// BTGPU_JIT_LANES=0 turns the form off.
+static bool lanes_on() {
+  static const bool v = [] {
+    const char* e = getenv("BTGPU_JIT_LANES");
+    return !(e && *e == '0');
+  }();
+  return v;
+}
+
 template <typename R>
 static bool build_fused(bt_plan* p, const std::vector<int>& take, uint64_t tilemask, int M, int NB, int c,
                         std::vector<int>& kept, FusedArgs<R>& a, int64_t* nph, std::vector<uint8_t>& ob0,
-                        std::vector<uint8_t>& ob1) {
+                        std::vector<uint8_t>& ob1, bool lanes = false) {
   memset(&a, 0, sizeof(a));
   a.nbits = p->nbits;
   a.M = M;
   a.c = c;
+  a.pbit = -1;
   int nb = 0, local[64];
   for (int b = 0; b < p->nbits; ++b) {
     local[b] = -1;
@@ -479,6 +496,22 @@ static bool build_fused(bt_plan* p, const std::vector<int>& take, uint64_t tilem
     }
   }
   a.lg_tiles = p->nbits - M;
+  int pbit = -1;
+  if (lanes && NB == 5 && M >= NB + 1) {
+    int cnt[32] = {0};
+    for (int gi : take) {
+      const PGate& g = p->gates[gi];
+      int perm[4] = {0, 1, 2, 3};
+      if (!g.var && classify(g, perm) == 2) continue;  // diagonal: per-lane coefficients
+      for (int i = 0; i < g.k; ++i) cnt[local[g.bits[i]]]++;
+    }
+    pbit = 0;
+    for (int b = 1; b < M; ++b)
+      if (cnt[b] < cnt[pbit]) pbit = b;
+    a.pbit = pbit;
+  }
+  const uint32_t pmask = pbit >= 0 ? 1u << pbit : 0u;
+  const int NF = NB - (pbit >= 0 ? 1 : 0);  // register bits a phase chooses
   const int maxreals = sizeof(R) == 4 ? BT_FUSED_MAX_REALS_F : BT_FUSED_MAX_REALS_D;
   // register phases: greedy over the pass's gates with blocking, in order
   std::vector<int> rem = take;
@@ -496,27 +529,34 @@ static bool build_fused(bt_plan* p, const std::vector<int>& take, uint64_t tilem
       const PGate& g = p->gates[gi];
       uint32_t lb = 0;
       for (int i = 0; i < g.k; ++i) lb |= 1u << local[g.bits[i]];
+      const uint32_t lf = lb & ~pmask;  // the lane bit is in every phase
       const int need = g.k == 1 ? 8 : 32;
-      if ((lb & blocked) || (fixed ? (lb & ~rs) != 0 : popc(regs | lb) > NB) ||
+      if ((lb & blocked) || (fixed ? (lf & ~rs) != 0 : popc(regs | lf) > NF) ||
           nop + (int)ph.size() + 1 > BT_FUSED_MAX_OPS || nr + need > maxreals) {
         blocked |= lb;
         rest.push_back(gi);
         continue;
       }
-      if (!fixed) regs |= lb;
+      if (!fixed) regs |= lf;
       ph.push_back(gi);
       nr += need;
     }
   };
+  // the tile bits a phase may choose, ascending (all but the lane bit)
+  std::vector<int> free_bits;
+  for (int b = 0; b < M; ++b)
+    if (b != pbit) free_bits.push_back(b);
   while (!rem.empty()) {
     if (a.nphase >= BT_FUSED_MAX_PHASES) break;
     uint32_t regs = 0, regs2 = 0;
     int nr = 0, nr2 = 0;
     std::vector<int> ph, rest, ph2, rest2;
     scan(0, false, ph, rest, regs, nr);
-    if (phase_windows_on())  // or NB consecutive tile bits, where they take more gates
-      for (int s = 0; s + NB <= M; ++s) {
-        scan(((1u << NB) - 1) << s, true, ph2, rest2, regs2, nr2);
+    if (phase_windows_on())  // or NF consecutive free tile bits, where they take more gates
+      for (int s = 0; s + NF <= (int)free_bits.size(); ++s) {
+        uint32_t w = 0;
+        for (int i = 0; i < NF; ++i) w |= 1u << free_bits[s + i];
+        scan(w, true, ph2, rest2, regs2, nr2);
         if (ph2.size() > ph.size()) {
           ph.swap(ph2);
           rest.swap(rest2);
@@ -526,8 +566,8 @@ static bool build_fused(bt_plan* p, const std::vector<int>& take, uint64_t tilem
       }
     if (ph.empty()) break;
     nreal = nr;
-    // pad the register set to NB bits with the highest unused tile bits
-    for (int b = M - 1; b >= 0 && popc(regs) < NB; --b) regs |= 1u << b;
+    // pad the register set to NF bits with the highest unused free tile bits
+    for (int i = (int)free_bits.size() - 1; i >= 0 && popc(regs) < NF; --i) regs |= 1u << free_bits[i];
     FPhase& P = a.ph[a.nphase++];
     int rb = 0, regidx[32];
     for (int b = 0; b < M; ++b)
@@ -535,6 +575,10 @@ static bool build_fused(bt_plan* p, const std::vector<int>& take, uint64_t tilem
         regidx[b] = rb;
         P.reg[rb++] = (uint8_t)b;
       }
+    if (pbit >= 0) {  // the lane: register bit NB - 1
+      regidx[pbit] = rb;
+      P.reg[rb++] = (uint8_t)pbit;
+    }
     P.nreg = (uint8_t)NB;
     P.op0 = (uint16_t)nop;
     P.nop = (uint16_t)ph.size();
@@ -933,8 +977,10 @@ int bt_plan_compile(bt_plan* p, int mode) {
     int64_t nph = 0;
     if (c64) {
       ps.args.resize(sizeof(FusedArgs<float>));
+      // pair-lane code where every pass gets a specialised kernel of 5 register bits
+      const bool lanes = mode == 0 && bt_jit_available() && NB == 5 && lanes_on();
       build_fused<float>(p, take, Q, M, NB, c, kept, *reinterpret_cast<FusedArgs<float>*>(ps.args.data()), &nph,
-                         ps.op_b0, ps.op_b1);
+                         ps.op_b0, ps.op_b1, lanes);
       // two-lane code where the pass has no dense two-qubit op: a dense 4x4 costs as
       // much either way and its packed form compiles several times slower
       FusedArgs<float>& fa = *reinterpret_cast<FusedArgs<float>*>(ps.args.data());

@@ -20,6 +20,8 @@
 #include <sys/stat.h>
 
 #include <algorithm>
+#include <functional>
+#include <array>
 #include <atomic>
 #include <map>
 #include <mutex>
@@ -97,6 +99,7 @@ typedef unsigned long long u64;
 struct __align__(8) cf { float x, y; };
 struct __align__(16) cd { double x, y; };
 struct __align__(16) f4 { float x, y, z, w; };
+struct __align__(16) pu { u64 x, y; };  // a shared-memory pair unit of the pair-lane form
 __device__ __forceinline__ float fm(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ double fm(double a, double b, double c) { return __fma_rn(a, b, c); }
 template <int NM> struct JitArgsF { i64 member_lo, nmem; int nbits, lg_tiles; float mat[NM]; };
@@ -921,17 +924,84 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
 // diagonal ops on P with per-lane coefficients) runs as two-lane FP32 code
 // (fma.rn.f32x2 / mul.rn.f32x2): one instruction for two amplitudes.  The pairs
 // never change between phases: the shared-memory tile holds one 16-byte unit per
-// pair, (re_a, re_b, im_a, im_b) for the amplitudes a (P = 0) and b (P = 1),
-// indexed by the tile index without P and swizzled u ^ ((u >> 3) & 7), so a phase
-// boundary is one 16-byte store and load per pair.  The remaining ops (non-diagonal
-// ops on P, dense two-qubit matrices) run as the scalar code on the unpacked
-// halves.  Global memory keeps its interleaved layout: the direct first/last phase
-// and the staged tile copies regroup the 16-byte accesses into pairs.
+// pair, (re_a, re_b | im_a, im_b) for the amplitudes a (P = 0) and b (P = 1),
+// indexed by the tile index without P, so a phase boundary is one 16-byte store
+// and load per pair.  The remaining ops (non-diagonal ops on P, dense two-qubit
+// matrices) run as the scalar code on the unpacked halves.  Global memory keeps
+// its interleaved layout: the direct first/last phase and the staged tile copies
+// regroup the 16-byte accesses into pairs.
+//
+// Bank conflicts: a 16-byte access is served a quarter warp (8 lanes) per
+// wavefront, which is conflict-free when the 8 lanes' units lie in 8 different
+// 16-byte bank groups (unit index mod 8).  Lanes 0..7 vary the three lowest
+// thread bits of the phase, so each phase boundary gets its own swizzle: unit u
+// is stored at u ^ sum_k u_k v_k over the unit-index bits k >= 3, with the bank
+// vectors v_k (3 bits) chosen so that the three lane bits of both the writing and
+// the reading phase map to independent bank vectors.  The map is XOR-linear and
+// leaves bits >= 3 unchanged, so a thread's address is its base XOR a constant.
+struct PairSwz {
+  int v[32] = {0};  // bank vector of unit-index bit k (k >= 3; bits 0..2 map to themselves)
+  int vec(int k) const { return k < 3 ? (1 << k) : v[k]; }
+  int apply(int u) const {
+    int s = u;
+    for (int k = 3; k < 31; ++k)
+      if ((u >> k) & 1) s ^= v[k];
+    return s;
+  }
+};
+
+static bool indep3(int a, int b, int c) { return a && b && c && a != b && a != c && b != c && (a ^ b) != c; }
+
+// bank vectors for the unit-index bits >= 3 satisfying every lane triple (each
+// three bit positions whose bank vectors must be independent): the XOR-fold of the
+// 3-bit digits (v_k = 1 << (k mod 3)) when it already does, else a backtracking
+// search over the positions the triples use; the fold if nothing satisfies them
+static PairSwz choose_swz(const std::vector<std::array<int, 3>>& triples, int nq) {
+  PairSwz S;
+  for (int k = 3; k < nq; ++k) S.v[k] = 1 << (k % 3);
+  auto ok = [&](const PairSwz& T) {
+    for (auto& t : triples)
+      if (!indep3(T.vec(t[0]), T.vec(t[1]), T.vec(t[2]))) return false;
+    return true;
+  };
+  if (ok(S)) return S;
+  std::vector<int> pos;  // the positions >= 3 that a triple uses
+  for (auto& t : triples)
+    for (int k : t)
+      if (k >= 3 && std::find(pos.begin(), pos.end(), k) == pos.end()) pos.push_back(k);
+  std::sort(pos.begin(), pos.end());
+  PairSwz T = S;
+  std::vector<char> set(32, 0);
+  for (int k = 0; k < 3; ++k) set[k] = 1;
+  for (int k = 0; k < 32; ++k)
+    if (std::find(pos.begin(), pos.end(), k) == pos.end()) set[k] = 1;
+  // a triple is checked once all its positions are assigned
+  auto consistent = [&]() {
+    for (auto& t : triples)
+      if (set[t[0]] && set[t[1]] && set[t[2]] && !indep3(T.vec(t[0]), T.vec(t[1]), T.vec(t[2]))) return false;
+    return true;
+  };
+  long long budget = 2000000;
+  std::function<bool(size_t)> rec = [&](size_t i) -> bool {
+    if (i == pos.size()) return true;
+    for (int v = 1; v < 8 && budget > 0; ++v, --budget) {
+      T.v[pos[i]] = v;
+      set[pos[i]] = 1;
+      if (consistent() && rec(i + 1)) return true;
+      set[pos[i]] = 0;
+    }
+    return false;
+  };
+  if (rec(0)) return T;
+  return S;  // unsatisfiable (not expected): the fold, with bank conflicts
+}
+
 static void gen_kernel_pl(std::ostringstream& o, const FusedArgs<float>& a, const std::string& name) {
   const int M = a.M, c = a.c, NB = 5, P = a.pbit;
   const int T = 1 << (M - NB);
   const int NM = BT_FUSED_MAX_REALS_F;
   const int NP = a.nphase;
+  const int NQ = M - 1;  // unit-index bits
   const char* mref = a.permem ? "cm" : "a.mat";
   o << "extern \"C\" __global__ void __launch_bounds__(" << T << ", " << bt_jit_min_blocks() << ") " << name
     << "(cf* __restrict__ psi, const JitArgsF<" << NM << "> a";
@@ -942,7 +1012,6 @@ static void gen_kernel_pl(std::ostringstream& o, const FusedArgs<float>& a, cons
     return;
   }
   auto qpos = [&](int bit) { return bit < P ? bit : bit - 1; };
-  auto swz16 = [](int u) { return u ^ ((u >> 3) & 7); };
   const int cmask = (1 << c) - 1;
   const bool dfirst = direct_ok(a.ph[0], NB, M, true);
   const bool dlast = direct_ok(a.ph[NP - 1], NB, M, true);
@@ -953,6 +1022,28 @@ static void gen_kernel_pl(std::ostringstream& o, const FusedArgs<float>& a, cons
     for (int b = 0; b < NB; ++b) m |= 1u << ph.reg[b];
     return m;
   };
+  // unit-index positions of a phase's thread bits, in threadIdx order
+  auto tpos = [&](const FPhase& ph) {
+    const uint32_t rm = regmask_of(ph);
+    std::vector<int> v;
+    for (int bit = 0; bit < M; ++bit)
+      if (!((rm >> bit) & 1)) v.push_back(qpos(bit));
+    return v;
+  };
+  // one swizzle for the whole pass, so that a phase writes its results to exactly
+  // the units it read (in place, no barrier between its reads and its writes):
+  // the lane bits of every phase that touches shared memory, and of the staged
+  // copies, must have independent bank vectors under it
+  std::vector<std::array<int, 3>> tr;
+  for (int p = 0; p < NP; ++p) {
+    const bool rd_direct = p == 0 && dfirst, wr_direct = p == NP - 1 && dlast;
+    if (rd_direct && wr_direct) continue;
+    auto t = tpos(a.ph[p]);
+    tr.push_back({t[0], t[1], t[2]});
+  }
+  if ((staged_in || staged_out) && P != 0) tr.push_back({1, 2, 3});  // staged copies: lanes on unit bits 1..3
+  const PairSwz swz1 = choose_swz(tr, NQ);
+  std::vector<PairSwz> swz(NP + 1, swz1);
   auto thread_off = [&](const FPhase& ph) {  // global offset of the thread's non-register tile bits
     const uint32_t rm = regmask_of(ph);
     std::ostringstream e;
@@ -968,13 +1059,37 @@ static void gen_kernel_pl(std::ostringstream& o, const FusedArgs<float>& a, cons
       if ((j >> b) & 1) v |= (int64_t)1 << a.tbits[ph.reg[b]];
     return v;
   };
+  // swizzled unit index of a thread's bits at unit-index positions tp (threadIdx order)
+  auto base_expr = [&](const std::vector<int>& tp, const PairSwz& S) {
+    std::ostringstream e;
+    e << "0";
+    for (size_t i = 0; i < tp.size(); ++i) {
+      const int k = tp[i];
+      const int val = (1 << k) ^ (k >= 3 ? S.v[k] : 0);
+      e << " ^ (-(int)((threadIdx.x >> " << i << ") & 1) & " << val << ")";
+    }
+    return e.str();
+  };
   const int64_t pofs = (int64_t)1 << a.tbits[P];
-  if (use_smem) o << "  extern __shared__ __align__(16) unsigned char smem_raw[];\n  f4* tile4 = reinterpret_cast<f4*>(smem_raw);\n";
+  if (use_smem) o << "  extern __shared__ __align__(16) unsigned char smem_raw[];\n  pu* tile2 = reinterpret_cast<pu*>(smem_raw);\n";
   if (staged_in || staged_out) {
     o << "  i64* runoff = reinterpret_cast<i64*>(smem_raw + " << (8 << M) << ");\n";
     o << "  for (int r = threadIdx.x; r < " << (1 << (M - c)) << "; r += " << T << ") { i64 v = 0;";
     for (int b = 0; b < M - c; ++b) o << " v |= (i64)((r >> " << b << ") & 1) << " << a.tbits[c + b] << ";";
     o << " runoff[r] = v; }\n  __syncthreads();\n";
+  }
+  // per-thread swizzled bases of the staged copies (unit u = threadIdx.x + i T, or
+  // twice that for a lane bit above 0) and of every phase's reads and writes
+  const int csh = P == 0 ? 0 : 1;
+  std::vector<int> tcopy;
+  for (int i = 0; (1 << i) < T; ++i) tcopy.push_back(i + csh);
+  if (staged_in) o << "  const int cin = " << base_expr(tcopy, swz[0]) << ";\n";
+  if (staged_out) o << "  const int cout = " << base_expr(tcopy, swz[NP]) << ";\n";
+  for (int p = 0; p < NP; ++p) {
+    const auto tp = tpos(a.ph[p]);
+    const bool rd_direct = p == 0 && dfirst, wr_direct = p == NP - 1 && dlast;
+    if (!rd_direct) o << "  const int ri" << p << " = " << base_expr(tp, swz[p]) << ";\n";
+    if (!wr_direct) o << "  const int wo" << p << " = " << base_expr(tp, swz[p + 1]) << ";\n";
   }
   if (dfirst) o << "  const i64 tf = " << thread_off(a.ph[0]) << ";\n";
   if (dlast) o << "  const i64 tl = " << thread_off(a.ph[NP - 1]) << ";\n";
@@ -987,7 +1102,9 @@ static void gen_kernel_pl(std::ostringstream& o, const FusedArgs<float>& a, cons
   }
   o << "    return psi + (mem << a.nbits) + base;\n  };\n";
   // global offset (from the tile's first amplitude) of tile index l
-  auto goff = [&](const std::string& l) { return "runoff[(" + l + ") >> " + std::to_string(c) + "] + ((" + l + ") & " + std::to_string(cmask) + ")"; };
+  auto goff = [&](const std::string& l) {
+    return "runoff[(" + l + ") >> " + std::to_string(c) + "] + ((" + l + ") & " + std::to_string(cmask) + ")";
+  };
   const int nruns = 1 << (M - c), run_bytes = 8 << c;
   const bool l2pf = l2_prefetch_on();
   if (l2pf) {
@@ -1009,13 +1126,14 @@ static void gen_kernel_pl(std::ostringstream& o, const FusedArgs<float>& a, cons
     }
     o << " }\n";
   }
-  const int NU = 1 << (M - 1);  // pair units of the tile
+  const int NU = 1 << NQ;  // pair units of the tile
   // tile index of pair unit u: u with a zero inserted at bit P
   auto expand = [&](const std::string& u) {
     return "(((" + u + ") >> " + std::to_string(P) + ") << " + std::to_string(P + 1) + ") | ((" + u + ") & " +
            std::to_string((1 << P) - 1) + ")";
   };
   if (staged_in) {
+    const PairSwz& S = swz[0];
     o << "    {\n";
     if (P == 0) {  // one 16-byte load is one pair (a, a+1)
       const int UPT = NU / T;
@@ -1023,8 +1141,8 @@ static void gen_kernel_pl(std::ostringstream& o, const FusedArgs<float>& a, cons
         o << "      const int u" << i << " = threadIdx.x + " << i * T << "; const f4 b" << i
           << " = *reinterpret_cast<const f4*>(g + " << goff("u" + std::to_string(i) + " << 1") << ");\n";
       for (int i = 0; i < UPT; ++i)
-        o << "      tile4[u" << i << " ^ ((u" << i << " >> 3) & 7)] = f4{b" << i << ".x, b" << i << ".z, b" << i
-          << ".y, b" << i << ".w};\n";
+        o << "      tile2[cin ^ " << S.apply(i * T) << "] = pu{pk(b" << i << ".x, b" << i << ".z), pk(b" << i << ".y, b" << i
+          << ".w)};\n";
     } else {  // two 16-byte loads (a, a+1) and (a|P, a|P+1) are two pairs
       const int H = NU / 2 / T;
       for (int i = 0; i < H; ++i) {
@@ -1035,44 +1153,28 @@ static void gen_kernel_pl(std::ostringstream& o, const FusedArgs<float>& a, cons
           << goff("l" + std::to_string(i) + " | " + std::to_string(1 << P)) << ");\n";
       }
       for (int i = 0; i < H; ++i)
-        o << "      tile4[u" << i << " ^ ((u" << i << " >> 3) & 7)] = f4{va" << i << ".x, vb" << i << ".x, va" << i
-          << ".y, vb" << i << ".y}; tile4[(u" << i << " + 1) ^ (((u" << i << " + 1) >> 3) & 7)] = f4{va" << i
-          << ".z, vb" << i << ".z, va" << i << ".w, vb" << i << ".w};\n";
+        o << "      tile2[cin ^ " << S.apply(2 * i * T) << "] = pu{pk(va" << i << ".x, vb" << i << ".x), pk(va" << i
+          << ".y, vb" << i << ".y)}; tile2[cin ^ " << S.apply(2 * i * T + 1) << "] = pu{pk(va" << i << ".z, vb" << i
+          << ".z), pk(va" << i << ".w, vb" << i << ".w)};\n";
     }
     o << "    }\n    __syncthreads();\n";
   }
   for (int p = 0; p < NP; ++p) {
     const FPhase& ph = a.ph[p];
     const bool rd_direct = p == 0 && dfirst, wr_direct = p == NP - 1 && dlast;
-    const uint32_t rm = regmask_of(ph);
     // 16-byte global accesses: along the lane bit when it is tile bit 0, else along
     // tile bit 0 when it is a register bit (reg[0], the register bits ascend)
     const int gcase = P == 0 ? 0 : (ph.reg[0] == 0 ? 1 : 2);
     o << "    { // phase " << p << "\n";
-    std::vector<int> offs(16);
-    std::vector<int> lows;
-    if (!rd_direct || !wr_direct) {
-      o << "    const int t = threadIdx.x; const int qb = 0";
-      int nb = 0;
-      for (int bit = 0; bit < M; ++bit)
-        if (!((rm >> bit) & 1)) {
-          o << " | (((t >> " << nb << ") & 1) << " << qpos(bit) << ")";
-          ++nb;
-        }
-      o << ";\n    const int sb = qb ^ ((qb >> 3) & 7);\n";
-      for (int j = 0; j < 16; ++j) {
-        int q = 0;
-        for (int b = 0; b < 4; ++b)
-          if ((j >> b) & 1) q |= 1 << qpos(ph.reg[b]);
-        offs[j] = swz16(q);  // XOR-linear: swz(qb | q) = swz(qb) ^ swz(q); above bit 2 an addition
-        if (std::find(lows.begin(), lows.end(), offs[j] & 7) == lows.end()) lows.push_back(offs[j] & 7);
-      }
-      for (size_t k = 0; k < lows.size(); ++k) o << "    const int s" << k << " = sb ^ " << lows[k] << ";\n";
-    }
-    auto saddr = [&](int j) {
-      const int lo = offs[j] & 7, hi = offs[j] & ~7;
-      const int k = (int)(std::find(lows.begin(), lows.end(), lo) - lows.begin());
-      return "s" + std::to_string(k) + (hi ? " + " + std::to_string(hi) : std::string());
+    // the register units' offsets under a boundary's swizzle: XOR with the thread's
+    // base in bits 0..2, an addition above them (the base has no register bits)
+    auto uaddr = [&](const char* base, const PairSwz& S, int j) {
+      int q = 0;
+      for (int b = 0; b < 4; ++b)
+        if ((j >> b) & 1) q |= 1 << qpos(ph.reg[b]);
+      const int sw = S.apply(q), lo = sw & 7, hi = sw & ~7;
+      std::string e = std::string("(") + base + (lo ? " ^ " + std::to_string(lo) : std::string()) + ")";
+      return hi ? e + " + " + std::to_string(hi) : e;
     };
     // ops that run as scalar code on the unpacked halves
     bool scalar = false;
@@ -1114,8 +1216,9 @@ static void gen_kernel_pl(std::ostringstream& o, const FusedArgs<float>& a, cons
       }
       o << "    }\n";
     } else {
+      const std::string rb = "ri" + std::to_string(p);
       for (int j = 0; j < 16; ++j)
-        o << "    { const f4 v = tile4[" << saddr(j) << "]; X" << j << " = pk(v.x, v.y); Y" << j << " = pk(v.z, v.w); }\n";
+        o << "    { const pu v = tile2[" << uaddr(rb.c_str(), swz[p], j) << "]; X" << j << " = v.x; Y" << j << " = v.y; }\n";
       // the tile's last shared-memory reads: the next tile may overwrite it once every warp is past them
       if (wr_direct) o << "    __syncthreads();\n";
     }
@@ -1156,33 +1259,34 @@ static void gen_kernel_pl(std::ostringstream& o, const FusedArgs<float>& a, cons
       }
       o << "    }\n    }\n";
     } else {
+      const std::string wb = "wo" + std::to_string(p);
       for (int j = 0; j < 16; ++j)
-        o << "    tile4[" << saddr(j) << "] = f4{plo(X" << j << "), phi(X" << j << "), plo(Y" << j << "), phi(Y" << j
-          << ")};\n";
+        o << "    tile2[" << uaddr(wb.c_str(), swz[p + 1], j) << "] = pu{X" << j << ", Y" << j << "};\n";
       o << "    __syncthreads();\n    }\n";
     }
   }
   if (staged_out) {
+    const PairSwz& S = swz[NP];
     o << "    {\n";
     if (P == 0) {
       const int UPT = NU / T;
       for (int i = 0; i < UPT; ++i)
-        o << "      const int u" << i << " = threadIdx.x + " << i * T << "; const f4 b" << i << " = tile4[u" << i
-          << " ^ ((u" << i << " >> 3) & 7)];\n";
+        o << "      const int u" << i << " = threadIdx.x + " << i * T << "; const pu b" << i << " = tile2[cout ^ "
+          << S.apply(i * T) << "];\n";
       for (int i = 0; i < UPT; ++i)
-        o << "      *reinterpret_cast<f4*>(g + " << goff("u" + std::to_string(i) + " << 1") << ") = f4{b" << i << ".x, b"
-          << i << ".z, b" << i << ".y, b" << i << ".w};\n";
+        o << "      *reinterpret_cast<f4*>(g + " << goff("u" + std::to_string(i) + " << 1") << ") = f4{plo(b" << i
+          << ".x), plo(b" << i << ".y), phi(b" << i << ".x), phi(b" << i << ".y)};\n";
     } else {
       const int H = NU / 2 / T;
       for (int i = 0; i < H; ++i)
         o << "      const int u" << i << " = (threadIdx.x + " << i * T << ") << 1; const int l" << i << " = "
-          << expand("u" + std::to_string(i)) << "; const f4 va" << i << " = tile4[u" << i << " ^ ((u" << i
-          << " >> 3) & 7)], vb" << i << " = tile4[(u" << i << " + 1) ^ (((u" << i << " + 1) >> 3) & 7)];\n";
+          << expand("u" + std::to_string(i)) << "; const pu va" << i << " = tile2[cout ^ " << S.apply(2 * i * T)
+          << "], vb" << i << " = tile2[cout ^ " << S.apply(2 * i * T + 1) << "];\n";
       for (int i = 0; i < H; ++i) {
-        o << "      *reinterpret_cast<f4*>(g + " << goff("l" + std::to_string(i)) << ") = f4{va" << i << ".x, va" << i
-          << ".z, vb" << i << ".x, vb" << i << ".z};\n";
+        o << "      *reinterpret_cast<f4*>(g + " << goff("l" + std::to_string(i)) << ") = f4{plo(va" << i << ".x), plo(va"
+          << i << ".y), plo(vb" << i << ".x), plo(vb" << i << ".y)};\n";
         o << "      *reinterpret_cast<f4*>(g + " << goff("l" + std::to_string(i) + " | " + std::to_string(1 << P))
-          << ") = f4{va" << i << ".y, va" << i << ".w, vb" << i << ".y, vb" << i << ".w};\n";
+          << ") = f4{phi(va" << i << ".x), phi(va" << i << ".y), phi(vb" << i << ".x), phi(vb" << i << ".y)};\n";
       }
     }
     o << "    }\n    __syncthreads();\n";

@@ -107,9 +107,11 @@ def test_headline_plan_equals_gate_path(ctx, n, prec, amp_tol, rel_tol, z_tol):
     # the reference's T (and T-dagger) entries are rounded to 10 significant
     # digits (src/gates.jl:32-33), so T is not exactly unitary: the norm drifts by
     # ~2e-11 per T gate (~140 in this circuit) on both paths alike
+    # (complex64 adds FP32 rounding: the per-gate path's norm moves by ~1e-5 over
+    # the 1470 gates, and the plan's stays within 1e-5 of it)
     na, nb = _norm2(a), _norm2(b)
     assert abs(na - nb) < (1e-5 if prec == "c64" else 1e-13), (na, nb)
-    assert abs(nb - 1) < 1e-7, nb
+    assert abs(nb - 1) < (1e-4 if prec == "c64" else 1e-7), nb
     b.free()
     # the inverse circuit (adjoints in reverse order) takes the plan's output back
     # to |0...0>, up to the same T rounding

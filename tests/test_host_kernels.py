@@ -1,7 +1,8 @@
 """The generated fused-pass kernels run on the host (tests/kernel_emulator.py)
 and compared with the oracle: brickworks wide enough for several tiles and the
 window planner, every factored one-qubit form, and random gate mixes, in
-complex64 (scalar and two-lane code) and complex128, with the first/last phases
+complex64 (pair-lane code, the default; scalar and per-phase two-lane code) and
+complex128, with the first/last phases
 direct to memory, staged through shared memory, or as the coalescing rule picks,
 and with register phases chosen among bit windows.
 The generator's knobs are read once per process, so each configuration runs in a
@@ -143,6 +144,8 @@ print("OK")
     ("c64", {"BTGPU_JIT_DIRECT": "2", "BTGPU_JIT_PACKED": "1"}),
     ("c128", {"BTGPU_JIT_DIRECT": "2"}),
     ("c64", {"BTGPU_PLAN_PHASE_WINDOWS": "0"}),
+    ("c64", {"BTGPU_JIT_LANES": "0"}),
+    ("c64", {"BTGPU_JIT_LANES": "0", "BTGPU_JIT_PACKED": "1"}),
 ])
 def test_generated_kernels_on_host(prec, env, tmp_path):
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))

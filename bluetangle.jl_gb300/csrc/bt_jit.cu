@@ -1059,15 +1059,22 @@ static void gen_kernel_pl(std::ostringstream& o, const FusedArgs<float>& a, cons
       if ((j >> b) & 1) v |= (int64_t)1 << a.tbits[ph.reg[b]];
     return v;
   };
-  // swizzled unit index of a thread's bits at unit-index positions tp (threadIdx order)
+  // swizzled unit index of a thread's bits at unit-index positions tp (threadIdx
+  // order): the unit index itself with its bank bits (0..2) XORed by the parity of
+  // its bits under each bank bit's mask; computed where a phase starts
   auto base_expr = [&](const std::vector<int>& tp, const PairSwz& S) {
+    std::ostringstream q;
+    q << "0";
+    for (size_t i = 0; i < tp.size(); ++i) q << " | (((int)(threadIdx.x >> " << i << ") & 1) << " << tp[i] << ")";
+    unsigned mask[3] = {0, 0, 0};
+    for (int k = 3; k < 31; ++k)
+      for (int r = 0; r < 3; ++r)
+        if ((S.v[k] >> r) & 1) mask[r] |= 1u << k;
     std::ostringstream e;
-    e << "0";
-    for (size_t i = 0; i < tp.size(); ++i) {
-      const int k = tp[i];
-      const int val = (1 << k) ^ (k >= 3 ? S.v[k] : 0);
-      e << " ^ (-(int)((threadIdx.x >> " << i << ") & 1) & " << val << ")";
-    }
+    e << "[&]() { const int q = " << q.str() << "; return q";
+    for (int r = 0; r < 3; ++r)
+      if (mask[r]) e << " ^ ((__popc((unsigned)q & " << mask[r] << "u) & 1) << " << r << ")";
+    e << "; }()";
     return e.str();
   };
   const int64_t pofs = (int64_t)1 << a.tbits[P];
@@ -1083,14 +1090,6 @@ static void gen_kernel_pl(std::ostringstream& o, const FusedArgs<float>& a, cons
   const int csh = P == 0 ? 0 : 1;
   std::vector<int> tcopy;
   for (int i = 0; (1 << i) < T; ++i) tcopy.push_back(i + csh);
-  if (staged_in) o << "  const int cin = " << base_expr(tcopy, swz[0]) << ";\n";
-  if (staged_out) o << "  const int cout = " << base_expr(tcopy, swz[NP]) << ";\n";
-  for (int p = 0; p < NP; ++p) {
-    const auto tp = tpos(a.ph[p]);
-    const bool rd_direct = p == 0 && dfirst, wr_direct = p == NP - 1 && dlast;
-    if (!rd_direct) o << "  const int ri" << p << " = " << base_expr(tp, swz[p]) << ";\n";
-    if (!wr_direct) o << "  const int wo" << p << " = " << base_expr(tp, swz[p + 1]) << ";\n";
-  }
   if (dfirst) o << "  const i64 tf = " << thread_off(a.ph[0]) << ";\n";
   if (dlast) o << "  const i64 tl = " << thread_off(a.ph[NP - 1]) << ";\n";
   o << "  const i64 per = 1LL << a.lg_tiles, total = per * a.nmem;\n";
@@ -1134,7 +1133,7 @@ static void gen_kernel_pl(std::ostringstream& o, const FusedArgs<float>& a, cons
   };
   if (staged_in) {
     const PairSwz& S = swz[0];
-    o << "    {\n";
+    o << "    {\n      const int cin = " << base_expr(tcopy, S) << ";\n";
     if (P == 0) {  // one 16-byte load is one pair (a, a+1)
       const int UPT = NU / T;
       for (int i = 0; i < UPT; ++i)
@@ -1176,6 +1175,7 @@ static void gen_kernel_pl(std::ostringstream& o, const FusedArgs<float>& a, cons
       std::string e = std::string("(") + base + (lo ? " ^ " + std::to_string(lo) : std::string()) + ")";
       return hi ? e + " + " + std::to_string(hi) : e;
     };
+    if (!rd_direct || !wr_direct) o << "    const int sb = " << base_expr(tpos(ph), swz[p]) << ";\n";
     // ops that run as scalar code on the unpacked halves
     bool scalar = false;
     std::vector<std::string> packed_src(ph.nop);
@@ -1216,9 +1216,8 @@ static void gen_kernel_pl(std::ostringstream& o, const FusedArgs<float>& a, cons
       }
       o << "    }\n";
     } else {
-      const std::string rb = "ri" + std::to_string(p);
       for (int j = 0; j < 16; ++j)
-        o << "    { const pu v = tile2[" << uaddr(rb.c_str(), swz[p], j) << "]; X" << j << " = v.x; Y" << j << " = v.y; }\n";
+        o << "    { const pu v = tile2[" << uaddr("sb", swz[p], j) << "]; X" << j << " = v.x; Y" << j << " = v.y; }\n";
       // the tile's last shared-memory reads: the next tile may overwrite it once every warp is past them
       if (wr_direct) o << "    __syncthreads();\n";
     }
@@ -1259,15 +1258,14 @@ static void gen_kernel_pl(std::ostringstream& o, const FusedArgs<float>& a, cons
       }
       o << "    }\n    }\n";
     } else {
-      const std::string wb = "wo" + std::to_string(p);
       for (int j = 0; j < 16; ++j)
-        o << "    tile2[" << uaddr(wb.c_str(), swz[p + 1], j) << "] = pu{X" << j << ", Y" << j << "};\n";
+        o << "    tile2[" << uaddr("sb", swz[p + 1], j) << "] = pu{X" << j << ", Y" << j << "};\n";
       o << "    __syncthreads();\n    }\n";
     }
   }
   if (staged_out) {
     const PairSwz& S = swz[NP];
-    o << "    {\n";
+    o << "    {\n      const int cout = " << base_expr(tcopy, S) << ";\n";
     if (P == 0) {
       const int UPT = NU / T;
       for (int i = 0; i < UPT; ++i)

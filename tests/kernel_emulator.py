@@ -42,6 +42,7 @@ static inline float __fmaf_rn(float a, float b, float c) { return std::fmaf(a, b
 static inline double __fma_rn(double a, double b, double c) { return std::fma(a, b, c); }
 static inline unsigned __float_as_uint(float f) { unsigned u; std::memcpy(&u, &f, 4); return u; }
 static inline float __uint_as_float(unsigned u) { float f; std::memcpy(&f, &u, 4); return f; }
+static inline int __popc(unsigned x) { return __builtin_popcount(x); }
 """
 
 LAUNCH = r"""

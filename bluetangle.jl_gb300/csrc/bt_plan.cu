@@ -468,12 +468,18 @@ static bool phase_windows_on() {
 // does not mix the two halves with two-lane FP32 instructions (fma.rn.f32x2) on
 // the pair.  The lane bit is the tile bit the fewest non-diagonal gates of the
 // pass touch (on the window planner's passes usually one of the low bits that no
-// gate of the pass acts on); a phase then chooses NB - 1 register bits.
-// BTGPU_JIT_LANES=0 turns the form off.
+// gate of the pass acts on); a phase then chooses NB - 1 register bits.  Off
+// unless BTGPU_JIT_LANES=1: on a GB300 the form cuts the instructions of a dense
+// 28-qubit pass by 26% (911M -> 673M: the FP32 instructions halve) but is slower
+// on 21 of the 23 passes of the 28-qubit brickwork (23.3 vs 21.8 ms per circuit;
+// 33 qubits: 0.828 vs 0.787 s): the FMA pipe time stays the same, each op's
+// coefficients must be broadcast into register pairs, and at 16 warps per SM and
+// the 128-register cap the halved instruction-level parallelism of a phase shows
+// as dependency and scoreboard stalls (issue 48% active against 70%).
 static bool lanes_on() {
   static const bool v = [] {
     const char* e = getenv("BTGPU_JIT_LANES");
-    return !(e && *e == '0');
+    return e && *e == '1';
   }();
   return v;
 }

@@ -1,7 +1,7 @@
 """The generated fused-pass kernels run on the host (tests/kernel_emulator.py)
 and compared with the oracle: brickworks wide enough for several tiles and the
 window planner, every factored one-qubit form, and random gate mixes, in
-complex64 (pair-lane code, the default; scalar and per-phase two-lane code) and
+complex64 (scalar code, the default; per-phase two-lane and pair-lane code) and
 complex128, with the first/last phases
 direct to memory, staged through shared memory, or as the coalescing rule picks,
 and with register phases chosen among bit windows.
@@ -144,8 +144,8 @@ print("OK")
     ("c64", {"BTGPU_JIT_DIRECT": "2", "BTGPU_JIT_PACKED": "1"}),
     ("c128", {"BTGPU_JIT_DIRECT": "2"}),
     ("c64", {"BTGPU_PLAN_PHASE_WINDOWS": "0"}),
-    ("c64", {"BTGPU_JIT_LANES": "0"}),
-    ("c64", {"BTGPU_JIT_LANES": "0", "BTGPU_JIT_PACKED": "1"}),
+    ("c64", {"BTGPU_JIT_LANES": "1"}),
+    ("c64", {"BTGPU_JIT_LANES": "1", "BTGPU_JIT_DIRECT": "0"}),
 ])
 def test_generated_kernels_on_host(prec, env, tmp_path):
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))

@@ -70,6 +70,7 @@ SIGNATURES = {
     "bt_plan_add_matrix": (i32, [P, i32, P, P, i32, P]),
     "bt_plan_add_kraus_sum": (i32, [P, i32, P, i32, P]),
     "bt_plan_compile": (i32, [P, i32]),
+    "bt_tc_tf32_peak": (i32, [P, i32, P]),
     "bt_plan_set_matrices": (i32, [P, i32, P, P]),
     "bt_plan_set_variable": (i32, [P, i32, P]),
     "bt_plan_stats": (i32, [P, P, P, P, P, P]),

@@ -36,6 +36,25 @@ def brickwork(n, depth, rng):
     return ops
 
 
+def haar_unitary(rng, d):
+    """A Haar-random d x d unitary (QR of a complex Gaussian matrix, phases fixed)."""
+    z = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    q, r = np.linalg.qr(z)
+    return q * (np.diag(r) / np.abs(np.diag(r)))
+
+
+def su4_brickwork(n, depth, rng):
+    """Brickwork of generic two-qubit gates: every layer a Haar-random 4 x 4 unitary
+    on each nearest-neighbour pair (q, q+1), pairs from qubit 1 on even layers and
+    from qubit 2 on odd ones -- the circuit where the factored one-qubit forms do
+    not apply and every gate is a dense 4 x 4 complex matrix."""
+    ops = []
+    for layer in range(depth):
+        for q in range(1 if layer % 2 == 0 else 2, n, 2):
+            ops.append(Op("U4", haar_unitary(rng, 4), q, q + 1))
+    return ops
+
+
 def noisy_brickwork_dm(n, depth, rng, p1=1e-3, p2=1e-2, gamma=5e-3):
     """Brickwork with channels after every gate (the density-matrix workload);
     returns (ops, readout) where readout is the final 2% bit flip per qubit."""

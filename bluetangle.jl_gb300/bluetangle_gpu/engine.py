@@ -482,11 +482,13 @@ class Plan:
         ctrls = [op.control] if op.control != -2 else []
         return self.add_matrix(mat, qs, ctrls)
 
-    def compile(self, fused=True, tiered=False):
+    def compile(self, fused=True, tiered=False, tensor_cores=False):
         """fused: tile passes (else one sweep per gate); tiered: run the generic
         kernel at once and switch to specialised kernels when their background
-        compile finishes."""
-        self.ctx.check(L.lib().bt_plan_compile(self.h, (2 if tiered else 0) if fused else 1))
+        compile finishes; tensor_cores (complex64 state vectors): every register
+        phase of a pass as one dense 32 x 32 block on the tensor cores."""
+        mode = 3 if tensor_cores else ((2 if tiered else 0) if fused else 1)
+        self.ctx.check(L.lib().bt_plan_compile(self.h, mode))
         return self
 
     def set_matrices(self, updates):

@@ -79,6 +79,7 @@ static int sync_and_status(bt_ctx* ctx, const char* what) {
     cudaStreamSynchronize(ctx->stream);
     if (st == 1) return bt_fail(ctx, BT_ERR_BAD_ARG, "measurement outcome with zero probability");
     if (st == 2) return bt_fail(ctx, BT_ERR_NO_BRANCH, "no Kraus branch satisfies u <= cumsum(p)");
+    if (st == 16) return bt_fail(ctx, BT_ERR_TIMEOUT, "tensor-core pass: an MMA completion wait ran out");
     return bt_fail(ctx, BT_ERR_BAD_ARG, "Kraus branch with zero norm");
   }
   return BT_OK;

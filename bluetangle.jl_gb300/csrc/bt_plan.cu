@@ -27,6 +27,7 @@
 
 #include "bt_fused.cuh"
 #include "bt_jit.cuh"
+#include "bt_tc.cuh"
 
 struct PGate {
   int k = 0;
@@ -56,6 +57,9 @@ struct PPass {
   // from a per-member table, and its specialised kernel
   std::vector<unsigned char> pm_args;
   void* pm_jit = nullptr;
+  // tensor-core form (compile mode 3): index of the pass's first phase block in
+  // the plan's device table of block images, or -1
+  int tc_block = -1;
 };
 
 struct bt_plan {
@@ -78,6 +82,9 @@ struct bt_plan {
   void* d_pm = nullptr;
   size_t d_pm_bytes = 0;
   int d_pm_device = -1;
+  // device table of the tensor-core phase blocks (compile mode 3)
+  float* d_tc = nullptr;
+  int d_tc_device = -1;
 };
 
 // reals of the matrices that bt_plan_set_matrices reads for these add indices
@@ -638,6 +645,10 @@ int bt_plan_free(bt_plan* p) {
     cudaSetDevice(p->d_pm_device);
     cudaFree(p->d_pm);
   }
+  if (p && p->d_tc) {
+    cudaSetDevice(p->d_tc_device);
+    cudaFree(p->d_tc);
+  }
   delete p;
   return BT_OK;
 }
@@ -856,6 +867,10 @@ int bt_plan_set_matrices(bt_plan* p, int count, const int64_t* add_index, const 
   int rc = assign_matrices(p, count, add_index, mats, touched);
   if (rc) return rc;
   if (!p->compiled) return BT_OK;
+  if (p->compile_mode == 3) {  // the phase blocks are products of the gates: rebuilt at the next run
+    p->compiled = false;
+    return BT_OK;
+  }
   for (auto& ps : p->passes) {
     if (ps.kind != 0) continue;
     const bool ok = p->prec == BT_PREC_C64 ? update_pass<float>(p, ps, touched) : update_pass<double>(p, ps, touched);
@@ -936,9 +951,94 @@ static void select_bits(const bt_plan* p, const std::vector<int>& rem, uint64_t 
   }
 }
 
+// Tensor-core form (compile mode 3): each register phase of a fused pass of
+// 2^13-amplitude tiles becomes one dense 32 x 32 block, the product of the phase's
+// gates on its 5 register bits (complex128, in order), stored as its TF32 MMA
+// operand image (bt_tc.cu) in a device table of the plan
+static void phase_block(const bt_plan* p, const FusedArgs<float>& a, const std::vector<int>& op_gate, int ph,
+                        std::vector<double>& u) {
+  const FPhase& P = a.ph[ph];
+  int regidx[64];
+  for (int b = 0; b < 64; ++b) regidx[b] = -1;
+  for (int b = 0; b < 5; ++b) regidx[a.tbits[P.reg[b]]] = b;  // global bit -> register bit
+  u.assign(2 * 32 * 32, 0.0);
+  for (int j = 0; j < 32; ++j) u[2 * (j * 32 + j)] = 1.0;
+  std::vector<double> nu(u.size());
+  for (int oi = P.op0; oi < P.op0 + P.nop; ++oi) {
+    const PGate& g = p->gates[op_gate[oi]];
+    const int k = g.k, d = 1 << k;
+    int rb[2];
+    uint32_t gm = 0;
+    for (int i = 0; i < k; ++i) {
+      rb[i] = regidx[g.bits[i]];
+      gm |= 1u << rb[i];
+    }
+    nu = u;
+    for (int col = 0; col < 32; ++col)
+      for (int x = 0; x < 32; ++x) {
+        if (x & gm) continue;
+        int idx[4];
+        for (int sidx = 0; sidx < d; ++sidx) {
+          int y = x;
+          for (int i = 0; i < k; ++i)
+            if ((sidx >> (k - 1 - i)) & 1) y |= 1 << rb[i];
+          idx[sidx] = y;
+        }
+        for (int r = 0; r < d; ++r) {
+          double re = 0, im = 0;
+          for (int sidx = 0; sidx < d; ++sidx) {
+            const double mr = g.m[2 * (r * d + sidx)], mi = g.m[2 * (r * d + sidx) + 1];
+            const double vr = u[2 * (idx[sidx] * 32 + col)], vi = u[2 * (idx[sidx] * 32 + col) + 1];
+            re += mr * vr - mi * vi;
+            im += mr * vi + mi * vr;
+          }
+          nu[2 * (idx[r] * 32 + col)] = re;
+          nu[2 * (idx[r] * 32 + col) + 1] = im;
+        }
+      }
+    u.swap(nu);
+  }
+}
+
+static int build_tc_blocks(bt_plan* p) {
+  std::vector<float> img;
+  std::vector<double> u;
+  int nblk = 0;
+  for (auto& ps : p->passes) {
+    ps.tc_block = -1;
+    if (ps.kind != 0) continue;
+    const FusedArgs<float>& a = *reinterpret_cast<const FusedArgs<float>*>(ps.args.data());
+    if (a.M != 13 || a.c != BT_TILE_LOW_C64 || a.nphase < 1 || a.ph[0].nreg != 5) continue;
+    ps.tc_block = nblk;
+    for (int ph = 0; ph < a.nphase; ++ph) {
+      phase_block(p, a, ps.op_gate, ph, u);
+      img.resize((size_t)(nblk + 1) * 8192);
+      bt_tc_block_image(u.data(), img.data() + (size_t)nblk * 8192);
+      ++nblk;
+    }
+  }
+  if (p->d_tc) {
+    cudaSetDevice(p->d_tc_device);
+    cudaFree(p->d_tc);
+    p->d_tc = nullptr;
+  }
+  if (!nblk) return BT_OK;
+  if (!p->ctx) return bt_fail(nullptr, BT_ERR_BAD_ARG, "tensor-core plans need a context (device memory)");
+  bt_ctx* ctx = p->ctx;
+  int rc = bt_cuda_check(ctx, cudaSetDevice(ctx->device), "cudaSetDevice");
+  if (!rc) rc = bt_cuda_check(ctx, cudaMalloc((void**)&p->d_tc, img.size() * sizeof(float)), "tensor-core block table");
+  if (!rc)
+    rc = bt_cuda_check(ctx, cudaMemcpy(p->d_tc, img.data(), img.size() * sizeof(float), cudaMemcpyHostToDevice),
+                       "tensor-core block table upload");
+  p->d_tc_device = ctx->device;
+  return rc;
+}
+
 int bt_plan_compile(bt_plan* p, int mode) {
   if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "plan is NULL");
-  if (mode < 0 || mode > 2) return bt_fail(p->ctx, BT_ERR_BAD_ARG, "compile mode must be 0, 1 or 2");
+  if (mode < 0 || mode > 3) return bt_fail(p->ctx, BT_ERR_BAD_ARG, "compile mode must be 0, 1, 2 or 3");
+  if (mode == 3 && (p->prec != BT_PREC_C64 || p->repr != BT_REPR_SV))
+    return bt_fail(p->ctx, BT_ERR_UNSUPPORTED, "tensor-core plans (mode 3) are complex64 state-vector plans");
   join_jit(p);  // a background compile reads the passes about to be rebuilt
   p->compile_mode = mode;
   p->passes.clear();
@@ -947,7 +1047,8 @@ int bt_plan_compile(bt_plan* p, int mode) {
   // register bits per thread: a tuned width only where every pass gets its
   // specialised kernel before the first run (the generic kernel has one width)
   const int rb_tuned = c64 ? (p->tune_rb ? p->tune_rb : bt_tile_rb(true)) : BT_TILE_RB_C128;
-  const int NB = (mode == 0 && bt_jit_available()) ? rb_tuned : (c64 ? BT_TILE_RB_C64 : BT_TILE_RB_C128);
+  const int NB = mode == 3 ? BT_TILE_RB_C64
+                           : ((mode == 0 && bt_jit_available()) ? rb_tuned : (c64 ? BT_TILE_RB_C64 : BT_TILE_RB_C128));
   const int packed = p->tune_packed >= 0 ? p->tune_packed : (int)bt_jit_packed_default();
   // the tile covers the whole state when the state is smaller than the default
   // tile, down to 2^(M - NB) = 32 threads per CTA; a tuned smaller tile spreads a
@@ -955,7 +1056,7 @@ int bt_plan_compile(bt_plan* p, int mode) {
   const int Mdef = c64 ? BT_TILE_M_C64 : BT_TILE_M_C128;
   const int M = std::min(p->tune_m ? std::min(p->tune_m, Mdef) : Mdef, p->nbits);
   const int c = c64 ? BT_TILE_LOW_C64 : BT_TILE_LOW_C128;
-  const bool fuse = (mode == 0 || mode == 2) && M >= NB + 5;
+  const bool fuse = (mode == 0 || mode == 2 || mode == 3) && M >= NB + 5;
   // specialised kernels compile in time superlinear in their length: bound the
   // ops of a pass when they will be specialised
   const int max_ops = bt_jit_available() ? (p->tune_max_ops ? p->tune_max_ops : bt_jit_max_ops()) : BT_FUSED_MAX_OPS;
@@ -1020,6 +1121,13 @@ int bt_plan_compile(bt_plan* p, int mode) {
   if (fuse && bt_jit_available()) {
     if (mode == 2) p->jit_thread = std::thread([p] { specialise(p); });
     else specialise(p);
+  }
+  if (mode == 3) {
+    const int rc = build_tc_blocks(p);
+    if (rc) {
+      p->compiled = false;
+      return rc;
+    }
   }
   return BT_OK;
 }
@@ -1307,6 +1415,21 @@ int bt_plan_run(bt_plan* p, bt_state* s, int64_t member) {
     if (ps.kind == 1) {
       const PGate& g = p->gates[ps.gate];
       rc = bt_launch_gate(s, g.k, g.bits, g.m.data(), g.cmask, lo, nm, nullptr, 0);
+    } else if (p->prec == BT_PREC_C64 && ps.tc_block >= 0 && p->d_tc) {
+      const FusedArgs<float>& a = *reinterpret_cast<const FusedArgs<float>*>(ps.args.data());
+      TcPass t;
+      t.nbits = a.nbits;
+      t.c = a.c;
+      t.nphase = a.nphase;
+      t.lg_tiles = a.lg_tiles;
+      t.member_lo = lo;
+      t.nmem = nm;
+      for (int b = 0; b < 16; ++b) t.tbits[b] = a.tbits[b];
+      for (int ph = 0; ph < a.nphase; ++ph)
+        for (int b = 0; b < 5; ++b) t.reg[ph][b] = a.ph[ph].reg[b];
+      t.bmat = p->d_tc + (size_t)ps.tc_block * 8192;
+      if (p->d_tc_device != ctx->device) rc = bt_fail(ctx, BT_ERR_BAD_ARG, "tensor-core plan compiled for another device");
+      else rc = bt_launch_tc_pass(ctx, s->d, t);
     } else if (p->prec == BT_PREC_C64) {
       FusedArgs<float>& a = *reinterpret_cast<FusedArgs<float>*>(ps.args.data());
       a.member_lo = lo;

@@ -180,7 +180,12 @@ int bt_plan_add_kraus_sum(bt_plan* p, int k, const int32_t* qubits, int nk, cons
 /* mode 0: fused passes, kernels specialised before returning;
  * mode 1: one sweep per gate (the unfused reference form);
  * mode 2: fused passes that run on the generic kernel at once while their
- *         specialised kernels compile on a background thread (tiered) */
+ *         specialised kernels compile on a background thread (tiered);
+ * mode 3: (complex64 state vectors) fused passes whose register phases each run
+ *         as one dense 32 x 32 block on the tensor cores (tcgen05.mma kind::tf32,
+ *         three TF32 products accumulated in FP32); passes of tiles smaller than
+ *         2^13 amplitudes run as in mode 0.  The blocks are rebuilt at the next
+ *         run after bt_plan_set_matrices. */
 int bt_plan_compile(bt_plan* p, int mode);
 /* new matrices for gates already in the plan (variational parameters: the
  * reference's type "f" ops evaluated at new pars, src/struct.jl:518-528):
@@ -334,6 +339,11 @@ int bt_serve_poll(bt_server* s, int64_t ticket, int64_t wait_ms, double* value, 
  * serves several requests) */
 int bt_serve_stats(bt_server* s, int64_t* completed, double* p50_s, double* p99_s, int64_t* resident,
                    uint64_t* hbm_used, int64_t* runs);
+
+/* dense TF32 throughput of the tensor cores (tcgen05.mma kind::tf32, M=128,
+ * N=256, K=8, one CTA per SM issuing `iters` x 4 MMAs): a diagnostic for the
+ * roofline of tensor-core plans (no counterpart in the reference) */
+int bt_tc_tf32_peak(bt_ctx* ctx, int iters, double* tflops);
 
 /* ---------------------------------------------------------------- sampling */
 /* one shot from every member: out[m] drawn from member m's |psi|^2 (or diag rho)

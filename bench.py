@@ -60,9 +60,10 @@ def parse():
                          "in complex128 and the line reports the infidelity and the <Z_i> deviation)")
     ap.add_argument("--autotune", action="store_true",
                     help="plan mode: time the fusion configurations on the state and keep the fastest")
-    ap.add_argument("--workload", default="brickwork", choices=["brickwork", "serve", "c1", "c2", "c3", "vqa"],
+    ap.add_argument("--workload", default="brickwork", choices=["brickwork", "serve", "c1", "c2", "c3", "vqa", "tc"],
                     help="brickwork: 33q c64 depth-30 (default); serve: the serving stream; c1: 12q c128 "
-                         "brickwork + <Z> + shots; c2: 10q noisy density matrix; c3: 20q trajectories")
+                         "brickwork + <Z> + shots; c2: 10q noisy density matrix; c3: 20q trajectories; tc: "
+                         "tensor-core plans against scalar plans on the brickwork and an SU(4) brickwork")
     ap.add_argument("--c3-n", type=int, default=20)
     ap.add_argument("--c3-members", type=int, default=4096)
     ap.add_argument("--c3-twirl", type=int, default=64, help="twirl instances (x3 ZNE scales)")
@@ -71,6 +72,15 @@ def parse():
     ap.add_argument("--lanes", type=int, default=8, help="serving: concurrent lanes (contexts/streams)")
     ap.add_argument("--python-server", action="store_true",
                     help="serving: the Python scheduler instead of the library's bt_serve engine")
+    ap.add_argument("--traj-max-n", type=int, default=14,
+                    help="serving: largest qubit count of the trajectory clients (the configuration's 26 runs "
+                         "their batches on the grouped executor)")
+    ap.add_argument("--sustained", action="store_true",
+                    help="serving: also run at 0.8x the served rate and report that latency")
+    ap.add_argument("--no-serve", dest="serve", action="store_false",
+                    help="headline: skip the serving measurement added to the default line")
+    ap.add_argument("--serve-requests", type=int, default=10000,
+                    help="headline: requests of the serving measurement added to the default line")
     return ap.parse_args()
 
 
@@ -419,9 +429,30 @@ def run_ours(args):
         s128.free()
         del ref
 
+    st.free()
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_baseline(args, args.cpu_seconds)
+    # the metric's serving clause on the same GPU: the configuration's stream at
+    # its offered rate (>= 10^4 requests), then at 0.8x the rate it served
+    serve = None
+    if rank == 0 and ws == 1 and args.serve and plan is not None:
+        try:
+            ctx.synchronize()
+            over = serve_measure(args.seed, args.rate, args.serve_requests, args.lanes)
+            sus = serve_measure(args.seed + 2, 0.8 * over["circuits_per_s"], max(2000, args.serve_requests // 5),
+                                args.lanes, plain=False)
+            serve = {"circuits_per_s": over["circuits_per_s"], "offered_req_per_s": over["offered_req_per_s"],
+                     "requests": over["requests"], "p50_ms": over["p50_ms"], "p99_ms": over["p99_ms"],
+                     "plain_c128_circuits_per_s": over["plain_c128_circuits_per_s"], "vs_plain": over["vs_plain"],
+                     "max_infidelity_c64": over["max_infidelity_c64"],
+                     "max_rel_dev_vs_c128": over["max_rel_dev_vs_c128"],
+                     "sustained": {"offered_req_per_s": sus["offered_req_per_s"],
+                                   "circuits_per_s": sus["circuits_per_s"], "p50_ms": sus["p50_ms"],
+                                   "p99_ms": sus["p99_ms"], "requests": sus["requests"]},
+                     "traj_n_max": over["traj_n_max"], "engine": over["engine"]}
+        except Exception as e:  # the headline stands without it
+            serve = {"error": f"{type(e).__name__}: {e}"[:300]}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
@@ -453,42 +484,47 @@ def run_ours(args):
                 "host_s": host_dt}
         if precision is not None:
             line["precision"] = precision
+        if serve is not None:
+            line["serve"] = serve
         print(json.dumps(line), flush=True)
-    st.free()
     ctx.close()
     if dist is not None:
         dist.destroy_process_group()
 
 
 # ------------------------------------------------------------------ serving workload
-def serve_specs(seed, clients=32):
+def serve_specs(seed, clients=32, traj_max_n=14):
     """The serving mix: 70% state-vector jobs (n ~ U{8..26}), 20% trajectory
-    batches of 64 (n ~ U{8..14}: each member in one CTA's shared memory, the whole
-    batch one launch), 10% density-matrix jobs (n ~ U{8..12}); hardware-efficient
-    ansatz of depth U{4..12}; <H> of 4n random 2-local Pauli terms."""
+    batches of 64 (n ~ U{8..traj_max_n}; up to 14 each member fits one CTA's
+    shared memory and the whole batch is one launch, above that the batch runs on
+    the grouped executor), 10% density-matrix jobs (n ~ U{8..12});
+    hardware-efficient ansatz of depth U{4..12}; <H> of 4n random 2-local Pauli
+    terms."""
     import bluetangle_gpu.serving as S
     rng = np.random.default_rng(seed)
     out = []
     for cid in range(clients):
         kind = rng.choice(["sv", "traj", "dm"], p=[0.7, 0.2, 0.1])
-        n = int(rng.integers(8, 27) if kind == "sv" else (rng.integers(8, 15) if kind == "traj" else rng.integers(8, 13)))
+        n = int(rng.integers(8, 27) if kind == "sv" else
+                (rng.integers(8, traj_max_n + 1) if kind == "traj" else rng.integers(8, 13)))
         out.append(S.make_client(rng, cid, str(kind), n, int(rng.integers(4, 13))))
     return out
 
 
-def run_serve(args):
+def serve_measure(seed, rate, total, lanes=8, native=True, traj_max_n=14, plain=True, checks=True):
+    """One serving run: `total` requests with Poisson arrivals at `rate` req/s from
+    the 32 clients of serve_specs; returns circuits/s, latency percentiles over all
+    requests, service and queueing, and (plain=True) the plain per-call complex128
+    rate on one request per client with the deviation of the served values."""
     import bluetangle_gpu as bt
     import bluetangle_gpu.serving as S
-    specs = serve_specs(args.seed)
-    rng = np.random.default_rng(args.seed + 1)
-    per = max(2, args.steps)
-    total = per * len(specs)
-    arrivals = np.cumsum(rng.exponential(1 / args.rate, total))
+    specs = serve_specs(seed, traj_max_n=traj_max_n)
+    rng = np.random.default_rng(seed + 1)
+    arrivals = np.cumsum(rng.exponential(1 / rate, total))
     owners = rng.integers(0, len(specs), total)
     reqs = [S.Request(i, int(owners[i]), rng.normal(0, 0.3, specs[owners[i]].nparams), seed=7000 + i)
             for i in range(total)]
-    native = not args.python_server
-    srv = (S.NativeServer if native else S.Server)(specs, lanes=args.lanes, prec="c64")
+    srv = (S.NativeServer if native else S.Server)(specs, lanes=lanes, prec="c64")
 
     def wait(r):
         if native:
@@ -527,61 +563,78 @@ def run_serve(args):
         raise errs[0]
     lat = np.array([r.t_done - r.t_submit for r in reqs]) * 1e3
     svc = np.array([r.t_done - r.t_start for r in reqs]) * 1e3
-    service = {k: float(np.mean([s for r, s in zip(reqs, svc) if specs[r.cid].kind == k] or [0]))
-               for k in ("sv", "traj", "dm")}
-    # share of lane time spent running requests over the makespan
-    busy = float(svc.sum() / 1e3 / (args.lanes * (max(r.t_done for r in reqs) - start)))
-    served = total / makespan
+    out = {"offered_req_per_s": rate, "requests": total, "circuits_per_s": total / makespan,
+           "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+           "mean_ms": float(lat.mean()), "mean_service_ms": float(svc.mean()),
+           "mean_queue_ms": float(lat.mean() - svc.mean()),
+           "mean_service_ms_by_kind": {k: float(np.mean([v for r, v in zip(reqs, svc) if specs[r.cid].kind == k]
+                                                       or [0])) for k in ("sv", "traj", "dm")},
+           "lane_busy_frac": float(svc.sum() / 1e3 / (lanes * makespan)),
+           "mix": {k: sum(1 for c in specs if c.kind == k) for k in ("sv", "traj", "dm")},
+           "traj_n_max": max([c.n for c in specs if c.kind == "traj"] or [0]),
+           "engine": "bt_serve (native lanes)" if native else "python Server"}
+    if not plain:
+        return out
     # plain per-call complex128 path on a sample: one request per client, serially
     pctx = bt.Context(0, seed=5)
     sample = [next(r for r in reqs if r.cid == c.cid) for c in specs if any(r.cid == c.cid for r in reqs)]
     t = time.perf_counter()
     plain_vals = [S.plain_request(specs[r.cid], r.theta, r.seed, pctx, prec="c128") for r in sample]
-    plain_rate = len(sample) / (time.perf_counter() - t)
+    out["plain_c128_circuits_per_s"] = len(sample) / (time.perf_counter() - t)
+    out["vs_plain"] = out["circuits_per_s"] / out["plain_c128_circuits_per_s"]
+
     def rel(r, v):
         return abs(r.value - v) / max(1e-12, sum(abs(x[0]) for x in specs[r.cid].terms))
 
-    if native:
-        # trajectory clients drew on the device (Philox keyed by the request seed):
-        # check them against complex128 runs with the same draws
-        dev = max([rel(r, v) for r, v in zip(sample, plain_vals) if specs[r.cid].kind != "traj"] or [0.0])
-        dctx = bt.Context(0, seed=1234)  # the engine's key (NativeServer's seed)
-        dev = max([dev] + [rel(r, S.program_request(specs[r.cid], r.theta, r.seed, dctx))
-                           for r in sample if specs[r.cid].kind == "traj"])
-        dctx.close()
-    else:
-        dev = max(rel(r, v) for r, v in zip(sample, plain_vals))
-    # state infidelity of the served precision (c64 fused plan) against c128 for the sv clients
-    infid = 0.0
-    for c in [c for c in specs if c.kind == "sv"][:6]:
-        th = rng.normal(0, 0.3, c.nparams)
-        a = bt.zero_state(c.n, "c64", ctx=pctx)
-        p = bt.Plan(c.n, "sv", "c64", pctx)
-        for op in S.hea_ops(c.n, c.depth, th):
-            p.add(op)
-        p.compile(True).run(a)
-        b = bt.apply(S.hea_ops(c.n, c.depth, th), bt.zero_state(c.n, "c128", ctx=pctx))
-        # 1 - |<psi64|psi128>|^2 with the complex64 state renormalised in FP64
-        nrm = np.empty(1)
-        a.ctx.check(bt.lib().bt_norm2(a.h, 0, nrm.ctypes.data_as(ctypes.c_void_p)))
-        infid = max(infid, 1 - bt.fidelity(a, b) / nrm[0])
-        a.free()
-        b.free()
+    if checks:
+        if native:
+            # trajectory clients drew on the device (Philox keyed by the request seed):
+            # check them against complex128 runs with the same draws
+            dev = max([rel(r, v) for r, v in zip(sample, plain_vals) if specs[r.cid].kind != "traj"] or [0.0])
+            dctx = bt.Context(0, seed=1234)  # the engine's key (NativeServer's seed)
+            dev = max([dev] + [rel(r, S.program_request(specs[r.cid], r.theta, r.seed, dctx))
+                               for r in sample if specs[r.cid].kind == "traj"])
+            dctx.close()
+        else:
+            dev = max(rel(r, v) for r, v in zip(sample, plain_vals))
+        out["max_rel_dev_vs_c128"] = dev
+        # state infidelity of the served precision (c64 fused plan) against c128
+        infid = 0.0
+        for c in [c for c in specs if c.kind == "sv"][:6]:
+            th = rng.normal(0, 0.3, c.nparams)
+            a = bt.zero_state(c.n, "c64", ctx=pctx)
+            p = bt.Plan(c.n, "sv", "c64", pctx)
+            for op in S.hea_ops(c.n, c.depth, th):
+                p.add(op)
+            p.compile(True).run(a)
+            b = bt.apply(S.hea_ops(c.n, c.depth, th), bt.zero_state(c.n, "c128", ctx=pctx))
+            # 1 - |<psi64|psi128>|^2 with both states' norms in FP64
+            na, nb = np.empty(1), np.empty(1)
+            a.ctx.check(bt.lib().bt_norm2(a.h, 0, na.ctypes.data_as(ctypes.c_void_p)))
+            b.ctx.check(bt.lib().bt_norm2(b.h, 0, nb.ctypes.data_as(ctypes.c_void_p)))
+            infid = max(infid, 1 - bt.fidelity(a, b) / (na[0] * nb[0]))
+            a.free()
+            b.free()
+        out["max_infidelity_c64"] = infid
     pctx.close()
-    line = {"metric": "served circuits/s", "value": served, "unit": "circuits/s", "n_gpus": 1, "steps": per,
-            "warmup": 1, "ms_per_step": makespan * 1e3 / per, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-            "config": {"workload": f"serving-{len(specs)}clients-poisson{args.rate:g}",
-                       "mix": {k: sum(1 for c in specs if c.kind == k) for k in ("sv", "traj", "dm")},
-                       "requests": total, "lanes": args.lanes,
-                       "engine": "bt_serve (native lanes)" if native else "python Server"},
-            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
-                           "mean": float(lat.mean())},
-            "mean_service_ms_by_kind": service, "lane_busy_frac": busy,
-            "mean_queue_ms": float(lat.mean() - svc.mean()),
-            "plain_c128_circuits_per_s": plain_rate, "vs_plain": served / plain_rate,
-            "max_rel_dev_vs_c128": dev, "max_infidelity_c64": infid,
-            "roofline": None, "cpu_baseline": None, "e2e": None, "gpu_launches": None}
+    return out
+
+
+def run_serve(args):
+    """The serving stream alone: args.rate offered, max(2, steps) requests per
+    client, and (--sustained) a second run at 0.8x the served rate for the latency
+    of a load the engine sustains."""
+    per = max(2, args.steps)
+    res = serve_measure(args.seed, args.rate, per * 32, args.lanes, not args.python_server, args.traj_max_n)
+    line = {"metric": "served circuits/s", "value": res["circuits_per_s"], "unit": "circuits/s", "n_gpus": 1,
+            "steps": per, "warmup": 1, "ms_per_step": 1e3 / res["circuits_per_s"] * 32, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+            "config": {"workload": f"serving-32clients-poisson{args.rate:g}", "requests": per * 32,
+                       "lanes": args.lanes, "traj_n_max": res["traj_n_max"]},
+            "serve": res, "roofline": None, "cpu_baseline": None, "e2e": None, "gpu_launches": None}
+    if args.sustained:
+        line["serve_sustained"] = serve_measure(args.seed + 2, 0.8 * res["circuits_per_s"], per * 32, args.lanes,
+                                                not args.python_server, args.traj_max_n, plain=False)
     print(json.dumps(line), flush=True)
 
 
@@ -1017,13 +1070,69 @@ def run_vqa(args):
     ctx.close()
 
 
+def run_tc(args):
+    """Tensor-core fused passes (every register phase a dense 32 x 32 block on
+    tcgen05, three TF32 products) against the scalar fused passes, complex64, on
+    the random brickwork and on a brickwork of Haar-random two-qubit unitaries,
+    both depth 30 at args.n qubits (default 30 here).  A step is one circuit.
+    Reports gate-apps/s of both forms, the tensor work per circuit against the
+    TF32 throughput measured on this GPU (bt_tc_tf32_peak), and the HBM fraction."""
+    import bluetangle_gpu as bt
+    import bluetangle_gpu.circuits as C
+    n = args.n if args.n != 33 else 30
+    ctx = bt.Context(0, seed=args.seed)
+    bt.Context._default = ctx
+    P = ctypes.c_void_p
+    peak_tf = ctypes.c_double(0)
+    ctx.check(bt.lib().bt_tc_tf32_peak(ctx.h, 4000, ctypes.byref(peak_tf)))
+    st = bt.zero_state(n, "c64", 1, ctx)
+    hbm, hkind = measured_peak()
+    cases = {}
+    for kind in ("brickwork", "su4"):
+        rng = np.random.default_rng(args.seed)
+        ops = C.brickwork(n, args.depth, rng) if kind == "brickwork" else C.su4_brickwork(n, args.depth, rng)
+        for tc in (False, True):
+            plan = bt.Plan(n, "sv", "c64", ctx)
+            for op in ops:
+                plan.add(op)
+            plan.compile(tensor_cores=tc)
+            ms, host, launches, clk = _timed(ctx, lambda i: plan.run(st), args.steps, args.warmup)
+            stt = plan.stats()
+            per = ms / args.steps
+            case = {"ms_per_circuit": per, "gate_apps_per_s": len(ops) / (per / 1e3), "gates": len(ops),
+                    "passes": stt["passes"], "phases": stt["phases"],
+                    "hbm_frac": stt["passes"] * 2 * (2 ** n) * 8 / (per / 1e3) / (hbm * 1e9), "clocks": clk,
+                    "gpu_launches": launches}
+            if tc:
+                # 48 MMAs of 128 x 64 x 8 per phase of a 2^13-amplitude tile
+                tiles = 2 ** (n - 13)
+                flops = stt["phases"] * tiles * 48 * 2 * 128 * 64 * 8
+                case["tensor_tflops"] = flops / (per / 1e3) / 1e12
+                case["tensor_frac_of_tf32_peak"] = case["tensor_tflops"] / peak_tf.value
+            cases[f"{kind}_{'tc' if tc else 'scalar'}"] = case
+    for kind in ("brickwork", "su4"):
+        cases[f"{kind}_tc_speedup"] = cases[f"{kind}_scalar"]["ms_per_circuit"] / cases[f"{kind}_tc"]["ms_per_circuit"]
+    head = cases["su4_tc"]
+    line = {"metric": "gate-apps/s", "value": head["gate_apps_per_s"], "unit": "gate-apps/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_circuit"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64 (3xTF32 tensor cores)",
+            "data": "synthetic",
+            "config": {"workload": f"su4-brickwork-{n}q-depth{args.depth} (tensor-core plan; + brickwork)",
+                       "l2": "state larger than L2, no flush needed", "cases": cases},
+            "tf32_peak_tflops_measured": peak_tf.value, "hbm_peak_gbs": hbm, "hbm_peak_kind": hkind,
+            "gpu_launches": head["gpu_launches"], "clocks": head["clocks"]}
+    print(json.dumps(line), flush=True)
+    st.free()
+    ctx.close()
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
     elif a.workload == "serve":
         run_serve(a)
-    elif a.workload in ("c1", "c2", "c3", "vqa"):
-        {"c1": run_c1, "c2": run_c2, "c3": run_c3, "vqa": run_vqa}[a.workload](a)
+    elif a.workload in ("c1", "c2", "c3", "vqa", "tc"):
+        {"c1": run_c1, "c2": run_c2, "c3": run_c3, "vqa": run_vqa, "tc": run_tc}[a.workload](a)
     else:
         run_ours(a)

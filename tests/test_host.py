@@ -1,6 +1,7 @@
 """Host-side mirror of the reference interface: gate table, noise tables, op
 descriptors, twirl frames.  CPU only (no kernels)."""
 import math
+import os
 
 import numpy as np
 import pytest
@@ -254,3 +255,18 @@ def test_paramshift_member_matrices():
     mm = paramshift_member_mats(base, var, shifted, owner, range(7))
     firsts = [[float(m[0, 0]) for m in member] for member in mm]
     assert firsts == [[1, 2], [10, 2], [11, 2], [1, 20], [1, 21], [1, 30], [1, 31]]
+
+
+def test_reference_arm_maps_no_engine_library():
+    """bench.py's reference arm builds its circuit with the host-only generator and
+    times the oracle: the process maps no libbtgpu.so (the package loads the
+    library at its first engine call, not at import)."""
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = ("import sys; sys.path.insert(0, sys.argv[1]); import bench; bench.layers_of(10, 4, 1); "
+            "import bluetangle_gpu, bluetangle_gpu.circuits; "
+            "maps = open('/proc/self/maps').read(); print('MAPPED' if 'libbtgpu' in maps else 'CLEAN')")
+    r = subprocess.run([sys.executable, "-c", code, root], capture_output=True, text=True, timeout=300, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.strip().endswith("CLEAN"), r.stdout

@@ -18,6 +18,7 @@
 #include <stdio.h>
 #include <string.h>
 #include <sys/stat.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <functional>
@@ -45,6 +46,7 @@ struct Nvrtc {
   nvrtcResult_t (*log_size)(nvrtcProgram_t, size_t*);
   nvrtcResult_t (*log)(nvrtcProgram_t, char*);
   nvrtcResult_t (*destroy)(nvrtcProgram_t*);
+  nvrtcResult_t (*version)(int*, int*) = nullptr;  // optional: part of the cubin cache key
 };
 
 static Nvrtc* nvrtc() {
@@ -63,6 +65,7 @@ static Nvrtc* nvrtc() {
     n.log_size = (decltype(n.log_size))dlsym(h, "nvrtcGetProgramLogSize");
     n.log = (decltype(n.log))dlsym(h, "nvrtcGetProgramLog");
     n.destroy = (decltype(n.destroy))dlsym(h, "nvrtcDestroyProgram");
+    n.version = (decltype(n.version))dlsym(h, "nvrtcVersion");
     n.ok = n.create && n.compile && n.cubin_size && n.cubin && n.log_size && n.log && n.destroy;
   });
   return n.ok ? &n : nullptr;
@@ -1363,9 +1366,26 @@ static std::string cache_dir() {
 
 static const char* kOpts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-default-device"};
 
-// compiles one source to a cubin (disk cache keyed by the source hash); "" on success
+// what besides the source decides a cubin: the compile options, the NVRTC and the
+// driver versions (a cubin built by an older toolkit is not reused after an upgrade)
+static const std::string& cache_salt() {
+  static const std::string salt = [] {
+    std::string k = "btk-cache-v2";
+    for (const char* o : kOpts) k += std::string("|") + o;
+    int ma = 0, mi = 0, drv = 0;
+    if (Nvrtc* nv = nvrtc())
+      if (nv->version) nv->version(&ma, &mi);
+    cudaDriverGetVersion(&drv);
+    k += "|nvrtc" + std::to_string(ma) + "." + std::to_string(mi) + "|driver" + std::to_string(drv);
+    return k;
+  }();
+  return salt;
+}
+
+// compiles one source to a cubin (disk cache keyed by the source, the options and
+// the NVRTC / driver versions); "" on success
 static std::string compile_cubin(const std::string& code, std::vector<char>& cubin) {
-  const std::string path = cache_dir() + "/btk_" + std::to_string(fnv1a(code + kOpts[0])) + ".cubin";
+  const std::string path = cache_dir() + "/btk_" + std::to_string(fnv1a(cache_salt() + "\n" + code)) + ".cubin";
   if (FILE* fd = fopen(path.c_str(), "rb")) {
     fseek(fd, 0, SEEK_END);
     long sz = ftell(fd);
@@ -1391,7 +1411,9 @@ static std::string compile_cubin(const std::string& code, std::vector<char>& cub
   cubin.resize(cs);
   nv->cubin(prog, cubin.data());
   nv->destroy(&prog);
-  const std::string tmp = path + ".tmp" + std::to_string((uint64_t)(uintptr_t)&cubin);
+  // a name no other process or thread writes: the pid and the thread's id
+  const std::string tmp = path + ".tmp" + std::to_string((long long)getpid()) + "_" +
+                          std::to_string(std::hash<std::thread::id>()(std::this_thread::get_id()));
   if (FILE* fd = fopen(tmp.c_str(), "wb")) {  // write-then-rename: concurrent processes never read a partial file
     fwrite(cubin.data(), 1, cubin.size(), fd);
     fclose(fd);

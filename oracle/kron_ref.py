@@ -99,40 +99,58 @@ def cp(lam):
 # src/noise.jl:52-131
 
 
+# Written from the channels' definitions, independently of the engine's table:
+# Pauli channels as weights over (I, X, Y, Z) with K = sqrt(w) sigma; the two
+# damping channels from their action on |1>; the coherent errors as the rotation
+# generators exp(-i theta sigma / 2).  The reference's quirks are part of the
+# definitions: `model == :phase_flip` compares a String with a Symbol, so
+# phase_flip uses Y like bit_phase_flip (src/noise.jl:78-81); rot_xyz divides the
+# three rotations by sqrt(3) (src/noise.jl:117); two-qubit channels are all
+# ordered kron pairs of the one-qubit set (src/noise.jl:126).
+_PAULI_WEIGHTS = {
+    "bit_flip": lambda p: {"I": 1 - p, "X": p},
+    "phase_flip": lambda p: {"I": 1 - p, "Y": p},
+    "bit_phase_flip": lambda p: {"I": 1 - p, "Y": p},
+    "depolarizing": lambda p: {"I": 1 - p, "X": p / 3, "Y": p / 3, "Z": p / 3},
+    "depolarizing_amp": lambda p: {"I": 1 - 3 * p / 4, "X": p / 4, "Y": p / 4, "Z": p / 4},
+}
+
+
+def _rot(axis, theta):
+    s = {"X": GATE["X"], "Y": GATE["Y"], "Z": GATE["Z"]}[axis]
+    return math.cos(theta / 2) * np.eye(2) - 1j * math.sin(theta / 2) * s
+
+
 def noise_model(model, p, two_qubit=False):
     model = model.lower()
-    I, X, Y, Z = GATE["I"], GATE["X"], GATE["Y"], GATE["Z"]
-    if model == "amplitude_damping":
-        ops = [np.array([[1.0, 0], [0, math.sqrt(1 - p)]], dtype=complex),
-               np.array([[0, math.sqrt(p)], [0, 0]], dtype=complex)]
-    elif model == "phase_damping":
-        ops = [np.array([[1.0, 0], [0, math.sqrt(1 - p)]], dtype=complex),
-               np.array([[0, 0], [0, math.sqrt(p)]], dtype=complex)]
-    elif model in ("phase_flip", "bit_flip", "bit_phase_flip"):
-        # `model == :phase_flip` compares a String with a Symbol and is never
-        # true, so phase_flip yields Y (src/noise.jl:78-81).
-        ops = [math.sqrt(1 - p) * I, math.sqrt(p) * (X if model == "bit_flip" else Y)]
-    elif model == "depolarizing_amp":
-        ops = [math.sqrt(1 - 3 * p / 4) * I, math.sqrt(p / 4) * X, math.sqrt(p / 4) * Y, math.sqrt(p / 4) * Z]
-    elif model == "depolarizing":
-        ops = [math.sqrt(1 - p) * I, math.sqrt(p / 3) * X, math.sqrt(p / 3) * Y, math.sqrt(p / 3) * Z]
-    elif model == "rot_z":
-        ops = [rz(p)]
-    elif model == "rot_y":
-        ops = [ry(p)]
-    elif model == "rot_x":
-        ops = [rx(p)]
+    if model in _PAULI_WEIGHTS:
+        ops = [math.sqrt(w) * GATE[name] for name, w in _PAULI_WEIGHTS[model](p).items()]
+    elif model in ("amplitude_damping", "phase_damping"):
+        keep = np.diag([1.0, math.sqrt(1 - p)])  # no-jump: |1> shrinks by sqrt(1 - gamma)
+        jump = np.zeros((2, 2))
+        if model == "amplitude_damping":
+            jump[0, 1] = math.sqrt(p)  # |1> -> |0>
+        else:
+            jump[1, 1] = math.sqrt(p)  # |1> -> |1>, phase information lost
+        ops = [keep, jump]
+    elif model in ("rot_x", "rot_y", "rot_z"):
+        ops = [_rot(model[-1].upper(), p)]
     elif model == "rot_p":
-        ops = [phase(p)]
+        ops = [np.diag([1.0, np.exp(1j * p)])]
     elif model == "rot_xyz":
-        ops = [rx(p) / math.sqrt(3), ry(p) / math.sqrt(3), rz(p) / math.sqrt(3)]
+        ops = [_rot(a, p) / math.sqrt(3) for a in "XYZ"]
     elif model in ("mz", "m(z)", "mx", "m(x)", "my", "m(y)", "mr", "m(r)"):
-        ops = [GATE["P0"].copy(), GATE["P1"].copy()]
+        ops = [np.diag([1.0, 0.0]), np.diag([0.0, 1.0])]
     else:
         raise ValueError("Unknown quantum error model")
+    ops = [np.asarray(o, dtype=complex) for o in ops]
     if not two_qubit:
         return ops
-    return [np.kron(a, b) for a in ops for b in ops]
+    out = []
+    for a in ops:
+        for b in ops:
+            out.append(np.einsum("ij,kl->ikjl", a, b).reshape(4, 4))
+    return out
 
 
 # ---------------------------------------------------------------- hilbert

@@ -27,8 +27,13 @@ def test_noise_tables_and_quirks(kref):
     for model in ("amplitude_damping", "phase_damping", "bit_flip", "phase_flip", "bit_phase_flip",
                   "depolarizing", "depolarizing_amp", "rot_x", "rot_y", "rot_z", "rot_p", "rot_xyz", "MZ"):
         for two in (False, True):
+            # kron_ref builds each set from the channel's definition (Pauli weights,
+            # damping actions, rotation generators), independently of noise.py: equal
+            # up to the last bit of the trigonometric forms
             a, b = noise_model(model, 0.13, two), kref.noise_model(model, 0.13, two)
-            assert len(a) == len(b) and all(np.array_equal(x, y) for x, y in zip(a, b)), model
+            assert len(a) == len(b) and all(np.allclose(x, y, rtol=0, atol=2e-16) for x, y in zip(a, b)), model
+            s = sum(k.conj().T @ k for k in a)
+            assert np.allclose(s, np.eye(s.shape[0]), atol=1e-14), model  # trace preserving
     # phase_flip yields Y (src/noise.jl:78-81); 2-qubit depolarizing is a 16-term product channel
     assert np.array_equal(noise_model("phase_flip", 0.25)[1], 0.5 * np.array([[0, -1j], [1j, 0]]))
     assert len(noise_model("depolarizing", 0.1, True)) == 16

@@ -895,51 +895,64 @@ def run_c3(args):
     frame_rng = np.random.default_rng(args.seed + 11)
     zne = [k % 3 for k in range(ncopy)]
 
-    st = bt.zero_state(n, "c64", B, ctx)
-    cp = bt.zero_state(n, "c64", ncopy, ctx) if ncopy else None
-    counts = {"ops": 0}
-    pre = [step_slots() for _ in range(args.warmup + args.steps)]
-    pre_c = []
-    if cp is not None:
-        for _ in range(args.warmup + args.steps):
+    # trajectories and copies are one batch of B + ncopy members: each step's
+    # slots hold the trajectories' ops (members [0, B)) and then the copies' ops
+    # (members [B, B + ncopy)), the other group idle there
+    tot = B + ncopy
+    groups = []
+    for _ in range(args.warmup + args.steps):
+        g = [(step_slots(), B)]
+        if ncopy:
             mo = T.member_programs([copy_step], n, ncopy, zne_ids=zne, twirl=True, frame_rng=frame_rng,
                                    measure_prob=0.1, measure_rng=mrng)
-            pre_c.append(T.build_slots(mo, noise))
+            g.append((T.build_slots(mo, noise), ncopy))
+        groups.append(g)
+    pre = [T.concat_slots(*g) for g in groups]
 
     def member_ops(slots):
         return sum(sum(1 for it in s.items if it is not None) for s in slots)
 
-    progs = progs_c = None
+    progs = None
     if args.c3_engine == "program":
-        # each step's slots compiled into a program (grouped executor: the members
-        # exceed shared memory), built before the timed region like the slots
-        progs = [T.compile_program(sl, n, B, "c64", ctx)[0] for sl in pre]
-        progs_c = [T.compile_program(sl, n, ncopy, "c64", ctx)[0] for sl in pre_c]
+        # each step's slots compiled into one program over the whole batch (grouped
+        # executor: the members exceed shared memory), built before the timed region
+        st = bt.zero_state(n, "c64", tot, ctx)
+        progs = [T.compile_program(sl, n, tot, "c64", ctx)[0] for sl in pre]
+    else:
+        # the lock-step engine launches over a whole batch per op: the trajectories
+        # and the copies keep a batch each
+        sts = [bt.zero_state(n, "c64", b, ctx) for _, b in groups[0]]
+        st = sts[0]
 
     def step(i):
         if progs is not None:
             progs[i].run(st, seed=1000 + i, records=False)
-            if cp is not None:
-                progs_c[i].run(cp, seed=5000 + i, records=False)
-            return
-        T.run_slots(st, pre[i], records=False)
-        if cp is not None:
-            T.run_slots(cp, pre_c[i], records=False)
+        else:
+            for (sl, _), s_ in zip(groups[i], sts):
+                T.run_slots(s_, sl, records=False)
 
     ms, host, launches, clk = _timed(ctx, step, args.steps, args.warmup)
-    timed_ops = sum(member_ops(pre[i]) + (member_ops(pre_c[i]) if pre_c else 0)
-                    for i in range(args.warmup, args.warmup + args.steps))
-    # algorithmic HBM bytes of the main batch per step: a gate pass reads and
-    # writes every member; a channel adds a reduction read unless it is a unitary
-    # mixture (depolarizing); a measurement reads once and rewrites (collapse)
-    S = B * (2 ** n) * 8
-    ngates = sum(1 for s in base if s.kind == "gate")
-    nch = sum(1 for s in base if s.kind == "channel")
-    nad = sum(1 for op in step_ops if isinstance(op, bt.OpQC) and op.name == "amplitude_damping")
-    bytes_step = ngates * 2 * S + nch * 2 * S + nad * S + n * (S + 2 * S)
-    if progs is not None:  # what the grouped executor moves (per group: reduction read + apply)
-        bytes_step = float(np.mean([T.grouped_bytes(pre[i], n, B, "c64")
-                                    for i in range(args.warmup, args.warmup + args.steps)]))
+    timed = range(args.warmup, args.warmup + args.steps)
+    timed_ops = sum(member_ops(pre[i]) for i in timed)
+    # algorithmic HBM bytes per step: per op pass (slots engine) a gate reads and
+    # writes every member it acts on, a channel adds a reduction read unless it is
+    # a unitary mixture, a measurement reads once and rewrites (collapse); the
+    # grouped executor moves, per group of ops within two qubits, a reduction read
+    # (when a decision needs one) and one read and write of each acting member
+    if progs is not None:
+        bytes_step = float(np.mean([T.grouped_bytes(pre[i], n, tot, "c64") for i in timed]))
+    else:
+        S1 = (2 ** n) * 8
+
+        def slot_bytes(sl):
+            k = sum(1 for it in sl.items if it is not None) * S1
+            if sl.kind == "gate":
+                return 2 * k
+            live = next(it for it in sl.items if it is not None)
+            if sl.kind == "channel":
+                return 2 * k + (0 if T._unitary_mix(live[0]) else k)
+            return 3 * k
+        bytes_step = float(np.mean([sum(slot_bytes(sl) for sl in pre[i]) for i in timed]))
     zs = bt.expect(st, "Z", member=-1)
     assert np.all(np.isfinite(zs))
     cpu = None
@@ -974,7 +987,9 @@ def run_c3(args):
     line = {"metric": "trajectory op-apps/s", "value": value, "unit": "member-ops/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-            "config": {"workload": f"tfim-{n}q-{B}traj+{ncopy}twirl/zne-copies", "members": B + ncopy,
+            "config": {"workload": f"tfim-{n}q-{B}traj+{ncopy}twirl/zne-copies", "members": tot,
+                       "launch": ("trajectories and copies in one program per step (member ranges)"
+                                  if progs is not None else "trajectories and copies as two batches"),
                        "step": "one Trotter step of every member (40 make the circuit)",
                        "ops_per_member_step": len(step_ops), "l2": f"states ({(B + ncopy) * 2 ** n * 8 / 2**30:.1f} GiB) larger than L2",
                        "engine": ("programs, grouped executor (ops within two qubits decided from one reduced "
@@ -983,7 +998,8 @@ def run_c3(args):
             "trajectory_steps_per_s": (B + ncopy) * args.steps / (ms / 1e3),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind, "traffic": None,
-                         "bytes_per_step_main_batch": bytes_step, "note": "algorithmic bytes of the main batch"},
+                         "bytes_per_step": bytes_step,
+                         "note": "algorithmic bytes of the whole batch (trajectories and copies)"},
             "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clk, "host_s": host}
     print(json.dumps(line), flush=True)
     ctx.close()

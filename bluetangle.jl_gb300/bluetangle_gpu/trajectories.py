@@ -84,6 +84,53 @@ def _op_slots(op, noise):
     return [("gate", (op.mat, qs, ctrls))] + [("channel", c) for c in _noise_ops(op, noise)]
 
 
+def explicit_noise(member_ops, noise):
+    """member_ops with the channels a NoiseModel adds after each noisy op written
+    out as OpQC ops (src/hilbert.jl:322-340), so that members built under
+    different noise settings can share one batch (build_slots(..., noise=False))."""
+    out = []
+    for segs in member_ops:
+        row = []
+        for seg in segs:
+            s2 = []
+            for op in seg:
+                s2.append(op)
+                if not isinstance(op, OpQC) and op.type != "🔬":  # as _op_slots: none after measurements
+                    for kraus, qs in _noise_ops(op, noise):
+                        s2.append(OpQC("noise", kraus, qs[0], qs[1] if len(qs) == 2 else -1))
+            row.append(s2)
+        out.append(row)
+    return out
+
+
+def concat_members(*groups):
+    """One batch from groups of members with different op sequences: each group's
+    segments stay in order and every other group gets empty segments there, so
+    at every slot the members of the other groups are idle (identity gates,
+    skipped channels and measurements) and the whole batch runs as one program."""
+    nseg = [len(g[0]) if g else 0 for g in groups]
+    out = []
+    for gi, g in enumerate(groups):
+        before, after = sum(nseg[:gi]), sum(nseg[gi + 1:])
+        for segs in g:
+            out.append([[] for _ in range(before)] + list(segs) + [[] for _ in range(after)])
+    return out
+
+
+def concat_slots(*groups):
+    """One slot list over the members of several groups, given as (slots, batch)
+    pairs: each group's slots in order, the other groups' members idle (None) in
+    them, so that compile_program gives each slot its group's member range."""
+    out = []
+    total = sum(b for _, b in groups)
+    lo = 0
+    for slots, b in groups:
+        for sl in slots:
+            out.append(Slot(sl.kind, [None] * lo + list(sl.items) + [None] * (total - lo - b)))
+        lo += b
+    return out
+
+
 def build_slots(member_ops, noise=False):
     """Aligns per-member op sequences into lock-step slots.  member_ops[m] is a list
     of segments (one per circuit position), each a list of ops for that member;
@@ -213,6 +260,7 @@ class Program:
         self.h = h
         self.nops = 0
         self.rec_masks = []  # per record slot: bool per member, True where the member is measured
+        self._range = (0, batch)
 
     def __del__(self):
         try:
@@ -221,6 +269,12 @@ class Program:
                 self.h = None
         except Exception:
             pass
+
+    def set_range(self, lo=0, hi=-1):
+        """Ops added next act on members [lo, hi) only (bt_program_set_range)."""
+        self.ctx.check(L.lib().bt_program_set_range(self.h, int(lo), int(hi)))
+        self._range = (lo, self.batch if hi < 0 else hi)
+        return self
 
     def add_gate(self, mats, qubits):
         """mats: one matrix, or batch matrices (per member) as a list or a
@@ -258,7 +312,10 @@ class Program:
     def add_measure(self, qubit, skip=None):
         sk = None if skip is None else _i32(skip)
         self.ctx.check(L.lib().bt_program_add_measure(self.h, int(qubit), _ptr(sk)))
-        self.rec_masks.append(np.ones(self.batch, bool) if skip is None else ~np.asarray(skip, bool))
+        mask = np.ones(self.batch, bool) if skip is None else ~np.asarray(skip, bool)
+        mask[:self._range[0]] = False
+        mask[self._range[1]:] = False
+        self.rec_masks.append(mask)
         self.nops += 1
         return self.nops - 1
 
@@ -328,7 +385,15 @@ def grouped_bytes(slots, n, batch, prec="c64"):
             q, need, act = [], False, np.zeros(batch, dtype=bool)
         q = sorted(set(q) | set(qs))
         if sl.kind == "gate":
-            act[:] = True
+            on = [i for i, it in enumerate(sl.items) if it is not None]
+            sub = sl.items[on[0]:on[-1] + 1]
+            if _same_gate(sub):  # one matrix for the range: every member in it acts
+                act[on[0]:on[-1] + 1] = True
+            else:  # per-member matrices: idle members and exact identities are passed over
+                for i in on:
+                    mat = np.asarray(sl.items[i][0])
+                    if not np.array_equal(mat, np.eye(mat.shape[0])):
+                        act[i] = True
         else:
             act |= np.array([it is not None for it in sl.items])
             if sl.kind == "measure" or not _unitary_mix(live[0][0]):
@@ -361,12 +426,27 @@ def compile_program(slots, n, batch, prec="c64", ctx=None, unitary_mix=True):
     the program op index of slot i (gates only, else None)."""
     prog = Program(n, batch, prec, ctx)
     gate_ops = []
+    cur = (0, batch)
     for sl in slots:
         items = sl.items
-        live = [it for it in items if it is not None]
-        if not live:
+        on = [i for i, it in enumerate(items) if it is not None]
+        if not on:
             gate_ops.append(None)
             continue
+        # the slot's ops act on the members between its first and last live one;
+        # members outside idle there (groups of members concatenated into one batch)
+        rng_ = (on[0], on[-1] + 1)
+        if rng_ != cur:
+            prog.set_range(rng_[0], rng_[1] if rng_[1] < batch else -1)
+            cur = rng_
+        items = items[rng_[0]:rng_[1]]
+        live = [it for it in items if it is not None]
+        full_range = len(live) == len(items)
+
+        def skip_of():  # skip table over the whole batch (the range bounds it already)
+            return None if full_range else [0] * rng_[0] + [0 if it is not None else 1 for it in items] + \
+                [0] * (batch - rng_[1])
+
         if sl.kind == "gate":
             def full(it):
                 mat, qs, ctrls = it
@@ -385,20 +465,19 @@ def compile_program(slots, n, batch, prec="c64", ctx=None, unitary_mix=True):
             if any(it[1] != qs or (it[0] is not kraus and not all(np.array_equal(a, b) for a, b in zip(it[0], kraus)))
                    for it in live):
                 raise ValueError("members disagree on the channel at one position")
-            skip = None if len(live) == batch else [0 if it is not None else 1 for it in items]
-            prog.add_channel(kraus, list(qs), skip, unitary_mix and _unitary_mix(kraus))
+            prog.add_channel(kraus, list(qs), skip_of(), unitary_mix and _unitary_mix(kraus))
             gate_ops.append(None)
         else:
             name, qubit = live[0]
             up = name.upper()
             rot = None if up in ("MZ", "M(Z)") else (gate["H"] if up in ("MX", "M(X)") else gate["HSP"])
-            skip = None if len(live) == batch else [0 if it is not None else 1 for it in items]
-            if rot is not None:
-                prog.add_gate(rot if skip is None else [rot if not s else _ID2 for s in skip], [qubit])
-            prog.add_measure(qubit, skip)
+            skip = skip_of()
             if rot is not None:
                 rd = rot.conj().T
-                prog.add_gate(rd if skip is None else [rd if not s else _ID2 for s in skip], [qubit])
+                prog.add_gate(rot if full_range else [rot if it is not None else _ID2 for it in items], [qubit])
+            prog.add_measure(qubit, skip)
+            if rot is not None:
+                prog.add_gate(rd if full_range else [rd if it is not None else _ID2 for it in items], [qubit])
             gate_ops.append(None)
     return prog, gate_ops
 

@@ -33,6 +33,7 @@ struct PGOp {
   int skip_off;    // offset into the skip table (one byte per member), -1: none
   int rand_idx;    // index of this op's draw, -1: none
   int rec_idx;     // measurement: record slot
+  int mlo, mhi;    // members [mlo, mhi) take part; per-member matrices are indexed from mlo
 };
 
 // A group of consecutive ops acting inside one set Q of at most two qubits (the
@@ -46,6 +47,7 @@ struct PGGroup {
   int q0, q1;    // bit positions, q0 = most significant bit of the group index
   int op0, nop;  // ops [op0, op0 + nop)
   int need_rho;  // some op's decision depends on the state
+  int mlo, mhi;  // members [mlo, mhi) hold every member active in the group (launch range)
 };
 
 struct bt_program {
@@ -62,6 +64,7 @@ struct bt_program {
   std::vector<double> km;   // Kraus sets, row-major interleaved FP64
   std::vector<int8_t> skip;
   int ndraws = 0, nrec = 0;
+  int range_lo = 0, range_hi = -1;  // member range of the ops added next (-1: to the batch's end)
   // device copies
   bool uploaded = false;
   bool gm_dirty = false;     // gate matrices rewritten since the upload
@@ -250,15 +253,15 @@ __global__ void __launch_bounds__(PG_THREADS) k_program(typename CT<R>::T* __res
   __syncthreads();
   for (int oi = 0; oi < nops; ++oi) {
     const PGOp op = ops[oi];
-    if (op.skip_off >= 0 && skip[op.skip_off + m]) {  // uniform across the block
+    if (m < op.mlo || m >= op.mhi || (op.skip_off >= 0 && skip[op.skip_off + m])) {  // uniform across the block
       if (op.type == PG_MEASURE && threadIdx.x == 0) rec[(int64_t)m * nrec + op.rec_idx] = -1;
       continue;
     }
     if (op.type == PG_GATE1) {
-      apply1<R>(st, nbits, op.b0, gm + op.moff + (int64_t)op.mstride * m);
+      apply1<R>(st, nbits, op.b0, gm + op.moff + (int64_t)op.mstride * (m - op.mlo));
       __syncthreads();
     } else if (op.type == PG_GATE2) {
-      apply2<R>(st, nbits, op.b0, op.b1, gm + op.moff + (int64_t)op.mstride * m);
+      apply2<R>(st, nbits, op.b0, op.b1, gm + op.moff + (int64_t)op.mstride * (m - op.mlo));
       __syncthreads();
     } else if (op.type == PG_CHANNEL) {
       const int D = 1 << op.k;
@@ -443,18 +446,19 @@ __global__ void k_group_decide(const PGGroup g, const PGOp* __restrict__ ops, co
                                const int8_t* __restrict__ act, const double* __restrict__ u, uint64_t key,
                                uint64_t stream, int batch, const double* __restrict__ rho_in, R* __restrict__ mat_out,
                                int32_t* __restrict__ rec, int nrec, int* __restrict__ status) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= batch) return;
+  const int m = g.mlo + blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= g.mhi) return;
   const int D = 1 << g.nb;
   const bool on = act[m];
   double M[32], rho[32], E[32], t[32], K[32], rop[32];
   for (int e = 0; e < 2 * D * D; ++e) {
     M[e] = (e % (2 * D + 2)) == 0 ? 1.0 : 0.0;
-    rho[e] = g.need_rho && on ? rho_in[(int64_t)m * 32 + e] : 0.0;
+    // the reduction's layout: 2 D^2 reals per member, from the group's first member
+    rho[e] = g.need_rho && on ? rho_in[(int64_t)(m - g.mlo) * 2 * D * D + e] : 0.0;
   }
   for (int oi = g.op0; oi < g.op0 + g.nop; ++oi) {
     const PGOp op = ops[oi];
-    const bool skipped = !on || (op.skip_off >= 0 && skip[op.skip_off + m]);
+    const bool skipped = !on || m < op.mlo || m >= op.mhi || (op.skip_off >= 0 && skip[op.skip_off + m]);
     if (skipped) {
       if (op.type == PG_MEASURE) rec[(int64_t)m * nrec + op.rec_idx] = -1;
       continue;
@@ -462,7 +466,7 @@ __global__ void k_group_decide(const PGGroup g, const PGOp* __restrict__ ops, co
     const int opk = op.type == PG_GATE2 ? 2 : (op.type == PG_CHANNEL ? op.k : 1);
     const int d = 1 << opk;
     if (op.type == PG_GATE1 || op.type == PG_GATE2) {
-      const R* src = gm + op.moff + (int64_t)op.mstride * m;
+      const R* src = gm + op.moff + (int64_t)op.mstride * (m - op.mlo);
       for (int e = 0; e < 2 * d * d; ++e) K[e] = (double)src[e];
     } else if (op.type == PG_CHANNEL) {
       const bool umix = op.flags & 2;
@@ -552,14 +556,26 @@ int bt_program_free(bt_program* p) {
   return BT_OK;
 }
 
+int bt_program_set_range(bt_program* p, int64_t lo, int64_t hi) {
+  if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "program is NULL");
+  if (hi < 0) hi = p->batch;
+  if (lo < 0 || lo >= hi || hi > p->batch) return bt_fail(p->ctx, BT_ERR_BAD_ARG, "member range outside the batch");
+  p->range_lo = (int)lo;
+  p->range_hi = (int)hi;
+  return BT_OK;
+}
+
 int bt_program_add_gate(bt_program* p, int k, const int32_t* qubits, const double* mats, int per_member) {
   if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "program is NULL");
   int rc = prog_qubits(p, k, qubits);
   if (rc) return rc;
   if (!mats) return bt_fail(p->ctx, BT_ERR_BAD_ARG, "matrix is NULL");
   const int d = 1 << k;
-  const int cnt = per_member ? p->batch : 1;
+  const int lo = p->range_lo, hi = p->range_hi < 0 ? p->batch : p->range_hi;
+  const int cnt = per_member ? hi - lo : 1;
   PGOp op = {};
+  op.mlo = lo;
+  op.mhi = hi;
   op.type = k == 1 ? PG_GATE1 : PG_GATE2;
   op.b0 = p->n - qubits[0];
   op.b1 = k == 2 ? p->n - qubits[1] : 0;
@@ -589,6 +605,8 @@ int bt_program_add_channel(bt_program* p, int k, const int32_t* qubits, int nk, 
   if (nk > PG_MAX_KRAUS) return bt_fail(p->ctx, BT_ERR_UNSUPPORTED, "programs take at most 64 Kraus operators per channel");
   const int d = 1 << k;
   PGOp op = {};
+  op.mlo = p->range_lo;
+  op.mhi = p->range_hi < 0 ? p->batch : p->range_hi;
   op.type = PG_CHANNEL;
   op.k = k;
   op.nk = nk;
@@ -617,6 +635,8 @@ int bt_program_add_measure(bt_program* p, int qubit, const int32_t* skip) {
   int rc = prog_qubits(p, 1, &qubit);
   if (rc) return rc;
   PGOp op = {};
+  op.mlo = p->range_lo;
+  op.mhi = p->range_hi < 0 ? p->batch : p->range_hi;
   op.type = PG_MEASURE;
   op.b0 = p->n - qubit;
   op.skip_off = prog_skip(p, skip);
@@ -627,14 +647,18 @@ int bt_program_add_measure(bt_program* p, int qubit, const int32_t* skip) {
   return BT_OK;
 }
 
+static bool use_grouped(const bt_program* p);
+
 int bt_program_set_gate(bt_program* p, int64_t op_index, const double* mats) {
   if (!p || !mats) return bt_fail(p ? p->ctx : nullptr, BT_ERR_BAD_ARG, "NULL argument");
   if (op_index < 0 || op_index >= (int64_t)p->ops.size())
     return bt_fail(p->ctx, BT_ERR_BAD_ARG, "op index out of range");
   const PGOp& op = p->ops[op_index];
   if (op.type != PG_GATE1 && op.type != PG_GATE2) return bt_fail(p->ctx, BT_ERR_BAD_ARG, "op is not a gate");
+  // the grouped executor's member activity depends on which matrices are identities
+  if (op.mstride && use_grouped(p)) p->uploaded = false;
   const int d = op.type == PG_GATE1 ? 2 : 4;
-  const int cnt = op.mstride ? p->batch : 1;
+  const int cnt = op.mstride ? op.mhi - op.mlo : 1;
   double* dst = p->gm.data() + op.moff;
   for (int m = 0; m < cnt; ++m) {
     const double* cm = mats + (size_t)m * 2 * d * d;
@@ -710,15 +734,38 @@ static void form_groups(bt_program* p, std::vector<int8_t>& gact) {
     p->groups.push_back(g);
     i = j;
   }
+  // a member is active in a group when one of the group's ops does something to
+  // it: not skipped, and for a gate with per-member matrices not exactly the
+  // identity (members whose op sequence is shorter at a position -- trajectories
+  // beside ZNE or twirled copies in one batch -- carry identities there)
+  auto identity = [](const double* m, int d) {
+    for (int r = 0; r < d; ++r)
+      for (int c = 0; c < d; ++c)
+        if (m[2 * (r * d + c)] != (r == c ? 1.0 : 0.0) || m[2 * (r * d + c) + 1] != 0.0) return false;
+    return true;
+  };
   gact.assign(p->groups.size() * (size_t)p->batch, 0);
   for (size_t gi = 0; gi < p->groups.size(); ++gi) {
-    const PGGroup& g = p->groups[gi];
+    PGGroup& g = p->groups[gi];
     int8_t* row = gact.data() + gi * p->batch;
     for (int oi = g.op0; oi < g.op0 + g.nop; ++oi) {
       const PGOp& o = p->ops[oi];
-      for (int m = 0; m < p->batch; ++m)
-        if (o.skip_off < 0 || !p->skip[o.skip_off + m]) row[m] = 1;
+      const bool gate = o.type == PG_GATE1 || o.type == PG_GATE2;
+      const int d = o.type == PG_GATE1 ? 2 : 4;
+      for (int m = o.mlo; m < o.mhi; ++m) {
+        if (o.skip_off >= 0 && p->skip[o.skip_off + m]) continue;
+        if (gate && o.mstride && identity(p->gm.data() + o.moff + (size_t)(m - o.mlo) * o.mstride, d)) continue;
+        row[m] = 1;
+      }
     }
+    // the launches of the group cover its first to last active member only
+    g.mlo = 0;
+    g.mhi = 0;
+    for (int m = 0; m < p->batch; ++m)
+      if (row[m]) {
+        if (g.mhi == 0) g.mlo = m;
+        g.mhi = m + 1;
+      }
   }
 }
 
@@ -814,15 +861,21 @@ int bt_program_run(bt_program* p, bt_state* s, const double* uniforms, uint64_t 
   if (use_grouped(p)) {
     // per group: reduce rho_Q (when a decision needs it), decide per member,
     // apply the chosen matrices; members idle in a group are neither read nor written
+    // records of members a group does not reach stay -1
+    if (p->nrec && (rc = bt_cuda_check(ctx, cudaMemsetAsync(p->d_rec, 0xFF, (size_t)p->batch * p->nrec * 4,
+                                                            ctx->stream), "records")))
+      return rc;
     const int8_t* gact = (const int8_t*)p->d_gact;
     for (size_t gi = 0; gi < p->groups.size() && !rc; ++gi) {
       const PGGroup& g = p->groups[gi];
+      if (g.mhi <= g.mlo) continue;  // no member acts in this group
       const int8_t* act = gact + gi * p->batch;
       const int bits[2] = {g.q0, g.q1};
       const int D = 1 << g.nb;
-      if (g.need_rho) rc = bt_launch_rdm(s, g.nb, bits, 0, p->batch, (double*)p->d_rho, act);
+      const int64_t nm = g.mhi - g.mlo;
+      if (g.need_rho) rc = bt_launch_rdm(s, g.nb, bits, g.mlo, nm, (double*)p->d_rho, act);
       if (rc) break;
-      const unsigned grid = (unsigned)((p->batch + 127) / 128);
+      const unsigned grid = (unsigned)((nm + 127) / 128);
       if (f)
         k_group_decide<float><<<grid, 128, 0, ctx->stream>>>(
             g, (const PGOp*)p->d_ops, (const float*)p->d_gm, (const double*)p->d_km, (const int8_t*)p->d_skip, act,
@@ -835,7 +888,7 @@ int bt_program_run(bt_program* p, bt_state* s, const double* uniforms, uint64_t 
             ctx->d_status);
       ctx->launches++;
       if ((rc = bt_cuda_check(ctx, cudaGetLastError(), "group decide launch"))) break;
-      rc = bt_launch_gate(s, g.nb, bits, nullptr, 0, 0, p->batch, p->d_mat, 32, act);
+      rc = bt_launch_gate(s, g.nb, bits, nullptr, 0, g.mlo, nm, p->d_mat, 32, act);
       (void)D;
     }
     if (rc) return rc;

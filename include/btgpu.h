@@ -278,6 +278,13 @@ int bt_program_add_gate(bt_program* p, int k, const int32_t* qubits, const doubl
 int bt_program_add_channel(bt_program* p, int k, const int32_t* qubits, int nk, const double* kraus, int flags,
                            const int32_t* skip);
 int bt_program_add_measure(bt_program* p, int qubit, const int32_t* skip);
+/* ops added after this call act on members [lo, hi) only (hi = -1: to the end of
+ * the batch); the others pass over them (a gate leaves them as they are, a
+ * measurement records -1), and a per_member gate takes hi - lo matrices.  Groups
+ * of members running different circuits (trajectories beside twirled ZNE copies,
+ * src/ops.jl:555-573) share one program this way; the grouped executor reads and
+ * writes a member only in groups where it does something. */
+int bt_program_set_range(bt_program* p, int64_t lo, int64_t hi);
 int bt_program_info(const bt_program* p, int64_t* nops, int64_t* ndraws, int64_t* nrecords);
 /* new matrices for gate op `op_index` (counting every bt_program_add_* call from
  * 0), in the count it was added with (variational angles between runs) */

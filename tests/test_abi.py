@@ -47,3 +47,87 @@ def test_null_arguments_are_errors_not_crashes():
     assert lib.bt_state_free(None) == 0
     assert lib.bt_apply_matrix(None, 1, None, None, 0, None, -1) == L.BT_ERR_BAD_ARG
     assert lib.bt_last_error(None)
+
+
+def _prototypes():
+    """name -> (return type, [parameter types]) of every function in the header."""
+    src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    out = {}
+    pat = r"^\s*((?:const\s+)?(?:int|int64_t|uint64_t|double|char\s*\*|void))\s*(bt_\w+)\s*\(([^;]*?)\)\s*;"
+    for m in re.finditer(pat, src, flags=re.M | re.S):
+        params = " ".join(m.group(3).split())
+        types = [] if params in ("", "void") else [re.sub(r"\s*\b\w+$", "", p.strip()) for p in params.split(",")]
+        out[m.group(2)] = (" ".join(m.group(1).split()), types)
+    return out
+
+
+def _split_top(s):
+    """Comma-separated items at brace depth 0."""
+    items, depth, cur = [], 0, ""
+    for ch in s:
+        if ch == "{":
+            depth += 1
+        elif ch == "}":
+            depth -= 1
+        if ch == "," and depth == 0:
+            items.append(cur.strip())
+            cur = ""
+        else:
+            cur += ch
+    if cur.strip():
+        items.append(cur.strip())
+    return items
+
+
+_SCALAR = {"int": {"Cint", "Int32"}, "int64_t": {"Int64"}, "uint64_t": {"UInt64"}, "double": {"Float64", "Cdouble"}}
+_POINTEE = {"double": {"Float64", "ComplexF64", "Cdouble"}, "int32_t": {"Int32", "Cint"}, "int": {"Cint", "Int32"},
+            "int64_t": {"Int64"}, "uint64_t": {"UInt64"}, "uint8_t": {"UInt8"}}
+
+
+def _compatible(ctype, jtype):
+    c = ctype.replace("const", "").strip()
+    if "*" not in c:
+        return jtype in _SCALAR.get(c, set())
+    m = re.fullmatch(r"(Ptr|Ref)\{(.+)\}", jtype)
+    if not m:
+        return False
+    inner, base, stars = m.group(2), c.replace("*", "").strip(), c.count("*")
+    if stars == 2 or base.startswith("bt_") and stars == 2:
+        return inner == "Ptr{Cvoid}"
+    if base.startswith("bt_") or base == "void":
+        return inner == "Cvoid"
+    return inner in _POINTEE.get(base, set())
+
+
+def test_julia_binding_ccalls_match_the_header():
+    """julia/BlueTangleGPU.jl binds the library with ccall: every call names a
+    declared function with its parameter count and, per parameter, a Julia type
+    of the C type's size and kind (scalars by width, pointers as Ptr/Ref of a
+    matching element type, handles as Ptr{Cvoid})."""
+    jl = open(os.path.join(ROOT, "julia", "BlueTangleGPU.jl")).read()
+    protos = _prototypes()
+    assert len(protos) >= 60
+    calls = re.findall(r"ccall\(\(:(\w+),\s*lib\),\s*(\w+),\s*\(([^()]*)\)", jl)
+    assert len(calls) >= 40
+    seen = set()
+    for name, ret, args in calls:
+        assert name in protos, f"{name} is not declared in btgpu.h"
+        cret, ctypes_ = protos[name]
+        assert (ret == "Cstring") == cret.endswith("*"), (name, ret, cret)
+        if ret != "Cstring":
+            assert ret == "Cint" and cret == "int", (name, ret, cret)
+        jtypes = _split_top(args)
+        assert len(jtypes) == len(ctypes_), (name, jtypes, ctypes_)
+        for ct, jt in zip(ctypes_, jtypes):
+            assert _compatible(ct, jt), (name, ct, jt)
+        seen.add(name)
+    # the generics of the drop-in and the entry points they stand on are bound
+    for need in ("bt_apply_matrix", "bt_apply_kraus", "bt_measure_z", "bt_measure_z2", "bt_state_copy",
+                 "bt_sample", "bt_probabilities", "bt_expect_pauli", "bt_expect_z_all", "bt_fidelity",
+                 "bt_fidelity_dm", "bt_plan_run", "bt_program_run", "bt_sample_members", "bt_serve_submit"):
+        assert need in seen, need
+    # apply is functional (a copy, then the in-place form) as the reference's
+    assert re.search(r"apply\(s::GPUHandle, op::[^)]*\)\s*=\s*apply!\(copy\(s\)", jl)
+    # OpQC("RES") resets (src/hilbert.jl:489-490); controls enter programs as 4x4
+    assert re.search(r'uppercase\(op\.name\) in \("RES", "RESET"\)[^\n]*\n\s*_reset_Z!', jl)
+    assert "_program_gate!(p, _ctrl_matrix(op.mat), [op.control, op.qubit])" in jl

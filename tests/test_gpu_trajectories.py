@@ -216,3 +216,73 @@ def test_grouped_program_large_members_equal_slots_engine(ctx):
     assert sum(len(r) for r in ra) > 0
     for m in range(B):
         assert np.abs(a.to_numpy(m) - b.to_numpy(m)).max() < 2e-5
+
+
+@pytest.mark.parametrize("executor", ["shared", "grouped"])
+def test_trajectories_and_copies_in_one_program(ctx, oracle, kref, executor):
+    """Monte-Carlo trajectories and Pauli-twirled ZNE copies of another circuit in
+    one program (one launch sequence for the whole batch): the members of each
+    group are idle at the other group's slots (identity gates, skipped channels
+    and measurements) and equal the oracle replaying each member with the same
+    draws; with the grouped executor idle members are neither read nor written."""
+    import bluetangle_gpu as bt
+    import bluetangle_gpu.trajectories as T
+    from bluetangle_gpu.noise import NoiseModel
+    n, B, NC = 5, 4, 3
+    h = np.random.default_rng(3).uniform(0.5, 1.5, n)
+    steps = tfim_cnot_steps(n, 1, 0.3, h)
+    main = T.member_programs(steps, n, B, measure_prob=0.3, measure_rng=np.random.default_rng(8))
+    copy_ops = [bt.Op("CNOT", q, q + 1) for q in range(1, n)] + [bt.Op("RX(0.7)", q) for q in range(1, n + 1)]
+    copies = T.member_programs([copy_ops], n, NC, zne_ids=[0, 1, 2], twirl=True,
+                               frame_rng=np.random.default_rng(7))
+    noise = NoiseModel(bt.Noise1("depolarizing", 0.05), bt.Noise2("depolarizing", 0.08))
+    members = T.concat_members(main, T.explicit_noise(copies, noise))
+    slots = T.build_slots(members)
+    st = bt.zero_state(n, "c128", batch=B + NC)
+    prog, _ = T.compile_program(slots, n, B + NC, "c128", unitary_mix=False)
+    prog.set_executor(executor)
+    recs = prog.run(st, rng=np.random.default_rng(11))
+    ref, rrecs = replay(oracle, slots, B + NC, n, np.random.default_rng(11), kref)
+    for m in range(B + NC):
+        assert recs[m] == rrecs[m]
+        assert np.abs(st.to_numpy(m) - ref[m]).max() < 1e-12, m
+    # the copies' own circuit: the same as building their slots alone under the model
+    alone = T.build_slots(copies, noise)
+    assert sum(len([i for i in s.items if i is not None]) for s in alone) == \
+        sum(len([i for i in s.items[B:] if i is not None]) for s in slots)
+
+
+def test_grouped_program_one_qubit_groups(ctx):
+    """A group of ops on one qubit (a measurement between two-qubit gates on other
+    qubits) in the grouped executor: its reduced matrices (2 x 2 per member) are
+    read per member, so every member's outcome and state equal the one-CTA
+    executor's with the same draws."""
+    import bluetangle_gpu as bt
+    import bluetangle_gpu.trajectories as T
+    n, B = 5, 9
+
+    def runitary(rng):
+        q, r = np.linalg.qr(rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2)))
+        return q * (np.diag(r) / np.abs(np.diag(r)))
+
+    prog = {}
+    for ex in ("shared", "grouped"):
+        p = T.Program(n, B, "c128")
+        rng = np.random.default_rng(4)
+        for q in range(1, n + 1):
+            p.add_gate([runitary(rng) for _ in range(B)], [q])
+        p.add_gate(np.eye(4)[[0, 1, 3, 2]], [1, 2])
+        p.add_measure(5)
+        p.add_gate(np.eye(4)[[0, 1, 3, 2]], [3, 4])
+        p.add_measure(4, [m % 2 for m in range(B)])
+        p.add_gate(np.eye(4)[[0, 1, 3, 2]], [1, 2])
+        p.set_executor(ex)
+        prog[ex] = p
+    out = {}
+    for ex, p in prog.items():
+        st = bt.zero_state(n, "c128", batch=B)
+        recs = p.run(st, rng=np.random.default_rng(12))
+        out[ex] = (recs, [st.to_numpy(m) for m in range(B)])
+    assert out["shared"][0] == out["grouped"][0]
+    for a, b in zip(out["shared"][1], out["grouped"][1]):
+        assert np.abs(a - b).max() < 1e-12

@@ -275,3 +275,40 @@ def test_reference_arm_maps_no_engine_library():
     r = subprocess.run([sys.executable, "-c", code, root], capture_output=True, text=True, timeout=300, cwd=root)
     assert r.returncode == 0, r.stderr[-2000:]
     assert r.stdout.strip().endswith("CLEAN"), r.stdout
+
+
+def test_member_groups_share_one_slot_list():
+    """Groups of members with different circuits in one batch: concat_members and
+    concat_slots leave each group's slots in order with the other group idle;
+    explicit_noise writes a NoiseModel's channels out as OpQC ops (the slots equal
+    those build_slots adds under the model); grouped_bytes counts only the members
+    that act in each group of ops."""
+    import bluetangle_gpu as bt
+    import bluetangle_gpu.trajectories as T
+    from bluetangle_gpu.noise import NoiseModel
+    n = 4
+    noise = NoiseModel(bt.Noise1("depolarizing", 0.05), bt.Noise2("depolarizing", 0.08))
+    main = T.member_programs([[bt.Op("H", 1), bt.Op("CNOT", 1, 2)]], n, 3, measure_prob=0.5,
+                             measure_rng=np.random.default_rng(1))
+    copy_ops = [bt.Op("CNOT", q, q + 1) for q in range(1, n)]
+    copies = T.member_programs([copy_ops], n, 2, zne_ids=[0, 1], twirl=True, frame_rng=np.random.default_rng(2))
+    a = T.build_slots(T.explicit_noise(copies, noise))
+    b = T.build_slots(copies, noise)
+    assert [s.kind for s in a] == [s.kind for s in b]
+    for sa, sb in zip(a, b):
+        for ia, ib in zip(sa.items, sb.items):
+            assert (ia is None) == (ib is None)
+            if ia is not None and sa.kind == "channel":
+                assert ia[1] == ib[1] and all(np.array_equal(x, y) for x, y in zip(ia[0], ib[0]))
+    s1 = T.build_slots(T.concat_members(main, copies))
+    s2 = T.concat_slots((T.build_slots(main), 3), (T.build_slots(copies), 2))
+    assert len(s1) == len(s2)
+    for x, y in zip(s1, s2):
+        assert x.kind == y.kind and [i is None for i in x.items] == [i is None for i in y.items]
+        on = [m for m, it in enumerate(x.items) if it is not None]
+        assert on and (max(on) < 3 or min(on) >= 3)  # each slot belongs to one group
+    member = 2 ** n * 8
+    only_main = T.grouped_bytes(T.build_slots(main), n, 3)
+    only_copies = T.grouped_bytes(T.build_slots(copies), n, 2)
+    both = T.grouped_bytes(s2, n, 5)
+    assert both <= only_main + only_copies and both % member == 0 and both > 0

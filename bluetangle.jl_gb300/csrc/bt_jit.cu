@@ -126,9 +126,24 @@ static std::string fmt_u64(uint64_t v) {
 
 static int swz_host(bool f, int l) { return f ? (l ^ ((l >> 4) & 15)) : (l ^ ((l >> 3) & 7)); }
 
+// Complex-pair arithmetic (complex64, BTGPU_JIT_CPAIR=1; off by default): an op
+// with real coefficients applies the same real map to the real and the imaginary
+// part of its amplitudes, so (x_j, y_j) -- one amplitude, as it lies in memory and
+// in registers after a 64-bit load -- goes through one two-lane FP32 instruction
+// (fma.rn.f32x2 / mul.rn.f32x2) instead of two: the add/sub butterflies (H), the
+// factored real rotations (RY) and real 2x2 matrices.  Ops with complex
+// coefficients (phases, RX) mix the two parts and stay scalar.  Measured on the
+// 28- and 33-qubit brickwork: 8.5% fewer instructions, FMA pipe busier by as
+// much, pass times unchanged (the passes are bound by neither issue nor FMA).
+static bool cpair_on() {
+  static const bool v = env_int("BTGPU_JIT_CPAIR", 0, 0, 1) != 0;
+  return v;
+}
+
 // emits one op on the scalar registers x<j> (real) / y<j> (imaginary), j < 2^NB
 // mref: where the op's entries are read (the kernel parameters, or a per-member table)
-static void emit_op(std::ostringstream& o, const FOp& op, int NB, const char* mref = "a.mat") {
+// cp: complex-pair form of the real-coefficient ops (complex64 only)
+static void emit_op(std::ostringstream& o, const FOp& op, int NB, const char* mref = "a.mat", bool cp = false) {
   const int D = 1 << NB;
   auto M = [&](int e) {
     std::ostringstream s;
@@ -170,6 +185,16 @@ static void emit_op(std::ostringstream& o, const FOp& op, int NB, const char* mr
       o << "    }\n";
       break;
     case FOP_R1:
+      if (cp) {
+        o << "    { const u64 A0=bc(" << M(0) << "),A1=bc(" << M(1) << "),A2=bc(" << M(2) << "),A3=bc(" << M(3) << ");\n";
+        pairs(b0, [&](int j, int k) {
+          o << "      { const u64 A=pk(x" << j << ",y" << j << "), B=pk(x" << k << ",y" << k
+            << "); const u64 C=ffma2(A0,A,fmul2(A1,B)), E=ffma2(A2,A,fmul2(A3,B)); x" << j << "=plo(C); y" << j
+            << "=phi(C); x" << k << "=plo(E); y" << k << "=phi(E); }\n";
+        });
+        o << "    }\n";
+        break;
+      }
       o << "    { const R a0=" << M(0) << ",a1=" << M(1) << ",a2=" << M(2) << ",a3=" << M(3) << ";\n";
       pairs(b0, [&](int j, int k) {
         o << "      { const R ar=x" << j << ",ai=y" << j << ",br=x" << k << ",bi=y" << k << "; x" << j
@@ -194,6 +219,18 @@ static void emit_op(std::ostringstream& o, const FOp& op, int NB, const char* mr
       const char* s01 = (op.flags & 1) ? "-" : "+";
       const char* s10 = (op.flags & 2) ? "-" : "";
       const char* s11 = (op.flags & 4) ? "-" : "+";
+      if (cp && !((op.flags & 2) && (op.flags & 4))) {
+        // a + s01 b, then s10 a + s11 b as b + s10 a (s11 = +) or a + s11 b (s10 = +)
+        o << "    { const u64 S01=bc(" << ((op.flags & 1) ? "-1.0f" : "1.0f") << "), S2=bc("
+          << (((op.flags & 2) || (op.flags & 4)) ? "-1.0f" : "1.0f") << ");\n";
+        pairs(b0, [&](int j, int k) {
+          o << "      { const u64 A=pk(x" << j << ",y" << j << "), B=pk(x" << k << ",y" << k << "); const u64 C=ffma2(S01,B,A), E="
+            << ((op.flags & 2) ? "ffma2(S2,A,B)" : "ffma2(S2,B,A)") << "; x" << j << "=plo(C); y" << j << "=phi(C); x" << k
+            << "=plo(E); y" << k << "=phi(E); }\n";
+        });
+        o << "    }\n";
+        break;
+      }
       pairs(b0, [&](int j, int k) {
         o << "    { const R ar=x" << j << ",ai=y" << j << ",br=x" << k << ",bi=y" << k << "; x" << j << "=ar" << s01
           << "br; y" << j << "=ai" << s01 << "bi; x" << k << "=" << s10 << "ar" << s11 << "br; y" << k << "=" << s10
@@ -204,6 +241,22 @@ static void emit_op(std::ostringstream& o, const FOp& op, int NB, const char* mr
     case FOP_RN: {  // [[1, p], [q, s]] or [[p, 1], [s, q]]: one FMA per component
       const bool B = op.flags & 2;
       const char* sg = (op.flags & 1) ? "-" : "";
+      if (cp) {
+        // (x_j, y_j) = p b + a; (x_k, y_k) = q a + s b, with s = -1 as q a + (-1) b
+        o << "    { const u64 P=bc(" << M(0) << "),Q=bc(" << M(1) << ")" << ((op.flags & 1) ? ",N=bc(-1.0f)" : "")
+          << ";\n";
+        pairs(b0, [&](int j, int k) {
+          o << "      { const u64 A=pk(x" << j << ",y" << j << "), B=pk(x" << k << ",y" << k << ");";
+          o << " const u64 C=ffma2(P," << (B ? "A" : "B") << "," << (B ? "B" : "A") << ");";
+          if (op.flags & 1)
+            o << " const u64 E=ffma2(Q," << (B ? "B" : "A") << ",fmul2(N," << (B ? "A" : "B") << "));";
+          else
+            o << " const u64 E=ffma2(Q," << (B ? "B" : "A") << "," << (B ? "A" : "B") << ");";
+          o << " x" << j << "=plo(C); y" << j << "=phi(C); x" << k << "=plo(E); y" << k << "=phi(E); }\n";
+        });
+        o << "    }\n";
+        break;
+      }
       o << "    { const R p=" << M(0) << ",q=" << M(1) << ";\n";
       pairs(b0, [&](int j, int k) {
         o << "      { const R ar=x" << j << ",ai=y" << j << ",br=x" << k << ",bi=y" << k << ";";
@@ -879,7 +932,7 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
       }
       unpack();
     } else {
-      for (int oi = ph.op0; oi < ph.op0 + ph.nop; ++oi) emit_op(o, a.op[oi], NB, mref);
+      for (int oi = ph.op0; oi < ph.op0 + ph.nop; ++oi) emit_op(o, a.op[oi], NB, mref, f && cpair_on());
     }
     if (wr_direct) {
       o << "    { " << T2 << "* gp = g + tl;\n";

@@ -146,6 +146,8 @@ print("OK")
     ("c64", {"BTGPU_PLAN_PHASE_WINDOWS": "0"}),
     ("c64", {"BTGPU_JIT_LANES": "1"}),
     ("c64", {"BTGPU_JIT_LANES": "1", "BTGPU_JIT_DIRECT": "0"}),
+    ("c64", {"BTGPU_JIT_CPAIR": "1"}),
+    ("c64", {"BTGPU_JIT_CPAIR": "0"}),
 ])
 def test_generated_kernels_on_host(prec, env, tmp_path):
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -232,3 +234,4 @@ def test_per_member_matrices_on_host(prec, tmp_path):
     r = subprocess.run([sys.executable, "-c", _MEMBERS, root, prec], env=e, capture_output=True, text=True,
                        timeout=900)
     assert r.returncode == 0 and r.stdout.rstrip().endswith("OK"), r.stdout[-2000:] + r.stderr[-4000:]
+

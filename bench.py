@@ -35,9 +35,9 @@ METRIC = "gate-apps/s"
 # ncu-measured DRAM bytes per amplitude of one pass (read + write) of the dominant
 # kernel, from single-launch captures at 28 qubits (traffic grows in proportion to
 # the state, so it is scaled to the workload's 2^n amplitudes): the specialised
-# fused tile pass (plan mode) moved 2.15 GB read + 2.09 GB written per 2^28
+# fused tile pass (plan mode) moved 2.173 GB read + 2.087 GB written per 2^28
 # amplitudes, the dense k_gate sweep (layer modes) 2.148 + 2.087 GB.
-TRAFFIC_BYTES_PER_AMP = {"plan": (2.15e9 + 2.09e9) / 2 ** 28,
+TRAFFIC_BYTES_PER_AMP = {"plan": (2.173e9 + 2.087e9) / 2 ** 28,
                          "sweep": (2.147591e9 + 2.087163e9) / 2 ** 28}
 
 

@@ -160,6 +160,9 @@ int bt_launch_sample(bt_state* s, int64_t mem, int64_t shots, const double* d_u,
 int bt_launch_probs(bt_state* s, int64_t mem, int64_t offset, int64_t len, double* d_out);
 // one shot per member: d_out[m] from member m's weights (d_u[m] or Philox draw m)
 int bt_launch_sample_each(bt_state* s, const double* d_u, uint64_t seed_stream, int64_t* d_out);
+// bt_plan_run_members on members [0, nmem) of s only (bt_plan.cu)
+int bt_plan_run_members_n(bt_plan* p, bt_state* s, int64_t nmem, int count, const int64_t* add_index,
+                          const double* mats);
 
 // state maintenance
 int bt_launch_set_basis(bt_state* s, int64_t mem_lo, int64_t nmem, uint64_t index);

@@ -1448,17 +1448,27 @@ int bt_plan_run(bt_plan* p, bt_state* s, int64_t member) {
 }
 
 int bt_plan_run_members(bt_plan* p, bt_state* s, int count, const int64_t* add_index, const double* mats) {
+  if (!p || !s) return bt_fail(p ? p->ctx : nullptr, BT_ERR_BAD_ARG, "bad arguments");
+  return bt_plan_run_members_n(p, s, s->batch, count, add_index, mats);
+}
+
+}  // extern "C"
+
+// members [0, nmem) of s (the serving engine runs as many as it has requests)
+int bt_plan_run_members_n(bt_plan* p, bt_state* s, int64_t nmem, int count, const int64_t* add_index,
+                          const double* mats) {
   if (!p || !s || count < 1 || !add_index || !mats) return bt_fail(p ? p->ctx : nullptr, BT_ERR_BAD_ARG, "bad arguments");
   bt_ctx* ctx = s->ctx;
   if (s->n != p->n || s->repr != p->repr || s->prec != p->prec)
     return bt_fail(ctx, BT_ERR_BAD_ARG, "plan and state differ in n, repr or prec");
+  if (nmem < 1 || nmem > s->batch) return bt_fail(ctx, BT_ERR_BAD_ARG, "member count outside the batch");
   std::vector<char> touched;
   int rc = prepare_members(p, count, add_index, touched);
   if (rc) return rc;
   size_t per = 0;
   rc = bt_plan_gate_dims(p, add_index, count, &per);
   if (rc) return rc;
-  const int64_t B = s->batch;
+  const int64_t B = nmem;
   const bool c64 = p->prec == BT_PREC_C64;
   rc = bt_cuda_check(ctx, cudaSetDevice(ctx->device), "cudaSetDevice");
   for (size_t i = 0; i < p->passes.size() && !rc; ++i) {
@@ -1529,9 +1539,19 @@ int bt_plan_run_members(bt_plan* p, bt_state* s, int count, const int64_t* add_i
   return rc;
 }
 
-}  // extern "C"
-
 // ------------------------------------------------------------------ serving hooks (bt_serve.cu)
+// add indices whose gates are all variable (the gates a client's requests rewrite)
+int bt_plan_variable_adds(const bt_plan* p, std::vector<int64_t>& idx) {
+  if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "plan is NULL");
+  idx.clear();
+  for (size_t a = 0; a < p->adds.size(); ++a) {
+    bool var = p->adds[a].second > 0;
+    for (int j = 0; j < p->adds[a].second; ++j) var &= p->gates[p->adds[a].first + j].var;
+    if (var) idx.push_back((int64_t)a);
+  }
+  return BT_OK;
+}
+
 int bt_plan_shape(const bt_plan* p, int* n, int* repr, int* prec) {
   if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "plan is NULL");
   *n = p->n;

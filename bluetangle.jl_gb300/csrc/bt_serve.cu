@@ -16,6 +16,12 @@
 //   * packs small circuits into one launch: a packed client is a program whose
 //     members are independent requests, so up to its width of queued requests run
 //     as one shared-memory program launch (one CTA per request);
+//   * runs the queued requests of a plan client whose state is too small to fill
+//     the GPU (fewer than 2^22 amplitudes) together: its resident state holds
+//     2^(22-n) members (at most 8), and up to that many requests naming the same
+//     gates run as one plan run over the members, each with its own matrices
+//     (bt_plan_run_members: the passes holding those gates read per-member
+//     entries, the others launch once for all);
 //   * records submit-to-done latency per request for p50/p99.
 // A request carries new matrices for some of the client's gates (plan add
 // indices, or program op indices) and a seed for the program's draws.
@@ -66,6 +72,7 @@ struct Client {
   // requests naming the same gates run in one launch
   bool packed = false;
   std::vector<char> per_member;
+  int width = 1;  // plan client: requests per plan run (members of its state)
   size_t footprint = 0;
   bt_state* state = nullptr;  // resident state (nullptr: not resident)
   bool reserved = false;      // admitted, state being allocated by `lane`
@@ -102,6 +109,7 @@ struct bt_server {
 int bt_program_gate_dims(const bt_program* p, std::vector<int>& dims, int* n, int* prec, int* batch,
                          std::vector<char>* per_member);
 int bt_plan_shape(const bt_plan* p, int* n, int* repr, int* prec);
+int bt_plan_variable_adds(const bt_plan* p, std::vector<int64_t>& idx);
 int bt_plan_gate_dims(const bt_plan* p, const int64_t* idx, int count, size_t* reals);
 
 static Client* pick(bt_server* s, int lane) {
@@ -136,14 +144,49 @@ static bool admit(bt_server* s, Client* c, int lane, std::vector<bt_state*>& to_
   return true;
 }
 
+// <H> / norm of member m of the client's state
+static int member_value(Client* c, int64_t m, double* value) {
+  const int nt = (int)c->coef.size();
+  std::vector<double> ev(nt);
+  double nrm = 0;
+  int rc = nt ? bt_expect_pauli(c->state, nt, c->x.data(), c->z.data(), c->coef.data(), m, ev.data()) : BT_OK;
+  if (!rc) rc = bt_norm2(c->state, m, &nrm);
+  if (rc) return rc;
+  double h = 0;
+  for (int t = 0; t < nt; ++t) h += ev[t];
+  *value = h / nrm;
+  return BT_OK;
+}
+
+// requests rs of a plan client: one request on member 0 with the plan's own
+// matrices; several (all naming the same gates) as one run over members
+// [0, k), member m with request m's matrices
+static int run_plan(Client* c, const std::vector<Req*>& rs, std::vector<double>& values) {
+  const int k = (int)rs.size();
+  values.assign(k, 0.0);
+  int rc = BT_OK;
+  if (k == 1 || rs[0]->idx.empty()) {
+    for (int i = 0; i < k && !rc; ++i) {
+      if (!rs[i]->idx.empty())
+        rc = bt_plan_set_matrices(c->plan, (int)rs[i]->idx.size(), rs[i]->idx.data(), rs[i]->mats.data());
+      if (!rc) rc = bt_state_set_zero(c->state, 0);
+      if (!rc) rc = bt_plan_run(c->plan, c->state, 0);
+      if (!rc) rc = member_value(c, 0, &values[i]);
+    }
+    return rc;
+  }
+  std::vector<double> mats;
+  for (Req* r : rs) mats.insert(mats.end(), r->mats.begin(), r->mats.end());
+  for (int m = 0; m < k && !rc; ++m) rc = bt_state_set_zero(c->state, m);
+  if (!rc)
+    rc = bt_plan_run_members_n(c->plan, c->state, k, (int)rs[0]->idx.size(), rs[0]->idx.data(), mats.data());
+  for (int m = 0; m < k && !rc; ++m) rc = member_value(c, m, &values[m]);
+  return rc;
+}
+
 static int run_request(bt_ctx* ctx, Client* c, Req* r, double* value) {
   int rc = BT_OK;
-  if (c->plan) {
-    if (!r->idx.empty())
-      rc = bt_plan_set_matrices(c->plan, (int)r->idx.size(), r->idx.data(), r->mats.data());
-    if (!rc) rc = bt_state_set_zero(c->state, -1);
-    if (!rc) rc = bt_plan_run(c->plan, c->state, -1);
-  } else {
+  {
     size_t off = 0;
     for (size_t i = 0; i < r->idx.size() && !rc; ++i) {
       const int64_t oi = r->idx[i];
@@ -230,8 +273,10 @@ static void worker(bt_server* s, int lane) {
       alloc = c->state == nullptr;
       rs.push_back(c->queue.front());
       c->queue.pop_front();
-      // a packed client takes the queued requests that name the same gates, up to its width
-      while (c->packed && (int)rs.size() < c->batch && !c->queue.empty() && c->queue.front()->idx == rs[0]->idx) {
+      // a packed client (and a plan client of several members) takes the queued
+      // requests that name the same gates, up to its width
+      const int width = c->packed ? c->batch : (c->plan ? c->width : 1);
+      while ((int)rs.size() < width && !c->queue.empty() && c->queue.front()->idx == rs[0]->idx) {
         rs.push_back(c->queue.front());
         c->queue.pop_front();
       }
@@ -252,7 +297,7 @@ static void worker(bt_server* s, int lane) {
     }
     const double t0 = now_s();
     std::vector<double> v(rs.size(), 0.0);
-    if (!rc) rc = c->packed ? run_packed(c, rs, v) : run_request(ctx, c, rs[0], &v[0]);
+    if (!rc) rc = c->packed ? run_packed(c, rs, v) : (c->plan ? run_plan(c, rs, v) : run_request(ctx, c, rs[0], &v[0]));
     const double t = now_s();
     std::string err;
     if (rc) err = bt_last_error(nullptr);  // every failure also lands in this thread's message
@@ -348,6 +393,19 @@ int bt_serve_add_plan_client(bt_server* s, bt_plan* plan, int nterms, const uint
     delete c;
     return rc;
   }
+  // a state vector of fewer than 2^22 amplitudes leaves most SMs idle: hold up to
+  // 8 requests' members, so that queued requests run together; the per-member
+  // kernels of the variable gates are built now rather than at the first such run
+  if (c->repr == BT_REPR_SV && c->n < 22) {
+    std::vector<int64_t> var;
+    if (!bt_plan_variable_adds(plan, var) && !var.empty() &&
+        !bt_plan_prepare_members(plan, (int)var.size(), var.data()))
+      c->width = std::min(8, 1 << (22 - c->n));
+    // within the server's HBM budget, or the client could never be admitted
+    const size_t member = ((size_t)1 << c->n) * (c->prec == BT_PREC_C64 ? 8 : 16);
+    while (c->width > 1 && member * c->width > s->budget) c->width /= 2;
+  }
+  c->batch = c->width;
   return add_client(s, c, nterms, xmask, zmask, coef, client);
 }
 

@@ -228,3 +228,32 @@ def test_native_server_admission_by_footprint(ctx):
             assert abs(match.value - req.value) <= 1e-6 * max(1.0, abs(req.value))
     finally:
         one.close()
+
+
+def test_native_server_runs_queued_plan_requests_together(ctx):
+    """A plan client of 16 qubits (a state too small to fill the GPU) holds 8
+    members: eight of its requests queued at once run as one plan run over the
+    members, each with its own matrices, and each equals its value served alone."""
+    import bluetangle_gpu.serving as S
+    sp = specs(43)[5:6]  # sv, 16 qubits: a fused plan
+    reqs = requests(sp, per_client=8, seed=47)
+    srv = S.NativeServer(sp, lanes=1)
+    try:
+        for req in reqs:
+            srv.submit(req)
+        for req in reqs:
+            srv.wait(req)
+            assert req.error is None, req.error
+        st = srv.stats()
+    finally:
+        srv.close()
+    assert st["completed"] == len(reqs) and st["runs"] < len(reqs)  # requests shared plan runs
+    one = S.NativeServer(sp, lanes=1)
+    try:
+        for r in requests(sp, per_client=8, seed=47):
+            one.submit(r)
+            one.wait(r)
+            match = [q for q in reqs if q.rid == r.rid][0]
+            assert abs(match.value - r.value) <= 1e-6 * max(1.0, abs(r.value)), (match.value, r.value)
+    finally:
+        one.close()

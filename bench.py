@@ -917,7 +917,7 @@ def run_c3(args):
         # each step's slots compiled into one program over the whole batch (grouped
         # executor: the members exceed shared memory), built before the timed region
         st = bt.zero_state(n, "c64", tot, ctx)
-        progs = [T.compile_program(sl, n, tot, "c64", ctx)[0] for sl in pre]
+        progs = [T.compile_program(sl, n, tot, "c64", ctx)[0].prepare() for sl in pre]
     else:
         # the lock-step engine launches over a whole batch per op: the trajectories
         # and the copies keep a batch each

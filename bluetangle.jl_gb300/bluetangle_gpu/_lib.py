@@ -87,6 +87,7 @@ SIGNATURES = {
     "bt_program_add_channel": (i32, [P, i32, P, i32, P, i32, P]),
     "bt_program_add_measure": (i32, [P, i32, P]),
     "bt_program_set_range": (i32, [P, i64, i64]),
+    "bt_program_prepare": (i32, [P, P]),
     "bt_program_info": (i32, [P, P, P, P]),
     "bt_program_set_gate": (i32, [P, i64, P]),
     "bt_program_run": (i32, [P, P, P, u64, P]),

@@ -290,6 +290,11 @@ class Program:
         self.nops += 1
         return self.nops - 1
 
+    def prepare(self):
+        """Moves the program's tables to the device now (else the first run does)."""
+        self.ctx.check(L.lib().bt_program_prepare(self.h, self.ctx.h))
+        return self
+
     def set_executor(self, name):
         """"auto", "shared" (one CTA per member) or "grouped"."""
         self.ctx.check(L.lib().bt_program_set_executor(self.h, EXECUTORS[name]))

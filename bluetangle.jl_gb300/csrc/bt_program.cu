@@ -830,6 +830,15 @@ static int upload_gm(bt_program* p, bt_ctx* ctx) {
 
 static void launch_program(bt_program* p, bt_state* s, const double* du, uint64_t stream, int nrec);
 
+int bt_program_prepare(bt_program* p, bt_ctx* ctx) {
+  if (!p || !ctx) return bt_fail(p ? p->ctx : nullptr, BT_ERR_BAD_ARG, "NULL argument");
+  int rc = bt_cuda_check(ctx, cudaSetDevice(ctx->device), "cudaSetDevice");
+  if (!rc && !p->uploaded) rc = upload(p);
+  if (!rc && p->gm_dirty) rc = upload_gm(p, ctx);
+  if (!rc) rc = bt_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "program prepare");
+  return rc;
+}
+
 int bt_program_run(bt_program* p, bt_state* s, const double* uniforms, uint64_t seed, int32_t* records) {
   if (!p || !s) return bt_fail(p ? p->ctx : nullptr, BT_ERR_BAD_ARG, "NULL argument");
   bt_ctx* ctx = s->ctx;

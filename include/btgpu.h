@@ -292,6 +292,10 @@ int bt_program_set_gate(bt_program* p, int64_t op_index, const double* mats);
 /* 0: shared memory when the member fits, else grouped (default); 1: shared
  * memory; 2: grouped */
 int bt_program_set_executor(bt_program* p, int executor);
+/* moves the program's tables to the device of ctx now (the first bt_program_run
+ * otherwise does it): callers that compile programs ahead of a timed or
+ * latency-critical loop prepare them there too */
+int bt_program_prepare(bt_program* p, bt_ctx* ctx);
 /* runs on every member of s (n, prec and batch as created); records: batch x
  * nrecords int32, member-major (may be NULL) */
 int bt_program_run(bt_program* p, bt_state* s, const double* uniforms, uint64_t seed, int32_t* records);

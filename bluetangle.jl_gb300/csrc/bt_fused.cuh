@@ -42,7 +42,7 @@ struct FOp {
 };
 
 struct FPhase {
-  uint8_t reg[5];  // tile-local bits held in registers (ascending), register bit b = reg[b]
+  uint8_t reg[6];  // tile-local bits held in registers (ascending), register bit b = reg[b] (b < nreg)
   uint8_t nreg;
   uint16_t op0, nop;
 };

@@ -91,7 +91,7 @@ int bt_jit_max_ops() {
   return v;
 }
 int bt_tile_rb(bool c64) {
-  static const int v = env_int("BTGPU_TILE_RB", BT_TILE_RB_C64, 4, 5);
+  static const int v = env_int("BTGPU_TILE_RB", BT_TILE_RB_C64, 4, 6);
   return c64 ? v : BT_TILE_RB_C128;
 }
 
@@ -718,7 +718,11 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
   // per-member entries (a.permem): member m of the launch reads its ops' entries from
   // row m of the table mm (mstride reals per row) instead of the kernel parameters
   const char* mref = a.permem ? "cm" : "a.mat";
-  o << "extern \"C\" __global__ void __launch_bounds__(" << T << ", " << bt_jit_min_blocks() << ") " << name << "("
+  // six register bits: 128 threads of up to 170 registers, three CTAs per SM
+  // (BTGPU_JIT_MINB6 sets another count)
+  static const int minb6 = env_int("BTGPU_JIT_MINB6", 3, 1, 4);
+  const int minb = NB >= 6 ? minb6 : bt_jit_min_blocks();
+  o << "extern \"C\" __global__ void __launch_bounds__(" << T << ", " << minb << ") " << name << "("
     << T2 << "* __restrict__ psi, const "
     << (f ? "JitArgsF<" : "JitArgsD<") << NM << "> a";
   if (a.permem) o << ", const " << (f ? "float" : "double") << "* __restrict__ mm, const i64 mstride";
@@ -1372,7 +1376,7 @@ static std::string structure_key(const FusedArgs<R>& a) {
   for (int p = 0; p < a.nphase; ++p) {
     const FPhase& ph = a.ph[p];
     k << '|';
-    for (int b = 0; b < 5; ++b) k << (int)ph.reg[b] << '.';
+    for (int b = 0; b < ph.nreg; ++b) k << (int)ph.reg[b] << '.';
     for (int oi = ph.op0; oi < ph.op0 + ph.nop; ++oi) {
       const FOp& op = a.op[oi];
       k << (int)op.type << (int)op.b0 << (int)op.b1 << '_' << (int)op.flags << (int)op.unit << '@' << op.moff << ';';

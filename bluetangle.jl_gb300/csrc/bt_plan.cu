@@ -1135,10 +1135,10 @@ int bt_plan_compile(bt_plan* p, int mode) {
 int bt_plan_set_tuning(bt_plan* p, int max_ops, int tile_rb, int packed, int tile_bits) {
   if (!p) return bt_fail(nullptr, BT_ERR_BAD_ARG, "plan is NULL");
   const int mmin = p->prec == BT_PREC_C64 ? 10 : 9, mmax = p->prec == BT_PREC_C64 ? BT_TILE_M_C64 : BT_TILE_M_C128;
-  if (max_ops < 0 || max_ops > BT_FUSED_MAX_OPS || (tile_rb != 0 && tile_rb != 4 && tile_rb != 5) || packed < -1 ||
+  if (max_ops < 0 || max_ops > BT_FUSED_MAX_OPS || (tile_rb != 0 && (tile_rb < 4 || tile_rb > 6)) || packed < -1 ||
       packed > 1 || (tile_bits != 0 && (tile_bits < mmin || tile_bits > mmax)))
     return bt_fail(p->ctx, BT_ERR_BAD_ARG,
-                   "tuning: 0 <= max_ops <= 192, tile_rb in {0, 4, 5}, packed in {-1, 0, 1}, tile_bits 0 or "
+                   "tuning: 0 <= max_ops <= 192, tile_rb in {0, 4, 5, 6}, packed in {-1, 0, 1}, tile_bits 0 or "
                    "10..13 (complex64) / 9..12 (complex128)");
   join_jit(p);
   p->tune_max_ops = max_ops;

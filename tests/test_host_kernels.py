@@ -147,6 +147,7 @@ print("OK")
     ("c64", {"BTGPU_JIT_LANES": "1"}),
     ("c64", {"BTGPU_JIT_LANES": "1", "BTGPU_JIT_DIRECT": "0"}),
     ("c64", {"BTGPU_JIT_CPAIR": "1"}),
+    ("c64", {"BTGPU_TILE_RB": "6"}),
     ("c64", {"BTGPU_JIT_CPAIR": "0"}),
 ])
 def test_generated_kernels_on_host(prec, env, tmp_path):

@@ -469,6 +469,19 @@ static bool phase_windows_on() {
   return v;
 }
 
+// width of the beam search over register-phase sequences (BTGPU_PLAN_PHASE_BEAM;
+// 1: the greedy choice).  Ranked by phases plus staged first/last phases, width 8
+// plans the 33-qubit brickwork into 92 phases with one staged end instead of 96
+// with six: 0.787 -> 0.744 s per circuit on a GB300.
+static int phase_beam() {
+  static const int v = [] {
+    const char* e = getenv("BTGPU_PLAN_PHASE_BEAM");
+    const int x = e && *e ? atoi(e) : 8;
+    return x < 1 ? 1 : (x > 64 ? 64 : x);
+  }();
+  return v;
+}
+
 // Pair-lane form (complex64 specialised passes, bt_jit.cu): one tile bit of the
 // pass, the lane bit, is a register bit of every phase, so each thread holds its
 // amplitudes as pairs that differ only in that bit and applies every op that
@@ -526,15 +539,16 @@ static bool build_fused(bt_plan* p, const std::vector<int>& take, uint64_t tilem
   const uint32_t pmask = pbit >= 0 ? 1u << pbit : 0u;
   const int NF = NB - (pbit >= 0 ? 1 : 0);  // register bits a phase chooses
   const int maxreals = sizeof(R) == 4 ? BT_FUSED_MAX_REALS_F : BT_FUSED_MAX_REALS_D;
-  // register phases: greedy over the pass's gates with blocking, in order
-  std::vector<int> rem = take;
-  int nop = 0, nreal = 0;
-  kept.clear();
-  // the gates a phase with register set rs takes (in order, a gate left out blocks
-  // its bits): rs grown gate by gate up to NB bits, or given
-  auto scan = [&](uint32_t rs, bool fixed, std::vector<int>& ph, std::vector<int>& rest, uint32_t& regs, int& nr) {
+  // register phases over the pass's gates with blocking, in order.  A phase with
+  // register set rs takes the gates it can in order (a gate left out blocks its
+  // bits): rs grown gate by gate up to NF bits, or a window of NF consecutive free
+  // tile bits.  The sequence of phases is chosen by a beam search over those
+  // candidates that keeps the `beam` partial sequences with the fewest gates left
+  // (width 1: the greedy choice of the candidate taking the most gates).
+  auto scan = [&](const std::vector<int>& rem, int nop0, int nreal0, uint32_t rs, bool fixed, std::vector<int>& ph,
+                  std::vector<int>& rest, uint32_t& regs, int& nr) {
     regs = fixed ? rs : 0;
-    nr = nreal;
+    nr = nreal0;
     uint32_t blocked = 0;
     ph.clear();
     rest.clear();
@@ -545,7 +559,7 @@ static bool build_fused(bt_plan* p, const std::vector<int>& take, uint64_t tilem
       const uint32_t lf = lb & ~pmask;  // the lane bit is in every phase
       const int need = g.k == 1 ? 8 : 32;
       if ((lb & blocked) || (fixed ? (lf & ~rs) != 0 : popc(regs | lf) > NF) ||
-          nop + (int)ph.size() + 1 > BT_FUSED_MAX_OPS || nr + need > maxreals) {
+          nop0 + (int)ph.size() + 1 > BT_FUSED_MAX_OPS || nr + need > maxreals) {
         blocked |= lb;
         rest.push_back(gi);
         continue;
@@ -559,28 +573,107 @@ static bool build_fused(bt_plan* p, const std::vector<int>& take, uint64_t tilem
   std::vector<int> free_bits;
   for (int b = 0; b < M; ++b)
     if (b != pbit) free_bits.push_back(b);
-  while (!rem.empty()) {
-    if (a.nphase >= BT_FUSED_MAX_PHASES) break;
-    uint32_t regs = 0, regs2 = 0;
-    int nr = 0, nr2 = 0;
-    std::vector<int> ph, rest, ph2, rest2;
-    scan(0, false, ph, rest, regs, nr);
-    if (phase_windows_on())  // or NF consecutive free tile bits, where they take more gates
-      for (int s = 0; s + NF <= (int)free_bits.size(); ++s) {
-        uint32_t w = 0;
-        for (int i = 0; i < NF; ++i) w |= 1u << free_bits[s + i];
-        scan(w, true, ph2, rest2, regs2, nr2);
-        if (ph2.size() > ph.size()) {
-          ph.swap(ph2);
-          rest.swap(rest2);
-          regs = regs2;
-          nr = nr2;
-        }
+  struct Seq {
+    std::vector<int> rem;
+    std::vector<uint32_t> regs;             // per phase
+    std::vector<std::vector<int>> gates;    // per phase
+    int nop = 0, nreal = 0;
+  };
+  // whether the specialised kernel can move a phase with register set regs
+  // straight between HBM and registers (as bt_jit.cu decides it: the warp's lanes
+  // on the lowest non-register tile bits touch at most twice the 128-byte lines
+  // their bytes need); a first or last phase that cannot is staged through shared
+  // memory, which costs about one more phase
+  const bool f32 = sizeof(R) == 4;
+  auto direct = [&](uint32_t regs) {
+    const uint32_t all = pbit >= 0 ? (regs | pmask) : regs;
+    const bool pair = f32 && (all & 1);
+    const int bytes = pair ? 16 : (f32 ? 8 : 16), linebits = f32 ? 4 : 3;
+    int lanes = 0, outside = 0;
+    for (int b = 0; b < M && lanes < 5; ++b)
+      if (!((all >> b) & 1)) {
+        outside += b >= linebits;
+        ++lanes;
       }
-    if (ph.empty()) break;
-    nreal = nr;
-    // pad the register set to NF bits with the highest unused free tile bits
-    for (int i = (int)free_bits.size() - 1; i >= 0 && popc(regs) < NF; --i) regs |= 1u << free_bits[i];
+    return (1 << outside) <= 2 * std::max(1, 32 * bytes / 128);
+  };
+  auto cost = [&](const Seq& q) {
+    if (q.regs.empty()) return 0;
+    return (int)q.regs.size() + (direct(q.regs.front()) ? 0 : 1) + (direct(q.regs.back()) ? 0 : 1);
+  };
+  const int beam = phase_beam();
+  std::vector<Seq> cur(1), complete;
+  cur[0].rem = take;
+  Seq best;
+  for (int depth = 0; depth < BT_FUSED_MAX_PHASES && !cur.empty(); ++depth) {
+    // a sequence still open needs at least one more phase
+    if (!complete.empty()) {
+      int bc = 1 << 30;
+      for (const Seq& q : complete) bc = std::min(bc, cost(q));
+      if (bc <= depth + 1) break;
+    }
+    std::vector<Seq> next;
+    for (const Seq& sq : cur) {
+      std::vector<uint32_t> cands = {0u};
+      std::vector<char> fixed = {0};
+      if (phase_windows_on())
+        for (int s0 = 0; s0 + NF <= (int)free_bits.size(); ++s0) {
+          uint32_t w = 0;
+          for (int i = 0; i < NF; ++i) w |= 1u << free_bits[s0 + i];
+          cands.push_back(w);
+          fixed.push_back(1);
+        }
+      // candidates in order, the one taking the most gates first (ties: earlier)
+      std::vector<Seq> kids;
+      std::vector<uint32_t> seen;
+      for (size_t ci = 0; ci < cands.size(); ++ci) {
+        Seq k;
+        std::vector<int> ph;
+        uint32_t regs = 0;
+        int nr = 0;
+        scan(sq.rem, sq.nop, sq.nreal, cands[ci], fixed[ci] != 0, ph, k.rem, regs, nr);
+        if (ph.empty()) continue;
+        // pad the register set to NF bits with the highest unused free tile bits
+        for (int i = (int)free_bits.size() - 1; i >= 0 && popc(regs) < NF; --i) regs |= 1u << free_bits[i];
+        if (std::find(seen.begin(), seen.end(), regs) != seen.end()) continue;
+        seen.push_back(regs);
+        k.regs = sq.regs;
+        k.regs.push_back(regs);
+        k.gates = sq.gates;
+        k.gates.push_back(ph);
+        k.nop = sq.nop + (int)ph.size();
+        k.nreal = nr;
+        kids.push_back(std::move(k));
+      }
+      std::stable_sort(kids.begin(), kids.end(),
+                       [](const Seq& x, const Seq& y) { return x.rem.size() < y.rem.size(); });
+      for (size_t i = 0; i < kids.size() && (int)i < beam; ++i) next.push_back(std::move(kids[i]));
+    }
+    if (next.empty()) break;
+    std::stable_sort(next.begin(), next.end(), [&](const Seq& x, const Seq& y) {
+      if (x.rem.size() != y.rem.size()) return x.rem.size() < y.rem.size();
+      return direct(x.regs.front()) && !direct(y.regs.front());
+    });
+    if ((int)next.size() > beam) next.resize(beam);
+    cur.clear();
+    for (Seq& q : next) {
+      if (q.rem.empty()) complete.push_back(std::move(q));
+      else cur.push_back(std::move(q));
+    }
+    if (beam == 1 && !complete.empty()) break;  // the greedy sequence
+  }
+  if (complete.empty() && !cur.empty()) complete.push_back(cur[0]);  // phase cap reached
+  if (!complete.empty()) {
+    best = complete[0];
+    for (const Seq& q : complete)
+      if (cost(q) < cost(best)) best = q;
+  }
+  int nop = 0, nreal = 0;
+  kept.clear();
+  for (size_t q = 0; q < best.regs.size(); ++q) {
+    const uint32_t regs = best.regs[q];
+    const std::vector<int>& ph = best.gates[q];
+    for (int gi : ph) nreal += p->gates[gi].k == 1 ? 8 : 32;
     FPhase& P = a.ph[a.nphase++];
     int rb = 0, regidx[32];
     for (int b = 0; b < M; ++b)
@@ -598,15 +691,11 @@ static bool build_fused(bt_plan* p, const std::vector<int>& take, uint64_t tilem
     for (int gi : ph) {
       const PGate& g = p->gates[gi];
       FOp& o = a.op[nop++];
-      int perm[4] = {0, 1, 2, 3};
-      const int cls = classify(g, perm);
       o.moff = (uint16_t)(nreal - (g.k == 1 ? 8 : 32));  // provisional; rewritten below
       o.b0 = (uint8_t)regidx[local[g.bits[0]]];
       o.b1 = g.k == 2 ? (uint8_t)regidx[local[g.bits[1]]] : 0;
       kept.push_back(gi);
-      (void)cls;
     }
-    rem.swap(rest);
   }
   // write matrices compactly in op order
   ob0.clear();

@@ -179,10 +179,25 @@ def test_host_plan_headline_pass_count():
     st = plan.stats()
     assert st["gates"] == 1470 and st["passes"] <= 26, st
     if os.environ.get("BTGPU_PLAN_PHASE_WINDOWS") != "0":
-        assert st["phases"] <= 100, st  # register-bit windows: 92 phases instead of 117
+        assert st["phases"] <= 100, st  # register-bit windows: 96 phases instead of 117
+        if os.environ.get("BTGPU_PLAN_PHASE_BEAM", "8") != "1":
+            assert st["phases"] <= 92, st  # beam search over phase sequences
     f, b = ctypes.c_double(), ctypes.c_double()
     L.check(L.lib().bt_plan_cost(plan.h, ctypes.byref(f), ctypes.byref(b)))
     assert b.value == 16 * st["passes"] and f.value < 2600, (f.value, b.value)
+
+
+def test_host_plans_with_greedy_phases():
+    """The same checks with the greedy choice of register phases
+    (BTGPU_PLAN_PHASE_BEAM=1, read once per process: run in a child)."""
+    if os.environ.get("BTGPU_PLAN_PHASE_BEAM") == "1":
+        pytest.skip("already running with greedy phases")
+    env = dict(os.environ, BTGPU_PLAN_PHASE_BEAM="1")
+    r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-x", "-p", "no:cacheprovider", __file__, "-k",
+                        "not without_phase_windows"],
+                       env=env, cwd=os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]
 
 
 def test_host_plans_without_phase_windows():

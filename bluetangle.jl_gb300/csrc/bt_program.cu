@@ -345,68 +345,6 @@ __global__ void __launch_bounds__(PG_THREADS) k_program(typename CT<R>::T* __res
 }
 
 // ------------------------------------------------------------------ grouped executor: decisions
-// D x D complex matrices (D <= 4), row-major interleaved, FP64
-__device__ void cm_mul(const double* a, const double* b, double* c, int D) {  // c = a b
-  for (int r = 0; r < D; ++r)
-    for (int k = 0; k < D; ++k) {
-      double sr = 0, si = 0;
-      for (int j = 0; j < D; ++j) {
-        const double ar = a[2 * (r * D + j)], ai = a[2 * (r * D + j) + 1];
-        const double br = b[2 * (j * D + k)], bi = b[2 * (j * D + k) + 1];
-        sr += ar * br - ai * bi;
-        si += ar * bi + ai * br;
-      }
-      c[2 * (r * D + k)] = sr;
-      c[2 * (r * D + k) + 1] = si;
-    }
-}
-
-// c = a b a^dagger
-__device__ void cm_conj(const double* a, const double* b, double* c, int D) {
-  double t[32];
-  cm_mul(a, b, t, D);
-  for (int r = 0; r < D; ++r)
-    for (int k = 0; k < D; ++k) {
-      double sr = 0, si = 0;
-      for (int j = 0; j < D; ++j) {
-        const double tr = t[2 * (r * D + j)], ti = t[2 * (r * D + j) + 1];
-        const double ar = a[2 * (k * D + j)], ai = -a[2 * (k * D + j) + 1];  // conj(a[k][j])
-        sr += tr * ar - ti * ai;
-        si += tr * ai + ti * ar;
-      }
-      c[2 * (r * D + k)] = sr;
-      c[2 * (r * D + k) + 1] = si;
-    }
-}
-
-// op matrix (op bits x[, y], x = most significant) embedded into the group's
-// space (q0 = most significant bit of the group index)
-__device__ void embed(const double* K, int opk, int x, int y, const PGGroup& g, double* E) {
-  const int D = 1 << g.nb;
-  for (int e = 0; e < 2 * D * D; ++e) E[e] = 0;
-  if (g.nb == 1 || (opk == 2 && x == g.q0)) {  // the op spans the group in its order
-    for (int e = 0; e < 2 * D * D; ++e) E[e] = K[e];
-    return;
-  }
-  if (opk == 2) {  // (x, y) = (q1, q0): swap the two index bits
-    const int sw[4] = {0, 2, 1, 3};
-    for (int r = 0; r < 4; ++r)
-      for (int c = 0; c < 4; ++c) {
-        E[2 * (r * 4 + c)] = K[2 * (sw[r] * 4 + sw[c])];
-        E[2 * (r * 4 + c) + 1] = K[2 * (sw[r] * 4 + sw[c]) + 1];
-      }
-    return;
-  }
-  // one-qubit op in a two-qubit group: K (x) I if x = q0, I (x) K if x = q1
-  for (int a = 0; a < 2; ++a)
-    for (int b = 0; b < 2; ++b)
-      for (int c = 0; c < 2; ++c) {
-        const int r = x == g.q0 ? 2 * a + c : 2 * c + a, col = x == g.q0 ? 2 * b + c : 2 * c + b;
-        E[2 * (r * 4 + col)] = K[2 * (a * 2 + b)];
-        E[2 * (r * 4 + col) + 1] = K[2 * (a * 2 + b) + 1];
-      }
-}
-
 // the group's reduced matrix restricted to the op's qubits, in the op's order
 __device__ void restrict_rho(const double* rho, int opk, int x, const PGGroup& g, double* out) {
   const int D = 1 << g.nb;
@@ -436,81 +374,173 @@ __device__ void restrict_rho(const double* rho, int opk, int x, const PGGroup& g
     }
 }
 
-// One thread per member: every op of group g, decided from rho_Q; writes the
-// product of the chosen (renormalised) matrices in the state precision.  Failure
-// rules as in k_program: an op whose branch or outcome has zero probability is
-// skipped for that member (record -1) and reported through the status word.
+// A team of 16 threads per member (two members per warp): every op of group g,
+// decided from rho_Q; writes the product of the chosen (renormalised) matrices in
+// the state precision.  The 4x4 complex algebra of an op (the product E M, the
+// update E rho E^dagger) is split one matrix entry per thread, and a channel's
+// branch probabilities one Kraus operator per thread, in shared memory; the
+// decisions themselves (the cumulative sums against the member's draw) are made
+// by the team's first thread in the reference's order, so they equal the
+// one-thread form's.  GB300's FP64 rate is a small share of its FP32 rate: split
+// this way a member's chain of FP64 operations is 16 times shorter.  Failure rules
+// as in k_program: an op whose branch or outcome has zero probability is skipped
+// for that member (record -1) and reported through the status word.
+#define PGD_TEAM 16
+#define PGD_TEAMS 8  // members per block (128 threads)
+struct PGDShared {
+  double M[32], rho[32], tmp[32], E[32], K[32], rop[32], p[PG_MAX_KRAUS];
+  int ind, skipped;
+  double sc;
+};
+
 template <typename R>
-__global__ void k_group_decide(const PGGroup g, const PGOp* __restrict__ ops, const R* __restrict__ gm,
-                               const double* __restrict__ km, const int8_t* __restrict__ skip,
-                               const int8_t* __restrict__ act, const double* __restrict__ u, uint64_t key,
-                               uint64_t stream, int batch, const double* __restrict__ rho_in, R* __restrict__ mat_out,
-                               int32_t* __restrict__ rec, int nrec, int* __restrict__ status) {
-  const int m = g.mlo + blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= g.mhi) return;
+__global__ void __launch_bounds__(PGD_TEAM * PGD_TEAMS) k_group_decide(
+    const PGGroup g, const PGOp* __restrict__ ops, const R* __restrict__ gm, const double* __restrict__ km,
+    const int8_t* __restrict__ skip, const int8_t* __restrict__ act, const double* __restrict__ u, uint64_t key,
+    uint64_t stream, int batch, const double* __restrict__ rho_in, R* __restrict__ mat_out,
+    int32_t* __restrict__ rec, int nrec, int* __restrict__ status) {
+  __shared__ PGDShared shm[PGD_TEAMS];
+  const int team = threadIdx.x / PGD_TEAM, t = threadIdx.x % PGD_TEAM;
+  const unsigned mask = 0xFFFFu << (16 * (team & 1));  // the team's lanes of its warp
+  const int m = g.mlo + blockIdx.x * PGD_TEAMS + team;
+  if (m >= g.mhi) return;  // the whole team leaves together
+  PGDShared& S = shm[team];
   const int D = 1 << g.nb;
   const bool on = act[m];
-  double M[32], rho[32], E[32], t[32], K[32], rop[32];
-  for (int e = 0; e < 2 * D * D; ++e) {
-    M[e] = (e % (2 * D + 2)) == 0 ? 1.0 : 0.0;
-    // the reduction's layout: 2 D^2 reals per member, from the group's first member
-    rho[e] = g.need_rho && on ? rho_in[(int64_t)(m - g.mlo) * 2 * D * D + e] : 0.0;
+  const int r = t / D, c = t % D;  // the matrix entry of this thread (t < D*D)
+  const bool ent = t < D * D;
+  if (ent) {
+    S.M[2 * t] = r == c ? 1.0 : 0.0;
+    S.M[2 * t + 1] = 0.0;
+    S.rho[2 * t] = g.need_rho && on ? rho_in[(int64_t)(m - g.mlo) * 2 * D * D + 2 * t] : 0.0;
+    S.rho[2 * t + 1] = g.need_rho && on ? rho_in[(int64_t)(m - g.mlo) * 2 * D * D + 2 * t + 1] : 0.0;
   }
+  __syncwarp(mask);
   for (int oi = g.op0; oi < g.op0 + g.nop; ++oi) {
     const PGOp op = ops[oi];
     const bool skipped = !on || m < op.mlo || m >= op.mhi || (op.skip_off >= 0 && skip[op.skip_off + m]);
     if (skipped) {
-      if (op.type == PG_MEASURE) rec[(int64_t)m * nrec + op.rec_idx] = -1;
+      if (op.type == PG_MEASURE && t == 0) rec[(int64_t)m * nrec + op.rec_idx] = -1;
       continue;
     }
     const int opk = op.type == PG_GATE2 ? 2 : (op.type == PG_CHANNEL ? op.k : 1);
     const int d = 1 << opk;
     if (op.type == PG_GATE1 || op.type == PG_GATE2) {
       const R* src = gm + op.moff + (int64_t)op.mstride * (m - op.mlo);
-      for (int e = 0; e < 2 * d * d; ++e) K[e] = (double)src[e];
+      for (int e = t; e < 2 * d * d; e += PGD_TEAM) S.K[e] = (double)src[e];
     } else if (op.type == PG_CHANNEL) {
       const bool umix = op.flags & 2;
-      if (!umix) restrict_rho(rho, opk, op.b0, g, rop);
-      const double uu = u ? u[(int64_t)op.rand_idx * batch + m] : bt_uniform(key, stream ^ (uint64_t)op.rand_idx, m);
-      double cum = 0;
-      int ind = -1;
-      for (int i = 0; i < op.nk; ++i) {
-        cum += tr_krk(km + op.moff + (int64_t)i * 2 * d * d, rop, d, umix, (op.flags & 1) && opk == 2);
-        if (ind < 0 && uu <= cum) ind = i;
+      if (t == 0 && !umix) restrict_rho(S.rho, opk, op.b0, g, S.rop);
+      __syncwarp(mask);
+      for (int i = t; i < op.nk; i += PGD_TEAM)
+        S.p[i] = tr_krk(km + op.moff + (int64_t)i * 2 * d * d, S.rop, d, umix, (op.flags & 1) && opk == 2);
+      __syncwarp(mask);
+      if (t == 0) {
+        const double uu = u ? u[(int64_t)op.rand_idx * batch + m] : bt_uniform(key, stream ^ (uint64_t)op.rand_idx, m);
+        double cum = 0;
+        int ind = -1;
+        for (int i = 0; i < op.nk; ++i) {
+          cum += S.p[i];
+          if (ind < 0 && uu <= cum) ind = i;
+        }
+        const double nrm = ind >= 0 ? tr_krk(km + op.moff + (int64_t)ind * 2 * d * d, S.rop, d, umix, false) : 0.0;
+        S.skipped = ind < 0 || !(nrm > 0);
+        if (S.skipped) atomicExch(status, ind < 0 ? 2 : 3);
+        S.ind = ind < 0 ? 0 : ind;
+        S.sc = S.skipped ? 0.0 : 1.0 / sqrt(nrm);
       }
-      const double* Ki = km + op.moff + (int64_t)(ind < 0 ? 0 : ind) * 2 * d * d;
-      const double nrm = ind >= 0 ? tr_krk(Ki, rop, d, umix, false) : 0.0;
-      if (ind < 0 || !(nrm > 0)) {
-        atomicExch(status, ind < 0 ? 2 : 3);
-        continue;
-      }
-      const double sc = 1.0 / sqrt(nrm);
-      for (int e = 0; e < 2 * d * d; ++e) K[e] = Ki[e] * sc;
+      __syncwarp(mask);
+      if (S.skipped) continue;
+      const double* Ki = km + op.moff + (int64_t)S.ind * 2 * d * d;
+      for (int e = t; e < 2 * d * d; e += PGD_TEAM) S.K[e] = Ki[e] * S.sc;
     } else {  // measurement: outcome u < p0 ? 0 : 1 from the qubit's reduced matrix
-      restrict_rho(rho, 1, op.b0, g, rop);
-      const double s0 = rop[0], s1 = rop[6];
-      const double uu = u ? u[(int64_t)op.rand_idx * batch + m] : bt_uniform(key, stream ^ (uint64_t)op.rand_idx, m);
-      const int ind = uu < s0 ? 0 : 1;
-      const double keep = ind ? s1 : s0;
-      if (!(keep > 0)) {
-        atomicExch(status, 1);
-        rec[(int64_t)m * nrec + op.rec_idx] = -1;
-        continue;
+      if (t == 0) {
+        restrict_rho(S.rho, 1, op.b0, g, S.rop);
+        const double s0 = S.rop[0], s1 = S.rop[6];
+        const double uu = u ? u[(int64_t)op.rand_idx * batch + m] : bt_uniform(key, stream ^ (uint64_t)op.rand_idx, m);
+        const int ind = uu < s0 ? 0 : 1;
+        const double keep = ind ? s1 : s0;
+        S.skipped = !(keep > 0);
+        if (S.skipped) {
+          atomicExch(status, 1);
+          rec[(int64_t)m * nrec + op.rec_idx] = -1;
+        } else {
+          rec[(int64_t)m * nrec + op.rec_idx] = ind;
+          for (int e = 0; e < 8; ++e) S.K[e] = 0;
+          S.K[ind ? 6 : 0] = 1.0 / sqrt(keep);
+        }
       }
-      rec[(int64_t)m * nrec + op.rec_idx] = ind;
-      for (int e = 0; e < 8; ++e) K[e] = 0;
-      K[ind ? 6 : 0] = 1.0 / sqrt(keep);
+      __syncwarp(mask);
+      if (S.skipped) continue;
     }
-    embed(K, opk, op.b0, op.b1, g, E);
-    cm_mul(E, M, t, D);
-    for (int e = 0; e < 2 * D * D; ++e) M[e] = t[e];
-    if (g.need_rho) {
-      cm_conj(E, rho, t, D);
-      for (int e = 0; e < 2 * D * D; ++e) rho[e] = t[e];
+    __syncwarp(mask);
+    // E: the op's matrix in the group's space (q0 the most significant bit)
+    if (ent) {
+      double er = 0, ei = 0;
+      if (g.nb == 1 || (opk == 2 && op.b0 == g.q0)) {
+        er = S.K[2 * t];
+        ei = S.K[2 * t + 1];
+      } else if (opk == 2) {  // (x, y) = (q1, q0): the two index bits swapped
+        const int sw[4] = {0, 2, 1, 3};
+        er = S.K[2 * (sw[r] * 4 + sw[c])];
+        ei = S.K[2 * (sw[r] * 4 + sw[c]) + 1];
+      } else if (op.b0 == g.q0) {  // K (x) I
+        if ((r & 1) == (c & 1)) {
+          er = S.K[2 * ((r >> 1) * 2 + (c >> 1))];
+          ei = S.K[2 * ((r >> 1) * 2 + (c >> 1)) + 1];
+        }
+      } else {  // I (x) K
+        if ((r >> 1) == (c >> 1)) {
+          er = S.K[2 * ((r & 1) * 2 + (c & 1))];
+          ei = S.K[2 * ((r & 1) * 2 + (c & 1)) + 1];
+        }
+      }
+      S.E[2 * t] = er;
+      S.E[2 * t + 1] = ei;
     }
+    __syncwarp(mask);
+    // M <- E M; rho <- E rho E^dagger (every read of M and rho before the barrier,
+    // every write after it)
+    double sr = 0, si = 0;
+    if (ent) {
+      double tr_ = 0, ti = 0;
+      for (int k = 0; k < D; ++k) {
+        const double ar = S.E[2 * (r * D + k)], ai = S.E[2 * (r * D + k) + 1];
+        const double br = S.M[2 * (k * D + c)], bi = S.M[2 * (k * D + c) + 1];
+        sr += ar * br - ai * bi;
+        si += ar * bi + ai * br;
+        if (g.need_rho) {
+          const double cr = S.rho[2 * (k * D + c)], ci = S.rho[2 * (k * D + c) + 1];
+          tr_ += ar * cr - ai * ci;
+          ti += ar * ci + ai * cr;
+        }
+      }
+      S.tmp[2 * t] = tr_;
+      S.tmp[2 * t + 1] = ti;
+    }
+    __syncwarp(mask);
+    if (ent) {
+      S.M[2 * t] = sr;
+      S.M[2 * t + 1] = si;
+      if (g.need_rho) {
+        double qr = 0, qi = 0;
+        for (int k = 0; k < D; ++k) {
+          const double xr = S.tmp[2 * (r * D + k)], xi = S.tmp[2 * (r * D + k) + 1];
+          const double er = S.E[2 * (c * D + k)], ei = -S.E[2 * (c * D + k) + 1];  // conj(E[c][k])
+          qr += xr * er - xi * ei;
+          qi += xr * ei + xi * er;
+        }
+        S.rho[2 * t] = qr;
+        S.rho[2 * t + 1] = qi;
+      }
+    }
+    __syncwarp(mask);
   }
-  R* out = mat_out + (int64_t)m * 32;
-  for (int e = 0; e < 2 * D * D; ++e) out[e] = (R)M[e];
+  if (ent) {
+    R* out = mat_out + (int64_t)m * 32;
+    out[2 * t] = (R)S.M[2 * t];
+    out[2 * t + 1] = (R)S.M[2 * t + 1];
+  }
 }
 
 // ------------------------------------------------------------------ host API
@@ -884,14 +914,14 @@ int bt_program_run(bt_program* p, bt_state* s, const double* uniforms, uint64_t 
       const int64_t nm = g.mhi - g.mlo;
       if (g.need_rho) rc = bt_launch_rdm(s, g.nb, bits, g.mlo, nm, (double*)p->d_rho, act);
       if (rc) break;
-      const unsigned grid = (unsigned)((nm + 127) / 128);
+      const unsigned grid = (unsigned)((nm + PGD_TEAMS - 1) / PGD_TEAMS);
       if (f)
-        k_group_decide<float><<<grid, 128, 0, ctx->stream>>>(
+        k_group_decide<float><<<grid, PGD_TEAM * PGD_TEAMS, 0, ctx->stream>>>(
             g, (const PGOp*)p->d_ops, (const float*)p->d_gm, (const double*)p->d_km, (const int8_t*)p->d_skip, act,
             du, ctx->seed, stream, p->batch, (const double*)p->d_rho, (float*)p->d_mat, (int32_t*)p->d_rec, nrec,
             ctx->d_status);
       else
-        k_group_decide<double><<<grid, 128, 0, ctx->stream>>>(
+        k_group_decide<double><<<grid, PGD_TEAM * PGD_TEAMS, 0, ctx->stream>>>(
             g, (const PGOp*)p->d_ops, (const double*)p->d_gm, (const double*)p->d_km, (const int8_t*)p->d_skip, act,
             du, ctx->seed, stream, p->batch, (const double*)p->d_rho, (double*)p->d_mat, (int32_t*)p->d_rec, nrec,
             ctx->d_status);

@@ -116,6 +116,37 @@ __device__ __forceinline__ float phi(u64 r) { return __uint_as_float((unsigned)(
 __device__ __forceinline__ u64 ffma2(u64 a, u64 b, u64 c) { u64 d; asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c)); return d; }
 __device__ __forceinline__ u64 fmul2(u64 a, u64 b) { u64 d; asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b)); return d; }
 __device__ __forceinline__ u64 bc(float a) { return pk(a, a); }
+// float-float numbers (complex128 passes in FP32 arithmetic, BTGPU_JIT_FF): a
+// value is h + l with |l| <= ulp(h) / 2, 48 significant bits; sums by TwoSum and
+// products by FMA-exact TwoProduct (Dekker, Knuth; Joldes, Muller and Popescu's
+// accurate double-word algorithms), each renormalised by FastTwoSum
+struct ff {
+  float h, l;
+  __device__ __forceinline__ ff() {}
+  __device__ __forceinline__ ff(float a, float b) : h(a), l(b) {}
+  __device__ __forceinline__ ff(double d) {
+    h = __double2float_rn(d);
+    l = __double2float_rn(d - (double)h);
+  }
+  __device__ __forceinline__ operator double() const { return (double)h + (double)l; }
+};
+struct __align__(16) ffc2 { ff x, y; };
+__device__ __forceinline__ ff ff_fast(float s, float e) { const float t = s + e; return ff(t, e - (t - s)); }
+__device__ __forceinline__ ff operator+(ff a, ff b) {
+  const float s = a.h + b.h, bb = s - a.h, e = (a.h - (s - bb)) + (b.h - bb);
+  return ff_fast(s, e + (a.l + b.l));
+}
+__device__ __forceinline__ ff operator-(ff a) { return ff(-a.h, -a.l); }
+__device__ __forceinline__ ff operator-(ff a, ff b) { return a + (-b); }
+__device__ __forceinline__ ff operator*(ff a, ff b) {
+  const float p = a.h * b.h;
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, e));
+  return ff_fast(p, e);
+}
+__device__ __forceinline__ ff fm(ff a, ff b, ff c) { return a * b + c; }
+// coefficients arrive split on the host: each double slot holds the floats (h, l)
+__device__ __forceinline__ const ff* ffp(const double* p) { return reinterpret_cast<const ff*>(p); }
 )PRELUDE";
 
 static std::string fmt_u64(uint64_t v) {
@@ -135,6 +166,18 @@ static int swz_host(bool f, int l) { return f ? (l ^ ((l >> 4) & 15)) : (l ^ ((l
 // coefficients (phases, RX) mix the two parts and stay scalar.  Measured on the
 // 28- and 33-qubit brickwork: 8.5% fewer instructions, FMA pipe busier by as
 // much, pass times unchanged (the passes are bound by neither issue nor FMA).
+// complex128 fused passes in float-float arithmetic (on unless BTGPU_JIT_FF=0):
+// GB300 issues FP64 at a small share of its FP32 rate, so the passes' complex128
+// arithmetic runs as float-float on the FP32 pipe (48-bit significands: relative
+// error ~2^-48 per operation, far inside the 1e-12 the complex128 results are held
+// to); the tile keeps float-float pairs (16 bytes per amplitude, as a complex128
+// value), HBM keeps complex128, and coefficients are split on the host.  32-qubit
+// brickwork of depth 30: 12.17 -> 5.99 s per circuit on a GB300.
+bool bt_jit_ff_on() {
+  static const bool v = env_int("BTGPU_JIT_FF", 1, 0, 1) != 0;
+  return v;
+}
+
 static bool cpair_on() {
   static const bool v = env_int("BTGPU_JIT_CPAIR", 0, 0, 1) != 0;
   return v;
@@ -328,8 +371,8 @@ static void emit_op(std::ostringstream& o, const FOp& op, int NB, const char* mr
         o << ";";
         for (int r = 0; r < 4; ++r) {
           std::ostringstream re, im;
-          re << "0";
-          im << "0";
+          re << "(R)0";  // a zero of the arithmetic's type (float, double or float-float)
+          im << "(R)0";
           for (int c = 0; c < 4; ++c) {
             re.str("fm(g" + std::to_string(8 * r + 2 * c) + ",r" + std::to_string(c) + ",fm(-g" +
                    std::to_string(8 * r + 2 * c + 1) + ",i" + std::to_string(c) + "," + re.str() + "))");
@@ -715,9 +758,12 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
   const int T = 1 << (M - NB);
   const int NPT = (1 << M) / V / T;
   const char* T2 = f ? "cf" : "cd";
+  // float-float form of a complex128 pass (not the per-member kernels)
+  const bool ffm = !f && !a.permem && bt_jit_ff_on();
+  const char* TT = ffm ? "ffc2" : T2;  // the shared-memory tile's element
   // per-member entries (a.permem): member m of the launch reads its ops' entries from
   // row m of the table mm (mstride reals per row) instead of the kernel parameters
-  const char* mref = a.permem ? "cm" : "a.mat";
+  const char* mref = a.permem ? "cm" : (ffm ? "ffp(a.mat)" : "a.mat");
   // six register bits: 128 threads of up to 170 registers, three CTAs per SM
   // (BTGPU_JIT_MINB6 sets another count)
   static const int minb6 = env_int("BTGPU_JIT_MINB6", 3, 1, 4);
@@ -727,7 +773,7 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
     << (f ? "JitArgsF<" : "JitArgsD<") << NM << "> a";
   if (a.permem) o << ", const " << (f ? "float" : "double") << "* __restrict__ mm, const i64 mstride";
   o << ") {\n";
-  o << "  typedef " << (f ? "float" : "double") << " R;\n";
+  o << "  typedef " << (f ? "float" : (ffm ? "ff" : "double")) << " R;\n";
   const int NP = a.nphase;
   if (NP == 0) {  // nothing to apply
     o << "}\n";
@@ -742,7 +788,7 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
   // current one, so its load latency hides behind that phase's arithmetic and
   // stores.
   const bool dlast = direct_ok(a.ph[NP - 1], NB, M, f);
-  const bool pf = dlast && prefetch_on();
+  const bool pf = dlast && prefetch_on() && !ffm;
   const bool dfirst = !pf && direct_ok(a.ph[0], NB, M, f);
   const bool staged = pf || !dfirst || !dlast;
   const bool use_smem = staged || NP > 1;
@@ -764,7 +810,7 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
   };
   if (use_smem) {
     o << "  extern __shared__ __align__(16) unsigned char smem_raw[];\n";
-    o << "  " << T2 << "* tile = reinterpret_cast<" << T2 << "*>(smem_raw);\n";
+    o << "  " << TT << "* tile = reinterpret_cast<" << TT << "*>(smem_raw);\n";
   }
   if (staged) {
     o << "  i64* runoff = reinterpret_cast<i64*>(smem_raw + " << ((f ? 8 : 16) << M) << ");\n";
@@ -834,6 +880,9 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
         o << "      { const int s0 = l" << i << " ^ ((l" << i << " >> 4) & 15), s1 = (l" << i << " + 1) ^ (((l" << i
           << " + 1) >> 4) & 15); tile[s0] = cf{b" << i << ".x, b" << i << ".y}; tile[s1] = cf{b" << i << ".z, b" << i
           << ".w}; }\n";
+      else if (ffm)
+        o << "      { const cd d = *reinterpret_cast<const cd*>(&b" << i << "); tile[l" << i << " ^ ((l" << i
+          << " >> 3) & 7)] = ffc2{ff(d.x), ff(d.y)}; }\n";
       else
         o << "      *reinterpret_cast<f4*>(&tile[l" << i << " ^ ((l" << i << " >> 3) & 7)]) = b" << i << ";\n";
     }
@@ -896,7 +945,7 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
       o << "    }\n";
     } else {
       for (int j = 0; j < D; ++j)
-        o << "    { const " << T2 << " v = tile[" << saddr(j) << "]; x" << j << " = v.x; y" << j << " = v.y; }\n";
+        o << "    { const " << TT << " v = tile[" << saddr(j) << "]; x" << j << " = v.x; y" << j << " = v.y; }\n";
       // the tile's last shared-memory reads: the next tile may overwrite it once every warp is past them
       if (wr_direct) o << "    __syncthreads();\n";
       if (wr_direct && pf) o << "    fetch(tid + gridDim.x);\n";
@@ -950,7 +999,7 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
       }
       o << "    }\n    }\n";
     } else {
-      for (int j = 0; j < D; ++j) o << "    tile[" << saddr(j) << "] = " << T2 << "{x" << j << ", y" << j << "};\n";
+      for (int j = 0; j < D; ++j) o << "    tile[" << saddr(j) << "] = " << TT << "{x" << j << ", y" << j << "};\n";
       o << "    __syncthreads();\n    }\n";
     }
   }
@@ -962,6 +1011,9 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
         o << " const cf u" << i << " = tile[l" << i << " ^ ((l" << i << " >> 4) & 15)], v" << i << " = tile[(l" << i
           << " + 1) ^ (((l" << i << " + 1) >> 4) & 15)]; const f4 b" << i << " = f4{u" << i << ".x, u" << i << ".y, v"
           << i << ".x, v" << i << ".y};\n";
+      else if (ffm)
+        o << " f4 b" << i << "; { const ffc2 e = tile[l" << i << " ^ ((l" << i << " >> 3) & 7)]; const cd d = cd{(double)e.x, "
+          << "(double)e.y}; b" << i << " = *reinterpret_cast<const f4*>(&d); }\n";
       else
         o << " const f4 b" << i << " = *reinterpret_cast<const f4*>(&tile[l" << i << " ^ ((l" << i << " >> 3) & 7)]);\n";
     }
@@ -1612,6 +1664,15 @@ static int jit_launch_t(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<R>&
   h.nbits = a.nbits;
   h.lg_tiles = a.lg_tiles;
   memcpy(h.mat, a.mat, sizeof(h.mat));
+  if (sizeof(R) == 8 && !a.permem && bt_jit_ff_on()) {
+    // float-float kernels read each coefficient as the floats (h, l) packed in its slot
+    for (size_t i = 0; i < sizeof(h.mat) / sizeof(R); ++i) {
+      const double d = (double)a.mat[i];
+      const float hi = (float)d, lo = (float)(d - (double)hi);
+      float pair[2] = {hi, lo};
+      memcpy(reinterpret_cast<char*>(h.mat) + i * 8, pair, 8);
+    }
+  }
   void* args[] = {&psi, &h, &mm, &mstride};
   int64_t total = (1LL << a.lg_tiles) * a.nmem;
   int64_t grid = (int64_t)ctx->sm_count * bt_jit_min_blocks() * 4;

@@ -39,6 +39,7 @@ alignas(16) static unsigned char g_smem[1 << 18];
 #define __align__(n) alignas(n)
 #define __syncthreads() g_bar->arrive_and_wait()
 static inline float __fmaf_rn(float a, float b, float c) { return std::fmaf(a, b, c); }
+static inline float __double2float_rn(double d) { return (float)d; }
 static inline double __fma_rn(double a, double b, double c) { return std::fma(a, b, c); }
 static inline unsigned __float_as_uint(float f) { unsigned u; std::memcpy(&u, &f, 4); return u; }
 static inline float __uint_as_float(unsigned u) { float f; std::memcpy(&f, &u, 4); return f; }
@@ -125,6 +126,16 @@ def build(src, workdir, c64, permem=False):
     return lib, kernels
 
 
+def _ff_slots(mats, nreals):
+    """Each coefficient as the floats (h, l) packed in its double slot, as the
+    library's launcher passes them to float-float complex128 kernels."""
+    m = np.asarray(mats[:nreals], dtype=np.float64)
+    packed = np.empty(2 * nreals, dtype=np.float32)
+    packed[0::2] = m.astype(np.float32)
+    packed[1::2] = (m - packed[0::2].astype(np.float64)).astype(np.float32)
+    return packed.view(np.float64)
+
+
 def run_members(plan, psis, src, src_pm, workdir, indices, member_mats):
     """Member m of psis (a (members, 2^n) array) under the plan with member_mats[m]
     for the gates of these add indices, as bt_plan_run_members runs it: passes
@@ -166,8 +177,9 @@ def run_members(plan, psis, src, src_pm, workdir, indices, member_mats):
         a = Args()
         name, M, threads = kernels[fused]
         a.member_lo, a.nmem, a.nbits, a.lg_tiles = 0, B, nbits, nbits - M
+        vals = _ff_slots(mats, nreals) if (not c64 and os.environ.get("BTGPU_JIT_FF", "1") != "0") else mats
         for e in range(nreals):
-            a.mat[e] = mats[e]
+            a.mat[e] = vals[e]
         grid = min(B << (nbits - M), 3)
         rows = table[:B * used.value].reshape(B, used.value)
         # a pass without member-dependent gates has equal rows (members here differ in
@@ -201,6 +213,9 @@ def run(plan, psi, dump_src, workdir, members=1):
     x = np.asarray(psi, dtype=np.complex128).ravel(order="F").copy()
     nbits = int(x.size // members).bit_length() - 1
     state = x.astype(np.complex64 if c64 else np.complex128)
+    # float-float complex128 kernels read each coefficient as the floats (h, l)
+    # packed in its slot, as the library's launcher writes them
+    ffm = not c64 and os.environ.get("BTGPU_JIT_FF", "1") != "0"
     fused = 0
     for kind, ops, mats in E.passes(plan):
         if kind:
@@ -213,8 +228,9 @@ def run(plan, psi, dump_src, workdir, members=1):
         assert name == f"pass_{fused}"
         a = Args()
         a.member_lo, a.nmem, a.nbits, a.lg_tiles = 0, members, nbits, nbits - M
+        vals = _ff_slots(mats, nreals) if ffm else mats
         for e in range(nreals):
-            a.mat[e] = mats[e]
+            a.mat[e] = vals[e]
         grid = min(members << (nbits - M), 3)  # fewer CTAs than tiles: each loops over several
         rc = lib.run_pass(fused, state.ctypes.data_as(ctypes.c_void_p), ctypes.byref(a), grid, threads)
         assert rc == 0

@@ -148,6 +148,8 @@ print("OK")
     ("c64", {"BTGPU_JIT_LANES": "1", "BTGPU_JIT_DIRECT": "0"}),
     ("c64", {"BTGPU_JIT_CPAIR": "1"}),
     ("c64", {"BTGPU_TILE_RB": "6"}),
+    ("c128", {"BTGPU_JIT_FF": "0"}),
+    ("c128", {"BTGPU_JIT_FF": "0", "BTGPU_JIT_DIRECT": "0"}),
     ("c64", {"BTGPU_JIT_CPAIR": "0"}),
 ])
 def test_generated_kernels_on_host(prec, env, tmp_path):
@@ -236,3 +238,39 @@ def test_per_member_matrices_on_host(prec, tmp_path):
                        timeout=900)
     assert r.returncode == 0 and r.stdout.rstrip().endswith("OK"), r.stdout[-2000:] + r.stderr[-4000:]
 
+
+
+_COMPILE = r"""
+import os, sys
+import numpy as np
+root = sys.argv[1]
+sys.path[:0] = [os.path.join(root, "tests"), os.path.join(root, "bluetangle.jl_gb300")]
+import plan_emulator as E
+import bluetangle_gpu.circuits as C
+n = 14
+p = E.host_plan(n, prec=sys.argv[2])
+rng = np.random.default_rng(3)
+for o in C.random_ops(n, 3, rng) + C.brickwork(n, 3, rng):
+    p.add(o)
+p.compile()
+print("OK")
+"""
+
+
+@pytest.mark.parametrize("prec,env", [("c64", {}), ("c128", {}), ("c128", {"BTGPU_JIT_FF": "0"})])
+def test_generated_kernels_compile_for_sm103a(prec, env, tmp_path):
+    """The generated source of every op type (random gates of the reference's set,
+    dense two-qubit blocks included) compiles for sm_103a as the library's NVRTC
+    would compile it (nvcc on the host: no GPU needed)."""
+    import shutil
+    if not shutil.which("nvcc"):
+        pytest.skip("nvcc not on PATH")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "k.cu"
+    e = dict(os.environ, BTGPU_JIT_DUMP=str(src), BTGPU_JIT_DUMP_ONLY="1", **env)
+    e.pop("BTGPU_NO_JIT", None)
+    r = subprocess.run([sys.executable, "-c", _COMPILE, root, prec], env=e, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and r.stdout.rstrip().endswith("OK"), r.stderr[-3000:]
+    r = subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-cubin", "-O1", "-std=c++17",
+                        "-o", str(tmp_path / "k.cubin"), str(src)], capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-3000:]

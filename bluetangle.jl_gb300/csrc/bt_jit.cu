@@ -178,6 +178,15 @@ bool bt_jit_ff_on() {
   return v;
 }
 
+// a pass in float-float form: complex128, not a per-member kernel, and on a state
+// of at least 2^16 entries (smaller ones are latency-bound, where the longer
+// float-float chains cost more than the FP64 issue rate: 12-qubit plans ran 5%
+// slower in it)
+template <typename R>
+static bool ff_pass(const FusedArgs<R>& a) {
+  return sizeof(R) == 8 && !a.permem && a.nbits >= 16 && bt_jit_ff_on();
+}
+
 static bool cpair_on() {
   static const bool v = env_int("BTGPU_JIT_CPAIR", 0, 0, 1) != 0;
   return v;
@@ -759,7 +768,7 @@ static void gen_kernel(std::ostringstream& o, const FusedArgs<R>& a, int NB, con
   const int NPT = (1 << M) / V / T;
   const char* T2 = f ? "cf" : "cd";
   // float-float form of a complex128 pass (not the per-member kernels)
-  const bool ffm = !f && !a.permem && bt_jit_ff_on();
+  const bool ffm = ff_pass(a);
   const char* TT = ffm ? "ffc2" : T2;  // the shared-memory tile's element
   // per-member entries (a.permem): member m of the launch reads its ops' entries from
   // row m of the table mm (mstride reals per row) instead of the kernel parameters
@@ -1423,7 +1432,7 @@ static std::string structure_key(const FusedArgs<R>& a) {
   std::ostringstream k;
   k << (sizeof(R) == 4 ? 'f' : 'd') << a.M << ':' << a.c << ':' << bt_jit_min_blocks() << ':'
     << (a.nphase ? (int)a.ph[0].nreg : 0) << ':' << (sizeof(R) == 4 && a.packed ? 'p' : 's') << ':'
-    << (a.permem ? 'm' : 'k') << ':' << a.pbit << ':';
+    << (a.permem ? 'm' : 'k') << ':' << a.pbit << ':' << (ff_pass(a) ? 'F' : 'N') << ':';
   for (int i = 0; i < a.M; ++i) k << a.tbits[i] << ',';
   for (int p = 0; p < a.nphase; ++p) {
     const FPhase& ph = a.ph[p];
@@ -1664,7 +1673,7 @@ static int jit_launch_t(bt_ctx* ctx, void* entry, void* psi, const FusedArgs<R>&
   h.nbits = a.nbits;
   h.lg_tiles = a.lg_tiles;
   memcpy(h.mat, a.mat, sizeof(h.mat));
-  if (sizeof(R) == 8 && !a.permem && bt_jit_ff_on()) {
+  if (ff_pass(a)) {
     // float-float kernels read each coefficient as the floats (h, l) packed in its slot
     for (size_t i = 0; i < sizeof(h.mat) / sizeof(R); ++i) {
       const double d = (double)a.mat[i];

@@ -177,7 +177,7 @@ def run_members(plan, psis, src, src_pm, workdir, indices, member_mats):
         a = Args()
         name, M, threads = kernels[fused]
         a.member_lo, a.nmem, a.nbits, a.lg_tiles = 0, B, nbits, nbits - M
-        vals = _ff_slots(mats, nreals) if (not c64 and os.environ.get("BTGPU_JIT_FF", "1") != "0") else mats
+        vals = _ff_slots(mats, nreals) if (not c64 and nbits >= 16 and os.environ.get("BTGPU_JIT_FF", "1") != "0") else mats
         for e in range(nreals):
             a.mat[e] = vals[e]
         grid = min(B << (nbits - M), 3)
@@ -215,7 +215,7 @@ def run(plan, psi, dump_src, workdir, members=1):
     state = x.astype(np.complex64 if c64 else np.complex128)
     # float-float complex128 kernels read each coefficient as the floats (h, l)
     # packed in its slot, as the library's launcher writes them
-    ffm = not c64 and os.environ.get("BTGPU_JIT_FF", "1") != "0"
+    ffm = not c64 and nbits >= 16 and os.environ.get("BTGPU_JIT_FF", "1") != "0"
     fused = 0
     for kind, ops, mats in E.passes(plan):
         if kind:

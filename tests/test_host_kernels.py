@@ -57,6 +57,8 @@ def ops_seq(ops):
 
 n = 15 if prec == "c64" else 14
 check(n, ops_seq(C.random_ops(n, 1, rng) + C.brickwork(n, 6, rng)), "brickwork")
+if prec == "c128":  # 2^16 entries and more: the float-float form of complex128 passes
+    check(16, ops_seq(C.random_ops(16, 1, rng) + C.brickwork(16, 4, rng)), "brickwork 16")
 c, s = math.cos(0.3), math.sin(0.3)
 h = 1 / math.sqrt(2)
 forms = [np.diag([1, -1]), np.diag([1, 1j]), np.diag([1, -1j]), np.diag([1, np.exp(0.7j)]),

@@ -249,7 +249,7 @@ root = sys.argv[1]
 sys.path[:0] = [os.path.join(root, "tests"), os.path.join(root, "bluetangle.jl_gb300")]
 import plan_emulator as E
 import bluetangle_gpu.circuits as C
-n = 14
+n = 16  # complex128 passes of 2^16 entries take the float-float form
 p = E.host_plan(n, prec=sys.argv[2])
 rng = np.random.default_rng(3)
 for o in C.random_ops(n, 3, rng) + C.brickwork(n, 3, rng):

@@ -169,6 +169,10 @@ int bt_reduced_dm(const bt_state* s, int k, const int32_t* qubits, int64_t membe
  * src/ops.jl:278-329, :421-445).  Each fused pass applies every gate acting
  * inside a 13-bit (complex64) / 12-bit (complex128) tile in one HBM round trip;
  * the result equals applying the gates one by one (bt_apply_matrix).
+ * Specialised complex128 passes on states of 2^16 entries or more compute in
+ * float-float arithmetic on the FP32 pipe (48-bit significands: relative error
+ * ~2^-48 per operation, results within 1e-12 of FP64; environment BTGPU_JIT_FF=0
+ * keeps FP64).
  * ctx may be NULL: planning and kernel specialisation need no GPU. */
 int bt_plan_create(bt_ctx* ctx, int n, int repr, int prec, bt_plan** out);
 int bt_plan_free(bt_plan* p);

@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_pass(float2* __restrict__ 
                        : "memory");
         }
       }
-      __syncthreads();  // thread 0's verdict on the block copy
+      __syncthreads();  // thread 0's check of the block copy
       if (*sflag) {
         failed = true;
         break;

@@ -955,6 +955,42 @@ def run_c3(args):
         bytes_step = float(np.mean([sum(slot_bytes(sl) for sl in pre[i]) for i in timed]))
     zs = bt.expect(st, "Z", member=-1)
     assert np.all(np.isfinite(zs))
+    # complex128 check: 256 trajectories through five Trotter steps as the same
+    # programs in complex64 and complex128 with the same explicit draws (host
+    # uniforms): how many members took the same branches and outcomes, and how far
+    # their final states and <Z_i> are apart
+    prec_check = None
+    if progs is not None:
+        st.free()
+        K2, S2 = min(256, B), 5
+        sub = []
+        for i in range(S2):  # the step's gate and channel slots, then its measurement slots
+            sl = [T.Slot(b.kind, [b.items[0]] * K2) for b in base]
+            mr = np.random.default_rng(900 + i)
+            for q in range(1, n + 1):
+                mask = mr.random(K2) < 0.1
+                sl.append(T.Slot("measure", [meas_payload[q - 1] if x else None for x in mask]))
+            sub.append(sl)
+        finals, recs = {}, {}
+        for prec in ("c64", "c128"):
+            s2 = bt.zero_state(n, prec, K2, ctx)
+            rr = []
+            for i in range(S2):
+                pr, _ = T.compile_program(sub[i], n, K2, prec, ctx, unitary_mix=False)
+                rr.append(pr.run(s2, rng=np.random.default_rng(4000 + i)))
+            finals[prec] = s2
+            recs[prec] = rr
+        same = np.array([all(recs["c64"][i][m] == recs["c128"][i][m] for i in range(S2)) for m in range(K2)])
+        dz = np.abs(bt.expect(finals["c64"], "Z", member=-1)[same] - bt.expect(finals["c128"], "Z", member=-1)[same])
+        dmax = 0.0
+        for m in np.nonzero(same)[0][:16]:
+            dmax = max(dmax, float(np.abs(finals["c64"].to_numpy(int(m)) - finals["c128"].to_numpy(int(m))).max()))
+        prec_check = {"trajectories": K2, "steps": S2, "same_decisions": int(sum(same)),
+                      "max_abs_z_dev": float(dz.max()) if dz.size else None,
+                      "max_abs_amp_dev_16_members": dmax,
+                      "draws": "explicit host uniforms shared by both precisions"}
+        for v in finals.values():
+            v.free()
     cpu = None
     if not args.no_cpu:
         # CPU: the oracle on a sample of trajectories (one step each, complex128)
@@ -1000,7 +1036,8 @@ def run_c3(args):
                          "peak_kind": peak_kind, "traffic": None,
                          "bytes_per_step": bytes_step,
                          "note": "algorithmic bytes of the whole batch (trajectories and copies)"},
-            "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clk, "host_s": host}
+            "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clk, "host_s": host,
+            "precision_vs_c128": prec_check}
     print(json.dumps(line), flush=True)
     ctx.close()
 

@@ -671,6 +671,8 @@ function gpu_shots(ops::AbstractVector, N::Integer, shots::Integer; noise::Union
         elseif op.type == "🔬"
             _program_measure!(p, op)
             continue
+        elseif op.type == "f"
+            throw(ArgumentError("parametrised op $(op.name): evaluate its matrix at the pars first"))
         elseif op.control != -2
             _program_gate!(p, _ctrl_matrix(op.mat), [op.control, op.qubit])
         else

@@ -27,7 +27,7 @@ import BlueTangle: apply, sample, sample_exact, expect, correlation, born_measur
 export GPUContext, GPUState, GPUDensity, GPUPlan, GPUProgram, GPUServer, BTError
 export gpu_zero_state, gpu_zero_rho, gpu_state, gpu_rho, apply!, born_measure_Z!, apply_noise!
 export gpu_compile, gpu_compile_variational, run!, run_members!, set_matrices!, plan_cost
-export gpu_shots, gpu_shot_samples, gpu_product_state, add_client, submit, result, serve_stats
+export gpu_shots, gpu_shot_samples, gpu_measure, gpu_product_state, add_client, submit, result, serve_stats
 
 # the library: BTGPU_LIB, else the in-tree build next to this directory
 const lib = get(ENV, "BTGPU_LIB", joinpath(@__DIR__, "..", "bluetangle.jl_gb300", "libbtgpu.so"))
@@ -654,6 +654,13 @@ records[:, shot] the mid-circuit outcomes of that shot."""
 function gpu_shots(ops::AbstractVector, N::Integer, shots::Integer; noise::Union{NoiseModel,Bool}=false,
                    id::Integer=0, seed::Integer=rand(UInt64), prec::Symbol=:c64,
                    ctx::GPUContext=default_context())
+    p = _shot_program(_expanded_ops(ops, id), N, shots, noise, prec, ctx)
+    return _run_program(p, N, shots, prec, seed, ctx)
+end
+
+# the program of a circuit's ops (and the NoiseModel's channels after every noisy
+# op), one member per shot
+function _shot_program(ops, N, shots, noise, prec, ctx)
     r = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:bt_program_create, lib), Cint, (Ptr{Cvoid}, Cint, Cint, Cint, Ptr{Ptr{Cvoid}}),
                 ctx.h, N, PRECISIONS[prec], shots, r), ctx.h)
@@ -661,7 +668,7 @@ function gpu_shots(ops::AbstractVector, N::Integer, shots::Integer; noise::Union
         x.h != C_NULL && ccall((:bt_program_free, lib), Cint, (Ptr{Cvoid},), x.h)
         x.h = C_NULL
     end
-    for op in _expanded_ops(ops, id)
+    for op in ops
         if op isa ifOp
             throw(ArgumentError("classically controlled ops follow each shot's outcomes: apply! them per shot"))
         elseif op isa OpQC
@@ -687,6 +694,10 @@ function gpu_shots(ops::AbstractVector, N::Integer, shots::Integer; noise::Union
             end
         end
     end
+    return p
+end
+
+function _run_program(p::GPUProgram, N, shots, prec, seed, ctx)
     s = _alloc(GPUState, N, prec, shots, ctx)
     recs = Matrix{Int32}(undef, max(p.nrec, 1), shots)  # member-major: a column per shot
     check(ccall((:bt_program_run, lib), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, UInt64, Ptr{Int32}),
@@ -699,10 +710,100 @@ sample of the noisy measure(circuit, shots); measure(samples, N)
 (src/ops.jl:516) turns it into the reference's Measurement."""
 function gpu_shot_samples(ops::AbstractVector, N::Integer, shots::Integer; seed::Integer=rand(UInt64), kw...)
     s, _ = gpu_shots(ops, N, shots; seed=seed, kw...)
-    out = Vector{Int64}(undef, shots)
+    return _member_samples(s, seed)
+end
+
+function _member_samples(s::GPUState, seed)
+    out = Vector{Int64}(undef, s.batch)
     check(ccall((:bt_sample_members, lib), Cint, (Ptr{Cvoid}, Ptr{Float64}, UInt64, Ptr{Int64}),
                 s.h, C_NULL, (seed + 1) % UInt64, out), s.ctx.h)
     return out
+end
+
+# ------------------------------------------------------------------ measure(circuit, shots, id)
+# the rotation of _final_measurement (src/ops.jl:856-914) for a basis; "R" draws one
+# of H, HSP, I per qubit at every use
+_basis_rotation(basis::String) = basis == "Z" ? ComplexF64[1 0; 0 1] :
+                                 basis == "X" ? Matrix{ComplexF64}(BlueTangle.gate.H) :
+                                 basis == "Y" ? Matrix{ComplexF64}(BlueTangle.gate.HSP) :
+                                 basis == "R" ? Matrix{ComplexF64}([BlueTangle.gate.H, BlueTangle.gate.HSP, BlueTangle.gate.I][rand(1:3)]) :
+                                 throw("measurement_basis error!")
+
+# _final_measurement (src/ops.jl:856-914) in place: per qubit the basis rotation,
+# then the readout channel's branch
+function _final_measurement!(s::GPUState, o)
+    for q in 1:s.n
+        U = _basis_rotation(o.measurement_basis)
+        U == I || apply_matrix!(s, U, [q])
+        o.readout_noise isa QuantumChannel && apply_channel!(s, o.readout_noise.kraus, q)
+    end
+    return s
+end
+
+# sum_m w |psi_m><psi_m| of every member into a new density matrix (bt_rho_accumulate)
+function _density_of(s::GPUState, w::Float64)
+    rho = _alloc(GPUDensity, s.n, :c128, 1, s.ctx)
+    check(ccall((:bt_state_clear, lib), Cint, (Ptr{Cvoid}, Int64), rho.h, -1), s.ctx.h)
+    check(ccall((:bt_rho_accumulate, lib), Cint, (Ptr{Cvoid}, Int64, Ptr{Cvoid}, Float64), rho.h, 0, s.h, w), s.ctx.h)
+    return rho
+end
+
+"""gpu_measure(circuit, number_of_experiment, id): measure(circuit,
+number_of_experiment, id) (src/ops.jl:599-646) on the GPU, returning the
+reference's Measurement.  A noiseless circuit runs once and is sampled; otherwise
+every shot is one member of a batch: as one program (gpu_shots, with the final
+rotation and readout channel appended) where every shot runs the same ops, shot by
+shot (the reference's re-simulation, with apply!) where twirl frames, a random
+basis or classically controlled ops differ between shots.  The density matrix, when
+the options ask for it, is accumulated on the GPU and returned in the record as the
+reference's sparse matrix; mitigation uses the reference's own inverse."""
+function gpu_measure(circuit::Circuit, number_of_experiment::Int, id::Int=0; prec::Symbol=:c128,
+                     seed::Integer=rand(UInt64), ctx::GPUContext=default_context())
+    number_of_experiment > 0 || throw("`number_of_experiment` must be positive.")
+    N = circuit.stats.N
+    o = circuit.options
+    rho = nothing
+    noiseless = o.noise == false && circuit.stats.mid_measurement_count == 0 && !(o.readout_noise isa QuantumChannel)
+    if noiseless
+        s = _alloc(GPUState, N, prec, 1, ctx)
+        apply!(s, BlueTangle._expanded_ops_for_shot(circuit, 0))
+        _final_measurement!(s, o)
+        samples = collect(Int, sample(s, number_of_experiment))
+        o.density_matrix && (rho = _density_of(s, 1.0))
+    else
+        ops = BlueTangle._expanded_ops_for_shot(circuit, id)
+        per_shot = o.twirl || o.measurement_basis == "R" || any(op -> op isa ifOp, ops)
+        if per_shot
+            s = _alloc(GPUState, N, prec, number_of_experiment, ctx)
+            one = _alloc(GPUState, N, prec, 1, ctx)
+            for m in 0:number_of_experiment-1
+                set_zero!(one)
+                apply!(one, m == 0 ? ops : BlueTangle._expanded_ops_for_shot(circuit, id); noise=o.noise)
+                _final_measurement!(one, o)
+                copy_from!(s, one; dst_member=m, src_member=0)
+            end
+        else
+            p = _shot_program(ops, N, number_of_experiment, o.noise, prec, ctx)
+            U = _basis_rotation(o.measurement_basis)
+            for q in 1:N
+                U == I || _program_gate!(p, U, [q])
+                o.readout_noise isa QuantumChannel && _program_channel!(p, o.readout_noise.kraus, [q])
+            end
+            s, _ = _run_program(p, N, number_of_experiment, prec, seed, ctx)
+        end
+        samples = collect(Int, _member_samples(s, seed))
+        o.density_matrix && (rho = _density_of(s, 1.0 / number_of_experiment))
+    end
+    bitstr, avg_prob = BlueTangle.get_probs_from_sample(samples, N)
+    if o.measurement_mitigate && o.readout_noise isa QuantumChannel
+        avg_prob = normalize(abs.(BlueTangle._measurement_mitigate_inv_matrix(N, o.readout_noise) * avg_prob), 1)
+    end
+    fock = int2bin.(bitstr, N)
+    expect = [BlueTangle._sample_to_expectation((fock, avg_prob), [i]) for i = 1:N]
+    mag_moments_list = [mag_moments(N, bitstr, avg_prob, moment_order) for moment_order = 1:12]
+    rho_construct = rho === nothing ? BlueTangle.sa.spzeros(ComplexF64, 2^N, 2^N) : BlueTangle.sa.sparse(Matrix(rho))
+    return Measurement(bitstr, avg_prob, expect, mag_moments_list, o.measurement_basis, number_of_experiment,
+                       o.circuit_name, N, rho_construct)
 end
 
 # ------------------------------------------------------------------ serving

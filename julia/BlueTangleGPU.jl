@@ -28,6 +28,8 @@ export GPUContext, GPUState, GPUDensity, GPUPlan, GPUProgram, GPUServer, BTError
 export gpu_zero_state, gpu_zero_rho, gpu_state, gpu_rho, apply!, born_measure_Z!, apply_noise!
 export gpu_compile, gpu_compile_variational, run!, run_members!, set_matrices!, plan_cost
 export gpu_shots, gpu_shot_samples, gpu_measure, gpu_product_state, add_client, submit, result, serve_stats
+export gpu_to_state, gpu_to_rho, gpu_run, gpu_one_state, gpu_neel_state01, gpu_neel_state10, gpu_Z3, gpu_Z3_s,
+       gpu_neel_state_s, gpu_plus_state, gpu_minus_state, gpu_random_product_state, gpu_random_state
 
 # the library: BTGPU_LIB, else the in-tree build next to this directory
 const lib = get(ENV, "BTGPU_LIB", joinpath(@__DIR__, "..", "bluetangle.jl_gb300", "libbtgpu.so"))
@@ -184,12 +186,81 @@ function Base.copy(s::T) where {T<:GPUHandle}
     return c
 end
 
+# the basis index of a list of qubit values, qubit 1 the most significant bit:
+# _bin2state(Int(sign(x))) is |0> for 0 and |1> otherwise (src/bit.jl:59)
+_basis_index(bits) = foldl((a, b) -> (a << 1) | UInt64(sign(b) != 0), bits; init=UInt64(0))
+
 """product_state(list_of_qubits) (src/hilbert.jl:835): the basis state of the
-bits (qubit 1 the most significant)."""
-function gpu_product_state(bits::AbstractVector{<:Integer}; prec::Symbol=:c128, ctx::GPUContext=default_context())
+bits (qubit 1 the most significant; every non-zero entry is |1>)."""
+function gpu_product_state(bits::AbstractVector{<:Real}; prec::Symbol=:c128, ctx::GPUContext=default_context())
+    length(bits) <= 64 || throw(ArgumentError("at most 64 qubits"))
     s = _alloc(GPUState, length(bits), prec, 1, ctx)
-    index = foldl((a, b) -> (a << 1) | UInt64(b), bits; init=UInt64(0))
-    return set_basis!(s, index)
+    return set_basis!(s, _basis_index(bits))
+end
+
+"""one_state(N) (src/hilbert.jl:867): |1...1>."""
+gpu_one_state(N::Integer; prec::Symbol=:c128, ctx::GPUContext=default_context()) =
+    set_basis!(_alloc(GPUState, N, prec, 1, ctx), (UInt64(1) << N) - 1)
+
+"""neel_state01(N), neel_state10(N) (src/hilbert.jl:837-838)."""
+gpu_neel_state01(N::Integer; kw...) = gpu_product_state([isodd(i) ? 0 : 1 for i in 1:N]; kw...)
+gpu_neel_state10(N::Integer; kw...) = gpu_product_state([isodd(i) ? 1 : 0 for i in 1:N]; kw...)
+
+_z3_bits(N, j) = [mod(i + 2 - j + 1, 3) == 0 ? 1 : 0 for i in 1:N]
+
+"""Z3(N, j) (src/hilbert.jl:844)."""
+gpu_Z3(N::Integer, j::Integer=1; kw...) = gpu_product_state(_z3_bits(N, j); kw...)
+
+"""random_product_state(N) = product_state(rand([0, 1], N)) (src/hilbert.jl:859)."""
+gpu_random_product_state(N::Integer; kw...) = gpu_product_state(rand([0, 1], N); kw...)
+
+# normalize(sum of the basis states of indices): the state cleared, then each
+# distinct index written with its count over the norm
+function _superpose(N, indices, prec, ctx)
+    s = _alloc(GPUState, N, prec, 1, ctx)
+    check(ccall((:bt_state_clear, lib), Cint, (Ptr{Cvoid}, Int64), s.h, 0), ctx.h)
+    counts = Dict{UInt64,Float64}()
+    for i in indices
+        counts[i] = get(counts, i, 0.0) + 1.0
+    end
+    nrm = sqrt(sum(v^2 for v in values(counts)))
+    for (i, v) in counts
+        a = ComplexF64[v / nrm]
+        check(ccall((:bt_state_upload, lib), Cint, (Ptr{Cvoid}, Int64, Int64, Int64, Ptr{ComplexF64}),
+                    s.h, 0, Int64(i), 1, a), ctx.h)
+    end
+    return s
+end
+
+"""Z3_s(N) = normalize(Z3(N,1) + Z3(N,2) + Z3(N,3)) (src/hilbert.jl:849)."""
+gpu_Z3_s(N::Integer; prec::Symbol=:c128, ctx::GPUContext=default_context()) =
+    _superpose(N, [_basis_index(_z3_bits(N, j)) for j in 1:3], prec, ctx)
+
+"""neel_state_s(N) = (neel_state01(N) + neel_state10(N)) / sqrt(2) (src/hilbert.jl:854)."""
+gpu_neel_state_s(N::Integer; prec::Symbol=:c128, ctx::GPUContext=default_context()) =
+    _superpose(N, [_basis_index([isodd(i) ? 0 : 1 for i in 1:N]), _basis_index([isodd(i) ? 1 : 0 for i in 1:N])],
+               prec, ctx)
+
+# H on every qubit, as one compiled plan
+function _all_h!(s::GPUState)
+    p = gpu_compile([Op("H", q) for q in 1:s.n], s.n; prec=_prec_symbol(s), ctx=s.ctx)
+    return run!(p, s)
+end
+
+"""plus_state(N) (src/hilbert.jl:869) and minus_state(N) (:871-877): H on every
+qubit of |0...0> and of |1...1>."""
+gpu_plus_state(N::Integer; prec::Symbol=:c128, ctx::GPUContext=default_context()) =
+    _all_h!(_alloc(GPUState, N, prec, 1, ctx))
+gpu_minus_state(N::Integer; prec::Symbol=:c128, ctx::GPUContext=default_context()) =
+    _all_h!(gpu_one_state(N; prec=prec, ctx=ctx))
+
+"""random_state(N) = normalize(rand(ComplexF64, 2^N)) (src/hilbert.jl:882), drawn
+on the device (bt_state_random: real and imaginary parts uniform on [0, 1))."""
+function gpu_random_state(N::Integer; seed::Integer=rand(UInt64), prec::Symbol=:c128,
+                          ctx::GPUContext=default_context())
+    s = _alloc(GPUState, N, prec, 1, ctx)
+    check(ccall((:bt_state_random, lib), Cint, (Ptr{Cvoid}, Int64, UInt64), s.h, 0, seed % UInt64), ctx.h)
+    return s
 end
 
 # ------------------------------------------------------------------ low level
@@ -718,6 +789,62 @@ function _member_samples(s::GPUState, seed)
     check(ccall((:bt_sample_members, lib), Cint, (Ptr{Cvoid}, Ptr{Float64}, UInt64, Ptr{Int64}),
                 s.h, C_NULL, (seed + 1) % UInt64, out), s.ctx.h)
     return out
+end
+
+# ------------------------------------------------------------------ circuit drivers
+"""gpu_to_state(circuit, id): to_state(circuit, id) (src/ops.jl:790-795) on the GPU:
+the shot's ops (_expanded_ops_for_shot: twirl frames, ZNE repetitions) applied to
+|0...0> with the circuit's noise."""
+function gpu_to_state(circuit::Circuit, id::Int=0; prec::Symbol=:c128, ctx::GPUContext=default_context())
+    s = _alloc(GPUState, circuit.stats.N, prec, 1, ctx)
+    return apply!(s, BlueTangle._expanded_ops_for_shot(circuit, id); noise=circuit.options.noise)
+end
+
+"""gpu_to_rho(circuit; id): to_rho(circuit; id) (src/ops.jl:806-844) on the GPU,
+with that function's own expansion: 2id+1 repetitions of the ops named exactly
+CNOT or CX, apply_twirl around every two-qubit op when twirl is on, and the
+NoiseModel's channels as Kraus sums."""
+function gpu_to_rho(circuit::Circuit; id::Int=0, prec::Symbol=:c128, ctx::GPUContext=default_context())
+    rho = _alloc(GPUDensity, circuit.stats.N, prec, 1, ctx)
+    nm = circuit.options.noise
+    tw = circuit.options.twirl
+    for op in vcat(circuit.layers...)
+        if op.q == 2 && (op.name == "CNOT" || op.name == "CX") && id > 0
+            for _ in 1:(2id+1)
+                apply!(rho, tw ? BlueTangle.apply_twirl(op) : [op]; noise=nm)
+            end
+        elseif op.q == 2 && tw
+            apply!(rho, BlueTangle.apply_twirl(op); noise=nm)
+        else
+            apply!(rho, op; noise=nm)
+        end
+    end
+    return rho
+end
+
+"""gpu_run(circuit, shots; id): run(circuit, shots; backend=:statevector, id)
+(src/ops.jl:659-692) on the GPU: every shot's mid-circuit measurement outcomes.
+Shots that run the same ops are the members of one program (gpu_shots); with
+twirl frames or ifOps, which differ between shots, each shot runs with apply!."""
+function gpu_run(circuit::Circuit, number_of_experiment::Int=1; id::Int=0, prec::Symbol=:c128,
+                 seed::Integer=rand(UInt64), ctx::GPUContext=default_context())
+    number_of_experiment > 0 || throw(ArgumentError("`number_of_experiment` must be positive."))
+    N = circuit.stats.N
+    nm = circuit.options.noise
+    ops = BlueTangle._expanded_ops_for_shot(circuit, id)
+    if circuit.options.twirl || any(op -> op isa ifOp || op isa OpF, ops)
+        out = Vector{Vector{Int}}(undef, number_of_experiment)
+        s = _alloc(GPUState, N, prec, 1, ctx)
+        for shot in 1:number_of_experiment
+            set_zero!(s)
+            _, out[shot] = apply!(s, shot == 1 ? ops : BlueTangle._expanded_ops_for_shot(circuit, id);
+                                  noise=nm, track_measurements=true)
+        end
+        return out
+    end
+    p = _shot_program(ops, N, number_of_experiment, nm, prec, ctx)
+    _, recs = _run_program(p, N, number_of_experiment, prec, seed, ctx)
+    return [Int.(recs[:, m]) for m in 1:number_of_experiment]
 end
 
 # ------------------------------------------------------------------ measure(circuit, shots, id)

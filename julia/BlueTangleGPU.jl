@@ -28,6 +28,7 @@ export GPUContext, GPUState, GPUDensity, GPUPlan, GPUProgram, GPUServer, BTError
 export gpu_zero_state, gpu_zero_rho, gpu_state, gpu_rho, apply!, born_measure_Z!, apply_noise!
 export gpu_compile, gpu_compile_variational, run!, run_members!, set_matrices!, plan_cost
 export gpu_shots, gpu_shot_samples, gpu_measure, gpu_product_state, add_client, submit, result, serve_stats
+export gpu_variational_apply, gpu_loss, gpu_loss_and_grad_paramshift
 export gpu_to_state, gpu_to_rho, gpu_run, gpu_one_state, gpu_neel_state01, gpu_neel_state10, gpu_Z3, gpu_Z3_s,
        gpu_neel_state_s, gpu_plus_state, gpu_minus_state, gpu_random_product_state, gpu_random_state
 
@@ -648,6 +649,136 @@ function run_members!(p::GPUPlan, s::GPUState, idx::Vector{Int64}, mats::Vector{
                 p.h, s.h, length(idx), idx, buf), s.ctx.h)
     return s
 end
+
+# ------------------------------------------------------------------ variational circuits
+"""gpu_variational_apply(pars, opt; noise_override): variational_apply(pars, opt)
+(src/vqa.jl:420-456) on the GPU: opt.init uploaded, every op applied with its
+slice of pars, the NoiseModel (opt.noise, or noise_override) after each op."""
+function gpu_variational_apply(pars::AbstractVector, opt::AnsatzOptions; noise_override::Union{Bool,NoiseModel}=false,
+                               prec::Symbol=:c128, ctx::GPUContext=default_context())
+    s = _initial_members!(_alloc(GPUState, opt.N, prec, 1, ctx), opt.init)
+    noise = noise_override isa NoiseModel ? noise_override : opt.noise
+    c = 1
+    for (op, fn) in zip(opt.ops, opt.args)
+        fn > 0 ? apply!(s, op; pars=pars[c:c+fn-1]) : apply!(s, op)
+        c += fn
+        noise isa NoiseModel && !(op isa OpQC) && apply_noise!(s, op, noise)
+    end
+    return s
+end
+
+# every member set to the ansatz's initial state (|0...0> when it is one)
+function _initial_members!(s::GPUState, init)
+    flat = Vector{ComplexF64}(init)
+    length(flat) == (1 << s.n) || throw(ArgumentError("the initial state has $(length(flat)) entries, not 2^$(s.n)"))
+    if flat[1] == 1 && count(!iszero, flat) == 1
+        return set_zero!(s)
+    end
+    for m in 0:s.batch-1
+        _upload!(s, flat, m)
+    end
+    return s
+end
+
+# Hamiltonian terms [(coef, "Z,Z", [i, j]), ...] as Pauli strings (coef, xmask, zmask)
+function _hamiltonian_terms(terms, n)
+    out = Tuple{ComplexF64,UInt64,UInt64}[]
+    for (c, names, qubits) in terms
+        mats = [gates(String(strip(x))) for x in split(names, ",")]
+        length(mats) == length(qubits) || throw("qubit number does not match with operators")
+        append!(out, [(c * tc, x, z) for (tc, x, z) in _pauli_terms(mats, qubits, n)])
+    end
+    return out
+end
+
+# sum_t Re(c_t) <P_t> of every member (bt_expect_pauli over the batch, FP64 sums)
+function _expect_members(s::GPUState, terms)
+    isempty(terms) && return zeros(s.batch)
+    xs = UInt64[t[2] for t in terms]
+    zs = UInt64[t[3] for t in terms]
+    out = Vector{Float64}(undef, length(terms) * s.batch)
+    check(ccall((:bt_expect_pauli, lib), Cint,
+                (Ptr{Cvoid}, Cint, Ptr{UInt64}, Ptr{UInt64}, Ptr{Float64}, Int64, Ptr{Float64}),
+                s.h, length(terms), xs, zs, C_NULL, -1, out), s.ctx.h)
+    v = reshape(out, length(terms), s.batch)  # member-major
+    return [sum(real(t[1]) * v[i, m] for (i, t) in enumerate(terms)) for m in 1:s.batch]
+end
+
+# matrices of the parametrised ops at p, by op index
+function _bound_mats(opt::AnsatzOptions, p::AbstractVector)
+    sum(opt.args) == length(p) || throw(ArgumentError("the ansatz takes $(sum(opt.args)) parameters, $(length(p)) given"))
+    mats = Dict{Int,Matrix{ComplexF64}}()
+    c = 1
+    for (j, (op, fn)) in enumerate(zip(opt.ops, opt.args))
+        if fn > 0
+            mats[j] = Matrix{ComplexF64}(op.mat(p[c:c+fn-1]...))
+            c += fn
+        end
+    end
+    return mats
+end
+
+const _MEMBER_BUDGET = 16 << 30  # HBM for the members of one batched run
+
+# the loss of every evaluation (a Dict of the parametrised ops' matrices each):
+# noiseless ansatze as members of one compiled plan, each member with its own
+# matrices (bt_plan_run_members), in chunks that fit _MEMBER_BUDGET; noisy ones
+# one trajectory per evaluation, as the reference evaluates them
+function _losses(opt::AnsatzOptions, evals::Vector{Dict{Int,Matrix{ComplexF64}}}, params, terms, prec, ctx)
+    N = opt.N
+    hterms = terms === nothing ? nothing : _hamiltonian_terms(terms, N)
+    lossof(s, m) = hterms === nothing ? opt.loss(BlueTangle.sa.sparse(Vector(s; member=m))) :
+                   _expect_terms(s, hterms; member=m)
+    if opt.noise isa NoiseModel || any(op -> op isa OpQC || op.type == "🔬", opt.ops)
+        return [lossof(gpu_variational_apply(p, opt; prec=prec, ctx=ctx), 0) for p in params]
+    end
+    plan = gpu_compile_variational(opt.ops, N; prec=prec, ctx=ctx)
+    var = sort(collect(keys(evals[1])))
+    idx = Int64[j - 1 for j in var]
+    bytes = (1 << N) * (prec == :c64 ? 8 : 16)
+    chunk = max(1, min(length(evals), _MEMBER_BUDGET ÷ bytes))
+    vals = Vector{Float64}(undef, length(evals))
+    for e0 in 1:chunk:length(evals)
+        es = e0:min(length(evals), e0 + chunk - 1)
+        s = _initial_members!(_alloc(GPUState, N, prec, length(es), ctx), opt.init)
+        run_members!(plan, s, idx, [[evals[e][j] for j in var] for e in es])
+        vals[es] = hterms === nothing ? [lossof(s, m) for m in 0:length(es)-1] : _expect_members(s, hterms)
+    end
+    return vals
+end
+
+"""gpu_loss_and_grad_paramshift(p, opt; terms): loss_and_grad_paramshift(p, opt)
+(src/vqa.jl:590-611) on the GPU: the loss at p and, for every parameter i,
+g_i = (l(p + pi/2 e_i) - l(p - pi/2 e_i)) / 2, all 2P + 1 evaluations as one
+batch.  The loss is sum_t c_t <P_t> of `terms` [(coef, "Z,Z", [i, j]), ...] on
+the device, or, without terms, the ansatz's own opt.loss on each evaluated state
+(downloaded)."""
+function gpu_loss_and_grad_paramshift(p::Vector{Float64}, opt::AnsatzOptions; terms=nothing, prec::Symbol=:c128,
+                                      ctx::GPUContext=default_context())
+    SHIFT = pi / 2
+    base = _bound_mats(opt, p)
+    params = [copy(p)]
+    evals = [base]
+    owner = Int[]  # op of each parameter
+    for (j, fn) in enumerate(opt.args), _ in 1:fn
+        push!(owner, j)
+    end
+    for i in eachindex(p), sh in (SHIFT, -SHIFT)
+        q = copy(p)
+        q[i] += sh
+        push!(params, q)
+        m = copy(base)
+        m[owner[i]] = _bound_mats(opt, q)[owner[i]]
+        push!(evals, m)
+    end
+    vals = _losses(opt, evals, params, terms, prec, ctx)
+    g = [0.5 * (vals[2i] - vals[2i+1]) for i in eachindex(p)]
+    return (vals[1], g)
+end
+
+"""gpu_loss(p, opt; terms): the loss of the ansatz at p (_loss, src/vqa.jl:588)."""
+gpu_loss(p::Vector{Float64}, opt::AnsatzOptions; terms=nothing, prec::Symbol=:c128, ctx::GPUContext=default_context()) =
+    _losses(opt, [_bound_mats(opt, p)], [p], terms, prec, ctx)[1]
 
 # ------------------------------------------------------------------ noisy shots (programs)
 """A noisy circuit run on every member of a batch (bt_program): the per-shot loop

@@ -28,7 +28,7 @@ export GPUContext, GPUState, GPUDensity, GPUPlan, GPUProgram, GPUServer, BTError
 export gpu_zero_state, gpu_zero_rho, gpu_state, gpu_rho, apply!, born_measure_Z!, apply_noise!
 export gpu_compile, gpu_compile_variational, run!, run_members!, set_matrices!, plan_cost
 export gpu_shots, gpu_shot_samples, gpu_measure, gpu_product_state, add_client, submit, result, serve_stats
-export gpu_variational_apply, gpu_loss, gpu_loss_and_grad_paramshift
+export gpu_variational_apply, gpu_loss, gpu_loss_and_grad_paramshift, gpu_shadow
 export gpu_to_state, gpu_to_rho, gpu_run, gpu_one_state, gpu_neel_state01, gpu_neel_state10, gpu_Z3, gpu_Z3_s,
        gpu_neel_state_s, gpu_plus_state, gpu_minus_state, gpu_random_product_state, gpu_random_state
 
@@ -1062,6 +1062,67 @@ function gpu_measure(circuit::Circuit, number_of_experiment::Int, id::Int=0; pre
     rho_construct = rho === nothing ? BlueTangle.sa.spzeros(ComplexF64, 2^N, 2^N) : BlueTangle.sa.sparse(Matrix(rho))
     return Measurement(bitstr, avg_prob, expect, mag_moments_list, o.measurement_basis, number_of_experiment,
                        o.circuit_name, N, rho_construct)
+end
+
+# ------------------------------------------------------------------ classical shadows
+"""gpu_shadow(circuit, number_of_experiment): shadow(circuit, number_of_experiment)
+(src/ops.jl:145-185) on the GPU.  Every snapshot is one member of a batch: the
+circuit (to_state), a random basis per qubit (H, HSP or I, the reference's m_list)
+and a Z measurement of every qubit, whose joint outcome follows the rotated state's
+Born distribution as the reference's one sample does; the snapshots
+(x)_q (3 U'|b><b|U - I) / shots are summed into a density matrix on the device
+(bt_shadow_accumulate, n <= 14).  Twirled circuits and ifOps, which differ between
+shots, run shot by shot."""
+function gpu_shadow(circuit::Circuit, number_of_experiment::Int; prec::Symbol=:c128,
+                    seed::Integer=rand(UInt64), ctx::GPUContext=default_context())
+    number_of_experiment > 0 || throw(ArgumentError("`number_of_experiment` must be positive."))
+    N = circuit.stats.N
+    shots = number_of_experiment
+    m_list = [Matrix{ComplexF64}(BlueTangle.gate.H), Matrix{ComplexF64}(BlueTangle.gate.HSP), ComplexF64[1 0; 0 1]]
+    bases = rand(1:3, shots, N)
+    outcomes = Matrix{Int}(undef, shots, N)
+    ops = BlueTangle._expanded_ops_for_shot(circuit, 0)
+    if circuit.options.twirl || any(op -> op isa ifOp || op isa OpF, ops)
+        for m in 1:shots
+            s = gpu_to_state(circuit; prec=prec, ctx=ctx)
+            for q in 1:N
+                apply_matrix!(s, m_list[bases[m, q]], [q])
+            end
+            outcomes[m, :] = int2bin(Int(sample(s, 1)[1]), N)
+        end
+    else
+        p = _shot_program(ops, N, shots, circuit.options.noise, prec, ctx)
+        for q in 1:N
+            buf = reduce(vcat, [vec(m_list[bases[m, q]]) for m in 1:shots])
+            _program_check(p, ccall((:bt_program_add_gate, lib), Cint,
+                                    (Ptr{Cvoid}, Cint, Ptr{Int32}, Ptr{ComplexF64}, Cint), p.h, 1, Int32[q], buf, 1))
+        end
+        for q in 1:N
+            _program_check(p, ccall((:bt_program_add_measure, lib), Cint, (Ptr{Cvoid}, Cint, Ptr{Int32}),
+                                    p.h, q, C_NULL))
+            p.nrec += 1
+        end
+        _, recs = _run_program(p, N, shots, prec, seed, ctx)
+        outcomes .= permutedims(recs[end-N+1:end, :])
+        any(<(0), outcomes) && throw("a snapshot measurement failed")
+    end
+    # codes[m*N + q] (0-based) = 2*basis + outcome; the six factors row-major
+    codes = UInt8[2 * (bases[m, q] - 1) + outcomes[m, q] for q in 1:N, m in 1:shots]
+    tables = Float64[]
+    for U in m_list, o in 0:1
+        v = o == 0 ? ComplexF64[1, 0] : ComplexF64[0, 1]
+        T = 3 * (U' * v * v' * U) - I
+        for r in 1:2, c in 1:2
+            push!(tables, real(T[r, c]), imag(T[r, c]))
+        end
+    end
+    rho = _alloc(GPUDensity, N, prec, 1, ctx)
+    check(ccall((:bt_shadow_accumulate, lib), Cint, (Ptr{Cvoid}, Int64, Ptr{UInt8}, Ptr{Float64}),
+                rho.h, shots, vec(codes), tables), ctx.h)
+    t = Ref{Float64}(0.0)
+    check(ccall((:bt_norm2, lib), Cint, (Ptr{Cvoid}, Int64, Ref{Float64}), rho.h, 0, t), ctx.h)
+    isapprox(t[], 1) || throw("la.tr(rho)!≈1")
+    return rho
 end
 
 # ------------------------------------------------------------------ serving

@@ -978,6 +978,18 @@ function gpu_run(circuit::Circuit, number_of_experiment::Int=1; id::Int=0, prec:
     return [Int.(recs[:, m]) for m in 1:number_of_experiment]
 end
 
+"""gpu_run(ops, shots; options, layout, id) and gpu_run(qasm_or_path, shots; ...):
+the reference's run methods for op lists and OpenQASM (src/ops.jl:713-727): the
+ops compiled by the reference's compile (from_qasm first for QASM), then gpu_run
+of the circuit."""
+gpu_run(ops::Vector{<:QuantumOps}, number_of_experiment::Int=1; options::Options=Options(),
+        layout::Union{Layout,Int}=-1, id::Int=0, kw...) =
+    gpu_run(compile(ops, options; layout=layout), number_of_experiment; id=id, kw...)
+gpu_run(qasm_or_path::AbstractString, number_of_experiment::Int=1; options::Options=Options(),
+        layout::Union{Layout,Int}=-1, id::Int=0, is_file::Union{Nothing,Bool}=nothing, kw...) =
+    gpu_run(from_qasm(BlueTangle._qasm_to_source(qasm_or_path; is_file=is_file)), number_of_experiment;
+            options=options, layout=layout, id=id, kw...)
+
 # ------------------------------------------------------------------ measure(circuit, shots, id)
 # the rotation of _final_measurement (src/ops.jl:856-914) for a basis; "R" draws one
 # of H, HSP, I per qubit at every use

@@ -186,6 +186,46 @@ def test_ref_density_vs_state_and_trajectories(oracle, kref):
     assert abs(np.mean(mags) - mag_r) < 10 / 1000 * N
 
 
+def test_ref_channel_vs_stochastic_pauli_fidelity(oracle):
+    """N=1, depth 20, p=0.01: OpQC("depolarizing") after every op == the op with
+    NoiseModel("depolarizing") (t1), and fidelity(rho1, rho0) equals the mean over
+    1000 runs of fidelity(rho3, rho0), rho3 the ops with X, Y or Z drawn with
+    probability p after each, within atol 100/1000 (t2) (test/runtests.jl:134-190)."""
+    import scipy.linalg as sl
+
+    import bluetangle_gpu as bt
+    import bluetangle_gpu.circuits as C
+    from bluetangle_gpu.gates import gate
+    rng = np.random.default_rng(134)
+    N, p = 1, 0.01
+    ops = C.random_ops(N, 20, rng)
+    nm = bt.NoiseModel("depolarizing", p)
+    psi0 = rstate(rng, N)
+    rho0 = np.outer(psi0, psi0.conj())
+
+    def fid(r, s):  # fidelity(rho, sigma) = tr(sqrt(sqrt(rho) sigma sqrt(rho)))^2 (src/tensor.jl:222-229)
+        sr = sl.sqrtm(r)
+        return float(np.real(np.trace(sl.sqrtm(sr @ s @ sr)) ** 2))
+
+    rho1, rho2 = rho0.copy(), rho0.copy()
+    for o in ops:
+        rho1 = oracle.dm_hilbert1(rho1, o.mat, o.qubit)
+        rho1 = oracle.dm_channel(rho1, bt.OpQC("depolarizing", p, o.qubit).kraus, o.qubit)
+        rho2 = oracle.dm_hilbert1(rho2, o.mat, o.qubit)
+        rho2 = oracle.dm_channel(rho2, nm.q1.kraus, o.qubit)
+    assert np.linalg.norm(rho1 - rho2) < 1e-14
+    paulis = [gate["X"], gate["Y"], gate["Z"]]
+    avg = 0.0
+    for _ in range(1000):
+        rho3 = rho0.copy()
+        for o in ops:
+            rho3 = oracle.dm_hilbert1(rho3, o.mat, o.qubit)
+            if rng.random() <= p:
+                rho3 = oracle.dm_hilbert1(rho3, paulis[int(rng.integers(0, 3))], o.qubit)
+        avg += fid(rho3, rho0) / 1000
+    assert abs(fid(rho1, rho0) - avg) < 100 / 1000, (fid(rho1, rho0), avg)
+
+
 def test_ref_mid_circuit_exact_outcomes(oracle, kref):
     """X,RES,MZ -> [0]; X, ifOp(MZ, I, X) -> [1]; the 11-op circuit -> [1]
     (test/runtests.jl:195-231), for any uniform draw."""

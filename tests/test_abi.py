@@ -131,3 +131,74 @@ def test_julia_binding_ccalls_match_the_header():
     # OpQC("RES") resets (src/hilbert.jl:489-490); controls enter programs as 4x4
     assert re.search(r'uppercase\(op\.name\) in \("RES", "RESET"\)[^\n]*\n\s*_reset_Z!', jl)
     assert "_program_gate!(p, _ctrl_matrix(op.mat), [op.control, op.qubit])" in jl
+
+
+def _julia_code(src):
+    """The Julia source with strings, docstrings and comments blanked."""
+    out, i, n = [], 0, len(src)
+    while i < n:
+        if src.startswith('"""', i):
+            i = src.index('"""', i + 3) + 3
+            out.append('""')
+        elif src[i] == '"':
+            j = i + 1
+            while src[j] != '"':
+                j += 2 if src[j] == "\\" else 1
+            out.append('""')
+            i = j + 1
+        elif src[i] == "#":
+            j = src.find("\n", i)
+            i = n if j < 0 else j
+        else:
+            out.append(src[i])
+            i += 1
+    return "".join(out)
+
+
+def _julia_blocks(src):
+    """(block openers, `end`s) of the Julia source outside brackets (where `end`
+    indexes and `for`/`if` are comprehension clauses); brackets must pair."""
+    code = _julia_code(src)
+    flat, stack = [], []
+    pairs = {")": "(", "]": "[", "}": "{"}
+    for ch in code:
+        if ch in "([{":
+            stack.append(ch)
+        elif ch in ")]}":
+            assert stack and stack[-1] == pairs[ch], f"unpaired {ch}"
+            stack.pop()
+        elif not stack:
+            flat.append(ch)
+    assert not stack, f"unclosed {stack}"
+    flat = "".join(flat)
+    opens = len(re.findall(r"\b(function|if|for|while|let|begin|do|struct|try|module|quote|macro)\b", flat))
+    opens += len(re.findall(r"\b(abstract|primitive)\s+type\b", flat))
+    return opens, len(re.findall(r"\bend\b", flat))
+
+
+def test_julia_binding_is_well_formed():
+    """Julia is not installed here: the binding's brackets pair, every block
+    opener has its `end` (a dropped `end` is caught), and every exported name is
+    defined in the file."""
+    jl = open(os.path.join(ROOT, "julia", "BlueTangleGPU.jl")).read()
+    opens, ends = _julia_blocks(jl)
+    assert opens == ends, (opens, ends)
+    k = jl.rindex("\nend")
+    o2, e2 = _julia_blocks(jl[:k] + jl[k + 4:])
+    assert o2 == e2 + 1
+    code = _julia_code(jl)
+    exported = set()
+    for m in re.finditer(r"^export\b", code, flags=re.M):
+        j, stmt = m.end(), ""
+        while True:  # an export continues on the next line after a trailing comma
+            k = code.find("\n", j)
+            stmt += code[j:k] + " "
+            j = k + 1
+            if not code[:k].rstrip().endswith(","):
+                break
+        exported |= {x.strip() for x in stmt.split(",") if x.strip()}
+    assert len(exported) >= 45 and "gpu_random_state" in exported
+    for name in exported:
+        nm = re.escape(name) + r"(?![\w!])"
+        pat = rf"(function\s+{nm}|^{nm}\(.*\)\s*(where.*)?=|struct\s+{nm}|^const\s+{nm})"
+        assert re.search(pat, code, flags=re.M), f"{name} is exported but not defined"

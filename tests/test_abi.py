@@ -202,3 +202,7 @@ def test_julia_binding_is_well_formed():
         nm = re.escape(name) + r"(?![\w!])"
         pat = rf"(function\s+{nm}|^{nm}\(.*\)\s*(where.*)?=|struct\s+{nm}|^const\s+{nm})"
         assert re.search(pat, code, flags=re.M), f"{name} is exported but not defined"
+    # every private helper called (not the reference's BlueTangle._x) is defined here
+    calls = set(re.findall(r"(?<![\w.!])(_[A-Za-z]\w*!?)\(", code))
+    defined = set(re.findall(r"(?:function\s+|^\s*)(_[A-Za-z]\w*!?)\(", code, flags=re.M))
+    assert calls <= defined, sorted(calls - defined)

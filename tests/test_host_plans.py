@@ -234,3 +234,29 @@ def test_host_plan_tuning_configurations(oracle, cfg, monkeypatch):
     for op in ops:
         ref = oracle_op(oracle, ref, op)
     assert np.abs(E.run(plan, psi) - ref).max() < 2e-5
+
+
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-12), ("c64", 2e-5)])
+def test_host_plan_edge_sizes(oracle, prec, tol):
+    """An empty plan compiles to no passes and leaves the state as it was; states
+    of 1 to 8 qubits, narrower than a tile, run every gate as its own pass and
+    match the oracle."""
+    rng = np.random.default_rng(11)
+    p = E.host_plan(5, prec=prec)
+    p.compile()
+    psi = rstate(rng, 5)
+    assert p.stats()["passes"] == 0 and np.array_equal(E.run(p, psi), psi)
+    for n in range(1, 9):
+        p = E.host_plan(n, prec=prec)
+        psi = rstate(rng, n)
+        ref = psi.copy()
+        for _ in range(30):
+            if n >= 2 and rng.random() < 0.5:
+                qs = [int(x) for x in rng.choice(np.arange(1, n + 1), size=2, replace=False)]
+                U = runitary(rng, 4)
+            else:
+                qs, U = [int(rng.integers(1, n + 1))], runitary(rng, 2)
+            p.add_matrix(U, qs)
+            ref = oracle.apply_k(ref, U, qs, [])
+        p.compile()
+        assert np.abs(E.run(p, psi) - ref).max() < tol, n

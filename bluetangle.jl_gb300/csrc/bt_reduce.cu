@@ -558,12 +558,84 @@ int bt_launch_pauli_tile(bt_state* s, int M, uint64_t tilemask, int T, const uin
   return finalize(ctx, part, nblk, BT_PAULI_TILE_TERMS, nmem, out);
 }
 
+// float-float accumulation: x added to (hi, lo) by TwoSum, the rounding error of
+// each add kept in lo
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+  const float s = hi + x, bb = s - hi;
+  lo += (hi - (s - bb)) + (x - bb);
+  hi = s;
+}
+
 // ------------------------------------------------------------ per-bit sums
 // out[mem][0] = total weight, out[mem][1+b] = weight with bit b set (b < nsys).
 // A warp walks chunks of 1024 consecutive amplitudes, lane l taking entries
 // l + 32 j: bits 0-4 are the lane's, bits 5-9 the unrolled j's, and bits >= 10
 // are constant over the chunk, so each weight costs a handful of FP64 adds.
 #define BS_W 36
+// complex64 state vectors of at least 2^BS_SC amplitudes: a warp takes
+// super-chunks of 32 consecutive chunks.  The FP32 sums of 8 weights are
+// accumulated per lane in float-float (TwoSum) and reach FP64 once per
+// super-chunk: about 0.04 FP64 adds per amplitude instead of 1.7 (the chunk form
+// is FP64-issue bound on this part, 3.3x its HBM time at 33 qubits).  Bits 5-9
+// are the unrolled j's, bits 10-14 the chunk index k (the same in every lane of
+// the warp), bits >= 15 constant over the super-chunk.
+#define BS_SC 15
+__device__ __forceinline__ void bitsums_superchunks(const float2* __restrict__ s, int nsys, int lane, int64_t wid,
+                                                    int64_t warps_total, double (&acc)[BS_W]) {
+  const int64_t nsc = (1LL << nsys) >> BS_SC;
+  double lanetot = 0;
+  for (int64_t sc = wid; sc < nsc; sc += warps_total) {
+    float th = 0, tl = 0;                                     // the lane's total
+    float jh[5] = {0, 0, 0, 0, 0}, jl[5] = {0, 0, 0, 0, 0};  // bits 5-9
+    float kh[5] = {0, 0, 0, 0, 0}, kl[5] = {0, 0, 0, 0, 0};  // bits 10-14
+    const float2* base = s + ((uint64_t)sc << BS_SC) + lane;
+    for (int k = 0; k < 32; ++k) {
+      const float2* cp = base + ((uint64_t)k << 10);
+      float ch = 0, cl = 0;  // the chunk's total
+#pragma unroll
+      for (int g = 0; g < 4; ++g) {
+        float gs = 0, gb[3] = {0, 0, 0};
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) {
+          const float2 v = cp[(g * 8 + jj) << 5];
+          const float p = fmaf(v.x, v.x, v.y * v.y);
+          gs += p;
+#pragma unroll
+          for (int b = 0; b < 3; ++b)
+            if ((jj >> b) & 1) gb[b] += p;
+        }
+        two_sum_acc(ch, cl, gs);
+#pragma unroll
+        for (int b = 0; b < 3; ++b) two_sum_acc(jh[b], jl[b], gb[b]);
+        if (g & 1) two_sum_acc(jh[3], jl[3], gs);
+        if (g & 2) two_sum_acc(jh[4], jl[4], gs);
+      }
+      two_sum_acc(th, tl, ch);
+      tl += cl;
+#pragma unroll
+      for (int b = 0; b < 5; ++b)
+        if ((k >> b) & 1) {
+          two_sum_acc(kh[b], kl[b], ch);
+          kl[b] += cl;
+        }
+    }
+    const double tot = (double)th + (double)tl;
+    lanetot += tot;
+#pragma unroll
+    for (int b = 0; b < 5; ++b) {
+      acc[1 + 5 + b] += (double)jh[b] + (double)jl[b];
+      acc[1 + 10 + b] += (double)kh[b] + (double)kl[b];
+    }
+    const uint64_t hi = (uint64_t)sc << BS_SC;
+#pragma unroll
+    for (int b = BS_SC; b < BS_W - 1; ++b) acc[1 + b] += ((hi >> b) & 1) ? tot : 0.0;
+  }
+  acc[0] += lanetot;
+#pragma unroll
+  for (int b = 0; b < 5; ++b)
+    if ((lane >> b) & 1) acc[1 + b] += lanetot;
+}
+
 template <typename R>
 __global__ void __launch_bounds__(BT_THREADS) k_bitsums(const typename CT<R>::T* __restrict__ psi, int nbits,
                                                         int nsys, int dm, int64_t mem_lo, int nblk,
@@ -577,6 +649,13 @@ __global__ void __launch_bounds__(BT_THREADS) k_bitsums(const typename CT<R>::T*
   const int64_t nent = 1LL << nsys;
   const int64_t warps_total = (int64_t)nblk * (blockDim.x >> 5);
   const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if constexpr (sizeof(R) == 4) {
+    if (!dm && nsys >= BS_SC) {  // the same branch in every thread of the launch
+      bitsums_superchunks(s, nsys, lane, wid, warps_total, acc);
+      block_sum_store<BS_W>(acc, part + ((int64_t)blockIdx.y * nblk + blockIdx.x) * BS_W, BS_W);
+      return;
+    }
+  }
   if (nsys >= 10) {
     const int64_t nchunk = nent >> 10;
     double lanetot = 0;
@@ -637,12 +716,6 @@ __global__ void __launch_bounds__(BT_THREADS) k_bitsums(const typename CT<R>::T*
 // terms of a thread's 8-term groups are added with TwoSum into a float-float
 // (hi, lo) pair, so a group carries ~44 significant bits at FP32 issue rate;
 // groups, threads and blocks then sum in FP64.  complex128: FP64 throughout.
-__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
-  const float s = hi + x, bb = s - hi;
-  lo += (hi - (s - bb)) + (x - bb);
-  hi = s;
-}
-
 template <typename R>
 __global__ void __launch_bounds__(BT_THREADS) k_norm2(const typename CT<R>::T* __restrict__ psi, int nbits, int nsys,
                                                       int dm, int64_t mem_lo, int nblk, double* __restrict__ part) {
@@ -704,12 +777,33 @@ int bt_launch_norm2(bt_state* s, int64_t mem_lo, int64_t nmem, double* out) {
   return finalize(ctx, part, nblk, 1, nmem, out);
 }
 
+// blocks per member of the super-chunk form: every SM filled to the kernel's
+// occupancy (the grid loops, so no partial last wave) and at least one
+// super-chunk per warp
+static int superchunk_blocks(const bt_ctx* ctx, int64_t nsc, int64_t nmem) {
+  static std::atomic<int> occ{0};
+  int o = occ.load();
+  if (!o) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_bitsums<float>, BT_THREADS, 0) != cudaSuccess || o < 1) {
+      (void)cudaGetLastError();  // leave no error behind for the launch check
+      o = 1;
+    }
+    occ.store(o);
+  }
+  int64_t per = ((int64_t)ctx->sm_count * o + nmem - 1) / nmem;
+  const int64_t maxb = (nsc + BT_THREADS / 32 - 1) / (BT_THREADS / 32);
+  if (per > maxb) per = maxb;
+  if (per < 1) per = 1;
+  return (int)per;
+}
+
 int bt_launch_bitsums(bt_state* s, int64_t mem_lo, int64_t nmem, double* out) {
   bt_ctx* ctx = s->ctx;
   if (s->n > BS_W - 1) return bt_fail(ctx, BT_ERR_UNSUPPORTED, "too many qubits for per-bit sums");
   if (nmem > 65535) return bt_fail(ctx, BT_ERR_UNSUPPORTED, "at most 65535 members per reduction");
+  const bool superchunks = s->prec == BT_PREC_C64 && s->repr != BT_REPR_DM && s->n >= BS_SC;
   int64_t units = s->n >= 10 ? (1LL << s->n) / 32 : (1LL << s->n);
-  int nblk = blocks_per_member(ctx, units, nmem);
+  int nblk = superchunks ? superchunk_blocks(ctx, (1LL << s->n) >> BS_SC, nmem) : blocks_per_member(ctx, units, nmem);
   double* part;
   int rc = bt_work(ctx, sizeof(double) * (size_t)nmem * nblk * BS_W, &part);
   if (rc) return rc;

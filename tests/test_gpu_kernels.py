@@ -326,6 +326,31 @@ def test_pauli_expectations(ctx, oracle, prec):
     assert np.abs(np.array(zs) - [oracle.expect_pauli_dm(rho, 0, 1 << (5 - q)) for q in range(1, 6)]).max() < tol
 
 
+@pytest.mark.parametrize("prec,tol", [("c64", 2e-6), ("c128", 1e-12)])
+def test_z_all_large_and_batched(ctx, prec, tol):
+    """<Z_i> of every qubit (bt_expect_z_all: per-bit sums; complex64 states of
+    2^15 amplitudes and more take the super-chunk form) at 15, 16 and 20 qubits,
+    for one member and for all members of a batch of 3, against FP64 sums of the
+    stored amplitudes' |psi|^2 on the host."""
+    import bluetangle_gpu as bt
+    rng = np.random.default_rng(77)
+    for n in (15, 16, 20):
+        psis = [rstate(rng, n) for _ in range(3)]
+        st = bt.zero_state(n, prec, 3)
+        for m, psi in enumerate(psis):
+            st.upload(psi, m)
+        idx = np.arange(2 ** n)
+        refs = []
+        for psi in psis:
+            stored = psi.astype(np.complex64 if prec == "c64" else np.complex128).astype(np.complex128)
+            p = np.abs(stored) ** 2
+            refs.append(np.array([p.sum() - 2 * p[((idx >> (n - q)) & 1) == 1].sum() for q in range(1, n + 1)]))
+        allz = bt.expect(st, "Z", member=-1)
+        for m in range(3):
+            assert np.abs(np.asarray(bt.expect(st, "Z", member=m)) - refs[m]).max() < tol, (n, m)
+            assert np.abs(allz[m] - refs[m]).max() < tol, (n, m)
+
+
 def test_fidelity_and_norm(ctx):
     import bluetangle_gpu as bt
     rng = np.random.default_rng(21)

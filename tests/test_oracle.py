@@ -254,6 +254,30 @@ def test_ref_mid_circuit_exact_outcomes(oracle, kref):
         assert ind == 1
 
 
+def test_ref_docs_mid_measurement_ghz_or_111(oracle, kref):
+    """The reference's documented mid-measurement example: X on qubit 1,
+    ifOp("MX", 1, "Z", "H"), CNOT(1,2), CNOT(2,3) ends in (|000> - |111>)/sqrt(2)
+    after outcome 0 and in -|111> after outcome 1, each with probability 1/2
+    (docs/src/examples.md:257-262, :283; ifOp: rotate by H, measure Z, rotate back,
+    then the branch's ops, src/struct.jl:578-594)."""
+    H, X, Z, CX = (kref.GATE[g] for g in ("H", "X", "Z", "CX"))
+    want = {0: np.zeros(8, complex), 1: np.zeros(8, complex)}
+    want[0][0], want[0][7] = 1 / np.sqrt(2), -1 / np.sqrt(2)
+    want[1][7] = -1
+    for u, outcome in ((0.25, 0), (0.75, 1)):
+        s = np.zeros(8, complex)
+        s[0] = 1
+        s = oracle.hilbert1(s, X, 1)
+        s = oracle.hilbert1(s, H, 1)
+        s, ind, p0 = oracle.born_measure_z(s, 1, u=u)
+        s = oracle.hilbert1(s, H.conj().T, 1)
+        s = oracle.hilbert1(s, Z if ind == 0 else H, 1)
+        s = oracle.hilbert2(s, CX, 1, 2)
+        s = oracle.hilbert2(s, CX, 2, 3)
+        assert ind == outcome and abs(p0 - 0.5) < 1e-12
+        assert np.abs(s - want[outcome]).max() < 1e-12, (outcome, s)
+
+
 def test_ref_channel_cptp_and_sample_semantics(oracle):
     """weighted sample: first i with u <= cumsum(p) (src/hilbert.jl:810-819); sample
     picks the first index whose cumulative weight reaches u*sum (StatsBase direct)."""

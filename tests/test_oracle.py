@@ -278,6 +278,25 @@ def test_ref_docs_mid_measurement_ghz_or_111(oracle, kref):
         assert np.abs(s - want[outcome]).max() < 1e-12, (outcome, s)
 
 
+def test_ref_docs_reset_of_a_bell_state(oracle, kref):
+    """The reference's documented reset example: Op("RES", 1) on the Bell state
+    (|00> + |11>)/sqrt(2) leaves |00> or |01>, each with probability 1/2
+    (docs/src/examples.md:337-343; _reset_Z: measure, X on outcome 1,
+    src/hilbert.jl:752-759)."""
+    H, X, CX = (kref.GATE[g] for g in ("H", "X", "CX"))
+    for u, outcome, idx in ((0.25, 0, 0), (0.75, 1, 1)):
+        s = np.zeros(4, complex)
+        s[0] = 1
+        s = oracle.hilbert2(oracle.hilbert1(s, H, 1), CX, 1, 2)
+        s, ind, p0 = oracle.born_measure_z(s, 1, u=u)
+        if ind == 1:
+            s = oracle.hilbert1(s, X, 1)
+        want = np.zeros(4, complex)
+        want[idx] = 1
+        assert ind == outcome and abs(p0 - 0.5) < 1e-12
+        assert np.abs(s - want).max() < 1e-12, (outcome, s)
+
+
 def test_ref_channel_cptp_and_sample_semantics(oracle):
     """weighted sample: first i with u <= cumsum(p) (src/hilbert.jl:810-819); sample
     picks the first index whose cumulative weight reaches u*sum (StatsBase direct)."""

@@ -4,6 +4,8 @@
    reference's operator construction (tests/golden/make_golden.py).
 2. Against every property the reference's own test suite asserts for this
    path (BlueTangle.jl test/runtests.jl), run on the oracle.
+3. Against the outcomes the reference's documentation states for its
+   mid-measurement and reset examples (docs/src/examples.md).
 """
 import math
 import os

@@ -192,7 +192,7 @@ def test_ref_channel_vs_stochastic_pauli_fidelity(oracle):
     """N=1, depth 20, p=0.01: OpQC("depolarizing") after every op == the op with
     NoiseModel("depolarizing") (t1), and fidelity(rho1, rho0) equals the mean over
     1000 runs of fidelity(rho3, rho0), rho3 the ops with X, Y or Z drawn with
-    probability p after each, within atol 100/1000 (t2) (test/runtests.jl:134-190)."""
+    probability p after each, within atol 100/1000 (t2) (test/runtests.jl:136-193)."""
     import scipy.linalg as sl
 
     import bluetangle_gpu as bt
